@@ -1,0 +1,213 @@
+/*
+ * aieplace.h -- C ABI of the GB300 ePlace global-placement library.
+ *
+ * One handle holds one placement instance resident on one GPU.  Every call
+ * returns an int status (AP_OK == 0).  Arrays passed in are caller-owned host
+ * memory and are copied; nothing keeps a pointer past the call.  A handle is
+ * not re-entrant: calls on the same handle must not overlap.  Calls are
+ * synchronous with respect to the host unless a stream is set with
+ * ap_set_stream, in which case host-visible results are still complete when
+ * the call returns (results are read back through pinned memory on that
+ * stream).
+ *
+ * Coordinate conventions follow the reference host placer:
+ *   - a node's position (x, y) is its lower-left corner and every pin of the
+ *     node sits at that corner (Net.cpp:136-155 reads Node::getX/getY);
+ *   - bin maps are x-major: element [bx * bins_y + by] is bin column bx, row
+ *     by (Grid.h:16 m_bins[col][row], fft.cpp binDensity_[x][y]).
+ *
+ * Reference citations are paths inside searsm8/AIEplace.
+ */
+#ifndef AIEPLACE_H
+#define AIEPLACE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define AP_ABI_VERSION 1
+
+/* ---- status codes ------------------------------------------------------ */
+enum {
+    AP_OK = 0,
+    AP_ERR_INVALID_ARG = 1, /* null pointer, size out of range */
+    AP_ERR_BAD_NETLIST = 2, /* malformed CSR: non-monotone net_ptr, pin index out of range */
+    AP_ERR_NONFINITE = 3,   /* NaN / Inf in positions or sizes */
+    AP_ERR_CUDA = 4,        /* a CUDA runtime call failed */
+    AP_ERR_NO_DEVICE = 5,   /* no usable sm_103 device */
+    AP_ERR_UNSUPPORTED = 6, /* configuration the selected kernels do not handle */
+    AP_ERR_TIMEOUT = 7,     /* a bounded device-side wait gave up */
+    AP_ERR_STATE = 8,       /* call out of order (e.g. ap_step before positions exist) */
+    AP_ERR_DIVERGED = 9     /* the optimiser produced non-finite state */
+};
+
+/* ---- field solvers ----------------------------------------------------- */
+enum {
+    AP_FIELD_FP32 = 0,   /* dense per-axis transforms, FP32 SIMT contraction */
+    AP_FIELD_BF16X3 = 1  /* dense per-axis transforms, tcgen05 BF16 x3 split, FP32 accumulate */
+};
+
+/* Netlist in CSR form.  Replaces the object graph the reference builds from
+ * LEF/DEF (DataBase.cpp:351-416 add_def_* callbacks, Net.h:10-84, Node.h:31-158).
+ * Nets of degree < 2 are accepted and ignored.  Nodes with fixed != 0 never
+ * move; their x/y are final.  Zero-area nodes (IO pads) carry pins only. */
+typedef struct ap_netlist {
+    int32_t num_nodes;
+    int32_t num_nets;
+    int32_t num_pins;
+    const int32_t *net_ptr;     /* [num_nets + 1], net_ptr[0] == 0, non-decreasing */
+    const int32_t *pin_node;    /* [num_pins] node index of each pin */
+    const float *node_w;        /* [num_nodes] width  (die units) */
+    const float *node_h;        /* [num_nodes] height (die units) */
+    const float *node_x;        /* [num_nodes] initial lower-left x */
+    const float *node_y;        /* [num_nodes] initial lower-left y */
+    const uint8_t *node_fixed;  /* [num_nodes] 1 = fixed; may be NULL (all movable) */
+    float die_xl, die_yl, die_xh, die_yh;
+} ap_netlist;
+
+/* Placer parameters.  Key names follow host/config_aieplace.json where the
+ * reference has one (bins_per_row -> bins_x/bins_y, gamma, max_iterations). */
+typedef struct ap_params {
+    int32_t bins_x;             /* density bins along x (power of two, 16..4096) */
+    int32_t bins_y;             /* density bins along y (== bins_x) */
+    float target_density;       /* rho_t: bin capacity fraction used by overflow and fixed scaling */
+    float gamma_base_bins;      /* WA smoothing base, in bins; gamma = base*bin_w*10^(20/9 (tau-0.1) - 1) */
+    int32_t field_solver;       /* AP_FIELD_* */
+    float init_density_weight;  /* lambda_0 = this * |grad WL|_1 / |grad D|_1 */
+    float ref_delta_hpwl;       /* lambda update reference HPWL change; <= 0 selects 3.5e-5 * nets * bin_w */
+    float lambda_mu_max;        /* lambda multiplier bounds: mu in [mu_min, mu_max] */
+    float lambda_mu_min;
+    float init_step_coef;       /* first step: v_{-1} = v_0 - coef * g_0 (in bins) */
+    float target_overflow;      /* ap_run stops once overflow < this */
+    int32_t max_iterations;     /* ap_run upper bound */
+    int32_t check_interval;     /* ap_run reads the device status every this many iterations */
+    int32_t use_graph;          /* capture the iteration in a CUDA graph (1) or launch eagerly (0) */
+} ap_params;
+
+/* Per-iteration readout; the fields of printIterationResults (AIEplace.cpp:1048-1070)
+ * plus the optimiser scalars the reference lacks. */
+typedef struct ap_stats {
+    int32_t iteration;
+    int32_t status;
+    double hpwl;          /* sum over nets of bounding-box half perimeter (Net.cpp:136-155) */
+    double wa_wirelength; /* weighted-average wirelength at the same positions */
+    double overflow;      /* sum_b max(0, rho_b - rho_t*A_b) / movable area */
+    double overflow_abs;  /* reference form: sum_b max(0, overlap_b - A_b) (Grid.cpp:144-151) */
+    double lambda;        /* density weight */
+    double gamma;         /* WA smoothing, die units */
+    double alpha;         /* Nesterov step length */
+    double a_k;           /* Nesterov momentum sequence */
+} ap_stats;
+
+typedef struct ap_handle ap_handle;
+
+int ap_abi_version(void);
+const char *ap_status_string(int status);
+
+/* Fills defaults (bins 512, rho_t 1.0, gamma base 4 bins, FP32 solver, lambda_0 8e-5 ...). */
+int ap_params_default(ap_params *p);
+
+/* Builds the device-resident instance.  Replaces Placer::Placer
+ * (vck5000/host/src/AIEplace.cpp:87-138) and Grid::Grid (Grid.cpp:6-22). */
+int ap_create(const ap_netlist *netlist, const ap_params *params, ap_handle **out);
+int ap_destroy(ap_handle *h);
+
+/* Runs all following device work of this handle on `stream` (a cudaStream_t). */
+int ap_set_stream(ap_handle *h, void *cuda_stream);
+
+/* Sets movable positions from caller arrays indexed like the netlist (fixed
+ * entries ignored) and resets the optimiser.  Replaces the placement half of
+ * Placer::initializePlacement (AIEplace.cpp:187-243). */
+int ap_init_positions(ap_handle *h, const float *x, const float *y);
+
+/* Seeded initial placement: die centre plus N(0, sigma) per movable node
+ * (the reference uses unseeded rand() in +-dieW/4, AIEplace.cpp:200-213). */
+int ap_init_seeded(ap_handle *h, uint64_t seed, float sigma);
+
+/* n_iter iterations of the preconditioned Nesterov loop; one iteration is the
+ * reference's performIteration (AIEplace.cpp:9-39): wirelength gradient,
+ * density map, field solve, field gather and position update, HPWL and
+ * overflow readout. */
+int ap_step(ap_handle *h, int32_t n_iter);
+
+/* Iterates until overflow < params.target_overflow or max_iterations;
+ * replaces Placer::run (AIEplace.cpp:44-76). */
+int ap_run(ap_handle *h, int32_t *iterations_done);
+
+/* Host-buffer iteration for callers that own the positions, as the reference
+ * host does (Node::m_pos): x_in/y_in replace the current positions (NULL keeps
+ * them), one iteration runs, the new positions and readout are copied out.
+ * The optimiser state stays on the device. */
+int ap_step_host(ap_handle *h, const float *x_in, const float *y_in,
+                 float *x_out, float *y_out, ap_stats *stats);
+
+int ap_get_positions(ap_handle *h, float *x, float *y);
+int ap_get_stats(ap_handle *h, ap_stats *stats);
+
+/* Readout at the current positions: DataBase::computeTotalWirelength
+ * (DataBase.cpp:143-149) and Grid::computeTotalOverflow (Grid.cpp:144-151). */
+int ap_hpwl(ap_handle *h, double *hpwl);
+int ap_overflow(ap_handle *h, double *overflow, double *overflow_abs);
+
+/* ---- per-stage entry points (one per reference function) --------------- */
+
+/* WA wirelength gradient at the given node positions (all nodes, netlist
+ * order).  Replaces Placer::computeAllPartials_CPU / computeNetPartials_CPU
+ * (AIEplace.cpp:574-673) and the AIE partials graph (aie/src/partials/
+ * compute_abc.cpp:23-125, compute_partials.cpp:11-63).  Unlike the reference
+ * it covers every net degree >= 2 (the reference stops at 8, AIEplace.cpp:586).
+ * gx/gy receive dWA/dx, dWA/dy per node (fixed nodes included); wa/hpwl may be NULL. */
+int ap_wirelength_grad(ap_handle *h, const float *x, const float *y, float gamma,
+                       float *gx, float *gy, double *wa, double *hpwl);
+
+/* Density map at the given positions, int64 fixed point (2^32 per unit area),
+ * movable and fixed nodes at weight 1.  Replaces Placer::computeOverlaps
+ * (AIEplace.cpp:937-967) + Grid::computeBinOverlaps (Grid.cpp:38-110) +
+ * Grid::getRho (Grid.cpp:112-127).  rho_q has bins_x*bins_y entries, x-major. */
+int ap_density_map(ap_handle *h, const float *x, const float *y, int64_t *rho_q);
+
+/* Electrostatic solve on a caller density map (x-major, bins_x*bins_y) with
+ * the RePlAce conventions of python/AIEmath/fft_replace/fft.cpp:204-299
+ * (FFT::doFFT): DCT-II, halved edge rows, 4/(Mx My), phi = a/(wx^2+wy^2),
+ * Ex by sine-cosine, Ey by cosine-sine inverse transforms.  ex/ey receive the
+ * field per bin; the solver is params.field_solver or `solver` if >= 0. */
+int ap_field_solve(ap_handle *h, const float *density, float *ex, float *ey, int32_t solver);
+
+/* ---- checkpoint / resume ----------------------------------------------- */
+int ap_snapshot_size(ap_handle *h, size_t *bytes);
+int ap_snapshot(ap_handle *h, void *buf, size_t bytes);
+int ap_restore(ap_handle *h, const void *buf, size_t bytes);
+
+/* ---- seeded synthetic netlists ------------------------------------------ */
+/* Stands in for the ISPD suites the reference reads through LEF/DEF.  Nodes
+ * are ordered: movable cells, fixed macros, IO pads. */
+typedef struct ap_synth_config {
+    int32_t num_cells;        /* movable cells */
+    int32_t num_nets;
+    int32_t num_macros;       /* fixed macros */
+    int32_t num_pads;         /* zero-area fixed IO pads on the die boundary */
+    int32_t unit_cells;       /* 1: every cell 1x1; 0: width ~ LogNormal(ln 2, 0.5), height 1 */
+    int32_t degree_mix;       /* 0: 70% 2, 20% 3, 10% 4 pins; 1: 65% 2, 20% 3, 10% U[4,10], 5% U[11,64] */
+    float locality;           /* probability a pin is drawn within `window` node indices of the net anchor */
+    int32_t window;           /* locality window (node indices) */
+    float macro_area_min;     /* macro area U[min, max] (square-ish) */
+    float macro_area_max;
+    float target_density;     /* sizes the die: area = movable/rho_t + macros */
+    float die_side;           /* > 0 forces a square die of this side */
+    uint64_t seed;
+} ap_synth_config;
+
+int ap_synth_counts(const ap_synth_config *cfg, int32_t *num_nodes, int32_t *num_nets,
+                    int32_t *num_pins);
+/* Arrays sized by ap_synth_counts; die receives {xl, yl, xh, yh}. */
+int ap_synth_generate(const ap_synth_config *cfg, int32_t *net_ptr, int32_t *pin_node,
+                      float *node_w, float *node_h, float *node_x, float *node_y,
+                      uint8_t *node_fixed, float *die);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* AIEPLACE_H */

@@ -1,0 +1,255 @@
+"""ctypes front end of the CPU oracle (liboracle.so) and of the reference's own
+CPU code (_ref/libref.so, present only where the reference checkout was
+available at build time).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
+CPU legs of bench.py as the checker or the timed CPU baseline.  The product
+path (aieplace_gb300) never imports it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liboracle.so")
+REF_PATH = os.path.join(HERE, "_ref", "libref.so")
+REF_SRC = os.environ.get("AP_REFERENCE_DIR", "/root/reference")
+
+_f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+_f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+_i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+_i64p = np.ctypeslib.ndpointer(np.int64, flags="C_CONTIGUOUS")
+_u8p = np.ctypeslib.ndpointer(np.uint8, flags="C_CONTIGUOUS")
+
+
+def build(with_ref: bool | None = None) -> None:
+    """Compile liboracle.so, and _ref/libref.so when the reference checkout exists."""
+    subprocess.run(["make", "-s", "-C", HERE, "liboracle.so"], check=True)
+    if with_ref is None:
+        with_ref = os.path.isdir(REF_SRC)
+    if with_ref:
+        subprocess.run(["make", "-s", "-C", HERE, f"REF={REF_SRC}", "ref"], check=True)
+
+
+class OrGrid(C.Structure):
+    _fields_ = [("mx", C.c_int), ("my", C.c_int), ("die_w", C.c_float), ("die_h", C.c_float),
+                ("bw", C.c_float), ("bh", C.c_float), ("small_threshold", C.c_float),
+                ("bw_q", C.c_int64), ("bh_q", C.c_int64)]
+
+
+class OrParams(C.Structure):
+    _fields_ = [("mx", C.c_int), ("my", C.c_int), ("target_density", C.c_double),
+                ("gamma_base_bins", C.c_double), ("init_density_weight", C.c_double),
+                ("ref_delta_hpwl", C.c_double), ("mu_max", C.c_double), ("mu_min", C.c_double),
+                ("init_step_coef", C.c_double)]
+
+
+class OrStats(C.Structure):
+    _fields_ = [("iteration", C.c_int), ("hpwl", C.c_double), ("wa", C.c_double),
+                ("overflow", C.c_double), ("overflow_abs", C.c_double), ("lambda_", C.c_double),
+                ("gamma", C.c_double), ("alpha", C.c_double), ("a_k", C.c_double)]
+
+
+_lib = None
+_ref = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build(with_ref=False)
+        L = C.CDLL(LIB_PATH)
+        L.or_fast_exp.restype = C.c_double
+        L.or_fast_exp.argtypes = [C.c_double, C.c_int]
+        L.or_wa_terms_sorted.argtypes = [C.c_int, _f64p, C.c_double, C.c_int, _f64p, _f64p, _f64p, _f64p]
+        L.or_wa_grad.argtypes = [C.c_int, C.c_int, _i32p, _i32p, _f32p, _f32p, C.c_double, C.c_int,
+                                 C.c_int, _f64p, _f64p, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        L.or_grid_init.argtypes = [C.POINTER(OrGrid), C.c_float, C.c_float, C.c_int, C.c_int]
+        L.or_density_q.argtypes = [C.POINTER(OrGrid), C.c_int, _f32p, _f32p, _f32p, _f32p, C.c_void_p, _i64p]
+        L.or_overflow.argtypes = [C.POINTER(OrGrid), _i64p, C.c_void_p, C.c_void_p, C.c_double, C.c_double,
+                                  C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        L.or_scale_fixed.argtypes = [C.c_int, _i64p, C.c_double, _i64p]
+        L.or_density_float.argtypes = [C.POINTER(OrGrid), _i64p, C.c_void_p, _f32p]
+        L.or_field_solve.argtypes = [C.c_int, C.c_int, C.c_double, _f64p, C.c_void_p, _f64p, _f64p]
+        for n in ("or_dct_1d", "or_idct_1d", "or_idxst_1d"):
+            getattr(L, n).argtypes = [C.c_int, _f64p, _f64p]
+        L.or_create.restype = C.c_void_p
+        L.or_create.argtypes = [C.c_int, C.c_int, _i32p, _i32p, _f32p, _f32p, _f32p, _f32p, _u8p,
+                                C.c_float, C.c_float, C.POINTER(OrParams)]
+        L.or_init.argtypes = [C.c_void_p, _f32p, _f32p]
+        L.or_step.argtypes = [C.c_void_p, C.c_int]
+        L.or_get_stats.argtypes = [C.c_void_p, C.POINTER(OrStats)]
+        L.or_get_positions.argtypes = [C.c_void_p, _f32p, _f32p]
+        L.or_destroy.argtypes = [C.c_void_p]
+        L.or_set_threads.restype = C.c_int
+        L.or_set_threads.argtypes = [C.c_int]
+        _lib = L
+    return _lib
+
+
+def ref_lib():
+    """The reference's own CPU functions, or None where they were not built."""
+    global _ref
+    if _ref is None and os.path.exists(REF_PATH):
+        try:
+            R = C.CDLL(REF_PATH)
+        except OSError:
+            return None
+        R.ref_density.argtypes = [C.c_int, _f32p, _f32p, _f32p, _f32p, C.c_float, C.c_float, C.c_int,
+                                  _f32p, C.POINTER(C.c_double)]
+        R.ref_hpwl.restype = C.c_double
+        R.ref_hpwl.argtypes = [C.c_int, C.c_int, _i32p, _i32p, _f32p, _f32p]
+        for n in ("ref_dct", "ref_idct", "ref_idxst"):
+            getattr(R, n).argtypes = [C.c_int, _f32p, _f32p]
+        R.ref_replace_field.argtypes = [C.c_int, _f32p, C.c_void_p, _f32p, _f32p]
+        _ref = R
+    return _ref
+
+
+def set_threads(n: int) -> int:
+    return lib().or_set_threads(n)
+
+
+# ---------------------------------------------------------------- WA terms
+
+def fast_exp(a: float, prec: int = 16) -> float:
+    return lib().or_fast_exp(a, prec)
+
+
+def wa_terms_sorted(xs, gamma: float, fast: bool = False):
+    x = np.ascontiguousarray(xs, dtype=np.float64)
+    n = len(x)
+    ap, am, bc, part = (np.zeros(n), np.zeros(n), np.zeros(4), np.zeros(n))
+    lib().or_wa_terms_sorted(n, x, gamma, int(fast), ap, am, bc, part)
+    return ap, am, bc, part
+
+
+def wa_grad(net_ptr, pin_node, x, y, gamma, min_deg=2, max_deg=1 << 30):
+    n = len(x)
+    gx, gy = np.zeros(n), np.zeros(n)
+    wa, hp = C.c_double(), C.c_double()
+    lib().or_wa_grad(n, len(net_ptr) - 1, _i32(net_ptr), _i32(pin_node), _f32(x), _f32(y), gamma,
+                     min_deg, max_deg, gx, gy, C.byref(wa), C.byref(hp))
+    return gx, gy, wa.value, hp.value
+
+
+# ---------------------------------------------------------------- density
+
+def grid(die_w, die_h, mx, my=None) -> OrGrid:
+    g = OrGrid()
+    lib().or_grid_init(C.byref(g), die_w, die_h, mx, my or mx)
+    return g
+
+
+def density_q(g: OrGrid, x, y, w, h, include=None):
+    rho = np.zeros(g.mx * g.my, dtype=np.int64)
+    inc = None if include is None else np.ascontiguousarray(include, dtype=np.uint8)
+    lib().or_density_q(C.byref(g), len(x), _f32(x), _f32(y), _f32(w), _f32(h),
+                       None if inc is None else inc.ctypes.data, rho)
+    return rho
+
+
+def scale_fixed(fixed_q, rho_t):
+    out = np.zeros_like(fixed_q)
+    lib().or_scale_fixed(len(fixed_q), np.ascontiguousarray(fixed_q), rho_t, out)
+    return out
+
+
+def overflow(g: OrGrid, mov_q, fixed_q, fixed_scaled_q, rho_t, movable_area_q):
+    tau, ab = C.c_double(), C.c_double()
+    lib().or_overflow(C.byref(g), mov_q, fixed_q.ctypes.data, fixed_scaled_q.ctypes.data, rho_t,
+                      float(movable_area_q), C.byref(tau), C.byref(ab))
+    return tau.value, ab.value
+
+
+def density_float(g: OrGrid, mov_q, fixed_scaled_q):
+    d = np.zeros(g.mx * g.my, dtype=np.float32)
+    lib().or_density_float(C.byref(g), mov_q, fixed_scaled_q.ctypes.data, d)
+    return d
+
+
+# ---------------------------------------------------------------- spectral
+
+def field_solve(d, m: int, bin_ratio: float = 1.0, want_phi: bool = False):
+    d = np.ascontiguousarray(d, dtype=np.float64).reshape(-1)
+    ex, ey = np.zeros(m * m), np.zeros(m * m)
+    phi = np.zeros(m * m) if want_phi else None
+    lib().or_field_solve(m, m, bin_ratio, d, None if phi is None else phi.ctypes.data, ex, ey)
+    return (ex, ey, phi) if want_phi else (ex, ey)
+
+
+def dct_1d(v):
+    v = np.ascontiguousarray(v, dtype=np.float64)
+    o = np.zeros_like(v)
+    lib().or_dct_1d(len(v), v, o)
+    return o
+
+
+def idct_1d(v):
+    v = np.ascontiguousarray(v, dtype=np.float64)
+    o = np.zeros_like(v)
+    lib().or_idct_1d(len(v), v, o)
+    return o
+
+
+def idxst_1d(v):
+    v = np.ascontiguousarray(v, dtype=np.float64)
+    o = np.zeros_like(v)
+    lib().or_idxst_1d(len(v), v, o)
+    return o
+
+
+# ---------------------------------------------------------------- loop
+
+class Placer:
+    """FP64 ePlace loop oracle over a CSR netlist (movable nodes first)."""
+
+    def __init__(self, nl: dict, mx: int, target_density: float, gamma_base_bins=4.0,
+                 init_density_weight=8e-5, ref_delta_hpwl=0.0, mu_max=1.05, mu_min=0.95,
+                 init_step_coef=0.1):
+        p = OrParams(mx, mx, target_density, gamma_base_bins, init_density_weight, ref_delta_hpwl,
+                     mu_max, mu_min, init_step_coef)
+        self._keep = nl
+        die = nl["die"]
+        self.h = lib().or_create(len(nl["node_w"]), len(nl["net_ptr"]) - 1, _i32(nl["net_ptr"]),
+                                 _i32(nl["pin_node"]), _f32(nl["node_w"]), _f32(nl["node_h"]),
+                                 _f32(nl["node_x"]), _f32(nl["node_y"]),
+                                 np.ascontiguousarray(nl["node_fixed"], dtype=np.uint8),
+                                 float(die[2] - die[0]), float(die[3] - die[1]), C.byref(p))
+        self.n = len(nl["node_w"])
+
+    def init(self, x, y):
+        lib().or_init(self.h, _f32(x), _f32(y))
+
+    def step(self, n: int = 1):
+        lib().or_step(self.h, n)
+
+    def stats(self) -> dict:
+        s = OrStats()
+        lib().or_get_stats(self.h, C.byref(s))
+        return {"iteration": s.iteration, "hpwl": s.hpwl, "wa": s.wa, "overflow": s.overflow,
+                "overflow_abs": s.overflow_abs, "lambda": s.lambda_, "gamma": s.gamma,
+                "alpha": s.alpha, "a_k": s.a_k}
+
+    def positions(self):
+        x, y = np.zeros(self.n, np.float32), np.zeros(self.n, np.float32)
+        lib().or_get_positions(self.h, x, y)
+        return x, y
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().or_destroy(self.h)
+            self.h = None
+
+
+def _f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def _i32(a):
+    return np.ascontiguousarray(a, dtype=np.int32)

@@ -1,0 +1,168 @@
+"""Regenerates the golden fixtures in this folder from the reference checkout.
+
+Run here (not on the GPU machine, which has no reference checkout):
+
+    make -C oracle ref            # builds oracle/_ref/libref.so from the reference sources
+    python tests/golden/make_golden.py [/path/to/reference]
+
+Sources of each fixture:
+  aie_partials.npz   vck5000/aie/golden_data/partials/*.dat (createGoldenPartials.py:28-132)
+  aie_dct.npz        vck5000/aie/golden_data/density/*.dat  (createGoldenDCT.py:103-205)
+  computeterm.npz    python/AIEmath/computeTerm.py on seeded nets (fast_exp, gamma 4)
+  customdct.npz      python/AIEmath/customDCT.py dct/idct/idxst on seeded vectors
+  replace_field.npz  replace::FFT::doFFT (fft_replace/fft.cpp:204-299) via oracle/_ref
+  ref_grid.npz       Grid::computeBinOverlaps/getRho/computeTotalOverflow and
+                     Net::computeWirelength_HPWL via oracle/_ref
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(REPO, "oracle"))
+
+
+def read_dat(path):
+    with open(path) as f:
+        return np.array([float(t) for t in f.read().split()], dtype=np.float64)
+
+
+def aie_partials(ref):
+    d = os.path.join(ref, "vck5000", "aie", "golden_data", "partials")
+    out = {}
+    for b in range(4):
+        x_in = read_dat(os.path.join(d, f"x_in{b}.dat"))
+        out[f"ctrl{b}"] = x_in[:4]
+        # after the 4 control words: for pin order [max, min], 8 lanes each
+        out[f"x{b}"] = x_in[4:].reshape(2, 8)
+        for name in ("a_plus", "a_minus", "partials"):
+            out[f"{name}{b}"] = read_dat(os.path.join(d, f"{name}{b}.dat")).reshape(2, 8)
+        for name in ("b_plus", "b_minus", "c_plus", "c_minus"):
+            out[f"{name}{b}"] = read_dat(os.path.join(d, f"{name}{b}.dat"))
+    np.savez_compressed(os.path.join(HERE, "aie_partials.npz"), **out)
+
+
+def aie_dct(ref):
+    d = os.path.join(ref, "vck5000", "aie", "golden_data", "density")
+    out = {}
+    inp = read_dat(os.path.join(d, "input.dat"))
+    # complex pairs; the shipped file stops after 127.5 pairs (rows 0-7 complete)
+    n_re = (len(inp) + 1) // 2
+    re = inp[0::2][:n_re]
+    out["input_rows0_7"] = re[:128].reshape(8, 16)
+    for name in ("dct_output", "dct_2d_output", "idct_output", "idxst_output", "idct_2d_output",
+                 "idxst_2d_output"):
+        v = read_dat(os.path.join(d, f"{name}.dat"))
+        out[name] = v[0::2].reshape(16, 16)
+    np.savez_compressed(os.path.join(HERE, "aie_dct.npz"), **out)
+
+
+def computeterm(ref):
+    sys.path.insert(0, os.path.join(ref, "python", "AIEmath"))
+    import computeTerm  # noqa: E402  (reference module, read-only import)
+
+    rng = np.random.default_rng(20240601)
+    out = {}
+    k = 0
+    for deg in range(2, 9):
+        for rep in range(6):
+            lo = int(rng.integers(0, 10000))
+            xs = sorted(int(v) for v in rng.integers(lo, lo + 30 * deg, size=deg))
+            g = 4
+            ap = computeTerm.a_plus(xs, g)
+            am = computeTerm.a_minus(xs, g)
+            bp, bm = computeTerm.b_term(ap), computeTerm.b_term(am)
+            cp, cm = computeTerm.c_term(xs, ap), computeTerm.c_term(xs, am)
+            part = [computeTerm.WA_partial(xs[i], ap[i], bp, cp, am[i], bm, cm, g) for i in range(deg)]
+            out[f"x{k}"] = np.array(xs, dtype=np.float64)
+            out[f"ap{k}"] = np.array(ap)
+            out[f"am{k}"] = np.array(am)
+            out[f"bc{k}"] = np.array([bp, cp, bm, cm])
+            out[f"part{k}"] = np.array(part)
+            k += 1
+    out["count"] = np.array(k)
+    np.savez_compressed(os.path.join(HERE, "computeterm.npz"), **out)
+
+
+def customdct(ref):
+    sys.path.insert(0, os.path.join(ref, "python", "AIEmath"))
+    import customDCT  # noqa: E402
+
+    rng = np.random.default_rng(7)
+    out = {}
+    for n in (8, 16, 32):
+        v = rng.random(n)
+        out[f"in{n}"] = v
+        out[f"dct{n}"] = np.array(customDCT.dct(list(v)))
+        out[f"idct{n}"] = np.array(customDCT.idct(list(v)))
+        out[f"idxst{n}"] = np.array(customDCT.idxst(list(v)))
+    np.savez_compressed(os.path.join(HERE, "customdct.npz"), **out)
+
+
+def replace_field(R):
+    out = {}
+    cases = {"run_fft4": np.array([[1, 1, 99, 99], [1, 1, 99, 99], [99] * 4, [99] * 4], np.float32)}
+    rng = np.random.default_rng(11)
+    for m in (16, 32, 64):
+        cases[f"rand{m}"] = rng.random((m, m)).astype(np.float32)
+    for name, d in cases.items():
+        m = d.shape[0]
+        ex, ey, phi = (np.zeros(m * m, np.float32) for _ in range(3))
+        R.ref_replace_field(m, np.ascontiguousarray(d.reshape(-1)), phi.ctypes.data, ex, ey)
+        out[f"{name}_density"] = d
+        out[f"{name}_phi"] = phi.reshape(m, m)
+        out[f"{name}_ex"] = ex.reshape(m, m)
+        out[f"{name}_ey"] = ey.reshape(m, m)
+    np.savez_compressed(os.path.join(HERE, "replace_field.npz"), **out)
+
+
+def ref_grid(R):
+    rng = np.random.default_rng(5)
+    out = {}
+    # nodes straddling the die edge, small (area <= bin/16) and large ones
+    n, W, M = 2000, 40.0, 32
+    x = rng.uniform(-2.0, W, n).astype(np.float32)
+    y = rng.uniform(-2.0, W, n).astype(np.float32)
+    w = rng.choice([0.05, 0.2, 0.5, 1.0, 2.5, 6.0], n).astype(np.float32)
+    h = rng.choice([0.05, 0.3, 1.0, 1.7], n).astype(np.float32)
+    rho = np.zeros(M * M, np.float32)
+    ov = C.c_double()
+    R.ref_density(n, x, y, w, h, W, W, M, rho, C.byref(ov))
+    out.update(x=x, y=y, w=w, h=h, die=np.array([W, W], np.float32), m=np.array(M), rho=rho,
+               overflow=np.array(ov.value))
+    # HPWL of a small netlist
+    nn, ne = 300, 200
+    px = rng.uniform(0, 100, nn).astype(np.float32)
+    py = rng.uniform(0, 100, nn).astype(np.float32)
+    deg = rng.integers(1, 9, ne)
+    ptr = np.concatenate([[0], np.cumsum(deg)]).astype(np.int32)
+    pins = np.concatenate([rng.choice(nn, d, replace=False) for d in deg]).astype(np.int32)
+    hp = R.ref_hpwl(nn, ne, ptr, pins, px, py)
+    out.update(hp_x=px, hp_y=py, hp_ptr=ptr, hp_pins=pins, hpwl=np.array(hp))
+    np.savez_compressed(os.path.join(HERE, "ref_grid.npz"), **out)
+
+
+def main():
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("AP_REFERENCE_DIR", "/root/reference")
+    import oracle  # noqa: E402
+
+    oracle.REF_SRC = ref
+    oracle.build(with_ref=True)
+    R = oracle.ref_lib()
+    assert R is not None, "oracle/_ref/libref.so did not build"
+    aie_partials(ref)
+    aie_dct(ref)
+    computeterm(ref)
+    customdct(ref)
+    replace_field(R)
+    ref_grid(R)
+    print("fixtures written to", HERE)
+
+
+if __name__ == "__main__":
+    main()
