@@ -1,0 +1,132 @@
+// Kernel argument blocks and launchers of the placement iteration.
+#pragma once
+
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include "ap_common.cuh"
+
+namespace ap {
+
+// ---- wirelength -------------------------------------------------------------
+enum { WA_OUT_ONLY = 0, WA_LOOP = 1, WA_INIT = 2 };
+
+struct WaArgs {
+    const int *net_ptr;    // [n_nets + 1], nets of degree 2..8 first
+    const int *pin_node;   // internal node ids
+    int n_small, n_nets;
+    const float *px, *py;  // positions of all nodes (modes other than WA_LOOP)
+    const float *pxs[2], *pys[2];  // WA_LOOP: the trial point is buffer [1 - sc->cur]
+    float gamma;           // > 0 overrides sc->gamma
+    DevScalars *sc;
+    ull *gqx, *gqy;        // int64 fixed-point gradient accumulators
+    int n_grad;            // nodes [0, n_grad) receive gradient
+    double *partials;      // 2 * (small_grid + large_grid)
+    unsigned int *counter;
+    int small_blocks;
+    double *out;           // [2]: HPWL, WA
+    int mode;
+};
+void launch_wirelength(const WaArgs &a, int small_grid, int large_grid, cudaStream_t st);
+
+// ---- density scatter (+ Nesterov position update) ---------------------------
+struct ScatterArgs {
+    Grid g;
+    const float *w, *h;
+    // plain mode: scatter nodes [lo, hi) at (px, py)
+    const float *px, *py;
+    int lo, hi;
+    // update mode: movable nodes [0, n_mov) step from the accepted state
+    // (buffers [cur]) to the trial point (buffers [1 - cur]), then scatter
+    int update;
+    int n_mov;
+    float die_w, die_h;
+    float *ux[2], *uy[2];
+    float *vx[2], *vy[2];
+    const float *gx[2], *gy[2];
+    DevScalars *sc;
+    ull *rho_q;
+    double *partials;      // update mode: |u_{k+1} - u_k|^2 per block
+    unsigned int *counter;
+};
+void launch_scatter(const ScatterArgs &a, cudaStream_t st);
+
+// ---- density map -> solver input + overflow ---------------------------------
+enum { RHO_OUT_ONLY = 0, RHO_LOOP = 1, RHO_INIT = 2 };
+
+struct RhoArgs {
+    int nbins;
+    ull *mov_q;                 // read, then cleared for the next iteration
+    const long long *fix_q;     // fixed nodes at weight 1
+    const long long *fixs_q;    // fixed nodes scaled by rho_t
+    long long cap_q, ab_q;
+    double inv_ab;
+    float *d_f32;               // FP32 solver input, or null
+    __nv_bfloat16 *d_hi, *d_lo; // BF16x3 solver input, or null
+    DevScalars *sc;
+    long long *partials;        // 2 * grid
+    unsigned int *counter;
+    double *out;                // [2]: tau, tau_abs
+    int mode;
+};
+void launch_rho(const RhoArgs &a, cudaStream_t st);
+
+// ---- field gather + preconditioned gradient + optimiser scalars -------------
+enum { GATHER_STEP = 0, GATHER_INIT_NORMS = 1, GATHER_INIT_GRAD = 2, GATHER_INIT_PREV = 3,
+       GATHER_FORCE_ONLY = 4 };
+
+struct GatherArgs {
+    Grid g;
+    int n_mov;
+    int at;                 // evaluation buffer (GATHER_STEP: 1 - sc->cur)
+    float *vx[2], *vy[2];   // evaluation point [at], comparison point [1 - at]
+    const float *w, *h;
+    const float *ex, *ey;   // field per bin
+    ull *gqx, *gqy;         // WA gradient accumulators (cleared after reading)
+    const float *pins;      // pin count per movable node
+    const float *charge;    // area / bin area
+    float *gx[2], *gy[2];   // preconditioned gradient: output [at], comparison [1 - at]
+    float *fx, *fy;         // GATHER_FORCE_ONLY output: overlap-weighted field per node
+    DevScalars *sc;
+    double *partials;       // 4 * grid
+    unsigned int *counter;
+    int mode;
+};
+void launch_gather(const GatherArgs &a, cudaStream_t st);
+
+// v_{-1} = v_0 - s g_0, s = coef * bw / max|g_0| (first Lipschitz estimate)
+void launch_perturb(int n_mov, const float *vx, const float *vy, const float *gx, const float *gy,
+                    float *ox, float *oy, const double *gmax, float coef_bw, float die_w, float die_h,
+                    const float *w, const float *h, cudaStream_t st);
+
+// ---- field solve ------------------------------------------------------------
+// Spectral solver state for an m x m grid (square, m a multiple of 32).
+struct FieldSolver {
+    int m;
+    float bin_ratio;
+    // constant transform matrices, row-major m x m:
+    //   C[k][i] = cos(pi k (i+1/2)/m), Ct = C^T, St[i][k] = sin(pi k (i+1/2)/m)
+    float *C, *Ct, *St;
+    __nv_bfloat16 *C_hi, *C_lo, *Ct_hi, *Ct_lo, *St_hi, *St_lo;
+    float *wx, *wy;          // spectral frequencies per index
+    // scratch (fp32 path)
+    float *t0, *px, *py, *ux, *uy;
+    // scratch (bf16 path): hi/lo pairs
+    __nv_bfloat16 *b_t_hi, *b_t_lo, *b_px_hi, *b_px_lo, *b_py_hi, *b_py_lo, *b_ux_hi, *b_ux_lo,
+        *b_uy_hi, *b_uy_lo;
+    void *tc_maps;           // tensor maps of the tcgen05 path (device)
+    int tc_ready;
+    unsigned int *tc_status; // device error flag of the tcgen05 kernels
+};
+
+int field_solver_init(FieldSolver &f, int m, float bin_ratio, int want_bf16);
+void field_solver_free(FieldSolver &f);
+// density d (x-major) -> ex, ey; FP32 SIMT contraction
+void field_solve_fp32(FieldSolver &f, const float *d, float *ex, float *ey, cudaStream_t st);
+// density as bf16 hi/lo split -> ex, ey; tcgen05 BF16x3 contraction
+int field_solve_bf16x3(FieldSolver &f, const __nv_bfloat16 *d_hi, const __nv_bfloat16 *d_lo,
+                       float *ex, float *ey, cudaStream_t st);
+// float -> bf16 hi/lo split (for per-stage API calls)
+void launch_split_bf16(int n, const float *src, __nv_bfloat16 *hi, __nv_bfloat16 *lo, cudaStream_t st);
+
+}  // namespace ap

@@ -1,0 +1,979 @@
+// C ABI of the placement library: handle life cycle, the iteration sequence
+// (captured in CUDA graphs), initialisation, per-stage entry points, readout
+// and snapshots.  Host-side equivalent of Placer (vck5000/host/src/
+// AIEplace.cpp:9-138, 993-1124) over device-resident SoA state.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <cstdint>
+#include <vector>
+
+#include "../../include/aieplace.h"
+#include "ap_kernels.h"
+
+using namespace ap;
+
+namespace {
+
+#define CK(call)                                                               \
+    do {                                                                       \
+        cudaError_t e_ = (call);                                               \
+        if (e_ != cudaSuccess) {                                               \
+            fprintf(stderr, "aieplace: %s failed: %s\n", #call, cudaGetErrorString(e_)); \
+            return AP_ERR_CUDA;                                                \
+        }                                                                      \
+    } while (0)
+
+template <typename T>
+cudaError_t dalloc(T **p, size_t n) {
+    return cudaMalloc((void **)p, sizeof(T) * (n ? n : 1));
+}
+
+int max_blocks(int n, int cap) {
+    int b = (n + kThreads - 1) / kThreads;
+    return std::max(1, std::min(b, cap));
+}
+
+}  // namespace
+
+struct ap_handle {
+    // sizes
+    int n_nodes = 0, n_mov = 0, n_fixa = 0, n_nets = 0, n_pins = 0, n_small = 0;
+    std::vector<int> ext2int, int2ext;
+    bool identity = true;
+    float die_xl = 0, die_yl = 0, die_w = 0, die_h = 0;
+    ap_params p{};
+    Grid g{};
+    long long cap_q = 0, ab_q = 0;
+    double inv_ab = 0, mov_area_q = 0;
+    // device state
+    int *d_net_ptr = nullptr, *d_pin_node = nullptr;
+    float *d_w = nullptr, *d_h = nullptr;
+    float *d_px[2] = {nullptr, nullptr}, *d_py[2] = {nullptr, nullptr};
+    float *d_ux[2] = {nullptr, nullptr}, *d_uy[2] = {nullptr, nullptr};
+    float *d_gx[2] = {nullptr, nullptr}, *d_gy[2] = {nullptr, nullptr};
+    float *d_pins = nullptr, *d_charge = nullptr;
+    ull *d_gqx = nullptr, *d_gqy = nullptr;
+    ull *d_mov_q = nullptr;
+    long long *d_fix_q = nullptr, *d_fixs_q = nullptr;
+    float *d_dens = nullptr, *d_ex = nullptr, *d_ey = nullptr;
+    __nv_bfloat16 *d_dens_hi = nullptr, *d_dens_lo = nullptr;
+    float *d_sx = nullptr, *d_sy = nullptr;  // staging (external order / scratch positions)
+    DevScalars *d_sc = nullptr;
+    DevScalars *h_sc = nullptr;  // pinned
+    double *d_partials = nullptr;
+    long long *d_partials_ll = nullptr;
+    unsigned int *d_counters = nullptr;
+    double *d_out = nullptr;
+    double *h_out = nullptr;  // pinned [4]
+    int wa_small_grid = 1, wa_large_grid = 1;
+    FieldSolver fs{};
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    bool initialized = false;
+    cudaGraphExec_t graph = nullptr;  // one trial step (parity lives in device scalars)
+    bool graph_ok = false;
+};
+
+namespace {
+
+int solver_of(const ap_handle *h, int32_t solver) { return solver >= 0 ? solver : h->p.field_solver; }
+
+// density map (bf16 split or fp32 already in place) -> ex, ey
+int run_field(ap_handle *h, int solver, cudaStream_t st) {
+    if (solver == AP_FIELD_BF16X3) {
+        int r = field_solve_bf16x3(h->fs, h->d_dens_hi, h->d_dens_lo, h->d_ex, h->d_ey, st);
+        if (r != AP_OK) return r;
+    } else {
+        field_solve_fp32(h->fs, h->d_dens, h->d_ex, h->d_ey, st);
+    }
+    return AP_OK;
+}
+
+ScatterArgs scatter_args(ap_handle *h) {
+    ScatterArgs a{};
+    a.g = h->g;
+    a.w = h->d_w;
+    a.h = h->d_h;
+    a.die_w = h->die_w;
+    a.die_h = h->die_h;
+    a.sc = h->d_sc;
+    a.rho_q = h->d_mov_q;
+    a.n_mov = h->n_mov;
+    for (int b = 0; b < 2; ++b) {
+        a.ux[b] = h->d_ux[b];
+        a.uy[b] = h->d_uy[b];
+        a.vx[b] = h->d_px[b];
+        a.vy[b] = h->d_py[b];
+        a.gx[b] = h->d_gx[b];
+        a.gy[b] = h->d_gy[b];
+    }
+    a.partials = h->d_partials;
+    a.counter = h->d_counters + 3;
+    return a;
+}
+
+RhoArgs rho_args(ap_handle *h, int mode, double *out) {
+    RhoArgs a{};
+    a.nbins = h->p.bins_x * h->p.bins_y;
+    a.mov_q = h->d_mov_q;
+    a.fix_q = h->d_fix_q;
+    a.fixs_q = h->d_fixs_q;
+    a.cap_q = h->cap_q;
+    a.ab_q = h->ab_q;
+    a.inv_ab = h->inv_ab;
+    if (h->p.field_solver == AP_FIELD_BF16X3) {
+        a.d_hi = h->d_dens_hi;
+        a.d_lo = h->d_dens_lo;
+    } else {
+        a.d_f32 = h->d_dens;
+    }
+    a.sc = h->d_sc;
+    a.partials = h->d_partials_ll;
+    a.counter = h->d_counters + 1;
+    a.out = out;
+    a.mode = mode;
+    return a;
+}
+
+WaArgs wa_args(ap_handle *h, const float *px, const float *py, float gamma, int n_grad, int mode,
+               double *out) {
+    WaArgs a{};
+    a.net_ptr = h->d_net_ptr;
+    a.pin_node = h->d_pin_node;
+    a.n_small = h->n_small;
+    a.n_nets = h->n_nets;
+    a.px = px;
+    a.py = py;
+    for (int b = 0; b < 2; ++b) {
+        a.pxs[b] = h->d_px[b];
+        a.pys[b] = h->d_py[b];
+    }
+    a.gamma = gamma;
+    a.sc = h->d_sc;
+    a.gqx = h->d_gqx;
+    a.gqy = h->d_gqy;
+    a.n_grad = n_grad;
+    a.partials = h->d_partials;
+    a.counter = h->d_counters + 0;
+    a.out = out;
+    a.mode = mode;
+    return a;
+}
+
+GatherArgs gather_args(ap_handle *h, int at, int mode) {
+    GatherArgs a{};
+    a.g = h->g;
+    a.n_mov = h->n_mov;
+    a.at = at;
+    for (int b = 0; b < 2; ++b) {
+        a.vx[b] = h->d_px[b];
+        a.vy[b] = h->d_py[b];
+        a.gx[b] = h->d_gx[b];
+        a.gy[b] = h->d_gy[b];
+    }
+    a.w = h->d_w;
+    a.h = h->d_h;
+    a.ex = h->d_ex;
+    a.ey = h->d_ey;
+    a.gqx = h->d_gqx;
+    a.gqy = h->d_gqy;
+    a.pins = h->d_pins;
+    a.charge = h->d_charge;
+    a.sc = h->d_sc;
+    a.partials = h->d_partials;
+    a.counter = h->d_counters + 2;
+    a.mode = mode;
+    return a;
+}
+
+// One trial step from the accepted state (buffers [cur]) to buffers
+// [1 - cur]; cur lives in device scalars, so one captured graph serves every
+// launch.  The gather's last block accepts the trial or asks for a retry.
+int enqueue_iteration(ap_handle *h, cudaStream_t st) {
+    ScatterArgs s = scatter_args(h);
+    s.update = 1;
+    launch_scatter(s, st);
+    launch_rho(rho_args(h, RHO_LOOP, nullptr), st);
+    launch_wirelength(wa_args(h, nullptr, nullptr, 0.f, h->n_mov, WA_LOOP, nullptr), h->wa_small_grid,
+                      h->wa_large_grid, st);
+    int r = run_field(h, h->p.field_solver, st);
+    if (r != AP_OK) return r;
+    launch_gather(gather_args(h, 0, GATHER_STEP), st);
+    return cudaGetLastError() == cudaSuccess ? AP_OK : AP_ERR_CUDA;
+}
+
+// Density/overflow + WA + field at buffer `at` (no position update).
+int enqueue_eval(ap_handle *h, int at, int rho_mode, int wa_mode, cudaStream_t st) {
+    ScatterArgs s = scatter_args(h);
+    s.update = 0;
+    s.px = h->d_px[at];
+    s.py = h->d_py[at];
+    s.lo = 0;
+    s.hi = h->n_mov;
+    launch_scatter(s, st);
+    launch_rho(rho_args(h, rho_mode, h->d_out), st);
+    launch_wirelength(wa_args(h, h->d_px[at], h->d_py[at], 0.f, h->n_mov, wa_mode, h->d_out + 2),
+                      h->wa_small_grid, h->wa_large_grid, st);
+    return run_field(h, h->p.field_solver, st);
+}
+
+int sync(ap_handle *h) {
+    CK(cudaStreamSynchronize(h->stream));
+    return AP_OK;
+}
+
+void destroy_graphs(ap_handle *h) {
+    if (h->graph) {
+        cudaGraphExecDestroy(h->graph);
+        h->graph = nullptr;
+    }
+    h->graph_ok = false;
+}
+
+int build_graphs(ap_handle *h) {
+    destroy_graphs(h);
+    cudaGraph_t gr = nullptr;
+    CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    int r = enqueue_iteration(h, h->stream);
+    cudaError_t e = cudaStreamEndCapture(h->stream, &gr);
+    if (r != AP_OK || e != cudaSuccess) {
+        if (gr) cudaGraphDestroy(gr);
+        return r != AP_OK ? r : AP_ERR_CUDA;
+    }
+    e = cudaGraphInstantiate(&h->graph, gr, 0);
+    cudaGraphDestroy(gr);
+    if (e != cudaSuccess) return AP_ERR_CUDA;
+    h->graph_ok = true;
+    return AP_OK;
+}
+
+// external-order host arrays -> internal positions of buffer `at` (movable
+// nodes only; fixed nodes keep their place)
+int upload_positions(ap_handle *h, int at, const float *x, const float *y) {
+    std::vector<float> ix((size_t)h->n_mov), iy((size_t)h->n_mov);
+    for (int i = 0; i < h->n_mov; ++i) {
+        const int e = h->int2ext[(size_t)i];
+        ix[(size_t)i] = x[e] - h->die_xl;
+        iy[(size_t)i] = y[e] - h->die_yl;
+        if (!std::isfinite(ix[(size_t)i]) || !std::isfinite(iy[(size_t)i])) return AP_ERR_NONFINITE;
+    }
+    CK(cudaMemcpyAsync(h->d_px[at], ix.data(), sizeof(float) * h->n_mov, cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->d_py[at], iy.data(), sizeof(float) * h->n_mov, cudaMemcpyHostToDevice, h->stream));
+    return sync(h);
+}
+
+int read_scalars(ap_handle *h) {
+    CK(cudaMemcpyAsync(h->h_sc, h->d_sc, sizeof(DevScalars), cudaMemcpyDeviceToHost, h->stream));
+    return sync(h);
+}
+
+void fill_stats(const ap_handle *h, ap_stats *s) {
+    const DevScalars &c = *h->h_sc;
+    s->iteration = c.iteration;
+    s->status = c.status;
+    s->hpwl = c.hpwl;
+    s->wa_wirelength = c.wa;
+    s->overflow = c.tau;
+    s->overflow_abs = c.tau_abs;
+    s->lambda = c.lambda;
+    s->gamma = c.gamma;
+    s->alpha = c.alpha;
+    s->a_k = c.a_k;
+    s->evals = c.evals;
+    s->restarts = c.restarts;
+}
+
+// Evaluates v_0, lambda_0, g_0, the probe point v_{-1} and g_{-1}, and the
+// first step length (ePlace: Lipschitz prediction from two points).  Leaves
+// the accepted state in buffers [0].
+int init_optimizer(ap_handle *h) {
+    cudaStream_t st = h->stream;
+    destroy_graphs(h);
+    DevScalars sc{};
+    sc.a_k = 1.0;
+    sc.gamma_base = h->p.gamma_base_bins;
+    sc.bin_avg = 0.5 * ((double)h->g.bw + (double)h->g.bh);
+    sc.mu_max = h->p.lambda_mu_max;
+    sc.mu_min = h->p.lambda_mu_min;
+    sc.init_density_weight = h->p.init_density_weight;
+    sc.ref_dh = h->p.ref_delta_hpwl > 0 ? h->p.ref_delta_hpwl : 0.1 * h->n_nets * (double)h->g.bw;
+    sc.mov_area_q = h->mov_area_q;
+    sc.max_backtracks = h->p.max_backtracks;
+    sc.restart_mode = h->p.restart_mode;
+    sc.cur = 0;
+    CK(cudaMemcpyAsync(h->d_sc, &sc, sizeof(sc), cudaMemcpyHostToDevice, st));
+    CK(cudaMemsetAsync(h->d_gqx, 0, sizeof(ull) * h->n_nodes, st));
+    CK(cudaMemsetAsync(h->d_gqy, 0, sizeof(ull) * h->n_nodes, st));
+    CK(cudaMemsetAsync(h->d_mov_q, 0, sizeof(ull) * (size_t)h->p.bins_x * h->p.bins_y, st));
+    CK(cudaMemsetAsync(h->d_counters, 0, sizeof(unsigned int) * 8, st));
+    // u_0 = v_0
+    CK(cudaMemcpyAsync(h->d_ux[0], h->d_px[0], sizeof(float) * h->n_mov, cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemcpyAsync(h->d_uy[0], h->d_py[0], sizeof(float) * h->n_mov, cudaMemcpyDeviceToDevice, st));
+    int r = enqueue_eval(h, 0, RHO_INIT, WA_INIT, st);
+    if (r != AP_OK) return r;
+    launch_gather(gather_args(h, 0, GATHER_INIT_NORMS), st);
+    launch_gather(gather_args(h, 0, GATHER_INIT_GRAD), st);
+    launch_perturb(h->n_mov, h->d_px[0], h->d_py[0], h->d_gx[0], h->d_gy[0], h->d_px[1], h->d_py[1],
+                   &h->d_sc->gmax, h->p.init_step_coef * h->g.bw, h->die_w, h->die_h, h->d_w, h->d_h, st);
+    r = enqueue_eval(h, 1, RHO_OUT_ONLY, WA_OUT_ONLY, st);
+    if (r != AP_OK) return r;
+    launch_gather(gather_args(h, 1, GATHER_INIT_PREV), st);
+    CK(cudaGetLastError());
+    h->initialized = true;
+    r = sync(h);
+    if (r != AP_OK) return r;
+    if (h->p.use_graph) {
+        r = build_graphs(h);
+        if (r != AP_OK) return r;
+    }
+    return AP_OK;
+}
+
+// n trial launches (no host synchronisation)
+int launch_trials(ap_handle *h, int n) {
+    for (int i = 0; i < n; ++i) {
+        if (h->graph_ok) {
+            CK(cudaGraphLaunch(h->graph, h->stream));
+        } else {
+            int r = enqueue_iteration(h, h->stream);
+            if (r != AP_OK) return r;
+        }
+    }
+    CK(cudaGetLastError());
+    return AP_OK;
+}
+
+// Runs trials until `n` more iterations are accepted.  Launches in batches
+// of the remaining count (each accepted iteration needs at least one trial)
+// and reads the counters back between batches.
+int step_n(ap_handle *h, int n) {
+    int r = read_scalars(h);
+    if (r != AP_OK) return r;
+    const int target = h->h_sc->iteration + n;
+    for (int guard = 0; guard < 64; ++guard) {
+        const int left = target - h->h_sc->iteration;
+        if (left <= 0 || h->h_sc->status) break;
+        r = launch_trials(h, left);
+        if (r != AP_OK) return r;
+        r = read_scalars(h);
+        if (r != AP_OK) return r;
+    }
+    return h->h_sc->status;
+}
+
+}  // namespace
+
+extern "C" {
+
+int ap_abi_version(void) { return AP_ABI_VERSION; }
+
+const char *ap_status_string(int s) {
+    switch (s) {
+        case AP_OK: return "ok";
+        case AP_ERR_INVALID_ARG: return "invalid argument";
+        case AP_ERR_BAD_NETLIST: return "malformed netlist";
+        case AP_ERR_NONFINITE: return "non-finite input";
+        case AP_ERR_CUDA: return "CUDA error";
+        case AP_ERR_NO_DEVICE: return "no sm_103 device";
+        case AP_ERR_UNSUPPORTED: return "unsupported configuration";
+        case AP_ERR_TIMEOUT: return "device wait timed out";
+        case AP_ERR_STATE: return "call out of order";
+        case AP_ERR_DIVERGED: return "optimiser diverged";
+        default: return "unknown status";
+    }
+}
+
+int ap_params_default(ap_params *p) {
+    if (!p) return AP_ERR_INVALID_ARG;
+    memset(p, 0, sizeof(*p));
+    p->bins_x = 512;
+    p->bins_y = 512;
+    p->target_density = 1.0f;
+    p->gamma_base_bins = 4.0f;
+    p->field_solver = AP_FIELD_FP32;
+    p->init_density_weight = 8e-5f;
+    p->ref_delta_hpwl = 0.f;
+    p->lambda_mu_max = 1.05f;
+    p->lambda_mu_min = 0.95f;
+    p->init_step_coef = 0.1f;
+    p->target_overflow = 0.10f;
+    p->max_iterations = 5000;
+    p->check_interval = 16;
+    p->use_graph = 1;
+    p->max_backtracks = 10;
+    p->restart_mode = 3;
+    return AP_OK;
+}
+
+int ap_create(const ap_netlist *nl, const ap_params *params, ap_handle **out) {
+    if (!nl || !params || !out) return AP_ERR_INVALID_ARG;
+    *out = nullptr;
+    const ap_params &p = *params;
+    if (nl->num_nodes <= 0 || nl->num_nets < 0 || nl->num_pins < 0 || !nl->net_ptr ||
+        (nl->num_pins > 0 && !nl->pin_node) || !nl->node_w || !nl->node_h || !nl->node_x || !nl->node_y)
+        return AP_ERR_INVALID_ARG;
+    if (p.bins_x != p.bins_y || p.bins_x < 32 || p.bins_x > 4096 || (p.bins_x & (p.bins_x - 1)))
+        return AP_ERR_UNSUPPORTED;
+    if (!(p.target_density > 0.f) || !(p.gamma_base_bins > 0.f)) return AP_ERR_INVALID_ARG;
+    if (p.field_solver != AP_FIELD_FP32 && p.field_solver != AP_FIELD_BF16X3) return AP_ERR_INVALID_ARG;
+    const float die_w = nl->die_xh - nl->die_xl, die_h = nl->die_yh - nl->die_yl;
+    if (!(die_w > 0.f) || !(die_h > 0.f)) return AP_ERR_INVALID_ARG;
+    // CSR checks
+    if (nl->net_ptr[0] != 0 || nl->net_ptr[nl->num_nets] != nl->num_pins) return AP_ERR_BAD_NETLIST;
+    for (int e = 0; e < nl->num_nets; ++e)
+        if (nl->net_ptr[e + 1] < nl->net_ptr[e]) return AP_ERR_BAD_NETLIST;
+    for (int q = 0; q < nl->num_pins; ++q)
+        if (nl->pin_node[q] < 0 || nl->pin_node[q] >= nl->num_nodes) return AP_ERR_BAD_NETLIST;
+    for (int i = 0; i < nl->num_nodes; ++i)
+        if (!std::isfinite(nl->node_w[i]) || !std::isfinite(nl->node_h[i]) || !std::isfinite(nl->node_x[i]) ||
+            !std::isfinite(nl->node_y[i]) || nl->node_w[i] < 0.f || nl->node_h[i] < 0.f)
+            return AP_ERR_NONFINITE;
+    int dev = 0;
+    cudaDeviceProp prop;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaGetDeviceProperties(&prop, dev) != cudaSuccess)
+        return AP_ERR_NO_DEVICE;
+    if (prop.major != 10 || prop.minor != 3) return AP_ERR_NO_DEVICE;
+
+    ap_handle *h = new ap_handle();
+    h->p = p;
+    h->die_xl = nl->die_xl;
+    h->die_yl = nl->die_yl;
+    h->die_w = die_w;
+    h->die_h = die_h;
+    const int N = nl->num_nodes;
+    h->n_nodes = N;
+    // internal order: movable, fixed with area, zero-area fixed
+    h->ext2int.assign((size_t)N, -1);
+    for (int pass = 0; pass < 3; ++pass)
+        for (int i = 0; i < N; ++i) {
+            const bool fixed = nl->node_fixed && nl->node_fixed[i];
+            const bool area = nl->node_w[i] * nl->node_h[i] > 0.f;
+            const int cls = !fixed ? 0 : (area ? 1 : 2);
+            if (cls == pass) {
+                h->ext2int[(size_t)i] = (int)h->int2ext.size();
+                h->int2ext.push_back(i);
+                if (cls == 0) h->n_mov++;
+                if (cls == 1) h->n_fixa++;
+            }
+        }
+    for (int i = 0; i < N; ++i)
+        if (h->ext2int[(size_t)i] != i) h->identity = false;
+    // nets of degree >= 2: degree 2..8 first in degree order, then larger ones
+    std::vector<int> order;
+    for (int e = 0; e < nl->num_nets; ++e)
+        if (nl->net_ptr[e + 1] - nl->net_ptr[e] >= 2) order.push_back(e);
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+        const int da = nl->net_ptr[a + 1] - nl->net_ptr[a], db = nl->net_ptr[b + 1] - nl->net_ptr[b];
+        const int ka = da <= 8 ? da : 9, kb = db <= 8 ? db : 9;
+        return ka < kb;
+    });
+    std::vector<int> net_ptr(1, 0), pin_node;
+    std::vector<float> pins((size_t)N, 0.f);
+    for (int e : order) {
+        const int d = nl->net_ptr[e + 1] - nl->net_ptr[e];
+        if (d <= 8) h->n_small++;
+        for (int q = nl->net_ptr[e]; q < nl->net_ptr[e + 1]; ++q) {
+            const int in = h->ext2int[(size_t)nl->pin_node[q]];
+            pin_node.push_back(in);
+            pins[(size_t)in] += 1.f;
+        }
+        net_ptr.push_back((int)pin_node.size());
+    }
+    h->n_nets = (int)order.size();
+    h->n_pins = (int)pin_node.size();
+    // node arrays in internal order
+    std::vector<float> w((size_t)N), hh((size_t)N), x((size_t)N), y((size_t)N), charge((size_t)N);
+    for (int i = 0; i < N; ++i) {
+        const int e = h->int2ext[(size_t)i];
+        w[(size_t)i] = nl->node_w[e];
+        hh[(size_t)i] = nl->node_h[e];
+        x[(size_t)i] = nl->node_x[e] - nl->die_xl;
+        y[(size_t)i] = nl->node_y[e] - nl->die_yl;
+    }
+    // grid (Grid::init, Grid.cpp:6-22) and fixed-point constants
+    Grid &g = h->g;
+    g.mx = p.bins_x;
+    g.my = p.bins_y;
+    g.bw = die_w / (float)p.bins_x;
+    g.bh = die_h / (float)p.bins_y;
+    g.small_threshold = g.bw * g.bh / 16;
+    g.bw_q = llrintf(g.bw * 65536.0f);
+    g.bh_q = llrintf(g.bh * 65536.0f);
+    h->ab_q = g.bw_q * g.bh_q;
+    h->cap_q = llrint((double)p.target_density * (double)h->ab_q);
+    h->inv_ab = 1.0 / (double)h->ab_q;
+    g.inv_ab = (float)h->inv_ab;
+    double mov_area_q = 0.0;
+    for (int i = 0; i < h->n_mov; ++i) {
+        mov_area_q += (double)(llrintf(w[(size_t)i] * 65536.0f) * llrintf(hh[(size_t)i] * 65536.0f));
+        charge[(size_t)i] = (w[(size_t)i] * hh[(size_t)i]) / (g.bw * g.bh);
+    }
+    h->mov_area_q = mov_area_q;
+
+    const size_t nb = (size_t)p.bins_x * p.bins_y;
+    bool ok = true;
+    auto A = [&](cudaError_t e) { ok = ok && e == cudaSuccess; };
+    A(dalloc(&h->d_net_ptr, net_ptr.size()));
+    A(dalloc(&h->d_pin_node, pin_node.size()));
+    A(dalloc(&h->d_w, N));
+    A(dalloc(&h->d_h, N));
+    for (int b = 0; b < 2; ++b) {
+        A(dalloc(&h->d_px[b], N));
+        A(dalloc(&h->d_py[b], N));
+        A(dalloc(&h->d_gx[b], std::max(1, h->n_mov)));
+        A(dalloc(&h->d_gy[b], std::max(1, h->n_mov)));
+    }
+    for (int b = 0; b < 2; ++b) {
+        A(dalloc(&h->d_ux[b], std::max(1, h->n_mov)));
+        A(dalloc(&h->d_uy[b], std::max(1, h->n_mov)));
+    }
+    A(dalloc(&h->d_pins, N));
+    A(dalloc(&h->d_charge, N));
+    A(dalloc(&h->d_gqx, N));
+    A(dalloc(&h->d_gqy, N));
+    A(dalloc(&h->d_mov_q, nb));
+    A(dalloc(&h->d_fix_q, nb));
+    A(dalloc(&h->d_fixs_q, nb));
+    A(dalloc(&h->d_dens, nb));
+    A(dalloc(&h->d_dens_hi, nb));
+    A(dalloc(&h->d_dens_lo, nb));
+    A(dalloc(&h->d_ex, nb));
+    A(dalloc(&h->d_ey, nb));
+    A(dalloc(&h->d_sx, N));
+    A(dalloc(&h->d_sy, N));
+    A(dalloc(&h->d_sc, 1));
+    A(dalloc(&h->d_partials, 4 * 8192 + 64));
+    A(dalloc(&h->d_partials_ll, 2 * 4096 + 64));
+    A(dalloc(&h->d_counters, 8));
+    A(dalloc(&h->d_out, 8));
+    A(cudaMallocHost((void **)&h->h_sc, sizeof(DevScalars)));
+    A(cudaMallocHost((void **)&h->h_out, sizeof(double) * 8));
+    A(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+    h->own_stream = true;
+    if (!ok) {
+        ap_destroy(h);
+        return AP_ERR_CUDA;
+    }
+    A(cudaMemcpy(h->d_net_ptr, net_ptr.data(), sizeof(int) * net_ptr.size(), cudaMemcpyHostToDevice));
+    if (!pin_node.empty())
+        A(cudaMemcpy(h->d_pin_node, pin_node.data(), sizeof(int) * pin_node.size(), cudaMemcpyHostToDevice));
+    A(cudaMemcpy(h->d_w, w.data(), sizeof(float) * N, cudaMemcpyHostToDevice));
+    A(cudaMemcpy(h->d_h, hh.data(), sizeof(float) * N, cudaMemcpyHostToDevice));
+    for (int b = 0; b < 2; ++b) {
+        A(cudaMemcpy(h->d_px[b], x.data(), sizeof(float) * N, cudaMemcpyHostToDevice));
+        A(cudaMemcpy(h->d_py[b], y.data(), sizeof(float) * N, cudaMemcpyHostToDevice));
+    }
+    A(cudaMemcpy(h->d_pins, pins.data(), sizeof(float) * N, cudaMemcpyHostToDevice));
+    A(cudaMemcpy(h->d_charge, charge.data(), sizeof(float) * N, cudaMemcpyHostToDevice));
+    A(cudaMemset(h->d_mov_q, 0, sizeof(ull) * nb));
+    A(cudaMemset(h->d_counters, 0, sizeof(unsigned int) * 8));
+    A(cudaMemset(h->d_gqx, 0, sizeof(ull) * N));
+    A(cudaMemset(h->d_gqy, 0, sizeof(ull) * N));
+    if (!ok) {
+        ap_destroy(h);
+        return AP_ERR_CUDA;
+    }
+    // fixed-macro map, once: the scatter kernel over fixed nodes with area
+    {
+        ScatterArgs s = scatter_args(h);
+        s.update = 0;
+        s.px = h->d_px[0];
+        s.py = h->d_py[0];
+        s.lo = h->n_mov;
+        s.hi = h->n_mov + h->n_fixa;
+        launch_scatter(s, 0);
+        std::vector<long long> fq(nb), fs(nb);
+        A(cudaMemcpy(fq.data(), h->d_mov_q, sizeof(long long) * nb, cudaMemcpyDeviceToHost));
+        for (size_t b = 0; b < nb; ++b) fs[b] = llrint((double)p.target_density * (double)fq[b]);
+        A(cudaMemcpy(h->d_fix_q, fq.data(), sizeof(long long) * nb, cudaMemcpyHostToDevice));
+        A(cudaMemcpy(h->d_fixs_q, fs.data(), sizeof(long long) * nb, cudaMemcpyHostToDevice));
+        A(cudaMemset(h->d_mov_q, 0, sizeof(ull) * nb));
+    }
+    int r = ok ? field_solver_init(h->fs, p.bins_x, g.bh / g.bw, 1)
+               : AP_ERR_CUDA;
+    if (r != AP_OK) {
+        ap_destroy(h);
+        return r;
+    }
+    h->wa_small_grid = max_blocks(h->n_small, 4096);
+    h->wa_large_grid = max_blocks((h->n_nets - h->n_small) * 32, 2048);
+    if (cudaDeviceSynchronize() != cudaSuccess) {
+        ap_destroy(h);
+        return AP_ERR_CUDA;
+    }
+    *out = h;
+    return AP_OK;
+}
+
+int ap_destroy(ap_handle *h) {
+    if (!h) return AP_ERR_INVALID_ARG;
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    destroy_graphs(h);
+    field_solver_free(h->fs);
+    void *ptrs[] = {h->d_net_ptr, h->d_pin_node, h->d_w,      h->d_h,       h->d_px[0], h->d_px[1],
+                    h->d_py[0],   h->d_py[1],    h->d_gx[0],  h->d_gx[1],   h->d_gy[0], h->d_gy[1],
+                    h->d_ux[0],   h->d_uy[0],    h->d_ux[1],  h->d_uy[1],
+                    h->d_pins,    h->d_charge,   h->d_gqx,    h->d_gqy,
+                    h->d_mov_q,   h->d_fix_q,    h->d_fixs_q, h->d_dens,    h->d_ex,    h->d_ey,
+                    h->d_dens_hi, h->d_dens_lo,  h->d_sx,     h->d_sy,      h->d_sc,    h->d_partials,
+                    h->d_partials_ll, h->d_counters, h->d_out};
+    for (void *q : ptrs)
+        if (q) cudaFree(q);
+    if (h->h_sc) cudaFreeHost(h->h_sc);
+    if (h->h_out) cudaFreeHost(h->h_out);
+    if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+    return AP_OK;
+}
+
+int ap_set_stream(ap_handle *h, void *stream) {
+    if (!h) return AP_ERR_INVALID_ARG;
+    CK(cudaStreamSynchronize(h->stream));
+    destroy_graphs(h);
+    if (h->own_stream) cudaStreamDestroy(h->stream);
+    h->stream = (cudaStream_t)stream;
+    h->own_stream = false;
+    if (h->initialized && h->p.use_graph) return build_graphs(h);
+    return AP_OK;
+}
+
+int ap_init_positions(ap_handle *h, const float *x, const float *y) {
+    if (!h || !x || !y) return AP_ERR_INVALID_ARG;
+    int r = upload_positions(h, 0, x, y);
+    if (r != AP_OK) return r;
+    return init_optimizer(h);
+}
+
+int ap_init_seeded(ap_handle *h, uint64_t seed, float sigma) {
+    if (!h) return AP_ERR_INVALID_ARG;
+    // splitmix64 + Box-Muller, the generator's normal draw
+    std::vector<float> x((size_t)h->n_nodes, 0.f), y((size_t)h->n_nodes, 0.f);
+    uint64_t z = seed;
+    auto next = [&]() {
+        z += 0x9E3779B97F4A7C15ull;
+        uint64_t t = z;
+        t = (t ^ (t >> 30)) * 0xBF58476D1CE4E5B9ull;
+        t = (t ^ (t >> 27)) * 0x94D049BB133111EBull;
+        return t ^ (t >> 31);
+    };
+    auto uni = [&]() { return (double)(next() >> 11) * (1.0 / 9007199254740992.0); };
+    auto normal = [&]() {
+        double u1 = std::max(uni(), 1e-300), u2 = uni();
+        return sqrt(-2.0 * log(u1)) * cos(6.283185307179586 * u2);
+    };
+    const double cx = h->die_xl + 0.5 * h->die_w, cy = h->die_yl + 0.5 * h->die_h;
+    for (int i = 0; i < h->n_mov; ++i) {
+        const int e = h->int2ext[(size_t)i];
+        x[(size_t)e] = (float)(cx + sigma * normal());
+        y[(size_t)e] = (float)(cy + sigma * normal());
+    }
+    return ap_init_positions(h, x.data(), y.data());
+}
+
+int ap_step(ap_handle *h, int32_t n_iter) {
+    if (!h || n_iter < 0) return AP_ERR_INVALID_ARG;
+    if (!h->initialized) return AP_ERR_STATE;
+    int r = step_n(h, n_iter);
+    if (r != AP_OK) return r;
+    return sync(h);
+}
+
+int ap_step_async(ap_handle *h, int32_t n_trials) {
+    if (!h || n_trials < 0) return AP_ERR_INVALID_ARG;
+    if (!h->initialized) return AP_ERR_STATE;
+    return launch_trials(h, n_trials);
+}
+
+int ap_profile_stages(ap_handle *h, int32_t n_trials, float *stage_ms, int32_t *n_stages) {
+    if (!h || n_trials <= 0 || !stage_ms || !n_stages) return AP_ERR_INVALID_ARG;
+    if (!h->initialized) return AP_ERR_STATE;
+    constexpr int S = 5;
+    cudaEvent_t ev[S + 1];
+    for (int i = 0; i <= S; ++i) CK(cudaEventCreate(&ev[i]));
+    double acc[S] = {0, 0, 0, 0, 0};
+    cudaStream_t st = h->stream;
+    int r = AP_OK;
+    for (int t = 0; t < n_trials && r == AP_OK; ++t) {
+        ScatterArgs s = scatter_args(h);
+        s.update = 1;
+        CK(cudaEventRecord(ev[0], st));
+        launch_scatter(s, st);
+        CK(cudaEventRecord(ev[1], st));
+        launch_rho(rho_args(h, RHO_LOOP, nullptr), st);
+        CK(cudaEventRecord(ev[2], st));
+        launch_wirelength(wa_args(h, nullptr, nullptr, 0.f, h->n_mov, WA_LOOP, nullptr), h->wa_small_grid,
+                          h->wa_large_grid, st);
+        CK(cudaEventRecord(ev[3], st));
+        r = run_field(h, h->p.field_solver, st);
+        CK(cudaEventRecord(ev[4], st));
+        launch_gather(gather_args(h, 0, GATHER_STEP), st);
+        CK(cudaEventRecord(ev[5], st));
+        CK(cudaEventSynchronize(ev[5]));
+        for (int i = 0; i < S; ++i) {
+            float ms = 0.f;
+            CK(cudaEventElapsedTime(&ms, ev[i], ev[i + 1]));
+            acc[i] += ms;
+        }
+    }
+    for (int i = 0; i <= S; ++i) cudaEventDestroy(ev[i]);
+    if (r != AP_OK) return r;
+    CK(cudaGetLastError());
+    for (int i = 0; i < S; ++i) stage_ms[i] = (float)(acc[i] / n_trials);
+    *n_stages = S;
+    return AP_OK;
+}
+
+int ap_run(ap_handle *h, int32_t *iterations_done) {
+    if (!h) return AP_ERR_INVALID_ARG;
+    if (!h->initialized) return AP_ERR_STATE;
+    const int chunk = std::max(1, h->p.check_interval);
+    int r = read_scalars(h);
+    if (r != AP_OK) return r;
+    const int start = h->h_sc->iteration;
+    int done = 0;
+    while (done < h->p.max_iterations) {
+        const int n = std::min(chunk, h->p.max_iterations - done);
+        r = step_n(h, n);  // leaves fresh scalars in h_sc
+        done = h->h_sc->iteration - start;
+        if (r != AP_OK) {
+            if (iterations_done) *iterations_done = done;
+            return r;
+        }
+        if (h->h_sc->tau < h->p.target_overflow) break;
+    }
+    if (iterations_done) *iterations_done = done;
+    return AP_OK;
+}
+
+int ap_get_positions(ap_handle *h, float *x, float *y) {
+    if (!h || !x || !y) return AP_ERR_INVALID_ARG;
+    int r = read_scalars(h);
+    if (r != AP_OK) return r;
+    const int cur = h->h_sc->cur;
+    std::vector<float> ix((size_t)h->n_nodes), iy((size_t)h->n_nodes);
+    CK(cudaMemcpyAsync(ix.data(), h->d_px[cur], sizeof(float) * h->n_nodes, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaMemcpyAsync(iy.data(), h->d_py[cur], sizeof(float) * h->n_nodes, cudaMemcpyDeviceToHost, h->stream));
+    r = sync(h);
+    if (r != AP_OK) return r;
+    for (int i = 0; i < h->n_nodes; ++i) {
+        const int e = h->int2ext[(size_t)i];
+        x[e] = ix[(size_t)i] + h->die_xl;
+        y[e] = iy[(size_t)i] + h->die_yl;
+    }
+    return AP_OK;
+}
+
+int ap_step_host(ap_handle *h, const float *x_in, const float *y_in, float *x_out, float *y_out,
+                 ap_stats *stats) {
+    if (!h) return AP_ERR_INVALID_ARG;
+    if (!h->initialized) return AP_ERR_STATE;
+    const bool direct = h->identity && h->die_xl == 0.f && h->die_yl == 0.f;
+    int r = read_scalars(h);
+    if (r != AP_OK) return r;
+    if (x_in && y_in) {
+        const int cur = h->h_sc->cur;
+        if (direct) {
+            CK(cudaMemcpyAsync(h->d_px[cur], x_in, sizeof(float) * h->n_mov, cudaMemcpyHostToDevice, h->stream));
+            CK(cudaMemcpyAsync(h->d_py[cur], y_in, sizeof(float) * h->n_mov, cudaMemcpyHostToDevice, h->stream));
+        } else {
+            r = upload_positions(h, cur, x_in, y_in);
+            if (r != AP_OK) return r;
+        }
+    }
+    r = step_n(h, 1);
+    if (r != AP_OK) return r;
+    if (x_out && y_out) {
+        if (direct) {
+            const int cur = h->h_sc->cur;
+            CK(cudaMemcpyAsync(x_out, h->d_px[cur], sizeof(float) * h->n_nodes, cudaMemcpyDeviceToHost, h->stream));
+            CK(cudaMemcpyAsync(y_out, h->d_py[cur], sizeof(float) * h->n_nodes, cudaMemcpyDeviceToHost, h->stream));
+            r = sync(h);
+        } else {
+            r = ap_get_positions(h, x_out, y_out);
+        }
+        if (r != AP_OK) return r;
+    }
+    if (stats) fill_stats(h, stats);
+    return h->h_sc->status;
+}
+
+int ap_get_stats(ap_handle *h, ap_stats *s) {
+    if (!h || !s) return AP_ERR_INVALID_ARG;
+    int r = read_scalars(h);
+    if (r != AP_OK) return r;
+    fill_stats(h, s);
+    return AP_OK;
+}
+
+int ap_hpwl(ap_handle *h, double *hpwl) {
+    if (!h || !hpwl) return AP_ERR_INVALID_ARG;
+    if (!h->initialized) return AP_ERR_STATE;
+    int r = read_scalars(h);
+    if (r != AP_OK) return r;
+    *hpwl = h->h_sc->hpwl;
+    return AP_OK;
+}
+
+int ap_overflow(ap_handle *h, double *overflow, double *overflow_abs) {
+    if (!h || !overflow) return AP_ERR_INVALID_ARG;
+    if (!h->initialized) return AP_ERR_STATE;
+    int r = read_scalars(h);
+    if (r != AP_OK) return r;
+    *overflow = h->h_sc->tau;
+    if (overflow_abs) *overflow_abs = h->h_sc->tau_abs;
+    return AP_OK;
+}
+
+// ---- per-stage entry points ----------------------------------------------
+
+namespace {
+// external-order positions of all nodes -> internal scratch (d_sx, d_sy)
+int stage_positions(ap_handle *h, const float *x, const float *y) {
+    std::vector<float> ix((size_t)h->n_nodes), iy((size_t)h->n_nodes);
+    for (int i = 0; i < h->n_nodes; ++i) {
+        const int e = h->int2ext[(size_t)i];
+        ix[(size_t)i] = x[e] - h->die_xl;
+        iy[(size_t)i] = y[e] - h->die_yl;
+        if (!std::isfinite(ix[(size_t)i]) || !std::isfinite(iy[(size_t)i])) return AP_ERR_NONFINITE;
+    }
+    CK(cudaMemcpyAsync(h->d_sx, ix.data(), sizeof(float) * h->n_nodes, cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->d_sy, iy.data(), sizeof(float) * h->n_nodes, cudaMemcpyHostToDevice, h->stream));
+    return sync(h);
+}
+}  // namespace
+
+int ap_wirelength_grad(ap_handle *h, const float *x, const float *y, float gamma, float *gx, float *gy,
+                       double *wa, double *hpwl) {
+    if (!h || !x || !y || !gx || !gy || !(gamma > 0.f)) return AP_ERR_INVALID_ARG;
+    int r = stage_positions(h, x, y);
+    if (r != AP_OK) return r;
+    CK(cudaMemsetAsync(h->d_gqx, 0, sizeof(ull) * h->n_nodes, h->stream));
+    CK(cudaMemsetAsync(h->d_gqy, 0, sizeof(ull) * h->n_nodes, h->stream));
+    launch_wirelength(wa_args(h, h->d_sx, h->d_sy, gamma, h->n_nodes, WA_OUT_ONLY, h->d_out),
+                      h->wa_small_grid, h->wa_large_grid, h->stream);
+    CK(cudaGetLastError());
+    std::vector<long long> qx((size_t)h->n_nodes), qy((size_t)h->n_nodes);
+    CK(cudaMemcpyAsync(qx.data(), h->d_gqx, sizeof(ull) * h->n_nodes, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaMemcpyAsync(qy.data(), h->d_gqy, sizeof(ull) * h->n_nodes, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaMemcpyAsync(h->h_out, h->d_out, sizeof(double) * 2, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaMemsetAsync(h->d_gqx, 0, sizeof(ull) * h->n_nodes, h->stream));
+    CK(cudaMemsetAsync(h->d_gqy, 0, sizeof(ull) * h->n_nodes, h->stream));
+    r = sync(h);
+    if (r != AP_OK) return r;
+    for (int i = 0; i < h->n_nodes; ++i) {
+        const int e = h->int2ext[(size_t)i];
+        gx[e] = (float)ldexp((double)qx[(size_t)i], -32);
+        gy[e] = (float)ldexp((double)qy[(size_t)i], -32);
+    }
+    if (hpwl) *hpwl = h->h_out[0];
+    if (wa) *wa = h->h_out[1];
+    return AP_OK;
+}
+
+int ap_density_map(ap_handle *h, const float *x, const float *y, int64_t *rho_q) {
+    if (!h || !x || !y || !rho_q) return AP_ERR_INVALID_ARG;
+    int r = stage_positions(h, x, y);
+    if (r != AP_OK) return r;
+    const size_t nb = (size_t)h->p.bins_x * h->p.bins_y;
+    CK(cudaMemsetAsync(h->d_mov_q, 0, sizeof(ull) * nb, h->stream));
+    ScatterArgs s = scatter_args(h);
+    s.update = 0;
+    s.px = h->d_sx;
+    s.py = h->d_sy;
+    s.lo = 0;
+    s.hi = h->n_mov + h->n_fixa;
+    launch_scatter(s, h->stream);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(rho_q, h->d_mov_q, sizeof(long long) * nb, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaMemsetAsync(h->d_mov_q, 0, sizeof(ull) * nb, h->stream));
+    return sync(h);
+}
+
+int ap_field_solve(ap_handle *h, const float *density, float *ex, float *ey, int32_t solver) {
+    if (!h || !density || !ex || !ey) return AP_ERR_INVALID_ARG;
+    const int sv = solver_of(h, solver);
+    if (sv != AP_FIELD_FP32 && sv != AP_FIELD_BF16X3) return AP_ERR_INVALID_ARG;
+    const int nb = h->p.bins_x * h->p.bins_y;
+    if (sv == AP_FIELD_BF16X3 && !h->fs.C_hi) return AP_ERR_UNSUPPORTED;
+    CK(cudaMemcpyAsync(h->d_dens, density, sizeof(float) * nb, cudaMemcpyHostToDevice, h->stream));
+    if (sv == AP_FIELD_BF16X3) launch_split_bf16(nb, h->d_dens, h->d_dens_hi, h->d_dens_lo, h->stream);
+    int r = run_field(h, sv, h->stream);
+    if (r != AP_OK) return r;
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(ex, h->d_ex, sizeof(float) * nb, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaMemcpyAsync(ey, h->d_ey, sizeof(float) * nb, cudaMemcpyDeviceToHost, h->stream));
+    return sync(h);
+}
+
+// ---- snapshots ------------------------------------------------------------
+// layout: magic, n_nodes, n_mov, 0, DevScalars, px[2][N], py[2][N], ux[2], uy[2], gx[2], gy[2]
+
+static size_t snap_bytes(const ap_handle *h) {
+    return 4 * sizeof(int32_t) + sizeof(DevScalars) + sizeof(float) * (4 * (size_t)h->n_nodes + 8 * (size_t)h->n_mov);
+}
+
+int ap_snapshot_size(ap_handle *h, size_t *bytes) {
+    if (!h || !bytes) return AP_ERR_INVALID_ARG;
+    *bytes = snap_bytes(h);
+    return AP_OK;
+}
+
+int ap_snapshot(ap_handle *h, void *buf, size_t bytes) {
+    if (!h || !buf || bytes < snap_bytes(h)) return AP_ERR_INVALID_ARG;
+    if (!h->initialized) return AP_ERR_STATE;
+    CK(cudaStreamSynchronize(h->stream));
+    char *p = (char *)buf;
+    int32_t hdr[4] = {0x41505332, h->n_nodes, h->n_mov, 0};
+    memcpy(p, hdr, sizeof(hdr));
+    p += sizeof(hdr);
+    CK(cudaMemcpy(p, h->d_sc, sizeof(DevScalars), cudaMemcpyDeviceToHost));
+    p += sizeof(DevScalars);
+    const size_t N = (size_t)h->n_nodes, M = (size_t)h->n_mov;
+    float *arrs_n[4] = {h->d_px[0], h->d_px[1], h->d_py[0], h->d_py[1]};
+    for (float *a : arrs_n) {
+        CK(cudaMemcpy(p, a, sizeof(float) * N, cudaMemcpyDeviceToHost));
+        p += sizeof(float) * N;
+    }
+    float *arrs_m[8] = {h->d_ux[0], h->d_ux[1], h->d_uy[0], h->d_uy[1], h->d_gx[0], h->d_gx[1], h->d_gy[0], h->d_gy[1]};
+    for (float *a : arrs_m) {
+        CK(cudaMemcpy(p, a, sizeof(float) * M, cudaMemcpyDeviceToHost));
+        p += sizeof(float) * M;
+    }
+    return AP_OK;
+}
+
+int ap_restore(ap_handle *h, const void *buf, size_t bytes) {
+    if (!h || !buf || bytes < snap_bytes(h)) return AP_ERR_INVALID_ARG;
+    const char *p = (const char *)buf;
+    int32_t hdr[4];
+    memcpy(hdr, p, sizeof(hdr));
+    if (hdr[0] != 0x41505332 || hdr[1] != h->n_nodes || hdr[2] != h->n_mov) return AP_ERR_INVALID_ARG;
+    p += sizeof(hdr);
+    CK(cudaStreamSynchronize(h->stream));
+    CK(cudaMemcpy(h->d_sc, p, sizeof(DevScalars), cudaMemcpyHostToDevice));
+    p += sizeof(DevScalars);
+    const size_t N = (size_t)h->n_nodes, M = (size_t)h->n_mov;
+    float *arrs_n[4] = {h->d_px[0], h->d_px[1], h->d_py[0], h->d_py[1]};
+    for (float *a : arrs_n) {
+        CK(cudaMemcpy(a, p, sizeof(float) * N, cudaMemcpyHostToDevice));
+        p += sizeof(float) * N;
+    }
+    float *arrs_m[8] = {h->d_ux[0], h->d_ux[1], h->d_uy[0], h->d_uy[1], h->d_gx[0], h->d_gx[1], h->d_gy[0], h->d_gy[1]};
+    for (float *a : arrs_m) {
+        CK(cudaMemcpy(a, p, sizeof(float) * M, cudaMemcpyHostToDevice));
+        p += sizeof(float) * M;
+    }
+    CK(cudaMemset(h->d_gqx, 0, sizeof(ull) * N));
+    CK(cudaMemset(h->d_gqy, 0, sizeof(ull) * N));
+    CK(cudaMemset(h->d_mov_q, 0, sizeof(ull) * (size_t)h->p.bins_x * h->p.bins_y));
+    CK(cudaMemset(h->d_counters, 0, sizeof(unsigned int) * 8));
+    h->initialized = true;
+    if (h->p.use_graph && !h->graph_ok) return build_graphs(h);
+    return AP_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,361 @@
+// Density map, overflow, field gather and the Nesterov position update.
+//
+// scatter_kernel   Placer::computeOverlaps -> Grid::computeBinOverlaps
+//                  (vck5000/host/src/AIEplace.cpp:937-967, Grid.cpp:38-110,
+//                  Bin.h:78-121) as int64 fixed-point atomics, fused with the
+//                  position update that produces the evaluation point.
+// rho_kernel       Grid::getRho / computeTotalOverflow (Grid.cpp:112-151):
+//                  fixed-point map -> density per bin for the solver, overflow
+//                  in exact integer sums; clears the map for the next pass.
+// gather_kernel    Placer::nudgeNode (AIEplace.cpp:1004-1046): overlap-weighted
+//                  field per node, combined with the wirelength gradient and
+//                  preconditioned; FP64 norms re-predict the Lipschitz step and
+//                  decide whether the trial is accepted (ePlace) -- the
+//                  reference moves by a fixed learning rate instead.
+#include <math.h>
+
+#include "ap_common.cuh"
+#include "ap_kernels.h"
+
+namespace ap {
+
+namespace {
+
+__device__ __forceinline__ float clampf(float v, float lo, float hi) { return fminf(fmaxf(v, lo), hi); }
+
+// block max in a fixed shuffle tree; valid in thread 0
+__device__ __forceinline__ double block_max(double v, double *smem) {
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    if ((threadIdx.x & 31) == 0) smem[threadIdx.x >> 5] = v;
+    __syncthreads();
+    v = threadIdx.x < (blockDim.x >> 5) ? smem[threadIdx.x] : 0.0;
+    if (threadIdx.x < 32)
+        for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    __syncthreads();
+    return v;
+}
+
+}  // namespace
+
+__global__ void __launch_bounds__(kThreads) scatter_kernel(ScatterArgs a) {
+    __shared__ double red[32];
+    const int n = a.update ? a.n_mov : (a.hi - a.lo);
+    float alpha = 0.f, mom = 0.f;
+    int cur = 0;
+    if (a.update) {
+        alpha = (float)a.sc->alpha;
+        mom = (float)a.sc->mom;
+        cur = a.sc->cur;
+    }
+    const int nxt = 1 - cur;
+    const Grid g = a.g;
+    double du = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int node = a.update ? i : a.lo + i;
+        const float w = __ldg(a.w + node), h = __ldg(a.h + node);
+        float x, y;
+        if (a.update) {
+            const float xhi = fmaxf(a.die_w - w, 0.f), yhi = fmaxf(a.die_h - h, 0.f);
+            const float ux = a.ux[cur][i], uy = a.uy[cur][i];
+            const float nux = clampf(a.vx[cur][i] - alpha * a.gx[cur][i], 0.f, xhi);
+            const float nuy = clampf(a.vy[cur][i] - alpha * a.gy[cur][i], 0.f, yhi);
+            x = clampf(nux + mom * (nux - ux), 0.f, xhi);
+            y = clampf(nuy + mom * (nuy - uy), 0.f, yhi);
+            a.ux[nxt][i] = nux;
+            a.uy[nxt][i] = nuy;
+            a.vx[nxt][i] = x;
+            a.vy[nxt][i] = y;
+            du += (double)((nux - ux) * (nux - ux) + (nuy - uy) * (nuy - uy));
+        } else {
+            x = __ldg(a.px + node);
+            y = __ldg(a.py + node);
+        }
+        int c0, c1, r0, r1;
+        bool small;
+        if (!bin_range(g, x, y, w, h, c0, c1, r0, r1, small)) continue;
+        const long long xq = to_q(x), yq = to_q(y), wq = to_q(w), hq = to_q(h);
+        if (small) {
+            atomicAdd(a.rho_q + (long long)c0 * g.my + r0, (ull)(wq * hq));
+            continue;
+        }
+        for (int c = c0; c <= c1; ++c) {
+            const long long ow = overlap_1d((long long)c * g.bw_q, g.bw_q, xq, wq);
+            for (int r = r0; r <= r1; ++r) {
+                const long long oh = overlap_1d((long long)r * g.bh_q, g.bh_q, yq, hq);
+                atomicAdd(a.rho_q + (long long)c * g.my + r, (ull)(ow * oh));
+            }
+        }
+    }
+    if (!a.update) return;
+    du = block_sum(du, red);
+    if (threadIdx.x == 0) a.partials[blockIdx.x] = du;
+    if (arrive_last(a.counter)) {
+        const double t = reduce_partials(a.partials, gridDim.x, red);
+        if (threadIdx.x == 0) {
+            a.sc->t_du = t;
+            *a.counter = 0u;
+        }
+    }
+}
+
+void launch_scatter(const ScatterArgs &a, cudaStream_t st) {
+    const int n = a.update ? a.n_mov : (a.hi - a.lo);
+    if (n <= 0) return;
+    int blocks = (n + kThreads - 1) / kThreads;
+    if (a.update && blocks > 4096) blocks = 4096;
+    scatter_kernel<<<blocks, kThreads, 0, st>>>(a);
+}
+
+__device__ __forceinline__ double gamma_of(const DevScalars *sc, double tau) {
+    double e = (tau - 0.1) * 20.0 / 9.0 - 1.0;
+    e = fmin(fmax(e, -1.0), 1.0);
+    return sc->gamma_base * sc->bin_avg * pow(10.0, e);
+}
+
+__global__ void __launch_bounds__(kThreads) rho_kernel(RhoArgs a) {
+    __shared__ long long red[32];
+    long long over = 0, over_abs = 0;
+    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < a.nbins; b += gridDim.x * blockDim.x) {
+        const long long mov = (long long)a.mov_q[b];
+        a.mov_q[b] = 0ull;
+        const long long tot = mov + a.fixs_q[b];
+        const long long t = tot - a.cap_q;
+        over += t > 0 ? t : 0;
+        const long long ab = mov + a.fix_q[b] - a.ab_q;
+        over_abs += ab > 0 ? ab : 0;
+        const float d = (float)((double)tot * a.inv_ab);
+        if (a.d_f32) a.d_f32[b] = d;
+        if (a.d_hi) {
+            const __nv_bfloat16 hi = __float2bfloat16_rn(d);
+            a.d_hi[b] = hi;
+            a.d_lo[b] = __float2bfloat16_rn(d - __bfloat162float(hi));
+        }
+    }
+    over = block_sum(over, red);
+    over_abs = block_sum(over_abs, red);
+    if (threadIdx.x == 0) {
+        a.partials[2 * blockIdx.x] = over;
+        a.partials[2 * blockIdx.x + 1] = over_abs;
+    }
+    if (arrive_last(a.counter)) {
+        long long o = 0, oa = 0;
+        for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) {
+            o += __ldcg(a.partials + 2 * i);
+            oa += __ldcg(a.partials + 2 * i + 1);
+        }
+        o = block_sum(o, red);
+        oa = block_sum(oa, red);
+        if (threadIdx.x == 0) {
+            DevScalars *sc = a.sc;
+            const double tau = sc->mov_area_q > 0 ? (double)o / sc->mov_area_q : 0.0;
+            const double tau_abs = ldexp((double)oa, -32);
+            if (a.out) {
+                a.out[0] = tau;
+                a.out[1] = tau_abs;
+            }
+            if (a.mode == RHO_INIT) {
+                sc->tau = tau;
+                sc->tau_abs = tau_abs;
+            }
+            if (a.mode != RHO_OUT_ONLY) {
+                sc->t_tau = tau;
+                sc->t_tau_abs = tau_abs;
+                sc->gamma = gamma_of(sc, tau);
+            }
+            *a.counter = 0u;
+        }
+    }
+}
+
+void launch_rho(const RhoArgs &a, cudaStream_t st) {
+    int blocks = (a.nbins + kThreads - 1) / kThreads;
+    if (blocks > 2048) blocks = 2048;
+    rho_kernel<<<blocks, kThreads, 0, st>>>(a);
+}
+
+// Accept / retry decision of one trial (one thread).  Mirrors or_step in the
+// oracle: backtracking while the re-predicted step falls below 0.95 of the
+// step tried; on acceptance the momentum restart test, the density-penalty
+// update (RePlAce: mu = mu_max^(1 - dHPWL/ref) in [mu_min, mu_max]) and the
+// momentum coefficients of the next iteration.
+__device__ void finish_trial(DevScalars *sc, double dv2, double dg2) {
+    sc->sum_dv2 = dv2;
+    sc->sum_dg2 = dg2;
+    sc->evals += 1;
+    const double ahat = dg2 > 0.0 ? sqrt(dv2) / sqrt(dg2) : 0.0;
+    if (!isfinite(ahat) || !isfinite(dv2) || !isfinite(dg2)) {
+        sc->status = 9;
+        return;
+    }
+    if (ahat <= 0.95 * sc->alpha && sc->backtracks < sc->max_backtracks) {
+        sc->alpha = ahat;
+        sc->backtracks += 1;
+        return;
+    }
+    bool restart = false;
+    if (sc->restart_mode == 2) restart = true;
+    if (sc->restart_mode == 3) restart = sc->t_du < sc->du_prev;
+    if (sc->restart_mode == 4) restart = sc->t_tau > sc->tau_prev;
+    sc->du_prev = sc->t_du;
+    sc->tau_prev = sc->t_tau;
+    sc->alpha = ahat;
+    sc->a_k = restart ? 1.0 : sc->a_next;
+    if (restart && sc->restart_mode != 2) sc->restarts += 1;
+    sc->a_next = (1.0 + sqrt(4.0 * sc->a_k * sc->a_k + 1.0)) / 2.0;
+    sc->mom = (sc->a_k - 1.0) / sc->a_next;
+    const double pc = (sc->t_hpwl - sc->hpwl_prev) / sc->ref_dh;
+    double mu = pc < 0.0 ? sc->mu_max : pow(sc->mu_max, 1.0 - pc);
+    mu = fmin(fmax(mu, sc->mu_min), sc->mu_max);
+    sc->lambda *= mu;
+    sc->hpwl_prev = sc->t_hpwl;
+    sc->hpwl = sc->t_hpwl;
+    sc->wa = sc->t_wa;
+    sc->tau = sc->t_tau;
+    sc->tau_abs = sc->t_tau_abs;
+    sc->backtracks = 0;
+    sc->cur = 1 - sc->cur;
+    sc->iteration += 1;
+}
+
+__global__ void __launch_bounds__(kThreads) gather_kernel(GatherArgs a) {
+    __shared__ double red[32];
+    const Grid g = a.g;
+    const float lam = (float)a.sc->lambda;
+    const int at = a.mode == GATHER_STEP ? 1 - a.sc->cur : a.at;
+    const float *vx = a.vx[at], *vy = a.vy[at], *vpx = a.vx[1 - at], *vpy = a.vy[1 - at];
+    float *gx_out = a.gx[at], *gy_out = a.gy[at];
+    const float *gpx = a.gx[1 - at], *gpy = a.gy[1 - at];
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n_mov; i += gridDim.x * blockDim.x) {
+        const float x = vx[i], y = vy[i];
+        const float w = __ldg(a.w + i), h = __ldg(a.h + i);
+        float fx = 0.f, fy = 0.f;
+        int c0, c1, r0, r1;
+        bool small;
+        if (bin_range(g, x, y, w, h, c0, c1, r0, r1, small)) {
+            const long long xq = to_q(x), yq = to_q(y), wq = to_q(w), hq = to_q(h);
+            if (small) {
+                const long long b = (long long)c0 * g.my + r0;
+                const float wt = (float)(wq * hq) * g.inv_ab;
+                fx = wt * __ldg(a.ex + b);
+                fy = wt * __ldg(a.ey + b);
+            } else {
+                for (int c = c0; c <= c1; ++c) {
+                    const long long ow = overlap_1d((long long)c * g.bw_q, g.bw_q, xq, wq);
+                    for (int r = r0; r <= r1; ++r) {
+                        const long long oh = overlap_1d((long long)r * g.bh_q, g.bh_q, yq, hq);
+                        const long long b = (long long)c * g.my + r;
+                        const float wt = (float)(ow * oh) * g.inv_ab;
+                        fx += wt * __ldg(a.ex + b);
+                        fy += wt * __ldg(a.ey + b);
+                    }
+                }
+            }
+        }
+        if (a.mode == GATHER_FORCE_ONLY) {
+            a.fx[i] = fx;
+            a.fy[i] = fy;
+            continue;
+        }
+        const float wlx = __ll2float_rn((long long)a.gqx[i]) * kInvGradScale;
+        const float wly = __ll2float_rn((long long)a.gqy[i]) * kInvGradScale;
+        if (a.mode == GATHER_INIT_NORMS) {
+            s2 += (double)(fabsf(wlx) + fabsf(wly));
+            s3 += (double)(fabsf(fx) + fabsf(fy));
+            continue;
+        }
+        a.gqx[i] = 0ull;
+        a.gqy[i] = 0ull;
+        const float hd = fmaxf(1.f, a.pins[i] + lam * a.charge[i]);
+        const float gx = (wlx - lam * fx) / hd, gy = (wly - lam * fy) / hd;
+        gx_out[i] = gx;
+        gy_out[i] = gy;
+        if (a.mode == GATHER_INIT_GRAD) {
+            s2 = fmax(s2, (double)fmaxf(fabsf(gx), fabsf(gy)));
+        } else {
+            const float dx = x - vpx[i], dy = y - vpy[i];
+            const float ddx = gx - gpx[i], ddy = gy - gpy[i];
+            s0 += (double)(dx * dx + dy * dy);
+            s1 += (double)(ddx * ddx + ddy * ddy);
+        }
+    }
+    if (a.mode == GATHER_FORCE_ONLY) return;
+    const bool is_max = a.mode == GATHER_INIT_GRAD;
+    s0 = block_sum(s0, red);
+    s1 = block_sum(s1, red);
+    s2 = is_max ? block_max(s2, red) : block_sum(s2, red);
+    s3 = block_sum(s3, red);
+    if (threadIdx.x == 0) {
+        double *p = a.partials + 4 * blockIdx.x;
+        p[0] = s0;
+        p[1] = s1;
+        p[2] = s2;
+        p[3] = s3;
+    }
+    if (arrive_last(a.counter)) {
+        double t0 = 0.0, t1 = 0.0, t2 = 0.0, t3 = 0.0;
+        for (int k = threadIdx.x; k < (int)gridDim.x; k += blockDim.x) {
+            const double *p = a.partials + 4 * k;
+            t0 += __ldcg(p);
+            t1 += __ldcg(p + 1);
+            t2 = is_max ? fmax(t2, __ldcg(p + 2)) : t2 + __ldcg(p + 2);
+            t3 += __ldcg(p + 3);
+        }
+        t0 = block_sum(t0, red);
+        t1 = block_sum(t1, red);
+        t2 = is_max ? block_max(t2, red) : block_sum(t2, red);
+        t3 = block_sum(t3, red);
+        if (threadIdx.x == 0) {
+            DevScalars *sc = a.sc;
+            if (a.mode == GATHER_INIT_NORMS) {
+                sc->sum_gwl = t2;
+                sc->sum_f = t3;
+                sc->lambda = t3 > 0.0 ? sc->init_density_weight * t2 / t3 : sc->init_density_weight;
+            } else if (a.mode == GATHER_INIT_GRAD) {
+                sc->gmax = t2;
+            } else if (a.mode == GATHER_INIT_PREV) {
+                // first predicted step from v_0 and the probe point v_{-1}
+                sc->sum_dv2 = t0;
+                sc->sum_dg2 = t1;
+                sc->alpha = t1 > 0.0 ? sqrt(t0) / sqrt(t1) : 0.0;
+                sc->a_k = 1.0;
+                sc->a_next = (1.0 + sqrt(5.0)) / 2.0;
+                sc->mom = 0.0;
+                if (!isfinite(sc->alpha)) sc->status = 9;
+            } else {
+                finish_trial(sc, t0, t1);
+            }
+            *a.counter = 0u;
+        }
+    }
+}
+
+void launch_gather(const GatherArgs &a, cudaStream_t st) {
+    int blocks = (a.n_mov + kThreads - 1) / kThreads;
+    if (blocks > 4096) blocks = 4096;
+    if (blocks < 1) blocks = 1;
+    gather_kernel<<<blocks, kThreads, 0, st>>>(a);
+}
+
+__global__ void perturb_kernel(int n, const float *vx, const float *vy, const float *gx, const float *gy,
+                               float *ox, float *oy, const double *gmax, float coef_bw, float die_w,
+                               float die_h, const float *w, const float *h) {
+    const double gm = *gmax;
+    const float s = gm > 0.0 ? (float)(coef_bw / gm) : 0.f;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        ox[i] = clampf(vx[i] - s * gx[i], 0.f, fmaxf(die_w - w[i], 0.f));
+        oy[i] = clampf(vy[i] - s * gy[i], 0.f, fmaxf(die_h - h[i], 0.f));
+    }
+}
+
+void launch_perturb(int n_mov, const float *vx, const float *vy, const float *gx, const float *gy,
+                    float *ox, float *oy, const double *gmax, float coef_bw, float die_w, float die_h,
+                    const float *w, const float *h, cudaStream_t st) {
+    if (n_mov <= 0) return;
+    int blocks = (n_mov + kThreads - 1) / kThreads;
+    if (blocks > 4096) blocks = 4096;
+    perturb_kernel<<<blocks, kThreads, 0, st>>>(n_mov, vx, vy, gx, gy, ox, oy, gmax, coef_bw, die_w,
+                                                 die_h, w, h);
+}
+
+}  // namespace ap

@@ -1,0 +1,216 @@
+// Electrostatic field solve as dense per-axis transform contractions, FP32 SIMT.
+//
+// Restates replace::FFT::doFFT (python/AIEmath/fft_replace/fft.cpp:204-299)
+// and Placer::compute_a_uv_DCT / compute_eField_DCT (vck5000/host/src/
+// AIEplace.cpp:752-934): 2-D DCT-II of the density, halved edge rows,
+// 4/(Mx My), phi = a/(wx^2+wy^2), Ex = S^T (phi wx) C, Ey = C^T (phi wy) S.
+// Every stage is one TN contraction  D[i][j] = sum_k A[i][k] B[j][k]  with A a
+// constant transform matrix and B the data, both K-contiguous:
+//   S1  T[v][x]  = sum_y C[v][y]  d[x][y]
+//   S2  a[u][v]  = sum_x C[u][x]  T[v][x]      epilogue -> Px, Py
+//   S3  Ux[y][u] = sum_v Ct[y][v] Px[u][v]     Uy[y][u] = sum_v St[y][v] Py[u][v]
+//   S4  Ex[x][y] = sum_u St[x][u] Ux[y][u]     Ey[x][y] = sum_u Ct[x][u] Uy[y][u]
+#include <math.h>
+#include <stdio.h>
+
+#include <vector>
+
+#include "../../include/aieplace.h"
+#include "ap_kernels.h"
+
+namespace ap {
+
+namespace {
+
+constexpr int BK = 16;
+
+struct GemmSet {
+    const float *A[2];
+    const float *B[2];
+    float *C[2];
+};
+
+struct SpectralEpi {
+    float *px, *py;
+    const float *wx, *wy;
+    float scale;  // 4 / m^2
+};
+
+__device__ __forceinline__ void spectral_store(const SpectralEpi &e, int m, int u, int v, float acc) {
+    float px = 0.f, py = 0.f;
+    if (u != 0 || v != 0) {
+        const float wx = e.wx[u], wy = e.wy[v];
+        float c = acc * e.scale;
+        if (u == 0) c *= 0.5f;
+        if (v == 0) c *= 0.5f;
+        c = c / (wx * wx + wy * wy);
+        px = c * wx;
+        py = c * wy;
+    }
+    e.px[(size_t)u * m + v] = px;
+    e.py[(size_t)u * m + v] = py;
+}
+
+// D = A B^T on an m x m problem; BM x BM output tile per block, 256 threads.
+template <int BM, bool SPECTRAL>
+__global__ void __launch_bounds__(256) gemm_tn_simt(int m, GemmSet s, SpectralEpi e) {
+    constexpr int TM = BM / 16;
+    __shared__ __align__(16) float As[BK][BM + 4];
+    __shared__ __align__(16) float Bs[BK][BM + 4];
+    const int z = blockIdx.z;
+    const float *__restrict__ A = s.A[z];
+    const float *__restrict__ B = s.B[z];
+    const int i0 = blockIdx.y * BM, j0 = blockIdx.x * BM;
+    const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+    float acc[TM][TM];
+#pragma unroll
+    for (int i = 0; i < TM; ++i)
+#pragma unroll
+        for (int j = 0; j < TM; ++j) acc[i][j] = 0.f;
+    for (int k0 = 0; k0 < m; k0 += BK) {
+        for (int q = tid; q < BM * BK / 4; q += 256) {
+            const int row = q >> 2, kq = (q & 3) * 4;
+            const float4 va = *reinterpret_cast<const float4 *>(A + (size_t)(i0 + row) * m + k0 + kq);
+            const float4 vb = *reinterpret_cast<const float4 *>(B + (size_t)(j0 + row) * m + k0 + kq);
+            As[kq + 0][row] = va.x;
+            As[kq + 1][row] = va.y;
+            As[kq + 2][row] = va.z;
+            As[kq + 3][row] = va.w;
+            Bs[kq + 0][row] = vb.x;
+            Bs[kq + 1][row] = vb.y;
+            Bs[kq + 2][row] = vb.z;
+            Bs[kq + 3][row] = vb.w;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < BK; ++kk) {
+            float a[TM], b[TM];
+#pragma unroll
+            for (int i = 0; i < TM; ++i) a[i] = As[kk][ty * TM + i];
+#pragma unroll
+            for (int j = 0; j < TM; ++j) b[j] = Bs[kk][tx * TM + j];
+#pragma unroll
+            for (int i = 0; i < TM; ++i)
+#pragma unroll
+                for (int j = 0; j < TM; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int i = 0; i < TM; ++i) {
+        const int gi = i0 + ty * TM + i;
+#pragma unroll
+        for (int j = 0; j < TM; ++j) {
+            const int gj = j0 + tx * TM + j;
+            if (SPECTRAL)
+                spectral_store(e, m, gi, gj, acc[i][j]);
+            else
+                s.C[z][(size_t)gi * m + gj] = acc[i][j];
+        }
+    }
+}
+
+template <bool SPECTRAL>
+void gemm(int m, const GemmSet &s, int batch, const SpectralEpi &e, cudaStream_t st) {
+    if (m >= 512) {
+        dim3 grid(m / 64, m / 64, batch);
+        gemm_tn_simt<64, SPECTRAL><<<grid, 256, 0, st>>>(m, s, e);
+    } else {
+        dim3 grid(m / 32, m / 32, batch);
+        gemm_tn_simt<32, SPECTRAL><<<grid, 256, 0, st>>>(m, s, e);
+    }
+}
+
+__global__ void split_kernel(int n, const float *src, __nv_bfloat16 *hi, __nv_bfloat16 *lo) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float v = src[i];
+        const __nv_bfloat16 h = __float2bfloat16_rn(v);
+        hi[i] = h;
+        lo[i] = __float2bfloat16_rn(v - __bfloat162float(h));
+    }
+}
+
+template <typename T>
+int dmalloc(T **p, size_t n) {
+    return cudaMalloc((void **)p, sizeof(T) * (n ? n : 1)) == cudaSuccess ? 0 : -1;
+}
+
+}  // namespace
+
+void launch_split_bf16(int n, const float *src, __nv_bfloat16 *hi, __nv_bfloat16 *lo, cudaStream_t st) {
+    int blocks = (n + 255) / 256;
+    if (blocks > 4096) blocks = 4096;
+    split_kernel<<<blocks, 256, 0, st>>>(n, src, hi, lo);
+}
+
+int field_solver_init(FieldSolver &f, int m, float bin_ratio, int want_bf16) {
+    f = FieldSolver();
+    if (m < 32 || (m % 32) != 0) return AP_ERR_UNSUPPORTED;
+    f.m = m;
+    f.bin_ratio = bin_ratio;
+    const size_t nn = (size_t)m * m;
+    std::vector<float> C(nn), Ct(nn), St(nn), wx(m), wy(m);
+    const double pi = 3.14159265358979323846;
+    for (int k = 0; k < m; ++k)
+        for (int i = 0; i < m; ++i) {
+            const double t = pi * k * (i + 0.5) / m;
+            C[(size_t)k * m + i] = (float)cos(t);
+            Ct[(size_t)i * m + k] = (float)cos(t);
+            St[(size_t)i * m + k] = (float)sin(t);
+        }
+    for (int u = 0; u < m; ++u) {
+        wx[u] = (float)(pi * u / m);
+        wy[u] = (float)(pi * u / m * bin_ratio);
+    }
+    int e = 0;
+    e |= dmalloc(&f.C, nn) | dmalloc(&f.Ct, nn) | dmalloc(&f.St, nn) | dmalloc(&f.wx, m) |
+         dmalloc(&f.wy, m);
+    e |= dmalloc(&f.t0, nn) | dmalloc(&f.px, nn) | dmalloc(&f.py, nn) | dmalloc(&f.ux, nn) |
+         dmalloc(&f.uy, nn);
+    if (e) return AP_ERR_CUDA;
+    cudaMemcpy(f.C, C.data(), nn * 4, cudaMemcpyHostToDevice);
+    cudaMemcpy(f.Ct, Ct.data(), nn * 4, cudaMemcpyHostToDevice);
+    cudaMemcpy(f.St, St.data(), nn * 4, cudaMemcpyHostToDevice);
+    cudaMemcpy(f.wx, wx.data(), m * 4, cudaMemcpyHostToDevice);
+    cudaMemcpy(f.wy, wy.data(), m * 4, cudaMemcpyHostToDevice);
+    if (want_bf16) {
+        e |= dmalloc(&f.C_hi, nn) | dmalloc(&f.C_lo, nn) | dmalloc(&f.Ct_hi, nn) | dmalloc(&f.Ct_lo, nn) |
+             dmalloc(&f.St_hi, nn) | dmalloc(&f.St_lo, nn);
+        e |= dmalloc(&f.b_t_hi, nn) | dmalloc(&f.b_t_lo, nn) | dmalloc(&f.b_px_hi, nn) |
+             dmalloc(&f.b_px_lo, nn) | dmalloc(&f.b_py_hi, nn) | dmalloc(&f.b_py_lo, nn) |
+             dmalloc(&f.b_ux_hi, nn) | dmalloc(&f.b_ux_lo, nn) | dmalloc(&f.b_uy_hi, nn) |
+             dmalloc(&f.b_uy_lo, nn);
+        if (e) return AP_ERR_CUDA;
+        launch_split_bf16((int)nn, f.C, f.C_hi, f.C_lo, 0);
+        launch_split_bf16((int)nn, f.Ct, f.Ct_hi, f.Ct_lo, 0);
+        launch_split_bf16((int)nn, f.St, f.St_hi, f.St_lo, 0);
+    }
+    if (cudaDeviceSynchronize() != cudaSuccess) return AP_ERR_CUDA;
+    return AP_OK;
+}
+
+void field_solver_free(FieldSolver &f) {
+    void *ptrs[] = {f.C,       f.Ct,      f.St,      f.C_hi,    f.C_lo,    f.Ct_hi,   f.Ct_lo,
+                    f.St_hi,   f.St_lo,   f.wx,      f.wy,      f.t0,      f.px,      f.py,
+                    f.ux,      f.uy,      f.b_t_hi,  f.b_t_lo,  f.b_px_hi, f.b_px_lo, f.b_py_hi,
+                    f.b_py_lo, f.b_ux_hi, f.b_ux_lo, f.b_uy_hi, f.b_uy_lo, f.tc_maps, f.tc_status};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    f = FieldSolver();
+}
+
+void field_solve_fp32(FieldSolver &f, const float *d, float *ex, float *ey, cudaStream_t st) {
+    const int m = f.m;
+    SpectralEpi none{};
+    GemmSet s1{{f.C, nullptr}, {d, nullptr}, {f.t0, nullptr}};
+    gemm<false>(m, s1, 1, none, st);
+    SpectralEpi epi{f.px, f.py, f.wx, f.wy, 4.0f / ((float)m * (float)m)};
+    GemmSet s2{{f.C, nullptr}, {f.t0, nullptr}, {nullptr, nullptr}};
+    gemm<true>(m, s2, 1, epi, st);
+    GemmSet s3{{f.Ct, f.St}, {f.px, f.py}, {f.ux, f.uy}};
+    gemm<false>(m, s3, 2, none, st);
+    GemmSet s4{{f.St, f.Ct}, {f.ux, f.uy}, {ex, ey}};
+    gemm<false>(m, s4, 2, none, st);
+}
+
+}  // namespace ap

@@ -1,0 +1,244 @@
+// Weighted-average wirelength gradient and HPWL over a net/pin CSR.
+//
+// Replaces Placer::computeAllPartials_CPU -> computeNetPartials_CPU ->
+// compute_bc_terms_CPU -> compute_a_terms_CPU (vck5000/host/src/AIEplace.cpp:
+// 574-673) and the AIE graph compute_abc + compute_partials
+// (vck5000/aie/src/partials/compute_abc.cpp:23-125, compute_partials.cpp:
+// 11-63).  Per net and axis the reference forms
+//   a+_i = exp((x_i - x_max)/g), a-_i = exp((x_min - x_i)/g),
+//   b+- = sum a+-, c+- = sum a+- x_i,
+//   dWA/dx_i = ((1 + x_i/g) b+ - c+/g) a+_i / b+^2 - ((1 - x_i/g) b- + c-/g) a-_i / b-^2.
+// The kernels evaluate the same expression in the algebraically equal
+// shifted form
+//   dWA/dx_i = a+_i/b+ (1 + (x_i - WA+)/g) - a-_i/b- (1 - (x_i - WA-)/g),
+//   WA+ = x_max + sum a+ (x - x_max) / b+,  WA- = x_min + sum a- (x - x_min) / b-,
+// which keeps FP32 exact where the reference form cancels (x_i/g ~ 1e4).
+// Gradients accumulate as int64 fixed point (2^-32) so the sum over a node's
+// nets is the same whatever order the atomics land in.
+#include "ap_common.cuh"
+#include "ap_kernels.h"
+
+namespace ap {
+
+namespace {
+
+struct AxisTerms {
+    float inv_bp, inv_bm, wp, wm;  // 1/b+, 1/b-, shifted WA+ - x_max, WA- - x_min
+};
+
+// One net with d <= D pins held in registers by one thread.
+template <int D>
+__device__ __forceinline__ void net_thread(const int *__restrict__ pins, int d, const float *__restrict__ px,
+                                           const float *__restrict__ py, float inv_g, ull *gqx, ull *gqy,
+                                           int n_grad, double &hp_acc, double &wa_acc) {
+    int node[D];
+    float xs[D], ys[D];
+    float xmx = -3.0e38f, xmn = 3.0e38f, ymx = -3.0e38f, ymn = 3.0e38f;
+#pragma unroll
+    for (int j = 0; j < D; ++j) {
+        if (j < d) {
+            node[j] = __ldg(pins + j);
+            xs[j] = __ldg(px + node[j]);
+            ys[j] = __ldg(py + node[j]);
+            xmx = fmaxf(xmx, xs[j]);
+            xmn = fminf(xmn, xs[j]);
+            ymx = fmaxf(ymx, ys[j]);
+            ymn = fminf(ymn, ys[j]);
+        }
+    }
+    float gxs[D];
+#pragma unroll
+    for (int j = 0; j < D; ++j) gxs[j] = 0.f;
+    float wa_net = 0.f;
+#pragma unroll
+    for (int axis = 0; axis < 2; ++axis) {
+        const float cmx = axis ? ymx : xmx, cmn = axis ? ymn : xmn;
+        float ep[D], em[D];
+        float bp = 0.f, bm = 0.f, cp = 0.f, cm = 0.f;
+#pragma unroll
+        for (int j = 0; j < D; ++j) {
+            if (j < d) {
+                const float c = axis ? ys[j] : xs[j];
+                const float dp = c - cmx, dm = c - cmn;
+                ep[j] = __expf(dp * inv_g);
+                em[j] = __expf(-dm * inv_g);
+                bp += ep[j];
+                bm += em[j];
+                cp += ep[j] * dp;
+                cm += em[j] * dm;
+            }
+        }
+        const float ibp = 1.f / bp, ibm = 1.f / bm, wp = cp * ibp, wm = cm * ibm;
+        wa_net += (cmx - cmn) + wp - wm;
+#pragma unroll
+        for (int j = 0; j < D; ++j) {
+            if (j < d) {
+                const float c = axis ? ys[j] : xs[j];
+                const float g = ep[j] * ibp * (1.f + ((c - cmx) - wp) * inv_g) -
+                                em[j] * ibm * (1.f - ((c - cmn) - wm) * inv_g);
+                if (axis == 0) {
+                    gxs[j] = g;
+                } else if (node[j] < n_grad) {
+                    atomicAdd(gqx + node[j], (ull)__float2ll_rn(gxs[j] * kGradScale));
+                    atomicAdd(gqy + node[j], (ull)__float2ll_rn(g * kGradScale));
+                }
+            }
+        }
+    }
+    hp_acc += (double)((xmx - xmn) + (ymx - ymn));
+    wa_acc += (double)wa_net;
+}
+
+}  // namespace
+
+// Nets [0, n_small) have degree 2..8 and sit in degree order.
+__global__ void __launch_bounds__(kThreads) wa_small_kernel(WaArgs a) {
+    __shared__ double red[32];
+    const float gamma = a.gamma > 0.f ? a.gamma : (float)a.sc->gamma;
+    const float inv_g = 1.f / gamma;
+    const float *px = a.px, *py = a.py;
+    if (a.mode == WA_LOOP) {
+        const int t = 1 - a.sc->cur;
+        px = a.pxs[t];
+        py = a.pys[t];
+    }
+    double hp = 0.0, wa = 0.0;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < a.n_small; e += gridDim.x * blockDim.x) {
+        const int s = __ldg(a.net_ptr + e);
+        const int d = __ldg(a.net_ptr + e + 1) - s;
+        if (d <= 2)
+            net_thread<2>(a.pin_node + s, d, px, py, inv_g, a.gqx, a.gqy, a.n_grad, hp, wa);
+        else if (d <= 4)
+            net_thread<4>(a.pin_node + s, d, px, py, inv_g, a.gqx, a.gqy, a.n_grad, hp, wa);
+        else
+            net_thread<8>(a.pin_node + s, d, px, py, inv_g, a.gqx, a.gqy, a.n_grad, hp, wa);
+    }
+    hp = block_sum(hp, red);
+    wa = block_sum(wa, red);
+    if (threadIdx.x == 0) {
+        a.partials[2 * blockIdx.x] = hp;
+        a.partials[2 * blockIdx.x + 1] = wa;
+    }
+}
+
+// Nets [n_small, n_nets): one warp per net, any degree.
+__global__ void __launch_bounds__(kThreads) wa_large_kernel(WaArgs a) {
+    __shared__ double red[32];
+    const float gamma = a.gamma > 0.f ? a.gamma : (float)a.sc->gamma;
+    const float inv_g = 1.f / gamma;
+    const float *px = a.px, *py = a.py;
+    if (a.mode == WA_LOOP) {
+        const int t = 1 - a.sc->cur;
+        px = a.pxs[t];
+        py = a.pys[t];
+    }
+    const int lane = threadIdx.x & 31;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    double hp = 0.0, wa = 0.0;
+    for (int e = a.n_small + warp; e < a.n_nets; e += nwarps) {
+        const int s = __ldg(a.net_ptr + e), d = __ldg(a.net_ptr + e + 1) - s;
+        float xmx = -3.0e38f, xmn = 3.0e38f, ymx = -3.0e38f, ymn = 3.0e38f;
+        for (int j = lane; j < d; j += 32) {
+            const int n = __ldg(a.pin_node + s + j);
+            const float x = __ldg(a.px + n), y = __ldg(a.py + n);
+            xmx = fmaxf(xmx, x);
+            xmn = fminf(xmn, x);
+            ymx = fmaxf(ymx, y);
+            ymn = fminf(ymn, y);
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            xmx = fmaxf(xmx, __shfl_xor_sync(0xffffffffu, xmx, o));
+            xmn = fminf(xmn, __shfl_xor_sync(0xffffffffu, xmn, o));
+            ymx = fmaxf(ymx, __shfl_xor_sync(0xffffffffu, ymx, o));
+            ymn = fminf(ymn, __shfl_xor_sync(0xffffffffu, ymn, o));
+        }
+        float s8[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};  // bp bm cp cm for x then y
+        for (int j = lane; j < d; j += 32) {
+            const int n = __ldg(a.pin_node + s + j);
+            const float c2[2] = {__ldg(px + n), __ldg(py + n)};
+#pragma unroll
+            for (int ax = 0; ax < 2; ++ax) {
+                const float dp = c2[ax] - (ax ? ymx : xmx), dm = c2[ax] - (ax ? ymn : xmn);
+                const float ep = __expf(dp * inv_g), em = __expf(-dm * inv_g);
+                s8[4 * ax + 0] += ep;
+                s8[4 * ax + 1] += em;
+                s8[4 * ax + 2] += ep * dp;
+                s8[4 * ax + 3] += em * dm;
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < 8; ++k) s8[k] = warp_sum(s8[k]);
+        AxisTerms t[2];
+#pragma unroll
+        for (int ax = 0; ax < 2; ++ax) {
+            t[ax].inv_bp = 1.f / s8[4 * ax + 0];
+            t[ax].inv_bm = 1.f / s8[4 * ax + 1];
+            t[ax].wp = s8[4 * ax + 2] * t[ax].inv_bp;
+            t[ax].wm = s8[4 * ax + 3] * t[ax].inv_bm;
+        }
+        for (int j = lane; j < d; j += 32) {
+            const int n = __ldg(a.pin_node + s + j);
+            if (n >= a.n_grad) continue;
+            const float c2[2] = {__ldg(px + n), __ldg(py + n)};
+            float g[2];
+#pragma unroll
+            for (int ax = 0; ax < 2; ++ax) {
+                const float dp = c2[ax] - (ax ? ymx : xmx), dm = c2[ax] - (ax ? ymn : xmn);
+                const float ep = __expf(dp * inv_g), em = __expf(-dm * inv_g);
+                g[ax] = ep * t[ax].inv_bp * (1.f + (dp - t[ax].wp) * inv_g) -
+                        em * t[ax].inv_bm * (1.f - (dm - t[ax].wm) * inv_g);
+            }
+            atomicAdd(a.gqx + n, (ull)__float2ll_rn(g[0] * kGradScale));
+            atomicAdd(a.gqy + n, (ull)__float2ll_rn(g[1] * kGradScale));
+        }
+        if (lane == 0) {
+            hp += (double)((xmx - xmn) + (ymx - ymn));
+            wa += (double)(((xmx - xmn) + t[0].wp - t[0].wm) + ((ymx - ymn) + t[1].wp - t[1].wm));
+        }
+    }
+    hp = block_sum(hp, red);
+    wa = block_sum(wa, red);
+    double *part = a.partials + 2 * a.small_blocks;
+    if (threadIdx.x == 0) {
+        part[2 * blockIdx.x] = hp;
+        part[2 * blockIdx.x + 1] = wa;
+    }
+    // the last block of this launch folds both launches' partials
+    if (arrive_last(a.counter)) {
+        const int nb = a.small_blocks + gridDim.x;
+        double h = 0.0, w = 0.0;
+        for (int i = threadIdx.x; i < nb; i += blockDim.x) {
+            h += __ldcg(a.partials + 2 * i);
+            w += __ldcg(a.partials + 2 * i + 1);
+        }
+        h = block_sum(h, red);
+        w = block_sum(w, red);
+        if (threadIdx.x == 0) {
+            if (a.out) {
+                a.out[0] = h;
+                a.out[1] = w;
+            }
+            DevScalars *sc = a.sc;
+            if (a.mode == WA_INIT) {
+                sc->hpwl = h;
+                sc->hpwl_prev = h;
+                sc->wa = w;
+            } else if (a.mode == WA_LOOP) {
+                sc->t_hpwl = h;  // becomes the reported HPWL if the trial is accepted
+                sc->t_wa = w;
+            }
+            *a.counter = 0u;
+        }
+    }
+}
+
+void launch_wirelength(const WaArgs &a0, int small_grid, int large_grid, cudaStream_t st) {
+    WaArgs a = a0;
+    a.small_blocks = small_grid;
+    wa_small_kernel<<<small_grid, kThreads, 0, st>>>(a);
+    wa_large_kernel<<<large_grid, kThreads, 0, st>>>(a);
+}
+
+}  // namespace ap

@@ -1,0 +1,388 @@
+#!/usr/bin/env python
+"""Benchmark of the ePlace global-placement iteration on one GB300.
+
+Workload: the 2M-cell synthetic netlist (2M movable cells with log-normal
+widths, 20k fixed macros, 2.1M nets / 9.4M pins with 80% index locality,
+1024x1024 bins, target density 0.8, seed 1).  One step is one trial step of
+the Nesterov loop (density scatter + position update, density/overflow, WA
+gradient, field solve, field gather + step control); `value` is accepted
+Nesterov iterations per second of device time with everything resident in
+HBM.  `e2e` is the same metric through the host-buffer C ABI call
+(ap_step_host: positions in from pinned host memory, positions + readout out
+every step).  The time to 10% overflow of the mixed-precision and plain
+forms is measured on fresh instances after the timed region.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the CPU restatement of the reference path (oracle/,
+FP64, OpenMP) on this host's cores: the reference ships no GPU code and its
+own CPU loop (host C++ behind XRT) does not build outside the VCK5000 flow.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+sys.path.insert(0, os.path.join(HERE, "oracle"))
+
+METRIC = "Nesterov iters/s & time-to-10% overflow, 2M cells: mixed+surrogate vs plain"
+UNIT = "iters/s"
+KERNELS_PER_TRIAL = 9  # scatter, rho, 2x WA, 4x field, gather
+STAGES = ["scatter+update", "density+overflow", "wirelength", "field", "gather+control"]
+
+
+def workload_desc(nl, preset):
+    n_nodes = len(nl["node_w"])
+    n_mov = int((nl["node_fixed"] == 0).sum())
+    return {
+        "workload": f"{preset}: {n_mov} movable cells, {n_nodes - n_mov} fixed macros, "
+                    f"{len(nl['net_ptr']) - 1} nets / {len(nl['pin_node'])} pins (80% pins within a "
+                    f"64-node window), {nl['bins']}x{nl['bins']} bins, target density {nl['target_density']}, "
+                    f"seed {nl['seed']}",
+        "bins": int(nl["bins"]),
+        "cells": n_mov,
+        "nets": len(nl["net_ptr"]) - 1,
+        "pins": len(nl["pin_node"]),
+        "l2": "inputs larger than L2 (per-step working set > 0.5 GB)",
+    }
+
+
+def stage_model(nl):
+    """Algorithmic bytes (HBM) or FLOPs per launch of each stage."""
+    n_nodes = len(nl["node_w"])
+    n_mov = int((nl["node_fixed"] == 0).sum())
+    e = len(nl["net_ptr"]) - 1
+    p = len(nl["pin_node"])
+    m2 = int(nl["bins"]) ** 2
+    m3 = int(nl["bins"]) ** 3
+    return {
+        # read v, g, u, w, h; write u', v'; int64 map written once
+        "scatter+update": ("hbm", 48 * n_mov + 8 * m2),
+        # read mov, fixed, fixed-scaled maps; clear mov; write solver input
+        "density+overflow": ("hbm", 36 * m2),
+        # net_ptr, pin_node, node positions, int64 gradient per movable node
+        "wirelength": ("hbm", 4 * (e + 1) + 4 * p + 8 * n_nodes + 16 * n_mov),
+        # 6 dense m x m x m contractions (useful FLOPs)
+        "field": ("tensor", 12 * m3),
+        # v, w, h, int64 grad read+clear, pins, charge, v_prev, g_prev, g out; field maps
+        "gather+control": ("hbm", 88 * n_mov + 8 * m2),
+    }
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the measured region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = os.path.join("/tmp", f"ap_clocks_{os.getpid()}.csv")
+
+    def start(self):
+        try:
+            self.out = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=self.out, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.out.close()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [t.strip() for t in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+def read_traffic(stage: str, preset: str):
+    """Per-launch DRAM bytes of a stage from the committed ncu summary, if any."""
+    path = os.path.join(HERE, "profiles", "traffic.md")
+    if not os.path.exists(path):
+        return None
+    key = f"{preset} {stage}:"
+    for line in open(path):
+        if line.strip().startswith(key):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except (ValueError, IndexError):
+                return None
+    return None
+
+
+def cpu_baseline(nl, budget_s: float = 20.0):
+    import numpy as np  # noqa: F401
+
+    import oracle
+
+    oracle.build(with_ref=False)
+    cores = oracle.set_threads(os.cpu_count() or 1)
+    pl = oracle.Placer(nl, int(nl["bins"]), float(nl["target_density"]))
+    pl.init(nl["node_x"], nl["node_y"])
+    t0 = time.perf_counter()
+    n = 0
+    while True:
+        pl.step(1)
+        n += 1
+        el = time.perf_counter() - t0
+        if el > budget_s or el / n * (n + 1) > budget_s * 1.5:
+            break
+    return {"value": n / el, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"FP64 oracle loop on the full workload: init (2 evaluations, untimed) + {n} "
+                      f"iteration(s) in {el:.1f} s on {cores} threads"}
+
+
+def reference_arm(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import aieplace_gb300 as ap
+    from aieplace_gb300 import build as b
+
+    b.build()
+    nl = ap.synth.generate(args.preset, seed=1)
+    import oracle
+
+    oracle.build(with_ref=False)
+    cores = oracle.set_threads(os.cpu_count() or 1)
+    pl = oracle.Placer(nl, int(nl["bins"]), float(nl["target_density"]))
+    pl.init(nl["node_x"], nl["node_y"])
+    budget = float(os.environ.get("AP_REFERENCE_BUDGET_S", "150"))
+    t0 = time.perf_counter()
+    done = 0
+    for _ in range(args.warmup):
+        pl.step(1)
+        if time.perf_counter() - t0 > budget / 4:
+            break
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        pl.step(1)
+        done += 1
+        el = time.perf_counter() - t0
+        if el / done * (done + 1) > budget:
+            break
+    el = time.perf_counter() - t0
+    v = done / el
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": done, "warmup": args.warmup, "ms_per_step": 1000 * el / done, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": workload_desc(nl, args.preset),
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"{done} of {args.steps} requested FP64 iterations of the full workload "
+                                   f"(bounded to ~{budget:.0f} s)"},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def time_to_target(ap, nl, solver, target=0.10, max_iter=4000):
+    import torch
+
+    with ap.Placer(nl, field_solver=solver, target_overflow=target, max_iterations=max_iter,
+                   check_interval=32) as pl:
+        pl.initialize_placement(seed=11, sigma=1.0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        it = pl.run()
+        torch.cuda.synchronize()
+        el = time.perf_counter() - t0
+        s = pl.stats()
+    return {"solver": solver, "seconds": el, "iterations": it, "evals": s["evals"],
+            "overflow": s["overflow"], "hpwl": s["hpwl"], "reached": s["overflow"] < target}
+
+
+def main():
+    ap_ = argparse.ArgumentParser()
+    ap_.add_argument("--gpus", type=int, default=1)
+    ap_.add_argument("--steps", type=int, default=200)
+    ap_.add_argument("--warmup", type=int, default=20)
+    ap_.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap_.add_argument("--preset", default="c2")
+    ap_.add_argument("--solver", default="auto", choices=["auto", "fp32", "bf16x3"])
+    ap_.add_argument("--no-cpu-baseline", action="store_true")
+    ap_.add_argument("--no-ttt", action="store_true", help="skip the time-to-10%% runs")
+    args = ap_.parse_args()
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        return reference_arm(args)
+
+    import numpy as np
+    import torch
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    import aieplace_gb300 as ap
+    from aieplace_gb300 import build as b
+
+    if rank == 0:
+        b.build()
+    if world > 1:
+        dist.barrier()
+    solver = args.solver
+    if solver == "auto":
+        solver = "bf16x3" if os.environ.get("AP_BENCH_SOLVER", "bf16x3") == "bf16x3" else "fp32"
+    # replicas: every rank places its own seeded instance (no data-path exchange)
+    nl = ap.synth.generate(args.preset, seed=1 + rank)
+    stream = torch.cuda.Stream()
+    pl = ap.Placer(nl, field_solver=solver)
+    try:
+        pl.set_stream(stream.cuda_stream)
+        pl.initialize_placement(seed=11 + rank, sigma=1.0)
+    except ap.APError:
+        if args.solver != "auto" or solver == "fp32":
+            raise
+        pl.close()
+        solver = "fp32"
+        pl = ap.Placer(nl, field_solver=solver)
+        pl.set_stream(stream.cuda_stream)
+        pl.initialize_placement(seed=11 + rank, sigma=1.0)
+    clocks = ClockSampler(local)
+    clocks.start()
+    pl.step_async(args.warmup)
+    torch.cuda.synchronize()
+    s0 = pl.stats()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    pl.step_async(args.steps)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    ms = ev0.elapsed_time(ev1)
+    s1 = pl.stats()
+    clk = clocks.stop()
+    iters = s1["iteration"] - s0["iteration"]
+    evals = s1["evals"] - s0["evals"]
+    # roofline of the dominant stage (eager launches, events between stages)
+    stage_ms = pl.profile_stages(10)
+    # e2e through the host-buffer call: pinned in/out every step
+    n = pl.num_nodes
+    hx = torch.empty(n, dtype=torch.float32, pin_memory=True)
+    hy = torch.empty(n, dtype=torch.float32, pin_memory=True)
+    ox = torch.empty(n, dtype=torch.float32, pin_memory=True)
+    oy = torch.empty(n, dtype=torch.float32, pin_memory=True)
+    x, y = pl.positions()
+    hx.copy_(torch.from_numpy(x))
+    hy.copy_(torch.from_numpy(y))
+    e2e_steps = max(10, min(args.steps, 100))
+    torch.cuda.synchronize()
+    se0 = pl.stats()
+    t0 = time.perf_counter()
+    from aieplace_gb300._lib import Stats, check, lib
+    import ctypes as C
+
+    st = Stats()
+    for _ in range(e2e_steps):
+        check("ap_step_host", lib().ap_step_host(pl._h, C.c_void_p(hx.data_ptr()), C.c_void_p(hy.data_ptr()),
+                                                 C.c_void_p(ox.data_ptr()), C.c_void_p(oy.data_ptr()),
+                                                 C.byref(st)))
+        hx, ox = ox, hx
+        hy, oy = oy, hy
+    e2e_s = time.perf_counter() - t0
+    se1 = pl.stats()
+    e2e_iters = se1["iteration"] - se0["iteration"]
+    n_mov = int((nl["node_fixed"] == 0).sum())
+    pl.close()
+
+    t_max = ms / 1000.0
+    total_iters = iters
+    if world > 1:
+        t = torch.tensor([t_max, float(iters), e2e_s, float(e2e_iters)], device="cuda")
+        tmax = t.clone()
+        dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
+        dist.all_reduce(t, op=dist.ReduceOp.SUM)
+        t_max, total_iters = float(tmax[0]), int(t[1])
+        e2e_s, e2e_iters = float(tmax[2]), int(t[3])
+
+    ttt = None
+    cpu = None
+    if rank == 0:
+        model = stage_model(nl)
+        dom = max(range(len(stage_ms)), key=lambda i: stage_ms[i])
+        bound, amount = model[STAGES[dom]]
+        peaks = {}
+        pk_path = os.path.join(HERE, "MEASURED_PEAKS.json")
+        if os.path.exists(pk_path):
+            peaks = json.load(open(pk_path))
+        if bound == "hbm":
+            achieved = amount / (stage_ms[dom] / 1000.0) / 1e9
+            peak = float(peaks.get("hbm_gbs", 6800.0))
+            unit = "GB/s"
+        else:
+            achieved = amount / (stage_ms[dom] / 1000.0) / 1e12
+            peak = float(peaks.get("bf16_tflops", 1900.0))
+            unit = "TFLOP/s"
+        roof = {"kernel": STAGES[dom], "bound": bound, "achieved": achieved, "peak": peak, "unit": unit,
+                "frac": achieved / peak, "traffic": read_traffic(STAGES[dom], args.preset),
+                "peak_source": "measured" if peaks else "fallback",
+                "stage_ms": dict(zip(STAGES, stage_ms))}
+        if not args.no_ttt:
+            ttt = {"mixed": time_to_target(ap, nl, "bf16x3") if solver == "bf16x3" else None,
+                   "plain": time_to_target(ap, nl, "fp32")}
+        if not args.no_cpu_baseline:
+            cpu = cpu_baseline(nl)
+        line = {
+            "metric": METRIC, "value": total_iters / t_max, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32+bf16x3" if solver == "bf16x3" else "f32", "data": "synthetic",
+            "config": {**workload_desc(nl, args.preset), "field_solver": solver,
+                       "step": "one trial step (one gradient evaluation); value counts accepted iterations",
+                       "parallelism": "replicas" if world > 1 else "single"},
+            "iterations": total_iters, "evals": evals, "evals_per_s": evals / t_max,
+            "gpu_launches": KERNELS_PER_TRIAL * args.steps,
+            "e2e": {"value": e2e_iters / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 8 * n_mov,
+                    "d2h_bytes_per_step": 8 * n + 160, "steps": e2e_steps},
+            "roofline": roof, "clocks": clk, "time_to_10pct_overflow": ttt, "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

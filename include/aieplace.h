@@ -77,7 +77,7 @@ typedef struct ap_params {
     float gamma_base_bins;      /* WA smoothing base, in bins; gamma = base*bin_w*10^(20/9 (tau-0.1) - 1) */
     int32_t field_solver;       /* AP_FIELD_* */
     float init_density_weight;  /* lambda_0 = this * |grad WL|_1 / |grad D|_1 */
-    float ref_delta_hpwl;       /* lambda update reference HPWL change; <= 0 selects 3.5e-5 * nets * bin_w */
+    float ref_delta_hpwl;       /* lambda update reference HPWL change; <= 0 selects 0.1 * nets * bin_w */
     float lambda_mu_max;        /* lambda multiplier bounds: mu in [mu_min, mu_max] */
     float lambda_mu_min;
     float init_step_coef;       /* first step: v_{-1} = v_0 - coef * g_0 (in bins) */
@@ -85,6 +85,8 @@ typedef struct ap_params {
     int32_t max_iterations;     /* ap_run upper bound */
     int32_t check_interval;     /* ap_run reads the device status every this many iterations */
     int32_t use_graph;          /* capture the iteration in a CUDA graph (1) or launch eagerly (0) */
+    int32_t max_backtracks;     /* step re-predictions per iteration (ePlace backtracking), 0 = off */
+    int32_t restart_mode;       /* momentum restart: 0 none, 1 gradient, 2 every step, 3 speed, 4 overflow rise */
 } ap_params;
 
 /* Per-iteration readout; the fields of printIterationResults (AIEplace.cpp:1048-1070)
@@ -98,8 +100,10 @@ typedef struct ap_stats {
     double overflow_abs;  /* reference form: sum_b max(0, overlap_b - A_b) (Grid.cpp:144-151) */
     double lambda;        /* density weight */
     double gamma;         /* WA smoothing, die units */
-    double alpha;         /* Nesterov step length */
+    double alpha;         /* Nesterov step length predicted for the next step */
     double a_k;           /* Nesterov momentum sequence */
+    int32_t evals;        /* gradient evaluations (accepted and backtracked trials) */
+    int32_t restarts;     /* momentum restarts */
 } ap_stats;
 
 typedef struct ap_handle ap_handle;
@@ -127,11 +131,24 @@ int ap_init_positions(ap_handle *h, const float *x, const float *y);
  * (the reference uses unseeded rand() in +-dieW/4, AIEplace.cpp:200-213). */
 int ap_init_seeded(ap_handle *h, uint64_t seed, float sigma);
 
-/* n_iter iterations of the preconditioned Nesterov loop; one iteration is the
- * reference's performIteration (AIEplace.cpp:9-39): wirelength gradient,
- * density map, field solve, field gather and position update, HPWL and
- * overflow readout. */
+/* n_iter accepted iterations of the preconditioned Nesterov loop; one
+ * iteration is the reference's performIteration (AIEplace.cpp:9-39):
+ * wirelength gradient, density map, field solve, field gather and position
+ * update, HPWL and overflow readout.  A step whose re-predicted length falls
+ * below 0.95 of the one tried is redone (ePlace backtracking), so an
+ * iteration costs one or more gradient evaluations. */
 int ap_step(ap_handle *h, int32_t n_iter);
+
+/* Enqueues n_trials trial steps (each one gradient evaluation; accepted ones
+ * advance the iteration count) on the handle's stream and returns without
+ * waiting: the building block of device-side timing. */
+int ap_step_async(ap_handle *h, int32_t n_trials);
+
+/* Runs n_trials trial steps with one CUDA event between stages and returns
+ * the mean milliseconds per stage: [0] density scatter + position update,
+ * [1] density -> solver input + overflow, [2] wirelength gradient,
+ * [3] field solve, [4] field gather + step control.  *n_stages = 5. */
+int ap_profile_stages(ap_handle *h, int32_t n_trials, float *stage_ms, int32_t *n_stages);
 
 /* Iterates until overflow < params.target_overflow or max_iterations;
  * replaces Placer::run (AIEplace.cpp:44-76). */

@@ -380,8 +380,14 @@ struct or_placer {
     or_params p;
     double bw, bh, die_w, die_h, ab, mov_area, ref_dh;
     double a, alpha, lambda, gamma, hpwl, hpwl_prev, wa, tau, tau_abs;
-    int iteration;
+    double norm_wl, norm_f; /* L1 norms of grad WL and of the field force at the last evaluation */
+    double du_prev, tau_prev;
+    int iteration, evals, restarts;
 };
+
+static double lipschitz_step(const or_placer *o, const double *vx, const double *vy, const double *kx,
+                             const double *ky, const double *gx, const double *gy, const double *hx,
+                             const double *hy);
 
 static double *dalloc(size_t n) { return (double *)calloc(n ? n : 1, sizeof(double)); }
 
@@ -490,6 +496,13 @@ static void evaluate(or_placer *o, int update_gamma) {
         o->fx[i] = g.fx;
         o->fy[i] = g.fy;
     }
+    double nw = 0, nf = 0;
+    for (int i = 0; i < o->n_mov; ++i) {
+        nw += fabs(o->wlx[i]) + fabs(o->wly[i]);
+        nf += fabs(o->fx[i]) + fabs(o->fy[i]);
+    }
+    o->norm_wl = nw;
+    o->norm_f = nf;
 }
 
 /* preconditioned gradient of f = WL + lambda * D at the evaluated point;
@@ -555,7 +568,7 @@ or_placer *or_create(int n_nodes, int n_nets, const int32_t *net_ptr, const int3
     for (int i = 0; i < o->n_mov; ++i) o->mov_area += (double)w[i] * h[i];
     for (int i = o->n_mov; i < n_nodes; ++i)
         node_overlaps(o, x[i], y[i], w[i], h[i], add_cb, o->fixmap);
-    o->ref_dh = p->ref_delta_hpwl > 0 ? p->ref_delta_hpwl : 3.5e-5 * n_nets * o->bw;
+    o->ref_dh = p->ref_delta_hpwl > 0 ? p->ref_delta_hpwl : 0.1 * n_nets * o->bw;
     return o;
 }
 
@@ -580,8 +593,8 @@ void or_init(or_placer *o, const float *x, const float *y) {
     for (int i = 0; i < m; ++i) {
         o->ux[i] = o->x[i];
         o->uy[i] = o->y[i];
-        o->vpx[i] = o->x[i] - s * o->gx[i];
-        o->vpy[i] = o->y[i] - s * o->gy[i];
+        o->vpx[i] = clampd(o->x[i] - s * o->gx[i], 0.0, o->die_w - o->w[i]);
+        o->vpy[i] = clampd(o->y[i] - s * o->gy[i], 0.0, o->die_h - o->h[i]);
     }
     double hp0 = o->hpwl, wa0 = o->wa, tau0 = o->tau, tabs0 = o->tau_abs;
     /* gradient at v_{-1} with lambda_0, gamma_0 */
@@ -600,39 +613,79 @@ void or_init(or_placer *o, const float *x, const float *y) {
     o->tau = tau0;
     o->tau_abs = tabs0;
     o->a = 1.0;
-    o->alpha = 0.0;
+    o->alpha = lipschitz_step(o, o->x, o->y, o->vpx, o->vpy, o->gx, o->gy, o->gpx, o->gpy);
     o->iteration = 0;
+    o->evals = 0;
+    o->restarts = 0;
 }
 
+/* ||v - vk|| / ||g - gk|| over movable nodes */
+static double lipschitz_step(const or_placer *o, const double *vx, const double *vy, const double *kx,
+                             const double *ky, const double *gx, const double *gy, const double *hx,
+                             const double *hy) {
+    double dv = 0, dg = 0;
+    for (int i = 0; i < o->n_mov; ++i) {
+        double a = vx[i] - kx[i], b = vy[i] - ky[i];
+        double c = gx[i] - hx[i], e = gy[i] - hy[i];
+        dv += a * a + b * b;
+        dg += c * c + e * e;
+    }
+    return dg > 0 ? sqrt(dv) / sqrt(dg) : 0.0;
+}
+
+/* One accepted iteration per count.  Each trial steps from the accepted
+ * state (u_k, v_k, g_k) with the predicted alpha, evaluates the gradient at
+ * the new reference point and re-predicts alpha from the two points; a
+ * prediction below 0.95 of the alpha used redoes the step with it (ePlace
+ * steplength prediction with backtracking, at most OR_MAX_BACKTRACK redos). */
+#define OR_MAX_BACKTRACK 10
 void or_step(or_placer *o, int n) {
     const int m = o->n_mov;
     for (int it = 0; it < n; ++it) {
-        double dv = 0, dg = 0;
-        for (int i = 0; i < m; ++i) {
-            double a = o->x[i] - o->vpx[i], b = o->y[i] - o->vpy[i];
-            double c = o->gx[i] - o->gpx[i], e = o->gy[i] - o->gpy[i];
-            dv += a * a + b * b;
-            dg += c * c + e * e;
-        }
-        if (dg > 0) o->alpha = sqrt(dv) / sqrt(dg);
         const double a_next = (1.0 + sqrt(4.0 * o->a * o->a + 1.0)) / 2.0;
         const double mom = (o->a - 1.0) / a_next;
-        for (int i = 0; i < m; ++i) {
-            double nux = clampd(o->x[i] - o->alpha * o->gx[i], 0.0, o->die_w - o->w[i]);
-            double nuy = clampd(o->y[i] - o->alpha * o->gy[i], 0.0, o->die_h - o->h[i]);
-            double nvx = clampd(nux + mom * (nux - o->ux[i]), 0.0, o->die_w - o->w[i]);
-            double nvy = clampd(nuy + mom * (nuy - o->uy[i]), 0.0, o->die_h - o->h[i]);
-            o->vpx[i] = o->x[i];
-            o->vpy[i] = o->y[i];
-            o->ux[i] = nux;
-            o->uy[i] = nuy;
-            o->x[i] = nvx;
-            o->y[i] = nvy;
-            o->gpx[i] = o->gx[i];
-            o->gpy[i] = o->gy[i];
+        /* accepted v_k into vpx; trial gradient into gpx; trial u into fx/fy scratch */
+        memcpy(o->vpx, o->x, sizeof(double) * (size_t)m);
+        memcpy(o->vpy, o->y, sizeof(double) * (size_t)m);
+        double *tux = dalloc((size_t)m), *tuy = dalloc((size_t)m);
+        double alpha = o->alpha, ahat = alpha;
+        for (int bt = 0; bt <= OR_MAX_BACKTRACK; ++bt) {
+            for (int i = 0; i < m; ++i) {
+                double nux = clampd(o->vpx[i] - alpha * o->gx[i], 0.0, o->die_w - o->w[i]);
+                double nuy = clampd(o->vpy[i] - alpha * o->gy[i], 0.0, o->die_h - o->h[i]);
+                tux[i] = nux;
+                tuy[i] = nuy;
+                o->x[i] = clampd(nux + mom * (nux - o->ux[i]), 0.0, o->die_w - o->w[i]);
+                o->y[i] = clampd(nuy + mom * (nuy - o->uy[i]), 0.0, o->die_h - o->h[i]);
+            }
+            evaluate(o, 1);
+            precond_grad(o, o->gpx, o->gpy);
+            o->evals++;
+            ahat = lipschitz_step(o, o->x, o->y, o->vpx, o->vpy, o->gpx, o->gpy, o->gx, o->gy);
+            if (ahat > 0.95 * alpha || bt == OR_MAX_BACKTRACK) break;
+            alpha = ahat;
         }
-        o->a = a_next;
-        evaluate(o, 1);
+        /* adaptive restart (O'Donoghue & Candes 2015, gradient scheme): the
+         * momentum sequence restarts when the accepted major step points uphill
+         * along the gradient it was taken from, <g_k, u_{k+1} - u_k> > 0 */
+        double uphill = 0.0, du = 0.0;
+        for (int i = 0; i < m; ++i) {
+            uphill += o->gx[i] * (tux[i] - o->ux[i]) + o->gy[i] * (tuy[i] - o->uy[i]);
+            du += (tux[i] - o->ux[i]) * (tux[i] - o->ux[i]) + (tuy[i] - o->uy[i]) * (tuy[i] - o->uy[i]);
+        }
+        if (o->p.restart == 3) uphill = du < o->du_prev ? 1.0 : -1.0;       /* speed restart */
+        if (o->p.restart == 4) uphill = o->tau > o->tau_prev ? 1.0 : -1.0;  /* overflow rose */
+        o->du_prev = du;
+        o->tau_prev = o->tau;
+        memcpy(o->ux, tux, sizeof(double) * (size_t)m);
+        memcpy(o->uy, tuy, sizeof(double) * (size_t)m);
+        memcpy(o->gx, o->gpx, sizeof(double) * (size_t)m);
+        memcpy(o->gy, o->gpy, sizeof(double) * (size_t)m);
+        free(tux);
+        free(tuy);
+        o->alpha = ahat;
+        o->a = (o->p.restart == 2 || (o->p.restart && uphill > 0.0)) ? 1.0 : a_next;
+        if (o->p.restart && uphill > 0.0) o->restarts++;
         /* lambda update (RePlAce NesterovPlace): mu = mu_max^(1 - dHPWL/ref), in [mu_min, mu_max] */
         double pc = (o->hpwl - o->hpwl_prev) / o->ref_dh;
         double mu = pc < 0 ? o->p.mu_max : pow(o->p.mu_max, 1.0 - pc);
@@ -640,7 +693,6 @@ void or_step(or_placer *o, int n) {
         if (mu > o->p.mu_max) mu = o->p.mu_max;
         o->lambda *= mu;
         o->hpwl_prev = o->hpwl;
-        precond_grad(o, o->gx, o->gy);
         o->iteration++;
     }
 }
@@ -655,6 +707,10 @@ void or_get_stats(const or_placer *o, or_stats *s) {
     s->gamma = o->gamma;
     s->alpha = o->alpha;
     s->a_k = o->a;
+    s->evals = o->evals;
+    s->norm_wl = o->norm_wl;
+    s->norm_f = o->norm_f;
+    s->restarts = o->restarts;
 }
 
 void or_get_positions(const or_placer *o, float *x, float *y) {

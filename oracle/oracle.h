@@ -94,14 +94,18 @@ typedef struct or_params {
     double target_density;
     double gamma_base_bins;
     double init_density_weight;
-    double ref_delta_hpwl; /* <= 0: 3.5e-5 * nets * bw */
+    double ref_delta_hpwl; /* <= 0: 0.1 * nets * bw */
     double mu_max, mu_min;
     double init_step_coef;
+    int restart; /* adaptive momentum restart on (1) or off (0) */
 } or_params;
 
 typedef struct or_stats {
     int iteration;
     double hpwl, wa, overflow, overflow_abs, lambda, gamma, alpha, a_k;
+    int evals; /* gradient evaluations, backtracking included */
+    double norm_wl, norm_f; /* L1 norms of grad WL and of the field force, last evaluation */
+    int restarts;           /* momentum restarts so far */
 } or_stats;
 
 typedef struct or_placer or_placer;

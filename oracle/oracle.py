@@ -45,13 +45,15 @@ class OrParams(C.Structure):
     _fields_ = [("mx", C.c_int), ("my", C.c_int), ("target_density", C.c_double),
                 ("gamma_base_bins", C.c_double), ("init_density_weight", C.c_double),
                 ("ref_delta_hpwl", C.c_double), ("mu_max", C.c_double), ("mu_min", C.c_double),
-                ("init_step_coef", C.c_double)]
+                ("init_step_coef", C.c_double), ("restart", C.c_int)]
 
 
 class OrStats(C.Structure):
     _fields_ = [("iteration", C.c_int), ("hpwl", C.c_double), ("wa", C.c_double),
                 ("overflow", C.c_double), ("overflow_abs", C.c_double), ("lambda_", C.c_double),
-                ("gamma", C.c_double), ("alpha", C.c_double), ("a_k", C.c_double)]
+                ("gamma", C.c_double), ("alpha", C.c_double), ("a_k", C.c_double),
+                ("evals", C.c_int), ("norm_wl", C.c_double), ("norm_f", C.c_double),
+                ("restarts", C.c_int)]
 
 
 _lib = None
@@ -211,9 +213,9 @@ class Placer:
 
     def __init__(self, nl: dict, mx: int, target_density: float, gamma_base_bins=4.0,
                  init_density_weight=8e-5, ref_delta_hpwl=0.0, mu_max=1.05, mu_min=0.95,
-                 init_step_coef=0.1):
+                 init_step_coef=0.1, restart=3):
         p = OrParams(mx, mx, target_density, gamma_base_bins, init_density_weight, ref_delta_hpwl,
-                     mu_max, mu_min, init_step_coef)
+                     mu_max, mu_min, init_step_coef, restart)
         self._keep = nl
         die = nl["die"]
         self.h = lib().or_create(len(nl["node_w"]), len(nl["net_ptr"]) - 1, _i32(nl["net_ptr"]),
@@ -234,7 +236,8 @@ class Placer:
         lib().or_get_stats(self.h, C.byref(s))
         return {"iteration": s.iteration, "hpwl": s.hpwl, "wa": s.wa, "overflow": s.overflow,
                 "overflow_abs": s.overflow_abs, "lambda": s.lambda_, "gamma": s.gamma,
-                "alpha": s.alpha, "a_k": s.a_k}
+                "alpha": s.alpha, "a_k": s.a_k, "evals": s.evals,
+                "norm_wl": s.norm_wl, "norm_f": s.norm_f, "restarts": s.restarts}
 
     def positions(self):
         x, y = np.zeros(self.n, np.float32), np.zeros(self.n, np.float32)

@@ -1,0 +1,183 @@
+"""CUDA path against the CPU oracle, through the C ABI.
+
+Tolerances (stated per result, as the comparison is made):
+  density map      bit-exact int64 (same fixed-point definition)
+  overflow         bit-exact integer sum -> identical double
+  WA gradient      |dg| <= 1e-4 * max|g| per node, FP32 kernel vs FP64 oracle
+  HPWL / WA        1e-6 / 1e-5 relative
+  field (FP32)     max|dE| <= 1e-4 * max|E| vs the FP64 oracle
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ap():
+    import torch
+
+    if not torch.cuda.is_available():
+        pytest.skip("no GPU")
+    from aieplace_gb300 import build
+
+    build.build()
+    import aieplace_gb300
+
+    return aieplace_gb300
+
+
+def spread_positions(nl, rng, margin=3.0):
+    """Movable cells scattered over (and a little beyond) the die."""
+    W, H = float(nl["die"][2]), float(nl["die"][3])
+    x = nl["node_x"].copy()
+    y = nl["node_y"].copy()
+    mov = nl["node_fixed"] == 0
+    x[mov] = rng.uniform(-margin, W + margin, mov.sum()).astype(np.float32)
+    y[mov] = rng.uniform(-margin, H + margin, mov.sum()).astype(np.float32)
+    return x, y
+
+
+@pytest.mark.parametrize("preset,bins", [("c0", 32), ("c1_small", 128), ("c1_small", 512)])
+def test_density_map_bit_exact(ap, oracle_lib, preset, bins):
+    nl = ap.synth.generate(preset, seed=4)
+    rng = np.random.default_rng(0)
+    x, y = spread_positions(nl, rng)
+    with ap.Placer(nl, bins=bins) as pl:
+        got = pl.compute_overlaps(x, y)
+    g = oracle_lib.grid(float(nl["die"][2]), float(nl["die"][3]), bins)
+    area = (nl["node_w"] * nl["node_h"]) > 0
+    ref = oracle_lib.density_q(g, x, y, nl["node_w"], nl["node_h"], area.astype(np.uint8))
+    assert np.array_equal(got, ref)
+
+
+def test_density_map_bit_exact_full_size(ap, oracle_lib):
+    """2M cells / 1024^2 bins: the shipped mixed-precision workload."""
+    nl = ap.synth.generate("c2", seed=1)
+    rng = np.random.default_rng(1)
+    x, y = spread_positions(nl, rng, margin=0.0)
+    with ap.Placer(nl, bins=1024, target_density=0.8) as pl:
+        got = pl.compute_overlaps(x, y)
+        got2 = pl.compute_overlaps(x, y)
+    assert np.array_equal(got, got2)  # deterministic run to run
+    g = oracle_lib.grid(float(nl["die"][2]), float(nl["die"][3]), 1024)
+    area = (nl["node_w"] * nl["node_h"]) > 0
+    ref = oracle_lib.density_q(g, x, y, nl["node_w"], nl["node_h"], area.astype(np.uint8))
+    assert np.array_equal(got, ref)
+    assert got.sum() == ref.sum()
+
+
+@pytest.mark.parametrize("preset,gamma", [("c0", 4.0), ("c1_small", 0.7), ("c1_small", 25.0)])
+def test_wirelength_gradient(ap, oracle_lib, preset, gamma):
+    nl = ap.synth.generate(preset, seed=5)
+    rng = np.random.default_rng(2)
+    x, y = spread_positions(nl, rng, margin=0.0)
+    with ap.Placer(nl, bins=32 if preset == "c0" else 128) as pl:
+        gx, gy, wa, hp = pl.compute_all_partials(x, y, gamma)
+    rx, ry, rwa, rhp = oracle_lib.wa_grad(nl["net_ptr"], nl["pin_node"], x, y, gamma)
+    scale = max(np.abs(rx).max(), np.abs(ry).max())
+    assert np.abs(gx - rx).max() <= 1e-4 * scale
+    assert np.abs(gy - ry).max() <= 1e-4 * scale
+    assert abs(hp - rhp) <= 1e-6 * rhp
+    assert abs(wa - rwa) <= 1e-5 * rwa
+
+
+@pytest.mark.parametrize("m", [32, 128, 512])
+def test_field_fp32_against_oracle(ap, oracle_lib, m):
+    rng = np.random.default_rng(m)
+    d = rng.random((m, m)).astype(np.float32)
+    d[m // 4: m // 2, m // 3: m // 2] += 3.0  # a dense block: strong low frequencies
+    nl = ap.synth.generate("c0", seed=1)
+    with ap.Placer(nl, bins=m) as pl:
+        ex, ey = pl.compute_electric_fields(d, "fp32")
+    rex, rey = oracle_lib.field_solve(d.astype(np.float64), m)
+    for got, ref in ((ex, rex), (ey, rey)):
+        assert np.abs(got - ref).max() <= 1e-4 * np.abs(ref).max()
+
+
+def test_field_fp32_matches_reference_fft_golden(ap):
+    """replace::FFT::doFFT outputs (fft_replace/fft.cpp), committed fixture."""
+    from conftest import golden
+
+    g = golden("replace_field.npz")
+    nl = ap.synth.generate("c0", seed=1)
+    for case in ("rand32", "rand64"):
+        d = g[f"{case}_density"]
+        m = d.shape[0]
+        with ap.Placer(nl, bins=m) as pl:
+            ex, ey = pl.compute_electric_fields(d, "fp32")
+        for got, ref in ((ex, g[f"{case}_ex"]), (ey, g[f"{case}_ey"])):
+            ref = ref.reshape(-1)
+            assert np.abs(got - ref).max() <= 1e-4 * np.abs(ref).max()
+
+
+def test_loop_deterministic_and_resumable(ap):
+    nl = ap.synth.generate("c1_small", seed=2)
+    runs = []
+    for _ in range(2):
+        with ap.Placer(nl, bins=128) as pl:
+            pl.initialize_placement(seed=7, sigma=1.0)
+            pl.perform_iteration(40)
+            snap = pl.snapshot()
+            pl.perform_iteration(25)
+            runs.append(pl.positions())
+            s = pl.stats()
+            pl.restore(snap)
+            pl.perform_iteration(25)
+            again = pl.positions()
+        np.testing.assert_array_equal(runs[-1][0], again[0])
+        np.testing.assert_array_equal(runs[-1][1], again[1])
+        assert s["iteration"] == 65 and s["evals"] >= 65
+    np.testing.assert_array_equal(runs[0][0], runs[1][0])
+
+
+def test_step_host_matches_device_step(ap):
+    nl = ap.synth.generate("c0", seed=1)
+    with ap.Placer(nl, bins=32) as a, ap.Placer(nl, bins=32) as b:
+        a.initialize_placement(nl["node_x"], nl["node_y"])
+        b.initialize_placement(nl["node_x"], nl["node_y"])
+        x, y = b.positions()
+        xo, yo = np.zeros_like(x), np.zeros_like(y)
+        for _ in range(10):
+            a.perform_iteration(1)
+            s = b.step_host(x, y, xo, yo)
+            x, y = xo.copy(), yo.copy()
+        ax, ay = a.positions()
+        np.testing.assert_array_equal(ax, x)
+        np.testing.assert_array_equal(ay, y)
+        assert s["iteration"] == 10
+
+
+def test_errors_are_status_codes(ap):
+    from aieplace_gb300 import APError
+
+    nl = ap.synth.generate("c0", seed=1)
+    with ap.Placer(nl, bins=32) as pl:
+        with pytest.raises(APError) as e:
+            pl.perform_iteration(1)  # before any initial placement
+        assert e.value.status == 8
+        bad = nl["node_x"].copy()
+        bad[0] = np.inf
+        with pytest.raises(APError) as e:
+            pl.initialize_placement(bad, nl["node_y"])
+        assert e.value.status == 3
+
+
+def test_loop_c0_reaches_target_like_oracle(ap, oracle_lib):
+    """576-cell case: the GPU loop (FP32, fixed-point density) and the FP64
+    oracle loop both reach overflow < 0.10; final HPWL within 0.5%... of each
+    other is not implied by a non-convex trajectory, so the bound checked is 3%
+    on HPWL and 0.005 on overflow at the first iteration each goes below 0.10."""
+    nl = ap.synth.generate("c0", seed=1)
+    ref = oracle_lib.Placer(nl, 32, 1.0)
+    ref.init(nl["node_x"], nl["node_y"])
+    while ref.stats()["overflow"] >= 0.10 and ref.stats()["iteration"] < 3000:
+        ref.step(1)
+    rs = ref.stats()
+    with ap.Placer(nl, bins=32, target_density=1.0, check_interval=1) as pl:
+        pl.initialize_placement(nl["node_x"], nl["node_y"])
+        pl.run()
+        s = pl.stats()
+    assert s["overflow"] < 0.10 and rs["overflow"] < 0.10
+    assert abs(s["hpwl"] - rs["hpwl"]) <= 0.03 * rs["hpwl"], (s, rs)
+    assert abs(s["iteration"] - rs["iteration"]) <= 0.2 * rs["iteration"], (s, rs)
