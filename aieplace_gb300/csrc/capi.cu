@@ -198,7 +198,7 @@ int enqueue_iteration(ap_handle *h, cudaStream_t st) {
     s.update = 1;
     launch_scatter(s, st);
     launch_rho(rho_args(h, RHO_LOOP, nullptr), st);
-    launch_wirelength(wa_args(h, nullptr, nullptr, 0.f, h->n_mov, WA_LOOP, nullptr), h->wa_small_grid,
+    launch_wirelength(wa_args(h, h->d_px[0], h->d_py[0], 0.f, h->n_mov, WA_LOOP, nullptr), h->wa_small_grid,
                       h->wa_large_grid, st);
     int r = run_field(h, h->p.field_solver, st);
     if (r != AP_OK) return r;
@@ -705,7 +705,7 @@ int ap_profile_stages(ap_handle *h, int32_t n_trials, float *stage_ms, int32_t *
         CK(cudaEventRecord(ev[1], st));
         launch_rho(rho_args(h, RHO_LOOP, nullptr), st);
         CK(cudaEventRecord(ev[2], st));
-        launch_wirelength(wa_args(h, nullptr, nullptr, 0.f, h->n_mov, WA_LOOP, nullptr), h->wa_small_grid,
+        launch_wirelength(wa_args(h, h->d_px[0], h->d_py[0], 0.f, h->n_mov, WA_LOOP, nullptr), h->wa_small_grid,
                           h->wa_large_grid, st);
         CK(cudaEventRecord(ev[3], st));
         r = run_field(h, h->p.field_solver, st);

@@ -141,7 +141,7 @@ __global__ void __launch_bounds__(kThreads) wa_large_kernel(WaArgs a) {
         float xmx = -3.0e38f, xmn = 3.0e38f, ymx = -3.0e38f, ymn = 3.0e38f;
         for (int j = lane; j < d; j += 32) {
             const int n = __ldg(a.pin_node + s + j);
-            const float x = __ldg(a.px + n), y = __ldg(a.py + n);
+            const float x = __ldg(px + n), y = __ldg(py + n);
             xmx = fmaxf(xmx, x);
             xmn = fminf(xmn, x);
             ymx = fmaxf(ymx, y);
