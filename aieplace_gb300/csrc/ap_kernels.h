@@ -123,9 +123,14 @@ int field_solver_init(FieldSolver &f, int m, float bin_ratio, int want_bf16);
 void field_solver_free(FieldSolver &f);
 // density d (x-major) -> ex, ey; FP32 SIMT contraction
 void field_solve_fp32(FieldSolver &f, const float *d, float *ex, float *ey, cudaStream_t st);
-// density as bf16 hi/lo split -> ex, ey; tcgen05 BF16x3 contraction
+// Builds the TMA tensor maps of the tcgen05 path with (d_hi, d_lo) as the
+// density input; needs m a multiple of 128.
+int field_solver_bind_bf16(FieldSolver &f, const __nv_bfloat16 *d_hi, const __nv_bfloat16 *d_lo);
+// density as bf16 hi/lo split (the bound buffers) -> ex, ey; tcgen05 BF16x3 contraction
 int field_solve_bf16x3(FieldSolver &f, const __nv_bfloat16 *d_hi, const __nv_bfloat16 *d_lo,
                        float *ex, float *ey, cudaStream_t st);
+// nonzero once a bounded wait in a tcgen05 kernel gave up
+int field_solver_status(FieldSolver &f, unsigned int *out);
 // float -> bf16 hi/lo split (for per-stage API calls)
 void launch_split_bf16(int n, const float *src, __nv_bfloat16 *hi, __nv_bfloat16 *lo, cudaStream_t st);
 

@@ -223,6 +223,11 @@ int enqueue_eval(ap_handle *h, int at, int rho_mode, int wa_mode, cudaStream_t s
 
 int sync(ap_handle *h) {
     CK(cudaStreamSynchronize(h->stream));
+    if (h->fs.tc_ready) {
+        unsigned int st = 0;
+        if (field_solver_status(h->fs, &st) != AP_OK) return AP_ERR_CUDA;
+        if (st) return AP_ERR_TIMEOUT;
+    }
     return AP_OK;
 }
 
@@ -595,6 +600,12 @@ int ap_create(const ap_netlist *nl, const ap_params *params, ap_handle **out) {
     }
     int r = ok ? field_solver_init(h->fs, p.bins_x, g.bh / g.bw, 1)
                : AP_ERR_CUDA;
+    if (r == AP_OK && p.bins_x % 128 == 0) {
+        r = field_solver_bind_bf16(h->fs, h->d_dens_hi, h->d_dens_lo);
+        if (r != AP_OK && p.field_solver != AP_FIELD_BF16X3) r = AP_OK;  // tensor path optional here
+    } else if (r == AP_OK && p.field_solver == AP_FIELD_BF16X3) {
+        r = AP_ERR_UNSUPPORTED;  // the tcgen05 tiles need bins a multiple of 128
+    }
     if (r != AP_OK) {
         ap_destroy(h);
         return r;
@@ -898,7 +909,7 @@ int ap_field_solve(ap_handle *h, const float *density, float *ex, float *ey, int
     const int sv = solver_of(h, solver);
     if (sv != AP_FIELD_FP32 && sv != AP_FIELD_BF16X3) return AP_ERR_INVALID_ARG;
     const int nb = h->p.bins_x * h->p.bins_y;
-    if (sv == AP_FIELD_BF16X3 && !h->fs.C_hi) return AP_ERR_UNSUPPORTED;
+    if (sv == AP_FIELD_BF16X3 && !h->fs.tc_ready) return AP_ERR_UNSUPPORTED;
     CK(cudaMemcpyAsync(h->d_dens, density, sizeof(float) * nb, cudaMemcpyHostToDevice, h->stream));
     if (sv == AP_FIELD_BF16X3) launch_split_bf16(nb, h->d_dens, h->d_dens_hi, h->d_dens_lo, h->stream);
     int r = run_field(h, sv, h->stream);

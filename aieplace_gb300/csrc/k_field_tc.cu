@@ -1,13 +1,435 @@
-// tcgen05 BF16x3 transform contractions (placeholder until the tensor-core path lands).
+// Electrostatic field solve on the 5th-generation tensor cores (sm_103a).
+//
+// Same four contraction stages as the FP32 path (k_field_simt.cu, restating
+// replace::FFT::doFFT, python/AIEmath/fft_replace/fft.cpp:204-299), each
+//   D[i][j] = sum_k A[i][k] B[j][k]
+// with A a constant transform matrix and B the data, both stored as a BF16
+// pair (hi = bf16(x), lo = bf16(x - hi)).  Every k-step issues three MMAs into
+// one FP32 accumulator in tensor memory: A_hi B_hi + A_hi B_lo + A_lo B_hi
+// (the "bf16x3" split; the dropped A_lo B_lo term is 2^-16 relative).
+//
+// Kernel layout (one 128 x 64 output tile per CTA, 4 warps):
+//   warp 0 lane 0   TMA producer: 4-stage ring of {A_hi, A_lo, B_hi, B_lo}
+//                   128B-swizzled K-major tiles, mbarrier complete_tx
+//   warp 1 lane 0   MMA issuer: tcgen05.mma.cta_group::1.kind::f16, M=128,
+//                   N=64, K=16; tcgen05.commit frees stages / signals the end
+//   warps 0-3       epilogue: tcgen05.ld 32x32b (warp w owns TMEM lanes
+//                   32w..32w+31 = output rows), fused stage epilogue, stores
+// Every mbarrier wait is bounded; a wait that gives up sets the solver's
+// status word and the CTA drains and exits without further issue.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <stdlib.h>
+
 #include "../../include/aieplace.h"
 #include "ap_kernels.h"
 
 namespace ap {
+namespace tc {
+
+constexpr int BM = 128, BN = 64, BK = 64, STAGES = 4, THREADS = 128;
+constexpr int A_TILE = BM * BK * 2;                   // 16 KB
+constexpr int B_TILE = BN * BK * 2;                   // 8 KB
+constexpr int STAGE_BYTES = 2 * A_TILE + 2 * B_TILE;  // 48 KB
+constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
+constexpr uint32_t TMEM_COLS = 64;                    // FP32 accumulator, 128 lanes x 64 columns
+constexpr unsigned long long WAIT_NS = 2000000000ull;  // 2 s bound on any single wait
+
+enum { EPI_SPLIT = 0, EPI_SPECTRAL = 1, EPI_F32 = 2 };
+
+struct Maps {
+    CUtensorMap a_hi[2], a_lo[2], b_hi[2], b_lo[2];
+};
+
+struct Epi {
+    int m;
+    int mode;
+    __nv_bfloat16 *o_hi[2], *o_lo[2];  // EPI_SPLIT; EPI_SPECTRAL: [0] = Px, [1] = Py
+    float *o_f32[2];                   // EPI_F32
+    const float *wx, *wy;
+    float scale;
+    unsigned int *status;
+};
+
+// ---- PTX wrappers ----------------------------------------------------------
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Bounded wait: false (and the status flag set) if the phase did not complete in time.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, unsigned int *status) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const unsigned long long t0 = global_ns();
+    for (;;) {
+        for (int i = 0; i < 64; ++i)
+            if (mbar_try_wait(bar, parity)) return true;
+        if (global_ns() - t0 > WAIT_NS) {
+            atomicOr(status, 1u);
+            return false;
+        }
+    }
+}
+
+__device__ __forceinline__ void tma_load_2d(const CUtensorMap *map, uint64_t *bar, void *dst, int x, int y) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];" ::"r"(
+            smem_u32(dst)),
+        "l"((uint64_t)map), "r"(smem_u32(bar)), "r"(x), "r"(y)
+        : "memory");
+}
+
+__device__ __forceinline__ void tma_prefetch(const CUtensorMap *map) {
+    asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)map) : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// K-major operand in the 128B-swizzled canonical layout: 8-row x 128-byte
+// atoms stacked along M/N every 1024 bytes (stride byte offset), the leading
+// byte offset unused for swizzled K-major operands, descriptor version 1.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
+    uint64_t d = 0;
+    d |= (uint64_t)((addr & 0x3FFFFu) >> 4);
+    d |= (uint64_t)1 << 16;             // leading byte offset (16 B, ignored here)
+    d |= (uint64_t)(1024 >> 4) << 32;   // stride byte offset
+    d |= (uint64_t)1 << 46;             // descriptor version
+    d |= (uint64_t)2 << 61;             // 128-byte swizzle
+    return d;
+}
+
+// kind::f16 instruction descriptor: D f32, A and B bf16, both K-major.
+__host__ __device__ constexpr uint32_t idesc_bf16(int m, int n) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+        "l"(a), "l"(b), "r"(idesc), "r"(acc)
+        : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t *bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
+        "%14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+          "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]),
+          "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]),
+          "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
+    const __nv_bfloat162 v = __floats2bfloat162_rn(a, b);
+    return *reinterpret_cast<const uint32_t *>(&v);
+}
+
+// 32 FP32 values of one output row -> hi/lo BF16 rows (64 bytes each)
+__device__ __forceinline__ void store_split(const float (&v)[32], __nv_bfloat16 *hi, __nv_bfloat16 *lo) {
+    uint32_t h[16], l[16];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+        const __nv_bfloat16 a = __float2bfloat16_rn(v[2 * i]), b = __float2bfloat16_rn(v[2 * i + 1]);
+        const __nv_bfloat162 hp = __halves2bfloat162(a, b);
+        h[i] = *reinterpret_cast<const uint32_t *>(&hp);
+        l[i] = pack_bf16(v[2 * i] - __bfloat162float(a), v[2 * i + 1] - __bfloat162float(b));
+    }
+    uint4 *ph = reinterpret_cast<uint4 *>(hi), *pl = reinterpret_cast<uint4 *>(lo);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        ph[i] = make_uint4(h[4 * i], h[4 * i + 1], h[4 * i + 2], h[4 * i + 3]);
+        pl[i] = make_uint4(l[4 * i], l[4 * i + 1], l[4 * i + 2], l[4 * i + 3]);
+    }
+}
+
+__global__ void __launch_bounds__(THREADS, 1) gemm_bf16x3_kernel(const __grid_constant__ Maps maps, Epi e) {
+    extern __shared__ __align__(1024) uint8_t smem_raw[];
+    uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint64_t *full = (uint64_t *)(smem + STAGES * STAGE_BYTES);
+    uint64_t *empty = full + STAGES;
+    uint64_t *done = empty + STAGES;
+    uint32_t *tmem_slot = (uint32_t *)(done + 1);
+    volatile int *abort_flag = (volatile int *)(tmem_slot + 1);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int z = blockIdx.z;
+    const int n0 = blockIdx.x * BN, m0 = blockIdx.y * BM;
+    const int nk = e.m / BK;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < STAGES; ++s) {
+            mbar_init(full + s, 1);
+            mbar_init(empty + s, 1);
+        }
+        mbar_init(done, 1);
+        *abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        tma_prefetch(&maps.a_hi[z]);
+        tma_prefetch(&maps.a_lo[z]);
+        tma_prefetch(&maps.b_hi[z]);
+        tma_prefetch(&maps.b_lo[z]);
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+
+    int issued = 0;  // producer: k-blocks whose loads were issued
+    if (warp == 0 && lane == 0) {
+        for (int kb = 0; kb < nk; ++kb) {
+            const int s = kb % STAGES, round = kb / STAGES;
+            if (round > 0 && !mbar_wait(empty + s, (round - 1) & 1, e.status)) {
+                *abort_flag = 1;
+                break;
+            }
+            if (*abort_flag) break;
+            uint8_t *st = smem + s * STAGE_BYTES;
+            mbar_expect_tx(full + s, STAGE_BYTES);
+            tma_load_2d(&maps.a_hi[z], full + s, st, kb * BK, m0);
+            tma_load_2d(&maps.a_lo[z], full + s, st + A_TILE, kb * BK, m0);
+            tma_load_2d(&maps.b_hi[z], full + s, st + 2 * A_TILE, kb * BK, n0);
+            tma_load_2d(&maps.b_lo[z], full + s, st + 2 * A_TILE + B_TILE, kb * BK, n0);
+            issued = kb + 1;
+        }
+    } else if (warp == 1 && lane == 0) {
+        constexpr uint32_t idesc = idesc_bf16(BM, BN);
+        for (int kb = 0; kb < nk; ++kb) {
+            const int s = kb % STAGES, round = kb / STAGES;
+            if (!mbar_wait(full + s, round & 1, e.status)) {
+                *abort_flag = 1;
+                break;
+            }
+            tc_fence_after();
+            const uint32_t base = smem_u32(smem + s * STAGE_BYTES);
+            const uint64_t ahi = smem_desc(base), alo = smem_desc(base + A_TILE);
+            const uint64_t bhi = smem_desc(base + 2 * A_TILE), blo = smem_desc(base + 2 * A_TILE + B_TILE);
+#pragma unroll
+            for (int k = 0; k < BK / 16; ++k) {
+                const uint64_t adv = (uint64_t)((k * 32) >> 4);  // 16 bf16 = 32 bytes along K
+                mma_bf16(tmem, ahi + adv, bhi + adv, idesc, (kb | k) != 0);
+                mma_bf16(tmem, ahi + adv, blo + adv, idesc, 1u);
+                mma_bf16(tmem, alo + adv, bhi + adv, idesc, 1u);
+            }
+            mma_commit(empty + s);  // stage s reusable once these MMAs have read it
+        }
+        mma_commit(done);  // accumulator complete (or, after an abort, all issued MMAs retired)
+    }
+    __syncwarp();
+
+    // ---- epilogue ----------------------------------------------------------
+    const bool ok = mbar_wait(done, 0, e.status) && !*abort_flag;
+    tc_fence_after();
+    if (ok) {
+        const int row = m0 + warp * 32 + lane;
+#pragma unroll
+        for (int c0 = 0; c0 < BN; c0 += 32) {
+            uint32_t r[32];
+            tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, r);
+            float v[32];
+#pragma unroll
+            for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+            const size_t off = (size_t)row * e.m + n0 + c0;
+            if (e.mode == EPI_F32) {
+                float4 *o = reinterpret_cast<float4 *>(e.o_f32[z] + off);
+#pragma unroll
+                for (int i = 0; i < 8; ++i) o[i] = make_float4(v[4 * i], v[4 * i + 1], v[4 * i + 2], v[4 * i + 3]);
+            } else if (e.mode == EPI_SPLIT) {
+                store_split(v, e.o_hi[z] + off, e.o_lo[z] + off);
+            } else {
+                // spectral scaling of fft.cpp:217-273: halve row/column 0,
+                // 4/(Mx My), phi = a / (wx^2 + wy^2), Px = phi wx, Py = phi wy
+                const int u = row;
+                const float wx = e.wx[u];
+                float px[32], py[32];
+#pragma unroll
+                for (int i = 0; i < 32; ++i) {
+                    const int vv = n0 + c0 + i;
+                    const float wy = e.wy[vv];
+                    float c = v[i] * e.scale;
+                    if (u == 0) c *= 0.5f;
+                    if (vv == 0) c *= 0.5f;
+                    const float den = wx * wx + wy * wy;
+                    c = den > 0.f ? c / den : 0.f;
+                    px[i] = c * wx;
+                    py[i] = c * wy;
+                }
+                store_split(px, e.o_hi[0] + off, e.o_lo[0] + off);
+                store_split(py, e.o_hi[1] + off, e.o_lo[1] + off);
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (threadIdx.x == 0 && issued > 0) {
+        // after an abort, let every issued load land before the CTA exits
+        for (int kb = issued - 1; kb >= 0 && kb >= issued - STAGES; --kb)
+            mbar_wait(full + (kb % STAGES), (kb / STAGES) & 1, e.status);
+    }
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
+    }
+}
+
+// ---- host side ---------------------------------------------------------------
+
+PFN_cuTensorMapEncodeTiled_v12000 encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+    }
+    return fn;
+}
+
+// row-major m x m bf16 matrix, K (columns) innermost, box 64 x rows
+bool make_map(CUtensorMap *map, const __nv_bfloat16 *base, int m, int box_rows) {
+    PFN_cuTensorMapEncodeTiled_v12000 enc = encoder();
+    if (!enc || ((uintptr_t)base & 15)) return false;
+    cuuint64_t dims[2] = {(cuuint64_t)m, (cuuint64_t)m};
+    cuuint64_t strides[1] = {(cuuint64_t)m * 2};
+    cuuint32_t box[2] = {(cuuint32_t)BK, (cuuint32_t)box_rows};
+    cuuint32_t estr[2] = {1, 1};
+    return enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (void *)base, dims, strides, box, estr,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+struct StageMaps {
+    Maps s1, s2, s3, s4;
+};
+
+}  // namespace tc
+
+int field_solver_bind_bf16(FieldSolver &f, const __nv_bfloat16 *d_hi, const __nv_bfloat16 *d_lo) {
+    using namespace tc;
+    if (f.m < BM || (f.m % BM) != 0 || !f.C_hi) return AP_ERR_UNSUPPORTED;
+    StageMaps h{};
+    const int m = f.m;
+    bool ok = true;
+    // S1: T = C . d^T          S2: a = C . T^T (spectral epilogue)
+    ok &= make_map(&h.s1.a_hi[0], f.C_hi, m, BM) && make_map(&h.s1.a_lo[0], f.C_lo, m, BM);
+    ok &= make_map(&h.s1.b_hi[0], d_hi, m, BN) && make_map(&h.s1.b_lo[0], d_lo, m, BN);
+    ok &= make_map(&h.s2.a_hi[0], f.C_hi, m, BM) && make_map(&h.s2.a_lo[0], f.C_lo, m, BM);
+    ok &= make_map(&h.s2.b_hi[0], f.b_t_hi, m, BN) && make_map(&h.s2.b_lo[0], f.b_t_lo, m, BN);
+    // S3: Ux = Ct . Px^T, Uy = St . Py^T      S4: Ex = St . Ux^T, Ey = Ct . Uy^T
+    ok &= make_map(&h.s3.a_hi[0], f.Ct_hi, m, BM) && make_map(&h.s3.a_lo[0], f.Ct_lo, m, BM);
+    ok &= make_map(&h.s3.b_hi[0], f.b_px_hi, m, BN) && make_map(&h.s3.b_lo[0], f.b_px_lo, m, BN);
+    ok &= make_map(&h.s3.a_hi[1], f.St_hi, m, BM) && make_map(&h.s3.a_lo[1], f.St_lo, m, BM);
+    ok &= make_map(&h.s3.b_hi[1], f.b_py_hi, m, BN) && make_map(&h.s3.b_lo[1], f.b_py_lo, m, BN);
+    ok &= make_map(&h.s4.a_hi[0], f.St_hi, m, BM) && make_map(&h.s4.a_lo[0], f.St_lo, m, BM);
+    ok &= make_map(&h.s4.b_hi[0], f.b_ux_hi, m, BN) && make_map(&h.s4.b_lo[0], f.b_ux_lo, m, BN);
+    ok &= make_map(&h.s4.a_hi[1], f.Ct_hi, m, BM) && make_map(&h.s4.a_lo[1], f.Ct_lo, m, BM);
+    ok &= make_map(&h.s4.b_hi[1], f.b_uy_hi, m, BN) && make_map(&h.s4.b_lo[1], f.b_uy_lo, m, BN);
+    // the batch-1 slots of S1/S2 repeat batch 0 (never read: those launches have gridDim.z == 1)
+    h.s1.a_hi[1] = h.s1.a_hi[0]; h.s1.a_lo[1] = h.s1.a_lo[0]; h.s1.b_hi[1] = h.s1.b_hi[0]; h.s1.b_lo[1] = h.s1.b_lo[0];
+    h.s2.a_hi[1] = h.s2.a_hi[0]; h.s2.a_lo[1] = h.s2.a_lo[0]; h.s2.b_hi[1] = h.s2.b_hi[0]; h.s2.b_lo[1] = h.s2.b_lo[0];
+    if (!ok) return AP_ERR_UNSUPPORTED;
+    if (!f.tc_maps && !(f.tc_maps = malloc(sizeof(StageMaps)))) return AP_ERR_CUDA;
+    *reinterpret_cast<StageMaps *>(f.tc_maps) = h;
+    if (!f.tc_status && cudaMalloc(&f.tc_status, sizeof(unsigned int)) != cudaSuccess) return AP_ERR_CUDA;
+    if (cudaMemset(f.tc_status, 0, sizeof(unsigned int)) != cudaSuccess) return AP_ERR_CUDA;
+    if (cudaFuncSetAttribute(gemm_bf16x3_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES) !=
+        cudaSuccess)
+        return AP_ERR_CUDA;
+    f.tc_ready = 1;
+    return AP_OK;
+}
 
 int field_solve_bf16x3(FieldSolver &f, const __nv_bfloat16 *d_hi, const __nv_bfloat16 *d_lo, float *ex,
                        float *ey, cudaStream_t st) {
-    (void)f; (void)d_hi; (void)d_lo; (void)ex; (void)ey; (void)st;
-    return AP_ERR_UNSUPPORTED;
+    using namespace tc;
+    (void)d_hi;
+    (void)d_lo;  // bound into the stage-1 tensor maps by field_solver_bind_bf16
+    if (!f.tc_ready) return AP_ERR_UNSUPPORTED;
+    const StageMaps &h = *reinterpret_cast<const StageMaps *>(f.tc_maps);
+    const int m = f.m;
+    Epi e{};
+    e.m = m;
+    e.status = f.tc_status;
+    e.wx = f.wx;
+    e.wy = f.wy;
+    e.scale = 4.0f / ((float)m * (float)m);
+    const dim3 g1(m / BN, m / BM, 1), g2(m / BN, m / BM, 2);
+    e.mode = EPI_SPLIT;
+    e.o_hi[0] = f.b_t_hi;
+    e.o_lo[0] = f.b_t_lo;
+    gemm_bf16x3_kernel<<<g1, THREADS, SMEM_BYTES, st>>>(h.s1, e);
+    e.mode = EPI_SPECTRAL;
+    e.o_hi[0] = f.b_px_hi;
+    e.o_lo[0] = f.b_px_lo;
+    e.o_hi[1] = f.b_py_hi;
+    e.o_lo[1] = f.b_py_lo;
+    gemm_bf16x3_kernel<<<g1, THREADS, SMEM_BYTES, st>>>(h.s2, e);
+    e.mode = EPI_SPLIT;
+    e.o_hi[0] = f.b_ux_hi;
+    e.o_lo[0] = f.b_ux_lo;
+    e.o_hi[1] = f.b_uy_hi;
+    e.o_lo[1] = f.b_uy_lo;
+    gemm_bf16x3_kernel<<<g2, THREADS, SMEM_BYTES, st>>>(h.s3, e);
+    e.mode = EPI_F32;
+    e.o_f32[0] = ex;
+    e.o_f32[1] = ey;
+    gemm_bf16x3_kernel<<<g2, THREADS, SMEM_BYTES, st>>>(h.s4, e);
+    return cudaGetLastError() == cudaSuccess ? AP_OK : AP_ERR_CUDA;
+}
+
+int field_solver_status(FieldSolver &f, unsigned int *out) {
+    if (!f.tc_status) {
+        *out = 0;
+        return AP_OK;
+    }
+    return cudaMemcpy(out, f.tc_status, sizeof(unsigned int), cudaMemcpyDeviceToHost) == cudaSuccess ? AP_OK
+                                                                                               : AP_ERR_CUDA;
 }
 
 }  // namespace ap
