@@ -409,8 +409,8 @@ int ap_params_default(ap_params *p) {
     p->max_iterations = 5000;
     p->check_interval = 16;
     p->use_graph = 1;
-    p->max_backtracks = 10;
-    p->restart_mode = 3;
+    p->max_backtracks = 0;
+    p->restart_mode = 4;
     return AP_OK;
 }
 

@@ -637,8 +637,7 @@ static double lipschitz_step(const or_placer *o, const double *vx, const double 
  * state (u_k, v_k, g_k) with the predicted alpha, evaluates the gradient at
  * the new reference point and re-predicts alpha from the two points; a
  * prediction below 0.95 of the alpha used redoes the step with it (ePlace
- * steplength prediction with backtracking, at most OR_MAX_BACKTRACK redos). */
-#define OR_MAX_BACKTRACK 10
+ * steplength prediction with backtracking, at most max_backtracks redos). */
 void or_step(or_placer *o, int n) {
     const int m = o->n_mov;
     for (int it = 0; it < n; ++it) {
@@ -649,7 +648,7 @@ void or_step(or_placer *o, int n) {
         memcpy(o->vpy, o->y, sizeof(double) * (size_t)m);
         double *tux = dalloc((size_t)m), *tuy = dalloc((size_t)m);
         double alpha = o->alpha, ahat = alpha;
-        for (int bt = 0; bt <= OR_MAX_BACKTRACK; ++bt) {
+        for (int bt = 0; bt <= o->p.max_backtracks; ++bt) {
             for (int i = 0; i < m; ++i) {
                 double nux = clampd(o->vpx[i] - alpha * o->gx[i], 0.0, o->die_w - o->w[i]);
                 double nuy = clampd(o->vpy[i] - alpha * o->gy[i], 0.0, o->die_h - o->h[i]);
@@ -662,7 +661,7 @@ void or_step(or_placer *o, int n) {
             precond_grad(o, o->gpx, o->gpy);
             o->evals++;
             ahat = lipschitz_step(o, o->x, o->y, o->vpx, o->vpy, o->gpx, o->gpy, o->gx, o->gy);
-            if (ahat > 0.95 * alpha || bt == OR_MAX_BACKTRACK) break;
+            if (ahat > 0.95 * alpha || bt == o->p.max_backtracks) break;
             alpha = ahat;
         }
         /* adaptive restart (O'Donoghue & Candes 2015, gradient scheme): the

@@ -97,7 +97,8 @@ typedef struct or_params {
     double ref_delta_hpwl; /* <= 0: 0.1 * nets * bw */
     double mu_max, mu_min;
     double init_step_coef;
-    int restart; /* adaptive momentum restart on (1) or off (0) */
+    int restart;        /* momentum restart: 0 none, 1 gradient, 2 every step, 3 speed, 4 overflow rise */
+    int max_backtracks; /* step re-predictions per iteration */
 } or_params;
 
 typedef struct or_stats {

@@ -45,7 +45,7 @@ class OrParams(C.Structure):
     _fields_ = [("mx", C.c_int), ("my", C.c_int), ("target_density", C.c_double),
                 ("gamma_base_bins", C.c_double), ("init_density_weight", C.c_double),
                 ("ref_delta_hpwl", C.c_double), ("mu_max", C.c_double), ("mu_min", C.c_double),
-                ("init_step_coef", C.c_double), ("restart", C.c_int)]
+                ("init_step_coef", C.c_double), ("restart", C.c_int), ("max_backtracks", C.c_int)]
 
 
 class OrStats(C.Structure):
@@ -213,9 +213,9 @@ class Placer:
 
     def __init__(self, nl: dict, mx: int, target_density: float, gamma_base_bins=4.0,
                  init_density_weight=8e-5, ref_delta_hpwl=0.0, mu_max=1.05, mu_min=0.95,
-                 init_step_coef=0.1, restart=3):
+                 init_step_coef=0.1, restart=4, max_backtracks=0):
         p = OrParams(mx, mx, target_density, gamma_base_bins, init_density_weight, ref_delta_hpwl,
-                     mu_max, mu_min, init_step_coef, restart)
+                     mu_max, mu_min, init_step_coef, restart, max_backtracks)
         self._keep = nl
         die = nl["die"]
         self.h = lib().or_create(len(nl["node_w"]), len(nl["net_ptr"]) - 1, _i32(nl["net_ptr"]),

@@ -39,7 +39,7 @@ def test_library_exports_every_declared_symbol(lib):
 def test_params_default_and_status_strings(lib):
     p = lib.Params()
     assert lib.lib().ap_params_default(C.byref(p)) == 0
-    assert p.bins_x == 512 and p.max_backtracks == 10 and p.restart_mode == 3
+    assert p.bins_x == 512 and p.max_backtracks == 0 and p.restart_mode == 4
     assert lib.lib().ap_status_string(2) == b"malformed netlist"
 
 

@@ -181,3 +181,55 @@ def test_loop_c0_reaches_target_like_oracle(ap, oracle_lib):
     assert s["overflow"] < 0.10 and rs["overflow"] < 0.10
     assert abs(s["hpwl"] - rs["hpwl"]) <= 0.03 * rs["hpwl"], (s, rs)
     assert abs(s["iteration"] - rs["iteration"]) <= 0.2 * rs["iteration"], (s, rs)
+
+
+def density_like(m, rng):
+    """A placement-like density: ~0.8 background, a dense cluster, an empty macro."""
+    d = (0.8 + 0.1 * rng.standard_normal((m, m))).astype(np.float32)
+    d[m // 3: m // 2, m // 4: m // 2] += 2.5
+    d[m // 8: m // 5, m // 8: m // 5] = 0.0
+    return d
+
+
+@pytest.mark.parametrize("m", [128, 256, 512])
+def test_field_bf16x3_against_oracle(ap, oracle_lib, m):
+    """tcgen05 BF16x3 (FP32 accumulate) vs the FP64 oracle: 1e-4 of max."""
+    rng = np.random.default_rng(100 + m)
+    d = density_like(m, rng)
+    nl = ap.synth.generate("c0", seed=1)
+    with ap.Placer(nl, bins=m) as pl:
+        ex, ey = pl.compute_electric_fields(d, "bf16x3")
+        ex2, ey2 = pl.compute_electric_fields(d, "bf16x3")
+    np.testing.assert_array_equal(ex, ex2)  # deterministic
+    rex, rey = oracle_lib.field_solve(d.astype(np.float64), m)
+    for got, ref in ((ex, rex), (ey, rey)):
+        assert np.abs(got - ref).max() <= 1e-4 * np.abs(ref).max()
+
+
+def test_field_bf16x3_full_size_vs_fp32(ap):
+    """1024^2 bins: the tensor-core solve against the FP32 SIMT solve of the
+    same map, and linearity of the transform chain (E(2d) = 2 E(d))."""
+    rng = np.random.default_rng(7)
+    d = density_like(1024, rng)
+    nl = ap.synth.generate("c0", seed=1)
+    with ap.Placer(nl, bins=1024) as pl:
+        ex, ey = pl.compute_electric_fields(d, "bf16x3")
+        fx, fy = pl.compute_electric_fields(d, "fp32")
+        ex2, ey2 = pl.compute_electric_fields(2.0 * d, "bf16x3")
+    for got, ref in ((ex, fx), (ey, fy)):
+        assert np.abs(got - ref).max() <= 1e-4 * np.abs(ref).max()
+    assert np.abs(ex2 - 2 * ex).max() <= 1e-6 * np.abs(ex).max()
+
+
+def test_loop_bf16x3_matches_fp32_loop(ap):
+    """Same netlist, both solvers: the mixed-precision loop reaches the target
+    with HPWL within 1% of the plain FP32 loop."""
+    nl = ap.synth.generate("c1_small", seed=3)
+    res = {}
+    for solver in ("fp32", "bf16x3"):
+        with ap.Placer(nl, bins=128, field_solver=solver, max_iterations=3000) as pl:
+            pl.initialize_placement(seed=5, sigma=1.0)
+            pl.run()
+            res[solver] = pl.stats()
+    assert res["fp32"]["overflow"] < 0.10 and res["bf16x3"]["overflow"] < 0.10, res
+    assert abs(res["bf16x3"]["hpwl"] - res["fp32"]["hpwl"]) <= 0.01 * res["fp32"]["hpwl"], res
