@@ -215,4 +215,98 @@ void field_solve_fp32(FieldSolver &f, const float *d, float *ex, float *ey, cuda
     gemm<false>(m, s4, 2, none, st);
 }
 
+// ---- field solve without allocation -------------------------------------------
+// Some callers cannot allocate device memory at all: code that runs inside a
+// host framework which owns every device allocation and hands out only the
+// buffers it manages, or code on a path where a cudaMalloc would synchronise
+// the device or fail under a fixed memory budget.  For them the FP32 solve
+// also runs from one fixed scratch array in the library's static device
+// memory.  The array holds the transform tables and the intermediate maps of
+// one grid of up to kNoAllocMaxBins x kNoAllocMaxBins bins (8 m^2 + 2 m
+// floats, 2.1 MB at the maximum); every GPU that loads the library keeps it
+// until the process exits.
+
+namespace {
+
+constexpr int kNoAllocMaxBins = 256;
+constexpr size_t kNoAllocFloats = 8ull * kNoAllocMaxBins * kNoAllocMaxBins + 2ull * kNoAllocMaxBins;
+constexpr int kNoAllocMaxDevices = 64;
+
+static __device__ __align__(256) float g_field_scratch[kNoAllocFloats];
+
+// Per device: the device address of g_field_scratch (host code may not use the
+// symbol itself as an address) and the grid whose tables it currently holds.
+struct NoAllocState {
+    float *base;
+    int m;
+    float ratio;
+};
+static NoAllocState g_noalloc_state[kNoAllocMaxDevices];
+
+__global__ void noalloc_tables_kernel(float *C, float *Ct, float *St, float *wx, float *wy, int m, float ratio) {
+    const double pi = 3.14159265358979323846;
+    const int n = m * m;
+    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x) {
+        const int k = idx / m, i = idx % m;
+        double s, c;
+        sincospi((double)k * (i + 0.5) / m, &s, &c);
+        C[(size_t)k * m + i] = (float)c;
+        Ct[(size_t)i * m + k] = (float)c;
+        St[(size_t)i * m + k] = (float)s;
+        if (idx < m) {
+            wx[idx] = (float)(pi * idx / m);
+            wy[idx] = (float)(pi * idx / m * ratio);
+        }
+    }
+}
+
+}  // namespace
+
 }  // namespace ap
+
+// Same result as ap_field_solve with the FP32 solver, on caller-owned device
+// buffers and without allocating.  The first call on a device (and the first
+// call after the bin count or ratio changes) looks up the scratch address with
+// cudaGetSymbolAddress and fills the transform tables; make that first call
+// before any stream capture.  All calls share the one scratch array: calls
+// whose GPU work overlaps (other streams, other threads) race on it.
+extern "C" int ap_field_solve_noalloc(const float *density, float *ex, float *ey, int32_t bins, float bin_ratio,
+                                      void *stream) {
+    using namespace ap;
+    if (!density || !ex || !ey) return AP_ERR_INVALID_ARG;
+    if (bins < 32 || bins > kNoAllocMaxBins || (bins % 32) != 0) return AP_ERR_INVALID_ARG;
+    if (!(bin_ratio > 0.f)) return AP_ERR_INVALID_ARG;
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNoAllocMaxDevices) return AP_ERR_NO_DEVICE;
+    cudaStream_t st = (cudaStream_t)stream;
+    NoAllocState &s = g_noalloc_state[dev];
+    if (!s.base) {
+        void *p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_field_scratch) != cudaSuccess || !p) return AP_ERR_CUDA;
+        s.base = (float *)p;
+        s.m = 0;
+    }
+    const size_t mm = (size_t)bins * bins;
+    FieldSolver f{};
+    f.m = bins;
+    f.bin_ratio = bin_ratio;
+    f.C = s.base;
+    f.Ct = f.C + mm;
+    f.St = f.Ct + mm;
+    f.t0 = f.St + mm;
+    f.px = f.t0 + mm;
+    f.py = f.px + mm;
+    f.ux = f.py + mm;
+    f.uy = f.ux + mm;
+    f.wx = f.uy + mm;
+    f.wy = f.wx + bins;
+    if (s.m != bins || s.ratio != bin_ratio) {
+        noalloc_tables_kernel<<<(int)((mm + 255) / 256), 256, 0, st>>>(f.C, f.Ct, f.St, f.wx, f.wy, bins,
+                                                                      bin_ratio);
+        if (cudaGetLastError() != cudaSuccess) return AP_ERR_CUDA;
+        s.m = bins;
+        s.ratio = bin_ratio;
+    }
+    field_solve_fp32(f, density, ex, ey, st);  // writes every scratch element before reading it
+    return cudaGetLastError() == cudaSuccess ? AP_OK : AP_ERR_CUDA;
+}

@@ -193,6 +193,23 @@ int ap_density_map(ap_handle *h, const float *x, const float *y, int64_t *rho_q)
  * field per bin; the solver is params.field_solver or `solver` if >= 0. */
 int ap_field_solve(ap_handle *h, const float *density, float *ex, float *ey, int32_t solver);
 
+/* Allocation-free field solve.  No counterpart in the reference.  For callers
+ * that cannot allocate device memory -- a host framework that owns every
+ * device allocation and hands out only its own buffers, a fixed memory
+ * budget, a path where cudaMalloc must not run -- this is the FP32 solve of
+ * ap_field_solve on caller-owned DEVICE buffers (density in; ex, ey out;
+ * x-major bins*bins floats) that allocates nothing: its scratch is one fixed
+ * array in the library's static device memory, sized for bins <= 256 (2.1 MB,
+ * held on every GPU that loads the library until the process exits).  bins
+ * must be a multiple of 32 in [32, 256]; other sizes return
+ * AP_ERR_INVALID_ARG.  The first call on a device, and the first after bins
+ * or bin_ratio change, looks the scratch address up and fills its transform
+ * tables: make that call before any stream capture.  All calls share the one
+ * scratch array, so calls whose GPU work overlaps race on it.  Work is
+ * enqueued on `cuda_stream` (a cudaStream_t, NULL = legacy default stream). */
+int ap_field_solve_noalloc(const float *density, float *ex, float *ey, int32_t bins, float bin_ratio,
+                           void *cuda_stream);
+
 /* ---- checkpoint / resume ----------------------------------------------- */
 int ap_snapshot_size(ap_handle *h, size_t *bytes);
 int ap_snapshot(ap_handle *h, void *buf, size_t bytes);
