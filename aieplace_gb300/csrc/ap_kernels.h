@@ -11,23 +11,32 @@ namespace ap {
 // ---- wirelength -------------------------------------------------------------
 enum { WA_OUT_ONLY = 0, WA_LOOP = 1, WA_INIT = 2 };
 
+// Nets are bucketed by degree: [2], [3,4], [5,8] (one thread per net, pins in
+// registers) and > 8 (one warp per net); bucket b spans nets
+// [bucket_lo[b], bucket_lo[b+1]).
+constexpr int kWaBuckets = 4;
+
 struct WaArgs {
-    const int *net_ptr;    // [n_nets + 1], nets of degree 2..8 first
+    const int *net_ptr;    // [n_nets + 1], nets in bucket order
     const int *pin_node;   // internal node ids
     int n_small, n_nets;
+    int bucket_lo[kWaBuckets + 1];
+    int bucket_blocks[kWaBuckets];  // grid of each bucket's launch (filled by the launcher)
     const float *px, *py;  // positions of all nodes (modes other than WA_LOOP)
     const float *pxs[2], *pys[2];  // WA_LOOP: the trial point is buffer [1 - sc->cur]
     float gamma;           // > 0 overrides sc->gamma
     DevScalars *sc;
     ull *gqx, *gqy;        // int64 fixed-point gradient accumulators
     int n_grad;            // nodes [0, n_grad) receive gradient
-    double *partials;      // 2 * (small_grid + large_grid)
+    double *partials;      // 2 per block over all bucket launches
     unsigned int *counter;
-    int small_blocks;
+    int small_blocks;      // blocks of the three thread-per-net launches together
     double *out;           // [2]: HPWL, WA
     int mode;
 };
-void launch_wirelength(const WaArgs &a, int small_grid, int large_grid, cudaStream_t st);
+// launches the four bucket kernels; the last one (warp per net) folds the sums
+void launch_wirelength(const WaArgs &a, cudaStream_t st);
+constexpr int kWaMaxBlocks = 2048;  // per bucket launch
 
 // ---- density scatter (+ Nesterov position update) ---------------------------
 struct ScatterArgs {

@@ -32,11 +32,6 @@ cudaError_t dalloc(T **p, size_t n) {
     return cudaMalloc((void **)p, sizeof(T) * (n ? n : 1));
 }
 
-int max_blocks(int n, int cap) {
-    int b = (n + kThreads - 1) / kThreads;
-    return std::max(1, std::min(b, cap));
-}
-
 }  // namespace
 
 struct ap_handle {
@@ -69,7 +64,7 @@ struct ap_handle {
     unsigned int *d_counters = nullptr;
     double *d_out = nullptr;
     double *h_out = nullptr;  // pinned [4]
-    int wa_small_grid = 1, wa_large_grid = 1;
+    int bucket_lo[kWaBuckets + 1] = {0, 0, 0, 0, 0};
     FieldSolver fs{};
     cudaStream_t stream = nullptr;
     bool own_stream = false;
@@ -145,6 +140,7 @@ WaArgs wa_args(ap_handle *h, const float *px, const float *py, float gamma, int 
     a.net_ptr = h->d_net_ptr;
     a.pin_node = h->d_pin_node;
     a.n_small = h->n_small;
+    for (int b = 0; b <= kWaBuckets; ++b) a.bucket_lo[b] = h->bucket_lo[b];
     a.n_nets = h->n_nets;
     a.px = px;
     a.py = py;
@@ -198,8 +194,7 @@ int enqueue_iteration(ap_handle *h, cudaStream_t st) {
     s.update = 1;
     launch_scatter(s, st);
     launch_rho(rho_args(h, RHO_LOOP, nullptr), st);
-    launch_wirelength(wa_args(h, h->d_px[0], h->d_py[0], 0.f, h->n_mov, WA_LOOP, nullptr), h->wa_small_grid,
-                      h->wa_large_grid, st);
+    launch_wirelength(wa_args(h, h->d_px[0], h->d_py[0], 0.f, h->n_mov, WA_LOOP, nullptr), st);
     int r = run_field(h, h->p.field_solver, st);
     if (r != AP_OK) return r;
     launch_gather(gather_args(h, 0, GATHER_STEP), st);
@@ -216,8 +211,7 @@ int enqueue_eval(ap_handle *h, int at, int rho_mode, int wa_mode, cudaStream_t s
     s.hi = h->n_mov;
     launch_scatter(s, st);
     launch_rho(rho_args(h, rho_mode, h->d_out), st);
-    launch_wirelength(wa_args(h, h->d_px[at], h->d_py[at], 0.f, h->n_mov, wa_mode, h->d_out + 2),
-                      h->wa_small_grid, h->wa_large_grid, st);
+    launch_wirelength(wa_args(h, h->d_px[at], h->d_py[at], 0.f, h->n_mov, wa_mode, h->d_out + 2), st);
     return run_field(h, h->p.field_solver, st);
 }
 
@@ -467,20 +461,29 @@ int ap_create(const ap_netlist *nl, const ap_params *params, ap_handle **out) {
         }
     for (int i = 0; i < N; ++i)
         if (h->ext2int[(size_t)i] != i) h->identity = false;
-    // nets of degree >= 2: degree 2..8 first in degree order, then larger ones
-    std::vector<int> order;
-    for (int e = 0; e < nl->num_nets; ++e)
-        if (nl->net_ptr[e + 1] - nl->net_ptr[e] >= 2) order.push_back(e);
+    // nets of degree >= 2 in degree buckets [2], [3,4], [5,8], [9,...); within a
+    // bucket by their lowest internal node index, so neighbouring threads
+    // gather and accumulate neighbouring nodes
+    auto bucket_of = [](int d) { return d <= 2 ? 0 : (d <= 4 ? 1 : (d <= 8 ? 2 : 3)); };
+    std::vector<int> order, first((size_t)nl->num_nets, 0);
+    for (int e = 0; e < nl->num_nets; ++e) {
+        if (nl->net_ptr[e + 1] - nl->net_ptr[e] < 2) continue;
+        order.push_back(e);
+        int lo = INT32_MAX;
+        for (int q = nl->net_ptr[e]; q < nl->net_ptr[e + 1]; ++q) lo = std::min(lo, h->ext2int[(size_t)nl->pin_node[q]]);
+        first[(size_t)e] = lo;
+    }
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
-        const int da = nl->net_ptr[a + 1] - nl->net_ptr[a], db = nl->net_ptr[b + 1] - nl->net_ptr[b];
-        const int ka = da <= 8 ? da : 9, kb = db <= 8 ? db : 9;
-        return ka < kb;
+        const int ka = bucket_of(nl->net_ptr[a + 1] - nl->net_ptr[a]), kb = bucket_of(nl->net_ptr[b + 1] - nl->net_ptr[b]);
+        return ka != kb ? ka < kb : first[(size_t)a] < first[(size_t)b];
     });
     std::vector<int> net_ptr(1, 0), pin_node;
     std::vector<float> pins((size_t)N, 0.f);
+    for (int b = 0; b <= kWaBuckets; ++b) h->bucket_lo[b] = 0;
     for (int e : order) {
         const int d = nl->net_ptr[e + 1] - nl->net_ptr[e];
         if (d <= 8) h->n_small++;
+        for (int b = bucket_of(d) + 1; b <= kWaBuckets; ++b) h->bucket_lo[b]++;
         for (int q = nl->net_ptr[e]; q < nl->net_ptr[e + 1]; ++q) {
             const int in = h->ext2int[(size_t)nl->pin_node[q]];
             pin_node.push_back(in);
@@ -610,8 +613,6 @@ int ap_create(const ap_netlist *nl, const ap_params *params, ap_handle **out) {
         ap_destroy(h);
         return r;
     }
-    h->wa_small_grid = max_blocks(h->n_small, 4096);
-    h->wa_large_grid = max_blocks((h->n_nets - h->n_small) * 32, 2048);
     if (cudaDeviceSynchronize() != cudaSuccess) {
         ap_destroy(h);
         return AP_ERR_CUDA;
@@ -716,8 +717,7 @@ int ap_profile_stages(ap_handle *h, int32_t n_trials, float *stage_ms, int32_t *
         CK(cudaEventRecord(ev[1], st));
         launch_rho(rho_args(h, RHO_LOOP, nullptr), st);
         CK(cudaEventRecord(ev[2], st));
-        launch_wirelength(wa_args(h, h->d_px[0], h->d_py[0], 0.f, h->n_mov, WA_LOOP, nullptr), h->wa_small_grid,
-                          h->wa_large_grid, st);
+        launch_wirelength(wa_args(h, h->d_px[0], h->d_py[0], 0.f, h->n_mov, WA_LOOP, nullptr), st);
         CK(cudaEventRecord(ev[3], st));
         r = run_field(h, h->p.field_solver, st);
         CK(cudaEventRecord(ev[4], st));
@@ -864,8 +864,7 @@ int ap_wirelength_grad(ap_handle *h, const float *x, const float *y, float gamma
     if (r != AP_OK) return r;
     CK(cudaMemsetAsync(h->d_gqx, 0, sizeof(ull) * h->n_nodes, h->stream));
     CK(cudaMemsetAsync(h->d_gqy, 0, sizeof(ull) * h->n_nodes, h->stream));
-    launch_wirelength(wa_args(h, h->d_sx, h->d_sy, gamma, h->n_nodes, WA_OUT_ONLY, h->d_out),
-                      h->wa_small_grid, h->wa_large_grid, h->stream);
+    launch_wirelength(wa_args(h, h->d_sx, h->d_sy, gamma, h->n_nodes, WA_OUT_ONLY, h->d_out), h->stream);
     CK(cudaGetLastError());
     std::vector<long long> qx((size_t)h->n_nodes), qy((size_t)h->n_nodes);
     CK(cudaMemcpyAsync(qx.data(), h->d_gqx, sizeof(ull) * h->n_nodes, cudaMemcpyDeviceToHost, h->stream));

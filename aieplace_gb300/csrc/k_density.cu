@@ -37,8 +37,37 @@ __device__ __forceinline__ double block_max(double v, double *smem) {
 
 }  // namespace
 
+// Each block owns a contiguous chunk of kScatterChunk nodes.  Nodes with
+// nearby indices share nets and sit close together, so a chunk's bins usually
+// span a small rectangle: when that rectangle fits kScatterWindow bins the
+// block accumulates in shared memory and adds only its non-zero bins to the
+// global map (one global atomic per bin and block instead of one per node
+// and bin -- right after initial placement every node sits in a few bins).
+// Integer sums make both paths give the same map bit for bit.
+constexpr int kScatterPerThread = 8;
+constexpr int kScatterChunk = kThreads * kScatterPerThread;
+constexpr int kScatterWindow = 4096;
+
+template <typename F>
+__device__ __forceinline__ void for_each_overlap(const Grid &g, float x, float y, float w, float h, F &&f) {
+    int c0, c1, r0, r1;
+    bool small;
+    if (!bin_range(g, x, y, w, h, c0, c1, r0, r1, small)) return;
+    const long long xq = to_q(x), yq = to_q(y), wq = to_q(w), hq = to_q(h);
+    if (small) {
+        f(c0, r0, wq * hq);
+        return;
+    }
+    for (int c = c0; c <= c1; ++c) {
+        const long long ow = overlap_1d((long long)c * g.bw_q, g.bw_q, xq, wq);
+        for (int r = r0; r <= r1; ++r) f(c, r, ow * overlap_1d((long long)r * g.bh_q, g.bh_q, yq, hq));
+    }
+}
+
 __global__ void __launch_bounds__(kThreads) scatter_kernel(ScatterArgs a) {
     __shared__ double red[32];
+    __shared__ int box[4];  // bin bounding box of the chunk: c0, c1, r0, r1
+    __shared__ ull win[kScatterWindow];
     const int n = a.update ? a.n_mov : (a.hi - a.lo);
     float alpha = 0.f, mom = 0.f;
     int cur = 0;
@@ -49,8 +78,22 @@ __global__ void __launch_bounds__(kThreads) scatter_kernel(ScatterArgs a) {
     }
     const int nxt = 1 - cur;
     const Grid g = a.g;
+    if (threadIdx.x == 0) {
+        box[0] = box[2] = 0x7fffffff;
+        box[1] = box[3] = -1;
+    }
+    __syncthreads();
     double du = 0.0;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    float px[kScatterPerThread], py[kScatterPerThread], pw[kScatterPerThread], ph[kScatterPerThread];
+    int bc0 = 0x7fffffff, bc1 = -1, br0 = 0x7fffffff, br1 = -1;
+    const int base = blockIdx.x * kScatterChunk;
+#pragma unroll
+    for (int k = 0; k < kScatterPerThread; ++k) {
+        const int i = base + k * kThreads + threadIdx.x;
+        pw[k] = 0.f;  // zero area: nothing to scatter
+        ph[k] = 0.f;
+        px[k] = py[k] = 0.f;
+        if (i >= n) continue;
         const int node = a.update ? i : a.lo + i;
         const float w = __ldg(a.w + node), h = __ldg(a.h + node);
         float x, y;
@@ -70,20 +113,50 @@ __global__ void __launch_bounds__(kThreads) scatter_kernel(ScatterArgs a) {
             x = __ldg(a.px + node);
             y = __ldg(a.py + node);
         }
+        px[k] = x;
+        py[k] = y;
+        pw[k] = w;
+        ph[k] = h;
         int c0, c1, r0, r1;
         bool small;
-        if (!bin_range(g, x, y, w, h, c0, c1, r0, r1, small)) continue;
-        const long long xq = to_q(x), yq = to_q(y), wq = to_q(w), hq = to_q(h);
-        if (small) {
-            atomicAdd(a.rho_q + (long long)c0 * g.my + r0, (ull)(wq * hq));
-            continue;
+        if (bin_range(g, x, y, w, h, c0, c1, r0, r1, small)) {
+            bc0 = min(bc0, c0);
+            bc1 = max(bc1, c1);
+            br0 = min(br0, r0);
+            br1 = max(br1, r1);
         }
-        for (int c = c0; c <= c1; ++c) {
-            const long long ow = overlap_1d((long long)c * g.bw_q, g.bw_q, xq, wq);
-            for (int r = r0; r <= r1; ++r) {
-                const long long oh = overlap_1d((long long)r * g.bh_q, g.bh_q, yq, hq);
-                atomicAdd(a.rho_q + (long long)c * g.my + r, (ull)(ow * oh));
-            }
+    }
+    if (bc1 >= 0) {
+        atomicMin(box + 0, bc0);
+        atomicMax(box + 1, bc1);
+        atomicMin(box + 2, br0);
+        atomicMax(box + 3, br1);
+    }
+    __syncthreads();
+    const int wc0 = box[0], wr0 = box[2];
+    const int wc = box[1] - wc0 + 1, wr = box[3] - wr0 + 1;
+    const bool use_win = box[1] >= 0 && (long long)wc * wr <= kScatterWindow;
+    if (use_win) {
+        for (int t = threadIdx.x; t < wc * wr; t += kThreads) win[t] = 0ull;
+        __syncthreads();
+    }
+#pragma unroll
+    for (int k = 0; k < kScatterPerThread; ++k) {
+        if (use_win) {
+            for_each_overlap(g, px[k], py[k], pw[k], ph[k], [&](int c, int r, long long v) {
+                atomicAdd(win + (c - wc0) * wr + (r - wr0), (ull)v);
+            });
+        } else {
+            for_each_overlap(g, px[k], py[k], pw[k], ph[k], [&](int c, int r, long long v) {
+                atomicAdd(a.rho_q + (long long)c * g.my + r, (ull)v);
+            });
+        }
+    }
+    if (use_win) {
+        __syncthreads();
+        for (int t = threadIdx.x; t < wc * wr; t += kThreads) {
+            const ull v = win[t];
+            if (v) atomicAdd(a.rho_q + (long long)(wc0 + t / wr) * g.my + (wr0 + t % wr), v);
         }
     }
     if (!a.update) return;
@@ -101,8 +174,7 @@ __global__ void __launch_bounds__(kThreads) scatter_kernel(ScatterArgs a) {
 void launch_scatter(const ScatterArgs &a, cudaStream_t st) {
     const int n = a.update ? a.n_mov : (a.hi - a.lo);
     if (n <= 0) return;
-    int blocks = (n + kThreads - 1) / kThreads;
-    if (a.update && blocks > 4096) blocks = 4096;
+    const int blocks = (n + kScatterChunk - 1) / kScatterChunk;  // <= 8192 partials for 16M nodes
     scatter_kernel<<<blocks, kThreads, 0, st>>>(a);
 }
 

@@ -91,7 +91,8 @@ __device__ __forceinline__ void net_thread(const int *__restrict__ pins, int d, 
 
 }  // namespace
 
-// Nets [0, n_small) have degree 2..8 and sit in degree order.
+// Bucket B (degree <= D) of the thread-per-net nets: registers sized for D.
+template <int D, int B>
 __global__ void __launch_bounds__(kThreads) wa_small_kernel(WaArgs a) {
     __shared__ double red[32];
     const float gamma = a.gamma > 0.f ? a.gamma : (float)a.sc->gamma;
@@ -103,21 +104,20 @@ __global__ void __launch_bounds__(kThreads) wa_small_kernel(WaArgs a) {
         py = a.pys[t];
     }
     double hp = 0.0, wa = 0.0;
-    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < a.n_small; e += gridDim.x * blockDim.x) {
+    const int hi = a.bucket_lo[B + 1];
+    for (int e = a.bucket_lo[B] + blockIdx.x * blockDim.x + threadIdx.x; e < hi; e += gridDim.x * blockDim.x) {
         const int s = __ldg(a.net_ptr + e);
         const int d = __ldg(a.net_ptr + e + 1) - s;
-        if (d <= 2)
-            net_thread<2>(a.pin_node + s, d, px, py, inv_g, a.gqx, a.gqy, a.n_grad, hp, wa);
-        else if (d <= 4)
-            net_thread<4>(a.pin_node + s, d, px, py, inv_g, a.gqx, a.gqy, a.n_grad, hp, wa);
-        else
-            net_thread<8>(a.pin_node + s, d, px, py, inv_g, a.gqx, a.gqy, a.n_grad, hp, wa);
+        net_thread<D>(a.pin_node + s, d, px, py, inv_g, a.gqx, a.gqy, a.n_grad, hp, wa);
     }
     hp = block_sum(hp, red);
     wa = block_sum(wa, red);
+    int off = 0;
+#pragma unroll
+    for (int b = 0; b < B; ++b) off += a.bucket_blocks[b];
     if (threadIdx.x == 0) {
-        a.partials[2 * blockIdx.x] = hp;
-        a.partials[2 * blockIdx.x + 1] = wa;
+        a.partials[2 * (off + blockIdx.x)] = hp;
+        a.partials[2 * (off + blockIdx.x) + 1] = wa;
     }
 }
 
@@ -136,7 +136,7 @@ __global__ void __launch_bounds__(kThreads) wa_large_kernel(WaArgs a) {
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
     double hp = 0.0, wa = 0.0;
-    for (int e = a.n_small + warp; e < a.n_nets; e += nwarps) {
+    for (int e = a.bucket_lo[3] + warp; e < a.bucket_lo[4]; e += nwarps) {
         const int s = __ldg(a.net_ptr + e), d = __ldg(a.net_ptr + e + 1) - s;
         float xmx = -3.0e38f, xmn = 3.0e38f, ymx = -3.0e38f, ymn = 3.0e38f;
         for (int j = lane; j < d; j += 32) {
@@ -234,11 +234,19 @@ __global__ void __launch_bounds__(kThreads) wa_large_kernel(WaArgs a) {
     }
 }
 
-void launch_wirelength(const WaArgs &a0, int small_grid, int large_grid, cudaStream_t st) {
+void launch_wirelength(const WaArgs &a0, cudaStream_t st) {
     WaArgs a = a0;
-    a.small_blocks = small_grid;
-    wa_small_kernel<<<small_grid, kThreads, 0, st>>>(a);
-    wa_large_kernel<<<large_grid, kThreads, 0, st>>>(a);
+    auto grid = [](int items) {
+        int b = (items + kThreads - 1) / kThreads;
+        return b < 1 ? 1 : (b > kWaMaxBlocks ? kWaMaxBlocks : b);
+    };
+    for (int b = 0; b < 3; ++b) a.bucket_blocks[b] = grid(a.bucket_lo[b + 1] - a.bucket_lo[b]);
+    a.bucket_blocks[3] = grid((a.bucket_lo[4] - a.bucket_lo[3]) * 32);
+    a.small_blocks = a.bucket_blocks[0] + a.bucket_blocks[1] + a.bucket_blocks[2];
+    wa_small_kernel<2, 0><<<a.bucket_blocks[0], kThreads, 0, st>>>(a);
+    wa_small_kernel<4, 1><<<a.bucket_blocks[1], kThreads, 0, st>>>(a);
+    wa_small_kernel<8, 2><<<a.bucket_blocks[2], kThreads, 0, st>>>(a);
+    wa_large_kernel<<<a.bucket_blocks[3], kThreads, 0, st>>>(a);
 }
 
 }  // namespace ap

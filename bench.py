@@ -34,7 +34,7 @@ sys.path.insert(0, os.path.join(HERE, "oracle"))
 
 METRIC = "Nesterov iters/s & time-to-10% overflow, 2M cells: mixed+surrogate vs plain"
 UNIT = "iters/s"
-KERNELS_PER_TRIAL = 9  # scatter, rho, 2x WA, 4x field, gather
+KERNELS_PER_TRIAL = 11  # scatter, rho, 4x WA (degree buckets), 4x field, gather
 STAGES = ["scatter+update", "density+overflow", "wirelength", "field", "gather+control"]
 
 
@@ -208,6 +208,30 @@ def reference_arm(args):
     print(json.dumps(line), flush=True)
 
 
+def profile_mode(args):
+    """A capture target for ncu: the workload after `profile_after` iterations."""
+    import torch
+
+    import aieplace_gb300 as ap
+    from aieplace_gb300 import build as b
+
+    b.build()
+    nl = ap.synth.generate(args.preset, seed=1)
+    solver = "fp32" if args.solver == "fp32" else "bf16x3"
+    with ap.Placer(nl, field_solver=solver) as pl:
+        pl.initialize_placement(seed=11, sigma=1.0)
+        if args.profile_after:
+            pl.perform_iteration(args.profile_after)
+        torch.cuda.synchronize()
+        torch.cuda.nvtx.range_push("ap_profile")
+        ms = pl.profile_stages(1)
+        torch.cuda.nvtx.range_pop()
+        torch.cuda.synchronize()
+        s = pl.stats()
+    print(json.dumps({"profile_after": args.profile_after, "stage_ms": dict(zip(STAGES, ms)),
+                      "overflow": s["overflow"], "iteration": s["iteration"]}))
+
+
 def time_to_target(ap, nl, solver, target=0.10, max_iter=4000):
     import torch
 
@@ -234,10 +258,15 @@ def main():
     ap_.add_argument("--solver", default="auto", choices=["auto", "fp32", "bf16x3"])
     ap_.add_argument("--no-cpu-baseline", action="store_true")
     ap_.add_argument("--no-ttt", action="store_true", help="skip the time-to-10%% runs")
+    ap_.add_argument("--profile-after", type=int, default=-1,
+                     help="profiling mode: run this many iterations, then one eager trial step inside the "
+                          "NVTX range 'ap_profile' (for ncu --nvtx-include ap_profile/), print nothing else")
     args = ap_.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
         return reference_arm(args)
+    if args.profile_after >= 0:
+        return profile_mode(args)
 
     import numpy as np
     import torch
