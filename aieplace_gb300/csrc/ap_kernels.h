@@ -70,6 +70,7 @@ struct RhoArgs {
     const long long *fixs_q;    // fixed nodes scaled by rho_t
     long long cap_q, ab_q;
     double inv_ab;
+    float inv_ab_f;             // (float)(1 / ab_q): density = (float)tot * inv_ab_f
     float *d_f32;               // FP32 solver input, or null
     __nv_bfloat16 *d_hi, *d_lo; // BF16x3 solver input, or null
     DevScalars *sc;

@@ -120,6 +120,7 @@ RhoArgs rho_args(ap_handle *h, int mode, double *out) {
     a.cap_q = h->cap_q;
     a.ab_q = h->ab_q;
     a.inv_ab = h->inv_ab;
+    a.inv_ab_f = (float)h->inv_ab;
     if (h->p.field_solver == AP_FIELD_BF16X3) {
         a.d_hi = h->d_dens_hi;
         a.d_lo = h->d_dens_lo;

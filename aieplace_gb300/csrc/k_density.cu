@@ -83,7 +83,7 @@ __global__ void __launch_bounds__(kThreads) scatter_kernel(ScatterArgs a) {
         box[1] = box[3] = -1;
     }
     __syncthreads();
-    double du = 0.0;
+    float du = 0.f;  // per-thread partial in FP32; FP64 from the block sum on
     float px[kScatterPerThread], py[kScatterPerThread], pw[kScatterPerThread], ph[kScatterPerThread];
     int bc0 = 0x7fffffff, bc1 = -1, br0 = 0x7fffffff, br1 = -1;
     const int base = blockIdx.x * kScatterChunk;
@@ -108,7 +108,7 @@ __global__ void __launch_bounds__(kThreads) scatter_kernel(ScatterArgs a) {
             a.uy[nxt][i] = nuy;
             a.vx[nxt][i] = x;
             a.vy[nxt][i] = y;
-            du += (double)((nux - ux) * (nux - ux) + (nuy - uy) * (nuy - uy));
+            du += (nux - ux) * (nux - ux) + (nuy - uy) * (nuy - uy);
         } else {
             x = __ldg(a.px + node);
             y = __ldg(a.py + node);
@@ -160,8 +160,8 @@ __global__ void __launch_bounds__(kThreads) scatter_kernel(ScatterArgs a) {
         }
     }
     if (!a.update) return;
-    du = block_sum(du, red);
-    if (threadIdx.x == 0) a.partials[blockIdx.x] = du;
+    const double dub = block_sum((double)du, red);
+    if (threadIdx.x == 0) a.partials[blockIdx.x] = dub;
     if (arrive_last(a.counter)) {
         const double t = reduce_partials(a.partials, gridDim.x, red);
         if (threadIdx.x == 0) {
@@ -195,7 +195,7 @@ __global__ void __launch_bounds__(kThreads) rho_kernel(RhoArgs a) {
         over += t > 0 ? t : 0;
         const long long ab = mov + a.fix_q[b] - a.ab_q;
         over_abs += ab > 0 ? ab : 0;
-        const float d = (float)((double)tot * a.inv_ab);
+        const float d = __ll2float_rn(tot) * a.inv_ab_f;  // same float ops as or_density_float
         if (a.d_f32) a.d_f32[b] = d;
         if (a.d_hi) {
             const __nv_bfloat16 hi = __float2bfloat16_rn(d);
@@ -297,7 +297,9 @@ __global__ void __launch_bounds__(kThreads) gather_kernel(GatherArgs a) {
     const float *vx = a.vx[at], *vy = a.vy[at], *vpx = a.vx[1 - at], *vpy = a.vy[1 - at];
     float *gx_out = a.gx[at], *gy_out = a.gy[at];
     const float *gpx = a.gx[1 - at], *gpy = a.gy[1 - at];
-    double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+    // per-thread partials in FP32 (a thread owns a couple of nodes); FP64 from
+    // the block sums on -- the FP64 pipe of this part is narrow
+    float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n_mov; i += gridDim.x * blockDim.x) {
         const float x = vx[i], y = vy[i];
         const float w = __ldg(a.w + i), h = __ldg(a.h + i);
@@ -332,8 +334,8 @@ __global__ void __launch_bounds__(kThreads) gather_kernel(GatherArgs a) {
         const float wlx = __ll2float_rn((long long)a.gqx[i]) * kInvGradScale;
         const float wly = __ll2float_rn((long long)a.gqy[i]) * kInvGradScale;
         if (a.mode == GATHER_INIT_NORMS) {
-            s2 += (double)(fabsf(wlx) + fabsf(wly));
-            s3 += (double)(fabsf(fx) + fabsf(fy));
+            s2 += fabsf(wlx) + fabsf(wly);
+            s3 += fabsf(fx) + fabsf(fy);
             continue;
         }
         a.gqx[i] = 0ull;
@@ -343,26 +345,26 @@ __global__ void __launch_bounds__(kThreads) gather_kernel(GatherArgs a) {
         gx_out[i] = gx;
         gy_out[i] = gy;
         if (a.mode == GATHER_INIT_GRAD) {
-            s2 = fmax(s2, (double)fmaxf(fabsf(gx), fabsf(gy)));
+            s2 = fmaxf(s2, fmaxf(fabsf(gx), fabsf(gy)));
         } else {
             const float dx = x - vpx[i], dy = y - vpy[i];
             const float ddx = gx - gpx[i], ddy = gy - gpy[i];
-            s0 += (double)(dx * dx + dy * dy);
-            s1 += (double)(ddx * ddx + ddy * ddy);
+            s0 += dx * dx + dy * dy;
+            s1 += ddx * ddx + ddy * ddy;
         }
     }
     if (a.mode == GATHER_FORCE_ONLY) return;
     const bool is_max = a.mode == GATHER_INIT_GRAD;
-    s0 = block_sum(s0, red);
-    s1 = block_sum(s1, red);
-    s2 = is_max ? block_max(s2, red) : block_sum(s2, red);
-    s3 = block_sum(s3, red);
+    const double b0 = block_sum((double)s0, red);
+    const double b1 = block_sum((double)s1, red);
+    const double b2 = is_max ? block_max((double)s2, red) : block_sum((double)s2, red);
+    const double b3 = block_sum((double)s3, red);
     if (threadIdx.x == 0) {
         double *p = a.partials + 4 * blockIdx.x;
-        p[0] = s0;
-        p[1] = s1;
-        p[2] = s2;
-        p[3] = s3;
+        p[0] = b0;
+        p[1] = b1;
+        p[2] = b2;
+        p[3] = b3;
     }
     if (arrive_last(a.counter)) {
         double t0 = 0.0, t1 = 0.0, t2 = 0.0, t3 = 0.0;

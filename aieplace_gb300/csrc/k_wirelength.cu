@@ -30,7 +30,7 @@ struct AxisTerms {
 template <int D>
 __device__ __forceinline__ void net_thread(const int *__restrict__ pins, int d, const float *__restrict__ px,
                                            const float *__restrict__ py, float inv_g, ull *gqx, ull *gqy,
-                                           int n_grad, double &hp_acc, double &wa_acc) {
+                                           int n_grad, float &hp_acc, float &wa_acc) {
     int node[D];
     float xs[D], ys[D];
     float xmx = -3.0e38f, xmn = 3.0e38f, ymx = -3.0e38f, ymn = 3.0e38f;
@@ -85,8 +85,8 @@ __device__ __forceinline__ void net_thread(const int *__restrict__ pins, int d, 
             }
         }
     }
-    hp_acc += (double)((xmx - xmn) + (ymx - ymn));
-    wa_acc += (double)wa_net;
+    hp_acc += (xmx - xmn) + (ymx - ymn);
+    wa_acc += wa_net;
 }
 
 }  // namespace
@@ -103,15 +103,17 @@ __global__ void __launch_bounds__(kThreads) wa_small_kernel(WaArgs a) {
         px = a.pxs[t];
         py = a.pys[t];
     }
-    double hp = 0.0, wa = 0.0;
+    // per-thread partials in FP32 (a thread owns a few nets), FP64 from the
+    // block sum on: the FP64 pipe of this part is narrow
+    float hpf = 0.f, waf = 0.f;
     const int hi = a.bucket_lo[B + 1];
     for (int e = a.bucket_lo[B] + blockIdx.x * blockDim.x + threadIdx.x; e < hi; e += gridDim.x * blockDim.x) {
         const int s = __ldg(a.net_ptr + e);
         const int d = __ldg(a.net_ptr + e + 1) - s;
-        net_thread<D>(a.pin_node + s, d, px, py, inv_g, a.gqx, a.gqy, a.n_grad, hp, wa);
+        net_thread<D>(a.pin_node + s, d, px, py, inv_g, a.gqx, a.gqy, a.n_grad, hpf, waf);
     }
-    hp = block_sum(hp, red);
-    wa = block_sum(wa, red);
+    const double hp = block_sum((double)hpf, red);
+    const double wa = block_sum((double)waf, red);
     int off = 0;
 #pragma unroll
     for (int b = 0; b < B; ++b) off += a.bucket_blocks[b];
@@ -135,7 +137,9 @@ __global__ void __launch_bounds__(kThreads) wa_large_kernel(WaArgs a) {
     const int lane = threadIdx.x & 31;
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
-    double hp = 0.0, wa = 0.0;
+    // per-thread partials in FP32 (a thread owns a few nets), FP64 from the
+    // block sum on: the FP64 pipe of this part is narrow
+    float hpf = 0.f, waf = 0.f;
     for (int e = a.bucket_lo[3] + warp; e < a.bucket_lo[4]; e += nwarps) {
         const int s = __ldg(a.net_ptr + e), d = __ldg(a.net_ptr + e + 1) - s;
         float xmx = -3.0e38f, xmn = 3.0e38f, ymx = -3.0e38f, ymn = 3.0e38f;
@@ -194,12 +198,12 @@ __global__ void __launch_bounds__(kThreads) wa_large_kernel(WaArgs a) {
             atomicAdd(a.gqy + n, (ull)__float2ll_rn(g[1] * kGradScale));
         }
         if (lane == 0) {
-            hp += (double)((xmx - xmn) + (ymx - ymn));
-            wa += (double)(((xmx - xmn) + t[0].wp - t[0].wm) + ((ymx - ymn) + t[1].wp - t[1].wm));
+            hpf += (xmx - xmn) + (ymx - ymn);
+            waf += ((xmx - xmn) + t[0].wp - t[0].wm) + ((ymx - ymn) + t[1].wp - t[1].wm);
         }
     }
-    hp = block_sum(hp, red);
-    wa = block_sum(wa, red);
+    const double hp = block_sum((double)hpf, red);
+    const double wa = block_sum((double)waf, red);
     double *part = a.partials + 2 * a.small_blocks;
     if (threadIdx.x == 0) {
         part[2 * blockIdx.x] = hp;

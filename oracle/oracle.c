@@ -235,10 +235,10 @@ void or_overflow(const or_grid *g, const int64_t *mov_q, const int64_t *fixed_q,
 
 void or_density_float(const or_grid *g, const int64_t *mov_q, const int64_t *fixed_scaled_q,
                       float *d) {
-    const double inv_ab = 1.0 / (double)(g->bw_q * g->bh_q);
+    const float inv_ab = (float)(1.0 / (double)(g->bw_q * g->bh_q));
     const int nb = g->mx * g->my;
     for (int b = 0; b < nb; ++b)
-        d[b] = (float)((double)(mov_q[b] + (fixed_scaled_q ? fixed_scaled_q[b] : 0)) * inv_ab);
+        d[b] = (float)(mov_q[b] + (fixed_scaled_q ? fixed_scaled_q[b] : 0)) * inv_ab;
 }
 
 /* ---- spectral solve ---------------------------------------------------- */

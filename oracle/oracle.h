@@ -72,7 +72,7 @@ void or_overflow(const or_grid *g, const int64_t *mov_q, const int64_t *fixed_q,
 /* fixed_scaled_q[b] = llrint(rho_t * fixed_q[b]) */
 void or_scale_fixed(int nbins, const int64_t *fixed_q, double rho_t, int64_t *out);
 
-/* density d_b = (float)((double)tot_q * (1 / A_b_q)) as the solver input */
+/* density d_b = (float)tot_q * (float)(1 / A_b_q) (FP32 ops) as the solver input */
 void or_density_float(const or_grid *g, const int64_t *mov_q, const int64_t *fixed_scaled_q,
                       float *d);
 
