@@ -9,8 +9,11 @@ namespace ap {
 typedef unsigned long long ull;
 
 constexpr float kCoordScale = 65536.0f;                 // 2^16, coordinates
-constexpr float kGradScale = 4294967296.0f;             // 2^32, WA gradient accumulators
-constexpr float kInvGradScale = 1.0f / 4294967296.0f;
+// WA gradient: each pin's contribution is rounded to 2^-24 in int32 (|g| is
+// below 2 for a WA partial) and accumulated per node in int64
+constexpr float kGradScale = 16777216.0f;               // 2^24
+constexpr float kInvGradScale = 1.0f / 16777216.0f;
+constexpr float kGradClamp = 127.0f;                    // keeps g * 2^24 inside int32
 constexpr int kThreads = 256;
 
 // FP64 scalars of the optimiser; live in device memory so a whole iteration
@@ -54,7 +57,25 @@ struct Grid {
     long long bw_q, bh_q;
 };
 
-__device__ __forceinline__ long long to_q(float v) { return __float2ll_rn(__fmul_rn(v, kCoordScale)); }
+// Round-to-nearest conversion of v * 2^16 to an integer.  In int32 range the
+// 32-bit conversion gives the same integer as the 64-bit one and stays off the
+// FP64 pipe, which executes 64-bit integer conversions.
+__device__ __forceinline__ long long to_q(float v) {
+    const float s = __fmul_rn(v, kCoordScale);
+    if (fabsf(s) < 2147483520.0f) return (long long)__float2int_rn(s);
+    return __float2ll_rn(s);
+}
+
+// float of an int64 fixed-point value through two 32-bit conversions (within
+// one ulp of the correctly rounded conversion)
+__device__ __forceinline__ float i64_to_float(long long q) {
+    return fmaf(__int2float_rn((int)(q >> 32)), 4294967296.0f, __uint2float_rn((unsigned)q));
+}
+
+// per-pin WA contribution in the int64 accumulators' fixed point
+__device__ __forceinline__ ull grad_q(float g) {
+    return (ull)(long long)__float2int_rn(fminf(fmaxf(g, -kGradClamp), kGradClamp) * kGradScale);
+}
 
 // The bins a node touches under the reference rules (Grid.cpp:38-110,
 // Node.h:100-104); exactly the arithmetic of or_density_q.  Returns false if

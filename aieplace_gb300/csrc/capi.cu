@@ -877,8 +877,8 @@ int ap_wirelength_grad(ap_handle *h, const float *x, const float *y, float gamma
     if (r != AP_OK) return r;
     for (int i = 0; i < h->n_nodes; ++i) {
         const int e = h->int2ext[(size_t)i];
-        gx[e] = (float)ldexp((double)qx[(size_t)i], -32);
-        gy[e] = (float)ldexp((double)qy[(size_t)i], -32);
+        gx[e] = (float)ldexp((double)qx[(size_t)i], -24);  // kGradScale = 2^24
+        gy[e] = (float)ldexp((double)qy[(size_t)i], -24);
     }
     if (hpwl) *hpwl = h->h_out[0];
     if (wa) *wa = h->h_out[1];

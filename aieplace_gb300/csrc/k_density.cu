@@ -187,20 +187,32 @@ __device__ __forceinline__ double gamma_of(const DevScalars *sc, double tau) {
 __global__ void __launch_bounds__(kThreads) rho_kernel(RhoArgs a) {
     __shared__ long long red[32];
     long long over = 0, over_abs = 0;
-    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < a.nbins; b += gridDim.x * blockDim.x) {
-        const long long mov = (long long)a.mov_q[b];
-        a.mov_q[b] = 0ull;
-        const long long tot = mov + a.fixs_q[b];
-        const long long t = tot - a.cap_q;
-        over += t > 0 ? t : 0;
-        const long long ab = mov + a.fix_q[b] - a.ab_q;
-        over_abs += ab > 0 ? ab : 0;
-        const float d = __ll2float_rn(tot) * a.inv_ab_f;  // same float ops as or_density_float
-        if (a.d_f32) a.d_f32[b] = d;
+    // two bins per thread and step: 16-byte loads of the int64 maps
+    const int npairs = a.nbins >> 1;
+    longlong2 *mov2 = reinterpret_cast<longlong2 *>(a.mov_q);
+    const longlong2 *fs2 = reinterpret_cast<const longlong2 *>(a.fixs_q);
+    const longlong2 *fx2 = reinterpret_cast<const longlong2 *>(a.fix_q);
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < npairs; p += gridDim.x * blockDim.x) {
+        const longlong2 mov = mov2[p];
+        mov2[p] = make_longlong2(0, 0);
+        const longlong2 fs = fs2[p], fx = fx2[p];
+        const long long m[2] = {mov.x, mov.y}, s[2] = {fs.x, fs.y}, f[2] = {fx.x, fx.y};
+        float d[2];
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+            const long long tot = m[k] + s[k];
+            const long long t = tot - a.cap_q;
+            over += t > 0 ? t : 0;
+            const long long ab = m[k] + f[k] - a.ab_q;
+            over_abs += ab > 0 ? ab : 0;
+            d[k] = __ll2float_rn(tot) * a.inv_ab_f;  // same float ops as or_density_float
+        }
+        if (a.d_f32) reinterpret_cast<float2 *>(a.d_f32)[p] = make_float2(d[0], d[1]);
         if (a.d_hi) {
-            const __nv_bfloat16 hi = __float2bfloat16_rn(d);
-            a.d_hi[b] = hi;
-            a.d_lo[b] = __float2bfloat16_rn(d - __bfloat162float(hi));
+            const __nv_bfloat16 h0 = __float2bfloat16_rn(d[0]), h1 = __float2bfloat16_rn(d[1]);
+            reinterpret_cast<__nv_bfloat162 *>(a.d_hi)[p] = __halves2bfloat162(h0, h1);
+            reinterpret_cast<__nv_bfloat162 *>(a.d_lo)[p] = __floats2bfloat162_rn(
+                d[0] - __bfloat162float(h0), d[1] - __bfloat162float(h1));
         }
     }
     over = block_sum(over, red);
@@ -240,8 +252,8 @@ __global__ void __launch_bounds__(kThreads) rho_kernel(RhoArgs a) {
 }
 
 void launch_rho(const RhoArgs &a, cudaStream_t st) {
-    int blocks = (a.nbins + kThreads - 1) / kThreads;
-    if (blocks > 2048) blocks = 2048;
+    int blocks = (a.nbins / 2 + kThreads - 1) / kThreads;
+    if (blocks > 608) blocks = 608;  // 4 blocks per SM: each thread walks several bin pairs
     rho_kernel<<<blocks, kThreads, 0, st>>>(a);
 }
 
@@ -310,7 +322,8 @@ __global__ void __launch_bounds__(kThreads) gather_kernel(GatherArgs a) {
             const long long xq = to_q(x), yq = to_q(y), wq = to_q(w), hq = to_q(h);
             if (small) {
                 const long long b = (long long)c0 * g.my + r0;
-                const float wt = (float)(wq * hq) * g.inv_ab;
+                // both sides exact in float: one rounding, = (float)(wq * hq)
+                const float wt = (__int2float_rn((int)wq) * __int2float_rn((int)hq)) * g.inv_ab;
                 fx = wt * __ldg(a.ex + b);
                 fy = wt * __ldg(a.ey + b);
             } else {
@@ -319,7 +332,7 @@ __global__ void __launch_bounds__(kThreads) gather_kernel(GatherArgs a) {
                     for (int r = r0; r <= r1; ++r) {
                         const long long oh = overlap_1d((long long)r * g.bh_q, g.bh_q, yq, hq);
                         const long long b = (long long)c * g.my + r;
-                        const float wt = (float)(ow * oh) * g.inv_ab;
+                        const float wt = (__int2float_rn((int)ow) * __int2float_rn((int)oh)) * g.inv_ab;
                         fx += wt * __ldg(a.ex + b);
                         fy += wt * __ldg(a.ey + b);
                     }
@@ -331,8 +344,8 @@ __global__ void __launch_bounds__(kThreads) gather_kernel(GatherArgs a) {
             a.fy[i] = fy;
             continue;
         }
-        const float wlx = __ll2float_rn((long long)a.gqx[i]) * kInvGradScale;
-        const float wly = __ll2float_rn((long long)a.gqy[i]) * kInvGradScale;
+        const float wlx = i64_to_float((long long)a.gqx[i]) * kInvGradScale;
+        const float wly = i64_to_float((long long)a.gqy[i]) * kInvGradScale;
         if (a.mode == GATHER_INIT_NORMS) {
             s2 += fabsf(wlx) + fabsf(wly);
             s3 += fabsf(fx) + fabsf(fy);

@@ -79,8 +79,8 @@ __device__ __forceinline__ void net_thread(const int *__restrict__ pins, int d, 
                 if (axis == 0) {
                     gxs[j] = g;
                 } else if (node[j] < n_grad) {
-                    atomicAdd(gqx + node[j], (ull)__float2ll_rn(gxs[j] * kGradScale));
-                    atomicAdd(gqy + node[j], (ull)__float2ll_rn(g * kGradScale));
+                    atomicAdd(gqx + node[j], grad_q(gxs[j]));
+                    atomicAdd(gqy + node[j], grad_q(g));
                 }
             }
         }
@@ -142,6 +142,57 @@ __global__ void __launch_bounds__(kThreads) wa_large_kernel(WaArgs a) {
     float hpf = 0.f, waf = 0.f;
     for (int e = a.bucket_lo[3] + warp; e < a.bucket_lo[4]; e += nwarps) {
         const int s = __ldg(a.net_ptr + e), d = __ldg(a.net_ptr + e + 1) - s;
+        if (d <= 64) {
+            // pins lane and lane + 32 held in registers: one load pass, each
+            // exponential evaluated once
+            const bool v0 = lane < d, v1 = lane + 32 < d;
+            const int n0 = v0 ? __ldg(a.pin_node + s + lane) : 0;
+            const int n1 = v1 ? __ldg(a.pin_node + s + lane + 32) : 0;
+            const float c0[2] = {v0 ? __ldg(px + n0) : 0.f, v0 ? __ldg(py + n0) : 0.f};
+            const float c1[2] = {v1 ? __ldg(px + n1) : 0.f, v1 ? __ldg(py + n1) : 0.f};
+            float mx[2], mn[2];
+#pragma unroll
+            for (int ax = 0; ax < 2; ++ax) {
+                mx[ax] = fmaxf(v0 ? c0[ax] : -3.0e38f, v1 ? c1[ax] : -3.0e38f);
+                mn[ax] = fminf(v0 ? c0[ax] : 3.0e38f, v1 ? c1[ax] : 3.0e38f);
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    mx[ax] = fmaxf(mx[ax], __shfl_xor_sync(0xffffffffu, mx[ax], o));
+                    mn[ax] = fminf(mn[ax], __shfl_xor_sync(0xffffffffu, mn[ax], o));
+                }
+            }
+            float ep0[2], em0[2], ep1[2], em1[2], gsum[2][2];
+            float wa_net = 0.f;
+#pragma unroll
+            for (int ax = 0; ax < 2; ++ax) {
+                const float dp0 = c0[ax] - mx[ax], dm0 = c0[ax] - mn[ax];
+                const float dp1 = c1[ax] - mx[ax], dm1 = c1[ax] - mn[ax];
+                ep0[ax] = v0 ? __expf(dp0 * inv_g) : 0.f;
+                em0[ax] = v0 ? __expf(-dm0 * inv_g) : 0.f;
+                ep1[ax] = v1 ? __expf(dp1 * inv_g) : 0.f;
+                em1[ax] = v1 ? __expf(-dm1 * inv_g) : 0.f;
+                const float bp = warp_sum(ep0[ax] + ep1[ax]), bm = warp_sum(em0[ax] + em1[ax]);
+                const float cp = warp_sum(ep0[ax] * dp0 + ep1[ax] * dp1);
+                const float cm = warp_sum(em0[ax] * dm0 + em1[ax] * dm1);
+                const float ibp = 1.f / bp, ibm = 1.f / bm, wp = cp * ibp, wm = cm * ibm;
+                gsum[ax][0] = ep0[ax] * ibp * (1.f + (dp0 - wp) * inv_g) - em0[ax] * ibm * (1.f - (dm0 - wm) * inv_g);
+                gsum[ax][1] = ep1[ax] * ibp * (1.f + (dp1 - wp) * inv_g) - em1[ax] * ibm * (1.f - (dm1 - wm) * inv_g);
+                wa_net += (mx[ax] - mn[ax]) + wp - wm;
+            }
+            if (v0 && n0 < a.n_grad) {
+                atomicAdd(a.gqx + n0, grad_q(gsum[0][0]));
+                atomicAdd(a.gqy + n0, grad_q(gsum[1][0]));
+            }
+            if (v1 && n1 < a.n_grad) {
+                atomicAdd(a.gqx + n1, grad_q(gsum[0][1]));
+                atomicAdd(a.gqy + n1, grad_q(gsum[1][1]));
+            }
+            if (lane == 0) {
+                hpf += (mx[0] - mn[0]) + (mx[1] - mn[1]);
+                waf += wa_net;
+            }
+            continue;
+        }
         float xmx = -3.0e38f, xmn = 3.0e38f, ymx = -3.0e38f, ymn = 3.0e38f;
         for (int j = lane; j < d; j += 32) {
             const int n = __ldg(a.pin_node + s + j);
@@ -194,8 +245,8 @@ __global__ void __launch_bounds__(kThreads) wa_large_kernel(WaArgs a) {
                 g[ax] = ep * t[ax].inv_bp * (1.f + (dp - t[ax].wp) * inv_g) -
                         em * t[ax].inv_bm * (1.f - (dm - t[ax].wm) * inv_g);
             }
-            atomicAdd(a.gqx + n, (ull)__float2ll_rn(g[0] * kGradScale));
-            atomicAdd(a.gqy + n, (ull)__float2ll_rn(g[1] * kGradScale));
+            atomicAdd(a.gqx + n, grad_q(g[0]));
+            atomicAdd(a.gqy + n, grad_q(g[1]));
         }
         if (lane == 0) {
             hpf += (xmx - xmn) + (ymx - ymn);
