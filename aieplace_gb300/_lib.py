@@ -17,11 +17,14 @@ LIB_PATH = os.path.join(HERE, "libaieplace_gb300.so")
 EXPORTS = [
     "ap_abi_version", "ap_status_string", "ap_params_default", "ap_create", "ap_destroy",
     "ap_set_stream", "ap_init_positions", "ap_init_seeded", "ap_step", "ap_step_async",
-    "ap_profile_stages", "ap_run", "ap_step_host",
+    "ap_profile_stages", "ap_solver_info", "ap_run", "ap_step_host",
     "ap_get_positions", "ap_get_stats", "ap_hpwl", "ap_overflow", "ap_wirelength_grad",
-    "ap_density_map", "ap_field_solve", "ap_field_solve_noalloc", "ap_snapshot_size", "ap_snapshot",
+    "ap_density_map", "ap_field_solve", "ap_field_solve_noalloc", "ap_selftest_numerics",
+    "ap_snapshot_size", "ap_snapshot",
     "ap_restore",
     "ap_synth_counts", "ap_synth_generate",
+    "ap_create_batch", "ap_batch_destroy", "ap_batch_init_seeded", "ap_batch_step", "ap_batch_run",
+    "ap_batch_get_stats", "ap_batch_get_positions",
 ]
 
 AP_OK = 0
@@ -94,6 +97,7 @@ def lib():
         L.ap_init_seeded.argtypes = [vp, u64, f32]
         L.ap_step.argtypes = [vp, i32]
         L.ap_step_async.argtypes = [vp, i32]
+        L.ap_solver_info.argtypes = [vp, C.POINTER(i32), vp, C.POINTER(i32), vp]
         L.ap_profile_stages.argtypes = [vp, i32, vp, C.POINTER(i32)]
         L.ap_run.argtypes = [vp, C.POINTER(i32)]
         L.ap_step_host.argtypes = [vp, vp, vp, vp, vp, C.POINTER(Stats)]
@@ -105,10 +109,18 @@ def lib():
         L.ap_density_map.argtypes = [vp, vp, vp, vp]
         L.ap_field_solve.argtypes = [vp, vp, vp, vp, i32]
         L.ap_field_solve_noalloc.argtypes = [vp, vp, vp, i32, f32, vp]
+        L.ap_selftest_numerics.argtypes = [vp, C.c_int64]
         L.ap_snapshot_size.argtypes = [vp, C.POINTER(C.c_size_t)]
         L.ap_snapshot.argtypes = [vp, vp, C.c_size_t]
         L.ap_restore.argtypes = [vp, vp, C.c_size_t]
-        L.ap_synth_counts.argtypes = [C.POINTER(SynthConfig), C.POINTER(i32), C.POINTER(i32), C.POINTER(i32)]
+        L.ap_create_batch.argtypes = [i32, vp, vp, C.POINTER(vp)]
+        L.ap_batch_destroy.argtypes = [vp]
+        L.ap_batch_init_seeded.argtypes = [vp, u64, f32]
+        L.ap_batch_step.argtypes = [vp, i32]
+        L.ap_batch_run.argtypes = [vp, vp]
+        L.ap_batch_get_stats.argtypes = [vp, i32, C.POINTER(Stats)]
+        L.ap_batch_get_positions.argtypes = [vp, i32, vp, vp]
+        L.ap_synth_counts.argtypes =[C.POINTER(SynthConfig), C.POINTER(i32), C.POINTER(i32), C.POINTER(i32)]
         L.ap_synth_generate.argtypes = [C.POINTER(SynthConfig), vp, vp, vp, vp, vp, vp, vp, vp]
         _lib = L
     return _lib

@@ -9,11 +9,12 @@ namespace ap {
 typedef unsigned long long ull;
 
 constexpr float kCoordScale = 65536.0f;                 // 2^16, coordinates
-// WA gradient: each pin's contribution is rounded to 2^-24 in int32 (|g| is
-// below 2 for a WA partial) and accumulated per node in int64
-constexpr float kGradScale = 16777216.0f;               // 2^24
-constexpr float kInvGradScale = 1.0f / 16777216.0f;
-constexpr float kGradClamp = 127.0f;                    // keeps g * 2^24 inside int32
+// WA gradient: each pin's contribution is rounded to 2^-20 (|g| is below 2
+// for a WA partial) and accumulated per node in int64
+constexpr float kGradScale = 1048576.0f;                // 2^20
+constexpr float kInvGradScale = 1.0f / 1048576.0f;
+constexpr float kGradClamp = 3.99f;                     // |g| 2^20 < 2^22: magic-number rounding is exact
+constexpr double kLambdaMax = 1e30;                     // density penalty cap (the oracle's OR_LAMBDA_MAX)
 constexpr int kThreads = 256;
 
 // FP64 scalars of the optimiser; live in device memory so a whole iteration
@@ -46,7 +47,18 @@ struct DevScalars {
     int restarts;
     int cur;            // buffer index of the accepted state
     int status;
+    // FP32 copies of alpha, mom, lambda, gamma for the per-thread kernels
+    // (a double -> float conversion in every thread costs FP64-pipe time);
+    // refreshed by publish_f32 wherever the doubles change on the device
+    float f_alpha, f_mom, f_lambda, f_gamma;
 };
+
+__device__ __forceinline__ void publish_f32(DevScalars *sc) {
+    sc->f_alpha = (float)sc->alpha;
+    sc->f_mom = (float)sc->mom;
+    sc->f_lambda = (float)sc->lambda;
+    sc->f_gamma = (float)sc->gamma;
+}
 
 // Bin geometry, identical to or_grid in the oracle.
 struct Grid {
@@ -57,24 +69,84 @@ struct Grid {
     long long bw_q, bh_q;
 };
 
-// Round-to-nearest conversion of v * 2^16 to an integer.  In int32 range the
-// 32-bit conversion gives the same integer as the 64-bit one and stays off the
-// FP64 pipe, which executes 64-bit integer conversions.
+// Integer <-> float conversions execute on the FP64 pipe, which is narrow on
+// this part; the helpers below do them with integer and FMA-pipe arithmetic.
+
+// Round-to-nearest-even of s to an integer for |s| < 2^31, from the bit
+// fields of s (the same integer llrintf gives).
+__device__ __forceinline__ int f2i_rn_bits(float s) {
+    const unsigned b = __float_as_uint(s);
+    const unsigned ex = (b >> 23) & 0xFFu;
+    const unsigned m = ex ? ((b & 0x7FFFFFu) | 0x800000u) : 0u;
+    const int e = (int)ex - 150;  // |s| = m * 2^e
+    unsigned r;
+    if (e >= 0) {
+        r = m << e;
+    } else if (e < -24) {
+        r = 0u;  // |s| < 0.5
+    } else {
+        const unsigned sh = (unsigned)(-e), q = m >> sh, rem = m & ((1u << sh) - 1u), half = 1u << (sh - 1u);
+        r = q + ((rem > half || (rem == half && (q & 1u))) ? 1u : 0u);
+    }
+    return (b >> 31) ? -(int)r : (int)r;
+}
+
+// Truncation toward zero of s to an integer for |s| < 2^31 (= (int)s).
+__device__ __forceinline__ int f2i_rz_bits(float s) {
+    const unsigned b = __float_as_uint(s);
+    const unsigned ex = (b >> 23) & 0xFFu;
+    const unsigned m = (b & 0x7FFFFFu) | 0x800000u;
+    const int e = (int)ex - 150;
+    const unsigned r = e >= 0 ? m << e : (e < -23 ? 0u : m >> (unsigned)(-e));
+    return (b >> 31) ? -(int)r : (int)r;
+}
+
+// Round-to-nearest-even int64 -> float from integer arithmetic (= (float)v).
+__device__ __forceinline__ float ll2f_rn_bits(long long v) {
+    if (v == 0) return 0.0f;
+    const unsigned sign = v < 0 ? 0x80000000u : 0u;
+    const ull a = v < 0 ? 0ull - (ull)v : (ull)v;
+    int msb = 63 - __clzll((long long)a);
+    ull q;
+    if (msb <= 23) {
+        q = a << (23 - msb);
+    } else {
+        const int sh = msb - 23;
+        q = a >> sh;
+        const ull rem = a & ((1ull << sh) - 1ull), half = 1ull << (sh - 1);
+        if (rem > half || (rem == half && (q & 1ull))) {
+            q += 1ull;
+            if (q == (1ull << 24)) {
+                q >>= 1;
+                msb += 1;
+            }
+        }
+    }
+    return __uint_as_float(sign | ((unsigned)(msb + 127) << 23) | ((unsigned)q & 0x7FFFFFu));
+}
+
+// Exact int -> float for |v| < 2^22 (magic-number addition).
+__device__ __forceinline__ float i2f_small(int v) { return __int_as_float(v + 0x4B400000) - 12582912.0f; }
+
+// Round-to-nearest of v * 2^16 to an integer, equal to llrintf(v * 65536).
 __device__ __forceinline__ long long to_q(float v) {
     const float s = __fmul_rn(v, kCoordScale);
-    if (fabsf(s) < 2147483520.0f) return (long long)__float2int_rn(s);
+    if (fabsf(s) < 2147483520.0f) return (long long)f2i_rn_bits(s);
     return __float2ll_rn(s);
 }
 
-// float of an int64 fixed-point value through two 32-bit conversions (within
-// one ulp of the correctly rounded conversion)
+// float of an int64 fixed-point value (exact below 2^22, else through two
+// 32-bit conversions, within one ulp)
 __device__ __forceinline__ float i64_to_float(long long q) {
+    if (q > -4194304ll && q < 4194304ll) return i2f_small((int)q);
     return fmaf(__int2float_rn((int)(q >> 32)), 4294967296.0f, __uint2float_rn((unsigned)q));
 }
 
-// per-pin WA contribution in the int64 accumulators' fixed point
+// per-pin WA contribution in the int64 accumulators' fixed point: g 2^20
+// rounded to nearest by the magic-number FMA (|g 2^20| < 2^22)
 __device__ __forceinline__ ull grad_q(float g) {
-    return (ull)(long long)__float2int_rn(fminf(fmaxf(g, -kGradClamp), kGradClamp) * kGradScale);
+    const float c = fminf(fmaxf(g, -kGradClamp), kGradClamp);
+    return (ull)(long long)(__float_as_int(fmaf(c, kGradScale, 12582912.0f)) - 0x4B400000);
 }
 
 // The bins a node touches under the reference rules (Grid.cpp:38-110,
@@ -88,17 +160,17 @@ __device__ __forceinline__ bool bin_range(const Grid &g, float x, float y, float
     const float qx = __fdiv_rn(x, g.bw), qy = __fdiv_rn(y, g.bh);
     if (small) {
         if (!(qx > -1.0f) || !(qx < (float)g.mx) || !(qy > -1.0f) || !(qy < (float)g.my)) return false;
-        c0 = c1 = __float2int_rz(qx);
-        r0 = r1 = __float2int_rz(qy);
+        c0 = c1 = f2i_rz_bits(qx);
+        r0 = r1 = f2i_rz_bits(qy);
         return true;
     }
     if (!(qx > -1.0f) || !(qy > -1.0f)) return false;
     const float qx1 = __fdiv_rn(__fadd_rn(x, w), g.bw), qy1 = __fdiv_rn(__fadd_rn(y, h), g.bh);
     if (qx1 != qx1 || qy1 != qy1) return false;
-    c0 = qx >= (float)g.mx ? g.mx : __float2int_rz(qx);
-    r0 = qy >= (float)g.my ? g.my : __float2int_rz(qy);
-    c1 = qx1 >= (float)g.mx ? g.mx - 1 : __float2int_rz(qx1);
-    r1 = qy1 >= (float)g.my ? g.my - 1 : __float2int_rz(qy1);
+    c0 = qx >= (float)g.mx ? g.mx : f2i_rz_bits(qx);
+    r0 = qy >= (float)g.my ? g.my : f2i_rz_bits(qy);
+    c1 = qx1 >= (float)g.mx ? g.mx - 1 : f2i_rz_bits(qx1);
+    r1 = qy1 >= (float)g.my ? g.my - 1 : f2i_rz_bits(qy1);
     if (c1 > g.mx - 1) c1 = g.mx - 1;
     if (r1 > g.my - 1) r1 = g.my - 1;
     return c0 <= c1 && r0 <= r1;
@@ -128,6 +200,52 @@ __device__ __forceinline__ T block_sum(T v, T *smem /* >= 32 */) {
     if (wid == 0) v = warp_sum(v);
     __syncthreads();
     return v;
+}
+
+// Deterministic block sum of FP32 per-thread partials: warps reduce in FP32,
+// the 32 warp sums in FP64 (only warp 0 touches the FP64 pipe).  Valid in
+// thread 0.
+__device__ __forceinline__ double block_sum_f(float v, double *smem /* >= 32 */) {
+    v = warp_sum(v);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) smem[wid] = (double)v;
+    __syncthreads();
+    double d = 0.0;
+    if (wid == 0) {
+        const int nw = (blockDim.x + 31) >> 5;
+        d = lane < nw ? smem[lane] : 0.0;
+        d = warp_sum(d);
+    }
+    __syncthreads();
+    return d;
+}
+
+// Block sum entirely in FP32 (fixed shuffle tree); valid in thread 0.
+__device__ __forceinline__ float block_sum_ff(float v, float *smem /* >= 32 */) {
+    v = warp_sum(v);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) smem[wid] = v;
+    __syncthreads();
+    if (wid == 0) {
+        const int nw = (blockDim.x + 31) >> 5;
+        v = lane < nw ? smem[lane] : 0.f;
+        v = warp_sum(v);
+    }
+    __syncthreads();
+    return v;
+}
+
+// Compensated (Kahan) FP32 sum of partials[i0], partials[i0 + stride], ...
+// over i < n, by one thread in a fixed order.
+__device__ __forceinline__ float kahan_strided(const float *partials, int i0, int n, int stride, int step) {
+    float s = 0.f, c = 0.f;
+    for (int i = i0; i < n; i += stride) {
+        const float y = __ldcg(partials + (size_t)i * step) - c;
+        const float t = s + y;
+        c = (t - s) - y;
+        s = t;
+    }
+    return s;
 }
 
 // Last-block detection for grid-wide reductions without waiting: every block

@@ -36,7 +36,7 @@ struct WaArgs {
 };
 // launches the four bucket kernels; the last one (warp per net) folds the sums
 void launch_wirelength(const WaArgs &a, cudaStream_t st);
-constexpr int kWaMaxBlocks = 2048;  // per bucket launch
+constexpr int kWaMaxBlocks = 4096;  // per bucket launch (4 x 4096 x 2 partials fit the buffer)
 
 // ---- density scatter (+ Nesterov position update) ---------------------------
 struct ScatterArgs {
@@ -57,6 +57,10 @@ struct ScatterArgs {
     ull *rho_q;
     double *partials;      // update mode: |u_{k+1} - u_k|^2 per block
     unsigned int *counter;
+    // update mode, optional: each movable node's bin record (packed base bin
+    // or a sentinel; overlaps ow0, ow1, oh0, oh1) for the gather at the same point
+    int *rec_bin;
+    int4 *rec_ov;
 };
 void launch_scatter(const ScatterArgs &a, cudaStream_t st);
 
@@ -101,6 +105,9 @@ struct GatherArgs {
     double *partials;       // 4 * grid
     unsigned int *counter;
     int mode;
+    // GATHER_STEP, optional: the bin records the scatter wrote at this point
+    const int *rec_bin;
+    const int4 *rec_ov;
 };
 void launch_gather(const GatherArgs &a, cudaStream_t st);
 
@@ -124,9 +131,14 @@ struct FieldSolver {
     // scratch (bf16 path): hi/lo pairs
     __nv_bfloat16 *b_t_hi, *b_t_lo, *b_px_hi, *b_px_lo, *b_py_hi, *b_py_lo, *b_ux_hi, *b_ux_lo,
         *b_uy_hi, *b_uy_lo;
-    void *tc_maps;           // tensor maps of the tcgen05 path (device)
+    void *tc_maps;           // tensor maps of the tcgen05 path (host table)
     int tc_ready;
     unsigned int *tc_status; // device error flag of the tcgen05 kernels
+    // tile autotuner results
+    int tc_variant;          // 0: 128 x 64 tiles, 1: 128 x 128 tiles
+    float tc_tune_ms[2];     // measured solve time of each variant
+    int simt_bm;             // FP32 path tile (32 or 64); 0 = size rule
+    float simt_tune_ms[2];   // measured solve time with 32 / 64 tiles
 };
 
 int field_solver_init(FieldSolver &f, int m, float bin_ratio, int want_bf16);

@@ -51,6 +51,8 @@ struct ap_handle {
     float *d_ux[2] = {nullptr, nullptr}, *d_uy[2] = {nullptr, nullptr};
     float *d_gx[2] = {nullptr, nullptr}, *d_gy[2] = {nullptr, nullptr};
     float *d_pins = nullptr, *d_charge = nullptr;
+    int *d_rec_bin = nullptr;  // per movable node: bin record of the trial point
+    int4 *d_rec_ov = nullptr;
     ull *d_gqx = nullptr, *d_gqy = nullptr;
     ull *d_mov_q = nullptr;
     long long *d_fix_q = nullptr, *d_fixs_q = nullptr;
@@ -187,18 +189,32 @@ GatherArgs gather_args(ap_handle *h, int at, int mode) {
     return a;
 }
 
+// The loop's scatter (update mode, writes the bin records) and gather (reads them).
+ScatterArgs loop_scatter_args(ap_handle *h) {
+    ScatterArgs s = scatter_args(h);
+    s.update = 1;
+    s.rec_bin = h->d_rec_bin;
+    s.rec_ov = h->d_rec_ov;
+    return s;
+}
+
+GatherArgs loop_gather_args(ap_handle *h) {
+    GatherArgs a = gather_args(h, 0, GATHER_STEP);
+    a.rec_bin = h->d_rec_bin;
+    a.rec_ov = h->d_rec_ov;
+    return a;
+}
+
 // One trial step from the accepted state (buffers [cur]) to buffers
 // [1 - cur]; cur lives in device scalars, so one captured graph serves every
 // launch.  The gather's last block accepts the trial or asks for a retry.
 int enqueue_iteration(ap_handle *h, cudaStream_t st) {
-    ScatterArgs s = scatter_args(h);
-    s.update = 1;
-    launch_scatter(s, st);
+    launch_scatter(loop_scatter_args(h), st);
     launch_rho(rho_args(h, RHO_LOOP, nullptr), st);
     launch_wirelength(wa_args(h, h->d_px[0], h->d_py[0], 0.f, h->n_mov, WA_LOOP, nullptr), st);
     int r = run_field(h, h->p.field_solver, st);
     if (r != AP_OK) return r;
-    launch_gather(gather_args(h, 0, GATHER_STEP), st);
+    launch_gather(loop_gather_args(h), st);
     return cudaGetLastError() == cudaSuccess ? AP_OK : AP_ERR_CUDA;
 }
 
@@ -542,6 +558,8 @@ int ap_create(const ap_netlist *nl, const ap_params *params, ap_handle **out) {
     }
     A(dalloc(&h->d_pins, N));
     A(dalloc(&h->d_charge, N));
+    A(dalloc(&h->d_rec_bin, std::max(1, h->n_mov)));
+    A(dalloc(&h->d_rec_ov, std::max(1, h->n_mov)));
     A(dalloc(&h->d_gqx, N));
     A(dalloc(&h->d_gqy, N));
     A(dalloc(&h->d_mov_q, nb));
@@ -633,7 +651,7 @@ int ap_destroy(ap_handle *h) {
                     h->d_pins,    h->d_charge,   h->d_gqx,    h->d_gqy,
                     h->d_mov_q,   h->d_fix_q,    h->d_fixs_q, h->d_dens,    h->d_ex,    h->d_ey,
                     h->d_dens_hi, h->d_dens_lo,  h->d_sx,     h->d_sy,      h->d_sc,    h->d_partials,
-                    h->d_partials_ll, h->d_counters, h->d_out};
+                    h->d_partials_ll, h->d_counters, h->d_out, h->d_rec_bin, h->d_rec_ov};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     if (h->h_sc) cudaFreeHost(h->h_sc);
@@ -695,6 +713,21 @@ int ap_step(ap_handle *h, int32_t n_iter) {
     return sync(h);
 }
 
+int ap_solver_info(ap_handle *h, int32_t *tc_tile_n, float *tc_ms, int32_t *simt_tile, float *simt_ms) {
+    if (!h) return AP_ERR_INVALID_ARG;
+    if (tc_tile_n) *tc_tile_n = h->fs.tc_ready ? (h->fs.tc_variant ? 128 : 64) : 0;
+    if (tc_ms) {
+        tc_ms[0] = h->fs.tc_tune_ms[0];
+        tc_ms[1] = h->fs.tc_tune_ms[1];
+    }
+    if (simt_tile) *simt_tile = h->fs.simt_bm;
+    if (simt_ms) {
+        simt_ms[0] = h->fs.simt_tune_ms[0];
+        simt_ms[1] = h->fs.simt_tune_ms[1];
+    }
+    return AP_OK;
+}
+
 int ap_step_async(ap_handle *h, int32_t n_trials) {
     if (!h || n_trials < 0) return AP_ERR_INVALID_ARG;
     if (!h->initialized) return AP_ERR_STATE;
@@ -711,10 +744,8 @@ int ap_profile_stages(ap_handle *h, int32_t n_trials, float *stage_ms, int32_t *
     cudaStream_t st = h->stream;
     int r = AP_OK;
     for (int t = 0; t < n_trials && r == AP_OK; ++t) {
-        ScatterArgs s = scatter_args(h);
-        s.update = 1;
         CK(cudaEventRecord(ev[0], st));
-        launch_scatter(s, st);
+        launch_scatter(loop_scatter_args(h), st);
         CK(cudaEventRecord(ev[1], st));
         launch_rho(rho_args(h, RHO_LOOP, nullptr), st);
         CK(cudaEventRecord(ev[2], st));
@@ -722,7 +753,7 @@ int ap_profile_stages(ap_handle *h, int32_t n_trials, float *stage_ms, int32_t *
         CK(cudaEventRecord(ev[3], st));
         r = run_field(h, h->p.field_solver, st);
         CK(cudaEventRecord(ev[4], st));
-        launch_gather(gather_args(h, 0, GATHER_STEP), st);
+        launch_gather(loop_gather_args(h), st);
         CK(cudaEventRecord(ev[5], st));
         CK(cudaEventSynchronize(ev[5]));
         for (int i = 0; i < S; ++i) {
@@ -877,8 +908,8 @@ int ap_wirelength_grad(ap_handle *h, const float *x, const float *y, float gamma
     if (r != AP_OK) return r;
     for (int i = 0; i < h->n_nodes; ++i) {
         const int e = h->int2ext[(size_t)i];
-        gx[e] = (float)ldexp((double)qx[(size_t)i], -24);  // kGradScale = 2^24
-        gy[e] = (float)ldexp((double)qy[(size_t)i], -24);
+        gx[e] = (float)ldexp((double)qx[(size_t)i], -20);  // kGradScale = 2^20
+        gy[e] = (float)ldexp((double)qy[(size_t)i], -20);
     }
     if (hpwl) *hpwl = h->h_out[0];
     if (wa) *wa = h->h_out[1];
@@ -938,7 +969,7 @@ int ap_snapshot(ap_handle *h, void *buf, size_t bytes) {
     if (!h->initialized) return AP_ERR_STATE;
     CK(cudaStreamSynchronize(h->stream));
     char *p = (char *)buf;
-    int32_t hdr[4] = {0x41505332, h->n_nodes, h->n_mov, 0};
+    int32_t hdr[4] = {0x41505333, h->n_nodes, h->n_mov, 0};
     memcpy(p, hdr, sizeof(hdr));
     p += sizeof(hdr);
     CK(cudaMemcpy(p, h->d_sc, sizeof(DevScalars), cudaMemcpyDeviceToHost));
@@ -962,7 +993,7 @@ int ap_restore(ap_handle *h, const void *buf, size_t bytes) {
     const char *p = (const char *)buf;
     int32_t hdr[4];
     memcpy(hdr, p, sizeof(hdr));
-    if (hdr[0] != 0x41505332 || hdr[1] != h->n_nodes || hdr[2] != h->n_mov) return AP_ERR_INVALID_ARG;
+    if (hdr[0] != 0x41505333 || hdr[1] != h->n_nodes || hdr[2] != h->n_mov) return AP_ERR_INVALID_ARG;
     p += sizeof(hdr);
     CK(cudaStreamSynchronize(h->stream));
     CK(cudaMemcpy(h->d_sc, p, sizeof(DevScalars), cudaMemcpyHostToDevice));
@@ -985,6 +1016,164 @@ int ap_restore(ap_handle *h, const void *buf, size_t bytes) {
     h->initialized = true;
     if (h->p.use_graph && !h->graph_ok) return build_graphs(h);
     return AP_OK;
+}
+
+}  // extern "C"
+
+// ---- batched form ---------------------------------------------------------------
+
+struct ap_batch {
+    std::vector<ap_handle *> inst;
+    std::vector<char> active;
+    cudaStream_t main = nullptr;
+    cudaEvent_t fork = nullptr;
+    std::vector<cudaEvent_t> join;
+    cudaGraphExec_t graph = nullptr;
+};
+
+namespace {
+
+void batch_free_graph(ap_batch *b) {
+    if (b->graph) cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
+}
+
+// One graph: fork from the main stream to every active instance's stream,
+// one trial step per instance, join back.
+int batch_build_graph(ap_batch *b) {
+    batch_free_graph(b);
+    cudaGraph_t gr = nullptr;
+    CK(cudaStreamBeginCapture(b->main, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e = cudaEventRecord(b->fork, b->main);
+    int r = e == cudaSuccess ? AP_OK : AP_ERR_CUDA;
+    for (size_t i = 0; i < b->inst.size() && r == AP_OK; ++i) {
+        if (!b->active[i]) continue;
+        ap_handle *h = b->inst[i];
+        if (cudaStreamWaitEvent(h->stream, b->fork, 0) != cudaSuccess) r = AP_ERR_CUDA;
+        if (r == AP_OK) r = enqueue_iteration(h, h->stream);
+        if (r == AP_OK && cudaEventRecord(b->join[i], h->stream) != cudaSuccess) r = AP_ERR_CUDA;
+        if (r == AP_OK && cudaStreamWaitEvent(b->main, b->join[i], 0) != cudaSuccess) r = AP_ERR_CUDA;
+    }
+    e = cudaStreamEndCapture(b->main, &gr);
+    if (r != AP_OK || e != cudaSuccess) {
+        if (gr) cudaGraphDestroy(gr);
+        return r != AP_OK ? r : AP_ERR_CUDA;
+    }
+    e = cudaGraphInstantiate(&b->graph, gr, 0);
+    cudaGraphDestroy(gr);
+    return e == cudaSuccess ? AP_OK : AP_ERR_CUDA;
+}
+
+}  // namespace
+
+extern "C" {
+
+int ap_create_batch(int32_t n, const ap_netlist *netlists, const ap_params *params, ap_batch **out) {
+    if (n <= 0 || !netlists || !params || !out) return AP_ERR_INVALID_ARG;
+    *out = nullptr;
+    ap_batch *b = new ap_batch();
+    int r = AP_OK;
+    for (int i = 0; i < n && r == AP_OK; ++i) {
+        ap_params p = params[i];
+        p.use_graph = 0;  // the batch graph replaces the per-instance graphs
+        ap_handle *h = nullptr;
+        r = ap_create(&netlists[i], &p, &h);
+        if (r == AP_OK) b->inst.push_back(h);
+    }
+    if (r == AP_OK && (cudaStreamCreateWithFlags(&b->main, cudaStreamNonBlocking) != cudaSuccess ||
+                       cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) != cudaSuccess))
+        r = AP_ERR_CUDA;
+    for (int i = 0; i < n && r == AP_OK; ++i) {
+        cudaEvent_t ev;
+        if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) r = AP_ERR_CUDA;
+        else b->join.push_back(ev);
+    }
+    if (r != AP_OK) {
+        ap_batch_destroy(b);
+        return r;
+    }
+    b->active.assign((size_t)n, 1);
+    *out = b;
+    return AP_OK;
+}
+
+int ap_batch_destroy(ap_batch *b) {
+    if (!b) return AP_ERR_INVALID_ARG;
+    if (b->main) cudaStreamSynchronize(b->main);
+    batch_free_graph(b);
+    for (ap_handle *h : b->inst) ap_destroy(h);
+    for (cudaEvent_t e : b->join) cudaEventDestroy(e);
+    if (b->fork) cudaEventDestroy(b->fork);
+    if (b->main) cudaStreamDestroy(b->main);
+    delete b;
+    return AP_OK;
+}
+
+int ap_batch_init_seeded(ap_batch *b, uint64_t seed, float sigma) {
+    if (!b) return AP_ERR_INVALID_ARG;
+    for (size_t i = 0; i < b->inst.size(); ++i) {
+        int r = ap_init_seeded(b->inst[i], seed + i, sigma);
+        if (r != AP_OK) return r;
+    }
+    b->active.assign(b->inst.size(), 1);
+    return batch_build_graph(b);
+}
+
+int ap_batch_step(ap_batch *b, int32_t n_trials) {
+    if (!b || n_trials < 0) return AP_ERR_INVALID_ARG;
+    if (!b->graph) return AP_ERR_STATE;
+    for (int t = 0; t < n_trials; ++t) CK(cudaGraphLaunch(b->graph, b->main));
+    CK(cudaStreamSynchronize(b->main));
+    return AP_OK;
+}
+
+int ap_batch_run(ap_batch *b, int32_t *iterations) {
+    if (!b) return AP_ERR_INVALID_ARG;
+    if (!b->graph) return AP_ERR_STATE;
+    for (;;) {
+        int interval = 1;
+        for (size_t i = 0; i < b->inst.size(); ++i)
+            if (b->active[i]) interval = std::max(interval, b->inst[i]->p.check_interval);
+        for (int t = 0; t < interval; ++t) CK(cudaGraphLaunch(b->graph, b->main));
+        CK(cudaStreamSynchronize(b->main));
+        bool changed = false, any = false;
+        for (size_t i = 0; i < b->inst.size(); ++i) {
+            if (!b->active[i]) continue;
+            ap_handle *h = b->inst[i];
+            int r = read_scalars(h);
+            if (r != AP_OK) return r;
+            // a diverged instance leaves the graph; its stats report the status
+            if (h->h_sc->status || h->h_sc->tau < h->p.target_overflow ||
+                h->h_sc->iteration >= h->p.max_iterations) {
+                b->active[i] = 0;
+                changed = true;
+            } else {
+                any = true;
+            }
+        }
+        if (!any) break;
+        if (changed) {
+            int r = batch_build_graph(b);
+            if (r != AP_OK) return r;
+        }
+    }
+    if (iterations)
+        for (size_t i = 0; i < b->inst.size(); ++i) {
+            int r = read_scalars(b->inst[i]);
+            if (r != AP_OK) return r;
+            iterations[i] = b->inst[i]->h_sc->iteration;
+        }
+    return AP_OK;
+}
+
+int ap_batch_get_stats(ap_batch *b, int32_t i, ap_stats *s) {
+    if (!b || i < 0 || i >= (int32_t)b->inst.size()) return AP_ERR_INVALID_ARG;
+    return ap_get_stats(b->inst[(size_t)i], s);
+}
+
+int ap_batch_get_positions(ap_batch *b, int32_t i, float *x, float *y) {
+    if (!b || i < 0 || i >= (int32_t)b->inst.size()) return AP_ERR_INVALID_ARG;
+    return ap_get_positions(b->inst[(size_t)i], x, y);
 }
 
 }  // extern "C"

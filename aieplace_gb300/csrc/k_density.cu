@@ -23,16 +23,18 @@ namespace {
 
 __device__ __forceinline__ float clampf(float v, float lo, float hi) { return fminf(fmaxf(v, lo), hi); }
 
-// block max in a fixed shuffle tree; valid in thread 0
-__device__ __forceinline__ double block_max(double v, double *smem) {
-    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
-    if ((threadIdx.x & 31) == 0) smem[threadIdx.x >> 5] = v;
+// block max of non-negative FP32 values, FP64 result valid in thread 0
+__device__ __forceinline__ double block_max_f(float v, double *smem) {
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    if ((threadIdx.x & 31) == 0) smem[threadIdx.x >> 5] = (double)v;
     __syncthreads();
-    v = threadIdx.x < (blockDim.x >> 5) ? smem[threadIdx.x] : 0.0;
-    if (threadIdx.x < 32)
-        for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    double d = 0.0;
+    if (threadIdx.x < 32) {
+        d = threadIdx.x < (blockDim.x >> 5) ? smem[threadIdx.x] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) d = fmax(d, __shfl_xor_sync(0xffffffffu, d, o));
+    }
     __syncthreads();
-    return v;
+    return d;
 }
 
 }  // namespace
@@ -44,9 +46,81 @@ __device__ __forceinline__ double block_max(double v, double *smem) {
 // global map (one global atomic per bin and block instead of one per node
 // and bin -- right after initial placement every node sits in a few bins).
 // Integer sums make both paths give the same map bit for bit.
-constexpr int kScatterPerThread = 8;
-constexpr int kScatterChunk = kThreads * kScatterPerThread;
+constexpr int kScatterThreads = 512;
+constexpr int kScatterPerThread = 4;
+constexpr int kScatterChunk = kScatterThreads * kScatterPerThread;
 constexpr int kScatterWindow = 4096;
+
+// A node's contribution as a record of 5 int32: the base bin (c0, r0), the
+// spans nc, nr <= 8 and a small-node flag packed in `bin` (non-negative), the
+// node's fixed-point x and y relative to the base bin's corner and its
+// fixed-point width and height.  Column c0 + j overlaps the node by
+// overlap_1d(j bw, bw, xr, wq) -- the same integer as from absolute
+// coordinates.  Nodes that span more bins, or whose extents do not fit int32,
+// are re-evaluated in full (kRecFull).  Bin counts are at most 4096 per axis.
+constexpr int kRecNone = -1, kRecFull = -2;
+constexpr int kRecSmall = 1 << 30, kRecMaxSpan = 8;
+
+struct NodeRec {
+    int bin;  // c0 | r0 << 12 | (nc - 1) << 24 | (nr - 1) << 27 | small << 30
+    int xr, wq, yr, hq;
+};
+
+__device__ __forceinline__ int rec_c0(int b) { return b & 0xFFF; }
+__device__ __forceinline__ int rec_r0(int b) { return (b >> 12) & 0xFFF; }
+__device__ __forceinline__ int rec_nc(int b) { return ((b >> 24) & 7) + 1; }
+__device__ __forceinline__ int rec_nr(int b) { return ((b >> 27) & 7) + 1; }
+
+__device__ __forceinline__ bool fits_i32(long long v) { return v >= -2147483647ll && v <= 2147483647ll; }
+
+__device__ __forceinline__ NodeRec make_rec(const Grid &g, float x, float y, float w, float h, int &c0, int &c1,
+                                            int &r0, int &r1) {
+    NodeRec r{kRecNone, 0, 0, 0, 0};
+    bool small;
+    if (!bin_range(g, x, y, w, h, c0, c1, r0, r1, small)) {
+        c1 = r1 = -1;
+        return r;
+    }
+    const long long wq = to_q(w), hq = to_q(h);
+    if (small) {
+        if (!fits_i32(wq) || !fits_i32(hq)) {
+            r.bin = kRecFull;
+            return r;
+        }
+        r.bin = c0 | (r0 << 12) | kRecSmall;
+        r.wq = (int)wq;
+        r.hq = (int)hq;
+        return r;
+    }
+    const long long xr = to_q(x) - (long long)c0 * g.bw_q, yr = to_q(y) - (long long)r0 * g.bh_q;
+    if (c1 - c0 >= kRecMaxSpan || r1 - r0 >= kRecMaxSpan || !fits_i32(xr) || !fits_i32(yr) || !fits_i32(wq) ||
+        !fits_i32(hq)) {
+        r.bin = kRecFull;
+        return r;
+    }
+    r.bin = c0 | (r0 << 12) | ((c1 - c0) << 24) | ((r1 - r0) << 27);
+    r.xr = (int)xr;
+    r.wq = (int)wq;
+    r.yr = (int)yr;
+    r.hq = (int)hq;
+    return r;
+}
+
+// Calls add(c, r, value) for each bin of a record with the values
+// for_each_overlap produces, in the same order (column-major).
+template <typename F>
+__device__ __forceinline__ void emit_rec(const Grid &g, int bin, int xr, int wq, int yr, int hq, F &&add) {
+    const int c0 = rec_c0(bin), r0 = rec_r0(bin);
+    if (bin & kRecSmall) {
+        add(c0, r0, (long long)wq * hq);
+        return;
+    }
+    const int nc = rec_nc(bin), nr = rec_nr(bin);
+    for (int j = 0; j < nc; ++j) {
+        const long long ow = overlap_1d((long long)j * g.bw_q, g.bw_q, xr, wq);
+        for (int k = 0; k < nr; ++k) add(c0 + j, r0 + k, ow * overlap_1d((long long)k * g.bh_q, g.bh_q, yr, hq));
+    }
+}
 
 template <typename F>
 __device__ __forceinline__ void for_each_overlap(const Grid &g, float x, float y, float w, float h, F &&f) {
@@ -64,7 +138,7 @@ __device__ __forceinline__ void for_each_overlap(const Grid &g, float x, float y
     }
 }
 
-__global__ void __launch_bounds__(kThreads) scatter_kernel(ScatterArgs a) {
+__global__ void __launch_bounds__(kScatterThreads, 2) scatter_kernel(ScatterArgs a) {
     __shared__ double red[32];
     __shared__ int box[4];  // bin bounding box of the chunk: c0, c1, r0, r1
     __shared__ ull win[kScatterWindow];
@@ -72,8 +146,8 @@ __global__ void __launch_bounds__(kThreads) scatter_kernel(ScatterArgs a) {
     float alpha = 0.f, mom = 0.f;
     int cur = 0;
     if (a.update) {
-        alpha = (float)a.sc->alpha;
-        mom = (float)a.sc->mom;
+        alpha = a.sc->f_alpha;
+        mom = a.sc->f_mom;
         cur = a.sc->cur;
     }
     const int nxt = 1 - cur;
@@ -84,15 +158,13 @@ __global__ void __launch_bounds__(kThreads) scatter_kernel(ScatterArgs a) {
     }
     __syncthreads();
     float du = 0.f;  // per-thread partial in FP32; FP64 from the block sum on
-    float px[kScatterPerThread], py[kScatterPerThread], pw[kScatterPerThread], ph[kScatterPerThread];
+    NodeRec rec[kScatterPerThread];
     int bc0 = 0x7fffffff, bc1 = -1, br0 = 0x7fffffff, br1 = -1;
     const int base = blockIdx.x * kScatterChunk;
 #pragma unroll
     for (int k = 0; k < kScatterPerThread; ++k) {
-        const int i = base + k * kThreads + threadIdx.x;
-        pw[k] = 0.f;  // zero area: nothing to scatter
-        ph[k] = 0.f;
-        px[k] = py[k] = 0.f;
+        const int i = base + k * kScatterThreads + threadIdx.x;
+        rec[k].bin = kRecNone;
         if (i >= n) continue;
         const int node = a.update ? i : a.lo + i;
         const float w = __ldg(a.w + node), h = __ldg(a.h + node);
@@ -113,20 +185,28 @@ __global__ void __launch_bounds__(kThreads) scatter_kernel(ScatterArgs a) {
             x = __ldg(a.px + node);
             y = __ldg(a.py + node);
         }
-        px[k] = x;
-        py[k] = y;
-        pw[k] = w;
-        ph[k] = h;
         int c0, c1, r0, r1;
-        bool small;
-        if (bin_range(g, x, y, w, h, c0, c1, r0, r1, small)) {
+        rec[k] = make_rec(g, x, y, w, h, c0, c1, r0, r1);
+        if (a.update && a.rec_bin) {
+            a.rec_bin[i] = rec[k].bin;
+            a.rec_ov[i] = make_int4(rec[k].xr, rec[k].wq, rec[k].yr, rec[k].hq);
+        }
+        if (c1 >= 0) {
             bc0 = min(bc0, c0);
             bc1 = max(bc1, c1);
             br0 = min(br0, r0);
             br1 = max(br1, r1);
         }
     }
-    if (bc1 >= 0) {
+    // the chunk's bin bounding box: warp reduction, then one shared atomic per warp
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        bc0 = min(bc0, __shfl_xor_sync(0xffffffffu, bc0, o));
+        bc1 = max(bc1, __shfl_xor_sync(0xffffffffu, bc1, o));
+        br0 = min(br0, __shfl_xor_sync(0xffffffffu, br0, o));
+        br1 = max(br1, __shfl_xor_sync(0xffffffffu, br1, o));
+    }
+    if ((threadIdx.x & 31) == 0 && bc1 >= 0) {
         atomicMin(box + 0, bc0);
         atomicMax(box + 1, bc1);
         atomicMin(box + 2, br0);
@@ -137,33 +217,51 @@ __global__ void __launch_bounds__(kThreads) scatter_kernel(ScatterArgs a) {
     const int wc = box[1] - wc0 + 1, wr = box[3] - wr0 + 1;
     const bool use_win = box[1] >= 0 && (long long)wc * wr <= kScatterWindow;
     if (use_win) {
-        for (int t = threadIdx.x; t < wc * wr; t += kThreads) win[t] = 0ull;
+        for (int t = threadIdx.x; t < wc * wr; t += kScatterThreads) win[t] = 0ull;
         __syncthreads();
     }
+    // shared-space reduction (red.shared.add.u64) into the window
+    const unsigned win_s = (unsigned)__cvta_generic_to_shared(win);
+    auto add_win = [&](int c, int r, long long v) {
+        const unsigned addr = win_s + 8u * (unsigned)((c - wc0) * wr + (r - wr0));
+        asm volatile("red.shared.add.u64 [%0], %1;" ::"r"(addr), "l"(v) : "memory");
+    };
+    auto add_glb = [&](int c, int r, long long v) { atomicAdd(a.rho_q + (long long)c * g.my + r, (ull)v); };
 #pragma unroll
     for (int k = 0; k < kScatterPerThread; ++k) {
-        if (use_win) {
-            for_each_overlap(g, px[k], py[k], pw[k], ph[k], [&](int c, int r, long long v) {
-                atomicAdd(win + (c - wc0) * wr + (r - wr0), (ull)v);
-            });
-        } else {
-            for_each_overlap(g, px[k], py[k], pw[k], ph[k], [&](int c, int r, long long v) {
-                atomicAdd(a.rho_q + (long long)c * g.my + r, (ull)v);
-            });
+        if (rec[k].bin == kRecNone) continue;
+        if (rec[k].bin == kRecFull) {
+            // re-evaluated from the node's position (this thread wrote it above)
+            const int i = base + k * kScatterThreads + threadIdx.x;
+            const int node = a.update ? i : a.lo + i;
+            const float x = a.update ? a.vx[nxt][i] : __ldg(a.px + node);
+            const float y = a.update ? a.vy[nxt][i] : __ldg(a.py + node);
+            const float w = __ldg(a.w + node), h = __ldg(a.h + node);
+            if (use_win)
+                for_each_overlap(g, x, y, w, h, add_win);
+            else
+                for_each_overlap(g, x, y, w, h, add_glb);
+            continue;
         }
+        const NodeRec &q = rec[k];
+        if (use_win)
+            emit_rec(g, q.bin, q.xr, q.wq, q.yr, q.hq, add_win);
+        else
+            emit_rec(g, q.bin, q.xr, q.wq, q.yr, q.hq, add_glb);
     }
     if (use_win) {
         __syncthreads();
-        for (int t = threadIdx.x; t < wc * wr; t += kThreads) {
+        for (int t = threadIdx.x; t < wc * wr; t += kScatterThreads) {
             const ull v = win[t];
             if (v) atomicAdd(a.rho_q + (long long)(wc0 + t / wr) * g.my + (wr0 + t % wr), v);
         }
     }
     if (!a.update) return;
-    const double dub = block_sum((double)du, red);
-    if (threadIdx.x == 0) a.partials[blockIdx.x] = dub;
+    float *pf = reinterpret_cast<float *>(a.partials);
+    const float dub = block_sum_ff(du, reinterpret_cast<float *>(red));
+    if (threadIdx.x == 0) pf[blockIdx.x] = dub;
     if (arrive_last(a.counter)) {
-        const double t = reduce_partials(a.partials, gridDim.x, red);
+        const double t = block_sum_f(kahan_strided(pf, threadIdx.x, gridDim.x, blockDim.x, 1), red);
         if (threadIdx.x == 0) {
             a.sc->t_du = t;
             *a.counter = 0u;
@@ -175,7 +273,7 @@ void launch_scatter(const ScatterArgs &a, cudaStream_t st) {
     const int n = a.update ? a.n_mov : (a.hi - a.lo);
     if (n <= 0) return;
     const int blocks = (n + kScatterChunk - 1) / kScatterChunk;  // <= 8192 partials for 16M nodes
-    scatter_kernel<<<blocks, kThreads, 0, st>>>(a);
+    scatter_kernel<<<blocks, kScatterThreads, 0, st>>>(a);
 }
 
 __device__ __forceinline__ double gamma_of(const DevScalars *sc, double tau) {
@@ -205,7 +303,7 @@ __global__ void __launch_bounds__(kThreads) rho_kernel(RhoArgs a) {
             over += t > 0 ? t : 0;
             const long long ab = m[k] + f[k] - a.ab_q;
             over_abs += ab > 0 ? ab : 0;
-            d[k] = __ll2float_rn(tot) * a.inv_ab_f;  // same float ops as or_density_float
+            d[k] = ll2f_rn_bits(tot) * a.inv_ab_f;  // same float ops as or_density_float
         }
         if (a.d_f32) reinterpret_cast<float2 *>(a.d_f32)[p] = make_float2(d[0], d[1]);
         if (a.d_hi) {
@@ -245,6 +343,7 @@ __global__ void __launch_bounds__(kThreads) rho_kernel(RhoArgs a) {
                 sc->t_tau = tau;
                 sc->t_tau_abs = tau_abs;
                 sc->gamma = gamma_of(sc, tau);
+                sc->f_gamma = (float)sc->gamma;
             }
             *a.counter = 0u;
         }
@@ -290,7 +389,10 @@ __device__ void finish_trial(DevScalars *sc, double dv2, double dg2) {
     const double pc = (sc->t_hpwl - sc->hpwl_prev) / sc->ref_dh;
     double mu = pc < 0.0 ? sc->mu_max : pow(sc->mu_max, 1.0 - pc);
     mu = fmin(fmax(mu, sc->mu_min), sc->mu_max);
-    sc->lambda *= mu;
+    // capped where the density term dominates completely: keeps the FP32
+    // products finite when the target overflow is out of reach (lambda would
+    // otherwise grow 5% per iteration until it overflows)
+    sc->lambda = fmin(sc->lambda * mu, kLambdaMax);
     sc->hpwl_prev = sc->t_hpwl;
     sc->hpwl = sc->t_hpwl;
     sc->wa = sc->t_wa;
@@ -304,7 +406,7 @@ __device__ void finish_trial(DevScalars *sc, double dv2, double dg2) {
 __global__ void __launch_bounds__(kThreads) gather_kernel(GatherArgs a) {
     __shared__ double red[32];
     const Grid g = a.g;
-    const float lam = (float)a.sc->lambda;
+    const float lam = a.sc->f_lambda;
     const int at = a.mode == GATHER_STEP ? 1 - a.sc->cur : a.at;
     const float *vx = a.vx[at], *vy = a.vy[at], *vpx = a.vx[1 - at], *vpy = a.vy[1 - at];
     float *gx_out = a.gx[at], *gy_out = a.gy[at];
@@ -312,18 +414,43 @@ __global__ void __launch_bounds__(kThreads) gather_kernel(GatherArgs a) {
     // per-thread partials in FP32 (a thread owns a couple of nodes); FP64 from
     // the block sums on -- the FP64 pipe of this part is narrow
     float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
+    const bool use_rec = a.mode == GATHER_STEP && a.rec_bin != nullptr;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n_mov; i += gridDim.x * blockDim.x) {
         const float x = vx[i], y = vy[i];
-        const float w = __ldg(a.w + i), h = __ldg(a.h + i);
         float fx = 0.f, fy = 0.f;
         int c0, c1, r0, r1;
         bool small;
-        if (bin_range(g, x, y, w, h, c0, c1, r0, r1, small)) {
+        const int rb = use_rec ? __ldg(a.rec_bin + i) : kRecFull;
+        if (rb >= 0) {
+            // the scatter's record at this point: the weights of the path
+            // below, in the same order, without the bin arithmetic
+            const int4 o = __ldg(a.rec_ov + i);  // xr, wq, yr, hq
+            const int c0r = rec_c0(rb), r0r = rec_r0(rb);
+            if (rb & kRecSmall) {
+                const int b = c0r * g.my + r0r;
+                const float wt = (i64_to_float(o.y) * i64_to_float(o.w)) * g.inv_ab;
+                fx = wt * __ldg(a.ex + b);
+                fy = wt * __ldg(a.ey + b);
+            } else {
+                const int nc = rec_nc(rb), nr = rec_nr(rb);
+                for (int j = 0; j < nc; ++j) {
+                    const float fw = i64_to_float(overlap_1d((long long)j * g.bw_q, g.bw_q, o.x, o.y));
+                    const int bc = (c0r + j) * g.my + r0r;
+                    for (int k = 0; k < nr; ++k) {
+                        const float fh = i64_to_float(overlap_1d((long long)k * g.bh_q, g.bh_q, o.z, o.w));
+                        const float wt = (fw * fh) * g.inv_ab;
+                        fx += wt * __ldg(a.ex + bc + k);
+                        fy += wt * __ldg(a.ey + bc + k);
+                    }
+                }
+            }
+        } else if (rb == kRecFull && bin_range(g, x, y, __ldg(a.w + i), __ldg(a.h + i), c0, c1, r0, r1, small)) {
+            const float w = __ldg(a.w + i), h = __ldg(a.h + i);
             const long long xq = to_q(x), yq = to_q(y), wq = to_q(w), hq = to_q(h);
             if (small) {
                 const long long b = (long long)c0 * g.my + r0;
                 // both sides exact in float: one rounding, = (float)(wq * hq)
-                const float wt = (__int2float_rn((int)wq) * __int2float_rn((int)hq)) * g.inv_ab;
+                const float wt = (i64_to_float(wq) * i64_to_float(hq)) * g.inv_ab;
                 fx = wt * __ldg(a.ex + b);
                 fy = wt * __ldg(a.ey + b);
             } else {
@@ -332,7 +459,7 @@ __global__ void __launch_bounds__(kThreads) gather_kernel(GatherArgs a) {
                     for (int r = r0; r <= r1; ++r) {
                         const long long oh = overlap_1d((long long)r * g.bh_q, g.bh_q, yq, hq);
                         const long long b = (long long)c * g.my + r;
-                        const float wt = (__int2float_rn((int)ow) * __int2float_rn((int)oh)) * g.inv_ab;
+                        const float wt = (i64_to_float(ow) * i64_to_float(oh)) * g.inv_ab;
                         fx += wt * __ldg(a.ex + b);
                         fy += wt * __ldg(a.ey + b);
                     }
@@ -354,7 +481,8 @@ __global__ void __launch_bounds__(kThreads) gather_kernel(GatherArgs a) {
         a.gqx[i] = 0ull;
         a.gqy[i] = 0ull;
         const float hd = fmaxf(1.f, a.pins[i] + lam * a.charge[i]);
-        const float gx = (wlx - lam * fx) / hd, gy = (wly - lam * fy) / hd;
+        const float ihd = __frcp_rn(hd);
+        const float gx = (wlx - lam * fx) * ihd, gy = (wly - lam * fy) * ihd;
         gx_out[i] = gx;
         gy_out[i] = gy;
         if (a.mode == GATHER_INIT_GRAD) {
@@ -368,30 +496,34 @@ __global__ void __launch_bounds__(kThreads) gather_kernel(GatherArgs a) {
     }
     if (a.mode == GATHER_FORCE_ONLY) return;
     const bool is_max = a.mode == GATHER_INIT_GRAD;
-    const double b0 = block_sum((double)s0, red);
-    const double b1 = block_sum((double)s1, red);
-    const double b2 = is_max ? block_max((double)s2, red) : block_sum((double)s2, red);
-    const double b3 = block_sum((double)s3, red);
+    // per-block partials in FP32; the last block sums them with compensation
+    // and only its warp 0 adds in FP64 (the FP64 pipe of this part is narrow)
+    float *redf = reinterpret_cast<float *>(red);
+    const float b0 = block_sum_ff(s0, redf);
+    const float b1 = block_sum_ff(s1, redf);
+    const float b2 = is_max ? (float)block_max_f(s2, red) : block_sum_ff(s2, redf);
+    const float b3 = block_sum_ff(s3, redf);
+    float *pf = reinterpret_cast<float *>(a.partials);
     if (threadIdx.x == 0) {
-        double *p = a.partials + 4 * blockIdx.x;
+        float *p = pf + 4 * blockIdx.x;
         p[0] = b0;
         p[1] = b1;
         p[2] = b2;
         p[3] = b3;
     }
     if (arrive_last(a.counter)) {
-        double t0 = 0.0, t1 = 0.0, t2 = 0.0, t3 = 0.0;
-        for (int k = threadIdx.x; k < (int)gridDim.x; k += blockDim.x) {
-            const double *p = a.partials + 4 * k;
-            t0 += __ldcg(p);
-            t1 += __ldcg(p + 1);
-            t2 = is_max ? fmax(t2, __ldcg(p + 2)) : t2 + __ldcg(p + 2);
-            t3 += __ldcg(p + 3);
+        const int nb = (int)gridDim.x;
+        const double t0 = block_sum_f(kahan_strided(pf + 0, threadIdx.x, nb, blockDim.x, 4), red);
+        const double t1 = block_sum_f(kahan_strided(pf + 1, threadIdx.x, nb, blockDim.x, 4), red);
+        double t2;
+        if (is_max) {
+            float m = 0.f;
+            for (int k = threadIdx.x; k < nb; k += blockDim.x) m = fmaxf(m, __ldcg(pf + 4 * k + 2));
+            t2 = block_max_f(m, red);
+        } else {
+            t2 = block_sum_f(kahan_strided(pf + 2, threadIdx.x, nb, blockDim.x, 4), red);
         }
-        t0 = block_sum(t0, red);
-        t1 = block_sum(t1, red);
-        t2 = is_max ? block_max(t2, red) : block_sum(t2, red);
-        t3 = block_sum(t3, red);
+        const double t3 = block_sum_f(kahan_strided(pf + 3, threadIdx.x, nb, blockDim.x, 4), red);
         if (threadIdx.x == 0) {
             DevScalars *sc = a.sc;
             if (a.mode == GATHER_INIT_NORMS) {
@@ -412,6 +544,7 @@ __global__ void __launch_bounds__(kThreads) gather_kernel(GatherArgs a) {
             } else {
                 finish_trial(sc, t0, t1);
             }
+            publish_f32(sc);
             *a.counter = 0u;
         }
     }
@@ -445,4 +578,54 @@ void launch_perturb(int n_mov, const float *vx, const float *vy, const float *gx
                                                  die_h, w, h);
 }
 
+// Compares the integer-arithmetic conversions of ap_common.cuh with the
+// hardware conversion instructions they replace, on hashed samples that
+// include rounding ties and the carry of a mantissa that rounds up to 2^24.
+__global__ void numerics_selftest_kernel(long long n, ull seed, int *mism) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        ull z = seed + (ull)i * 0x9E3779B97F4A7C15ull;  // splitmix64
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        z ^= z >> 31;
+        const unsigned lo = (unsigned)z, hi = (unsigned)(z >> 32);
+        // float with |s| < 2^31 (biased exponent <= 157), or a tie k + 1/2
+        float s = __uint_as_float((lo & 0x807FFFFFu) | (((hi >> 8) % 158u) << 23));
+        if ((hi & 3u) == 0u) s = (float)((int)(lo & 0xFFFFFu) - 0x80000) + 0.5f;
+        if (f2i_rn_bits(s) != __float2int_rn(s)) atomicAdd(mism + 0, 1);
+        if (f2i_rz_bits(s) != __float2int_rz(s)) atomicAdd(mism + 1, 1);
+        // int64 of any magnitude; 1/8 exact ties, some with an all-ones mantissa
+        const int sh = (int)(hi & 63u);
+        long long v = (long long)(z >> sh);
+        if ((hi & 0x380u) == 0u) {
+            const ull m = (hi & 0x400u) ? 0xFFFFFFull : (0x800000ull | (lo & 0x7FFFFFu));
+            v = (long long)(((m << 1) | 1ull) << (sh % 38));
+        }
+        if (hi & 0x40u) v = (long long)(0ull - (ull)v);
+        if (__float_as_uint(ll2f_rn_bits(v)) != __float_as_uint(__ll2float_rn(v))) atomicAdd(mism + 2, 1);
+        const float c = (__uint_as_float(0x3F800000u | (lo >> 9)) - 1.5f) * 7.98f;  // [-3.99, 3.99)
+        if ((long long)grad_q(c) != (long long)__float2int_rn(c * kGradScale)) atomicAdd(mism + 3, 1);
+        const long long q = (long long)(lo % 8388607u) - 4194303ll;  // |q| < 2^22
+        if (__float_as_uint(i64_to_float(q)) != __float_as_uint(__ll2float_rn(q))) atomicAdd(mism + 4, 1);
+    }
+}
+
 }  // namespace ap
+
+/* Self-check of the conversion helpers; no counterpart in the reference.
+ * mismatches[0..4]: f2i_rn_bits, f2i_rz_bits, ll2f_rn_bits, grad_q,
+ * i64_to_float, each over `samples` hashed inputs. */
+extern "C" int ap_selftest_numerics(int32_t *mismatches, int64_t samples) {
+    if (!mismatches || samples <= 0 || samples > (1ll << 32)) return 1;  // AP_ERR_INVALID_ARG
+    int *d = nullptr;
+    if (cudaMalloc(&d, 5 * sizeof(int)) != cudaSuccess) return 4;  // AP_ERR_CUDA
+    int rc = 0;
+    if (cudaMemset(d, 0, 5 * sizeof(int)) != cudaSuccess) rc = 4;
+    if (!rc) {
+        ap::numerics_selftest_kernel<<<152 * 8, ap::kThreads>>>(samples, 0x243F6A8885A308D3ull, d);
+        if (cudaGetLastError() != cudaSuccess || cudaMemcpy(mismatches, d, 5 * sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
+            rc = 4;
+    }
+    cudaFree(d);
+    return rc;
+}

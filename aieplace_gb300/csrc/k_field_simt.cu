@@ -111,9 +111,11 @@ __global__ void __launch_bounds__(256) gemm_tn_simt(int m, GemmSet s, SpectralEp
     }
 }
 
+// bm: output tile side chosen by the autotuner in field_solver_init (0 = size rule)
 template <bool SPECTRAL>
-void gemm(int m, const GemmSet &s, int batch, const SpectralEpi &e, cudaStream_t st) {
-    if (m >= 512) {
+void gemm(int m, const GemmSet &s, int batch, const SpectralEpi &e, cudaStream_t st, int bm = 0) {
+    if (bm == 0) bm = m >= 512 ? 64 : 32;
+    if (bm == 64 && m % 64 == 0) {
         dim3 grid(m / 64, m / 64, batch);
         gemm_tn_simt<64, SPECTRAL><<<grid, 256, 0, st>>>(m, s, e);
     } else {
@@ -143,6 +145,8 @@ void launch_split_bf16(int n, const float *src, __nv_bfloat16 *hi, __nv_bfloat16
     if (blocks > 4096) blocks = 4096;
     split_kernel<<<blocks, 256, 0, st>>>(n, src, hi, lo);
 }
+
+static int tune_simt(FieldSolver &f);
 
 int field_solver_init(FieldSolver &f, int m, float bin_ratio, int want_bf16) {
     f = FieldSolver();
@@ -187,7 +191,7 @@ int field_solver_init(FieldSolver &f, int m, float bin_ratio, int want_bf16) {
         launch_split_bf16((int)nn, f.St, f.St_hi, f.St_lo, 0);
     }
     if (cudaDeviceSynchronize() != cudaSuccess) return AP_ERR_CUDA;
-    return AP_OK;
+    return tune_simt(f);
 }
 
 void field_solver_free(FieldSolver &f) {
@@ -205,14 +209,51 @@ void field_solve_fp32(FieldSolver &f, const float *d, float *ex, float *ey, cuda
     const int m = f.m;
     SpectralEpi none{};
     GemmSet s1{{f.C, nullptr}, {d, nullptr}, {f.t0, nullptr}};
-    gemm<false>(m, s1, 1, none, st);
+    gemm<false>(m, s1, 1, none, st, f.simt_bm);
     SpectralEpi epi{f.px, f.py, f.wx, f.wy, 4.0f / ((float)m * (float)m)};
     GemmSet s2{{f.C, nullptr}, {f.t0, nullptr}, {nullptr, nullptr}};
-    gemm<true>(m, s2, 1, epi, st);
+    gemm<true>(m, s2, 1, epi, st, f.simt_bm);
     GemmSet s3{{f.Ct, f.St}, {f.px, f.py}, {f.ux, f.uy}};
-    gemm<false>(m, s3, 2, none, st);
+    gemm<false>(m, s3, 2, none, st, f.simt_bm);
     GemmSet s4{{f.St, f.Ct}, {f.ux, f.uy}, {ex, ey}};
-    gemm<false>(m, s4, 2, none, st);
+    gemm<false>(m, s4, 2, none, st, f.simt_bm);
+}
+
+// Tile autotuner of the FP32 path: times a full solve with 32 and with 64
+// tiles (2 warm, 4 timed) on the solver's own scratch and keeps the faster.
+static int tune_simt(FieldSolver &f) {
+    if (f.m % 64 != 0) {
+        f.simt_bm = 32;
+        return AP_OK;
+    }
+    const size_t nn = (size_t)f.m * f.m;
+    float *din = nullptr, *eo = nullptr;
+    if (dmalloc(&din, 3 * nn)) return AP_ERR_CUDA;
+    eo = din + nn;
+    cudaEvent_t e0, e1;
+    int r = AP_OK;
+    if (cudaMemset(din, 0, sizeof(float) * nn) != cudaSuccess || cudaEventCreate(&e0) != cudaSuccess ||
+        cudaEventCreate(&e1) != cudaSuccess) {
+        cudaFree(din);
+        return AP_ERR_CUDA;
+    }
+    const int cand[2] = {32, 64};
+    for (int v = 0; v < 2 && r == AP_OK; ++v) {
+        f.simt_bm = cand[v];
+        for (int w = 0; w < 2; ++w) field_solve_fp32(f, din, eo, eo + nn, 0);
+        cudaEventRecord(e0, 0);
+        for (int t = 0; t < 4; ++t) field_solve_fp32(f, din, eo, eo + nn, 0);
+        cudaEventRecord(e1, 0);
+        if (cudaEventSynchronize(e1) != cudaSuccess) r = AP_ERR_CUDA;
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        f.simt_tune_ms[v] = ms / 4;
+    }
+    f.simt_bm = f.simt_tune_ms[0] <= f.simt_tune_ms[1] ? 32 : 64;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(din);
+    return r;
 }
 
 // ---- field solve without allocation -------------------------------------------

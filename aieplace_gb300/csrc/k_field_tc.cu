@@ -29,13 +29,22 @@
 namespace ap {
 namespace tc {
 
-constexpr int BM = 128, BN = 64, BK = 64, STAGES = 4, THREADS = 128;
+constexpr int BM = 128, BK = 64, THREADS = 128;
 constexpr int A_TILE = BM * BK * 2;                   // 16 KB
-constexpr int B_TILE = BN * BK * 2;                   // 8 KB
-constexpr int STAGE_BYTES = 2 * A_TILE + 2 * B_TILE;  // 48 KB
-constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
-constexpr uint32_t TMEM_COLS = 64;                    // FP32 accumulator, 128 lanes x 64 columns
 constexpr unsigned long long WAIT_NS = 2000000000ull;  // 2 s bound on any single wait
+
+// Output tile 128 x BN; the accumulator takes BN TMEM columns.  Both shapes
+// fit one CTA per SM; field_solver_bind_bf16 times them and keeps the faster.
+template <int BN_, int STAGES_>
+struct TileCfg {
+    static constexpr int BN = BN_, STAGES = STAGES_;
+    static constexpr int B_TILE = BN * BK * 2;
+    static constexpr int STAGE_BYTES = 2 * A_TILE + 2 * B_TILE;
+    static constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
+    static constexpr uint32_t TMEM_COLS = BN;
+};
+using Tile64 = TileCfg<64, 4>;    // 48 KB stages
+using Tile128 = TileCfg<128, 3>;  // 64 KB stages
 
 enum { EPI_SPLIT = 0, EPI_SPECTRAL = 1, EPI_F32 = 2 };
 
@@ -180,7 +189,10 @@ __device__ __forceinline__ void store_split(const float (&v)[32], __nv_bfloat16 
     }
 }
 
+template <class T>
 __global__ void __launch_bounds__(THREADS, 1) gemm_bf16x3_kernel(const __grid_constant__ Maps maps, Epi e) {
+    constexpr int BN = T::BN, STAGES = T::STAGES, STAGE_BYTES = T::STAGE_BYTES, B_TILE = T::B_TILE;
+    constexpr uint32_t TMEM_COLS = T::TMEM_COLS;
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint64_t *full = (uint64_t *)(smem + STAGES * STAGE_BYTES);
@@ -348,50 +360,37 @@ struct StageMaps {
     Maps s1, s2, s3, s4;
 };
 
-}  // namespace tc
-
-int field_solver_bind_bf16(FieldSolver &f, const __nv_bfloat16 *d_hi, const __nv_bfloat16 *d_lo) {
-    using namespace tc;
-    if (f.m < BM || (f.m % BM) != 0 || !f.C_hi) return AP_ERR_UNSUPPORTED;
-    StageMaps h{};
+// Tensor maps of the four stages for B tiles of `bn` rows.
+bool build_stage_maps(StageMaps &h, const FieldSolver &f, const __nv_bfloat16 *d_hi, const __nv_bfloat16 *d_lo,
+                      int bn) {
     const int m = f.m;
     bool ok = true;
     // S1: T = C . d^T          S2: a = C . T^T (spectral epilogue)
     ok &= make_map(&h.s1.a_hi[0], f.C_hi, m, BM) && make_map(&h.s1.a_lo[0], f.C_lo, m, BM);
-    ok &= make_map(&h.s1.b_hi[0], d_hi, m, BN) && make_map(&h.s1.b_lo[0], d_lo, m, BN);
+    ok &= make_map(&h.s1.b_hi[0], d_hi, m, bn) && make_map(&h.s1.b_lo[0], d_lo, m, bn);
     ok &= make_map(&h.s2.a_hi[0], f.C_hi, m, BM) && make_map(&h.s2.a_lo[0], f.C_lo, m, BM);
-    ok &= make_map(&h.s2.b_hi[0], f.b_t_hi, m, BN) && make_map(&h.s2.b_lo[0], f.b_t_lo, m, BN);
+    ok &= make_map(&h.s2.b_hi[0], f.b_t_hi, m, bn) && make_map(&h.s2.b_lo[0], f.b_t_lo, m, bn);
     // S3: Ux = Ct . Px^T, Uy = St . Py^T      S4: Ex = St . Ux^T, Ey = Ct . Uy^T
     ok &= make_map(&h.s3.a_hi[0], f.Ct_hi, m, BM) && make_map(&h.s3.a_lo[0], f.Ct_lo, m, BM);
-    ok &= make_map(&h.s3.b_hi[0], f.b_px_hi, m, BN) && make_map(&h.s3.b_lo[0], f.b_px_lo, m, BN);
+    ok &= make_map(&h.s3.b_hi[0], f.b_px_hi, m, bn) && make_map(&h.s3.b_lo[0], f.b_px_lo, m, bn);
     ok &= make_map(&h.s3.a_hi[1], f.St_hi, m, BM) && make_map(&h.s3.a_lo[1], f.St_lo, m, BM);
-    ok &= make_map(&h.s3.b_hi[1], f.b_py_hi, m, BN) && make_map(&h.s3.b_lo[1], f.b_py_lo, m, BN);
+    ok &= make_map(&h.s3.b_hi[1], f.b_py_hi, m, bn) && make_map(&h.s3.b_lo[1], f.b_py_lo, m, bn);
     ok &= make_map(&h.s4.a_hi[0], f.St_hi, m, BM) && make_map(&h.s4.a_lo[0], f.St_lo, m, BM);
-    ok &= make_map(&h.s4.b_hi[0], f.b_ux_hi, m, BN) && make_map(&h.s4.b_lo[0], f.b_ux_lo, m, BN);
+    ok &= make_map(&h.s4.b_hi[0], f.b_ux_hi, m, bn) && make_map(&h.s4.b_lo[0], f.b_ux_lo, m, bn);
     ok &= make_map(&h.s4.a_hi[1], f.Ct_hi, m, BM) && make_map(&h.s4.a_lo[1], f.Ct_lo, m, BM);
-    ok &= make_map(&h.s4.b_hi[1], f.b_uy_hi, m, BN) && make_map(&h.s4.b_lo[1], f.b_uy_lo, m, BN);
+    ok &= make_map(&h.s4.b_hi[1], f.b_uy_hi, m, bn) && make_map(&h.s4.b_lo[1], f.b_uy_lo, m, bn);
     // the batch-1 slots of S1/S2 repeat batch 0 (never read: those launches have gridDim.z == 1)
     h.s1.a_hi[1] = h.s1.a_hi[0]; h.s1.a_lo[1] = h.s1.a_lo[0]; h.s1.b_hi[1] = h.s1.b_hi[0]; h.s1.b_lo[1] = h.s1.b_lo[0];
     h.s2.a_hi[1] = h.s2.a_hi[0]; h.s2.a_lo[1] = h.s2.a_lo[0]; h.s2.b_hi[1] = h.s2.b_hi[0]; h.s2.b_lo[1] = h.s2.b_lo[0];
-    if (!ok) return AP_ERR_UNSUPPORTED;
-    if (!f.tc_maps && !(f.tc_maps = malloc(sizeof(StageMaps)))) return AP_ERR_CUDA;
-    *reinterpret_cast<StageMaps *>(f.tc_maps) = h;
-    if (!f.tc_status && cudaMalloc(&f.tc_status, sizeof(unsigned int)) != cudaSuccess) return AP_ERR_CUDA;
-    if (cudaMemset(f.tc_status, 0, sizeof(unsigned int)) != cudaSuccess) return AP_ERR_CUDA;
-    if (cudaFuncSetAttribute(gemm_bf16x3_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES) !=
-        cudaSuccess)
-        return AP_ERR_CUDA;
-    f.tc_ready = 1;
-    return AP_OK;
+    return ok;
 }
 
-int field_solve_bf16x3(FieldSolver &f, const __nv_bfloat16 *d_hi, const __nv_bfloat16 *d_lo, float *ex,
-                       float *ey, cudaStream_t st) {
-    using namespace tc;
-    (void)d_hi;
-    (void)d_lo;  // bound into the stage-1 tensor maps by field_solver_bind_bf16
-    if (!f.tc_ready) return AP_ERR_UNSUPPORTED;
-    const StageMaps &h = *reinterpret_cast<const StageMaps *>(f.tc_maps);
+struct TcState {
+    StageMaps maps[2];  // [0] 128 x 64 tiles, [1] 128 x 128 tiles
+};
+
+template <class T>
+void run_stages(const StageMaps &h, FieldSolver &f, float *ex, float *ey, cudaStream_t st) {
     const int m = f.m;
     Epi e{};
     e.m = m;
@@ -399,27 +398,99 @@ int field_solve_bf16x3(FieldSolver &f, const __nv_bfloat16 *d_hi, const __nv_bfl
     e.wx = f.wx;
     e.wy = f.wy;
     e.scale = 4.0f / ((float)m * (float)m);
-    const dim3 g1(m / BN, m / BM, 1), g2(m / BN, m / BM, 2);
+    const dim3 g1(m / T::BN, m / BM, 1), g2(m / T::BN, m / BM, 2);
     e.mode = EPI_SPLIT;
     e.o_hi[0] = f.b_t_hi;
     e.o_lo[0] = f.b_t_lo;
-    gemm_bf16x3_kernel<<<g1, THREADS, SMEM_BYTES, st>>>(h.s1, e);
+    gemm_bf16x3_kernel<T><<<g1, THREADS, T::SMEM_BYTES, st>>>(h.s1, e);
     e.mode = EPI_SPECTRAL;
     e.o_hi[0] = f.b_px_hi;
     e.o_lo[0] = f.b_px_lo;
     e.o_hi[1] = f.b_py_hi;
     e.o_lo[1] = f.b_py_lo;
-    gemm_bf16x3_kernel<<<g1, THREADS, SMEM_BYTES, st>>>(h.s2, e);
+    gemm_bf16x3_kernel<T><<<g1, THREADS, T::SMEM_BYTES, st>>>(h.s2, e);
     e.mode = EPI_SPLIT;
     e.o_hi[0] = f.b_ux_hi;
     e.o_lo[0] = f.b_ux_lo;
     e.o_hi[1] = f.b_uy_hi;
     e.o_lo[1] = f.b_uy_lo;
-    gemm_bf16x3_kernel<<<g2, THREADS, SMEM_BYTES, st>>>(h.s3, e);
+    gemm_bf16x3_kernel<T><<<g2, THREADS, T::SMEM_BYTES, st>>>(h.s3, e);
     e.mode = EPI_F32;
     e.o_f32[0] = ex;
     e.o_f32[1] = ey;
-    gemm_bf16x3_kernel<<<g2, THREADS, SMEM_BYTES, st>>>(h.s4, e);
+    gemm_bf16x3_kernel<T><<<g2, THREADS, T::SMEM_BYTES, st>>>(h.s4, e);
+}
+
+void run_variant(int v, FieldSolver &f, float *ex, float *ey, cudaStream_t st) {
+    const TcState &s = *reinterpret_cast<const TcState *>(f.tc_maps);
+    if (v == 1)
+        run_stages<Tile128>(s.maps[1], f, ex, ey, st);
+    else
+        run_stages<Tile64>(s.maps[0], f, ex, ey, st);
+}
+
+}  // namespace tc
+
+// Builds the tensor maps of both tile shapes, then times one full solve of
+// each (3 warm, 5 timed, CUDA events) and keeps the faster: the tile
+// autotuner of the tensor-core path.  The scratch outputs are overwritten.
+int field_solver_bind_bf16(FieldSolver &f, const __nv_bfloat16 *d_hi, const __nv_bfloat16 *d_lo) {
+    using namespace tc;
+    if (f.m < BM || (f.m % BM) != 0 || !f.C_hi) return AP_ERR_UNSUPPORTED;
+    TcState s{};
+    if (!build_stage_maps(s.maps[0], f, d_hi, d_lo, Tile64::BN) ||
+        !build_stage_maps(s.maps[1], f, d_hi, d_lo, Tile128::BN))
+        return AP_ERR_UNSUPPORTED;
+    if (!f.tc_maps && !(f.tc_maps = malloc(sizeof(TcState)))) return AP_ERR_CUDA;
+    *reinterpret_cast<TcState *>(f.tc_maps) = s;
+    if (!f.tc_status && cudaMalloc(&f.tc_status, sizeof(unsigned int)) != cudaSuccess) return AP_ERR_CUDA;
+    if (cudaMemset(f.tc_status, 0, sizeof(unsigned int)) != cudaSuccess) return AP_ERR_CUDA;
+    if (cudaFuncSetAttribute(gemm_bf16x3_kernel<Tile64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             Tile64::SMEM_BYTES) != cudaSuccess ||
+        cudaFuncSetAttribute(gemm_bf16x3_kernel<Tile128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             Tile128::SMEM_BYTES) != cudaSuccess)
+        return AP_ERR_CUDA;
+    // the input map holds whatever the caller's buffer holds; timing does not depend on values
+    if (cudaMemset((void *)d_hi, 0, sizeof(__nv_bfloat16) * (size_t)f.m * f.m) != cudaSuccess ||
+        cudaMemset((void *)d_lo, 0, sizeof(__nv_bfloat16) * (size_t)f.m * f.m) != cudaSuccess)
+        return AP_ERR_CUDA;
+    cudaEvent_t e0, e1;
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) return AP_ERR_CUDA;
+    float best = 1e30f;
+    f.tc_variant = 0;
+    for (int v = 0; v < 2; ++v) {
+        for (int w = 0; w < 3; ++w) run_variant(v, f, f.ux, f.uy, 0);
+        cudaEventRecord(e0, 0);
+        for (int t = 0; t < 5; ++t) run_variant(v, f, f.ux, f.uy, 0);
+        cudaEventRecord(e1, 0);
+        if (cudaEventSynchronize(e1) != cudaSuccess) {
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            return AP_ERR_CUDA;
+        }
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        f.tc_tune_ms[v] = ms / 5;
+        if (ms < best) {
+            best = ms;
+            f.tc_variant = v;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    unsigned int st = 0;
+    if (cudaMemcpy(&st, f.tc_status, sizeof(st), cudaMemcpyDeviceToHost) != cudaSuccess) return AP_ERR_CUDA;
+    if (st) return AP_ERR_TIMEOUT;
+    f.tc_ready = 1;
+    return AP_OK;
+}
+
+int field_solve_bf16x3(FieldSolver &f, const __nv_bfloat16 *d_hi, const __nv_bfloat16 *d_lo, float *ex,
+                       float *ey, cudaStream_t st) {
+    (void)d_hi;
+    (void)d_lo;  // bound into the stage-1 tensor maps by field_solver_bind_bf16
+    if (!f.tc_ready) return AP_ERR_UNSUPPORTED;
+    tc::run_variant(f.tc_variant, f, ex, ey, st);
     return cudaGetLastError() == cudaSuccess ? AP_OK : AP_ERR_CUDA;
 }
 

@@ -13,8 +13,8 @@
 //   dWA/dx_i = a+_i/b+ (1 + (x_i - WA+)/g) - a-_i/b- (1 - (x_i - WA-)/g),
 //   WA+ = x_max + sum a+ (x - x_max) / b+,  WA- = x_min + sum a- (x - x_min) / b-,
 // which keeps FP32 exact where the reference form cancels (x_i/g ~ 1e4).
-// Gradients accumulate as int64 fixed point (2^-32) so the sum over a node's
-// nets is the same whatever order the atomics land in.
+// Each pin's gradient is rounded to 2^-20 and accumulated per node in int64,
+// so the sum over a node's nets is the same whatever order the atomics land in.
 #include "ap_common.cuh"
 #include "ap_kernels.h"
 
@@ -25,6 +25,52 @@ namespace {
 struct AxisTerms {
     float inv_bp, inv_bm, wp, wm;  // 1/b+, 1/b-, shifted WA+ - x_max, WA- - x_min
 };
+
+// Warp sums of 8 values at once (transposed butterfly): halving exchanges at
+// offsets 16, 8, 4 leave lane L with a partial of quantity (L >> 2) & 7,
+// offsets 2, 1 finish it, and 8 broadcasts hand every lane every total --
+// 17 shuffles instead of 40.  Fixed order, so the same on every run.
+__device__ __forceinline__ void warp_sum8(float v[8]) {
+    const int lane = threadIdx.x & 31;
+    const bool a = lane & 16, b = lane & 8, c = lane & 4;
+    float u[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const float send = a ? v[k] : v[k + 4];
+        u[k] = (a ? v[k + 4] : v[k]) + __shfl_xor_sync(0xffffffffu, send, 16);
+    }
+    float t[2];
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        const float send = b ? u[k] : u[k + 2];
+        t[k] = (b ? u[k + 2] : u[k]) + __shfl_xor_sync(0xffffffffu, send, 8);
+    }
+    float s = (c ? t[1] : t[0]) + __shfl_xor_sync(0xffffffffu, c ? t[0] : t[1], 4);
+    s += __shfl_xor_sync(0xffffffffu, s, 2);
+    s += __shfl_xor_sync(0xffffffffu, s, 1);
+    // lane L holds quantity q = 4 a + 2 b + c = (L >> 2) & 7
+#pragma unroll
+    for (int q = 0; q < 8; ++q) v[q] = __shfl_sync(0xffffffffu, s, 4 * q);
+}
+
+// Warp maxima of 4 values at once, the same scheme: 10 shuffles instead of 20.
+__device__ __forceinline__ void warp_max4(float v[4]) {
+    const int lane = threadIdx.x & 31;
+    const bool a = lane & 16, b = lane & 8;
+    float u[2];
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        const float send = a ? v[k] : v[k + 2];
+        u[k] = fmaxf(a ? v[k + 2] : v[k], __shfl_xor_sync(0xffffffffu, send, 16));
+    }
+    float s = fmaxf(b ? u[1] : u[0], __shfl_xor_sync(0xffffffffu, b ? u[0] : u[1], 8));
+    s = fmaxf(s, __shfl_xor_sync(0xffffffffu, s, 4));
+    s = fmaxf(s, __shfl_xor_sync(0xffffffffu, s, 2));
+    s = fmaxf(s, __shfl_xor_sync(0xffffffffu, s, 1));
+    // lane L holds quantity q = 2 a + b = (L >> 3) & 3
+#pragma unroll
+    for (int q = 0; q < 4; ++q) v[q] = __shfl_sync(0xffffffffu, s, 8 * q);
+}
 
 // One net with d <= D pins held in registers by one thread.
 template <int D>
@@ -95,7 +141,7 @@ __device__ __forceinline__ void net_thread(const int *__restrict__ pins, int d, 
 template <int D, int B>
 __global__ void __launch_bounds__(kThreads) wa_small_kernel(WaArgs a) {
     __shared__ double red[32];
-    const float gamma = a.gamma > 0.f ? a.gamma : (float)a.sc->gamma;
+    const float gamma = a.gamma > 0.f ? a.gamma : a.sc->f_gamma;
     const float inv_g = 1.f / gamma;
     const float *px = a.px, *py = a.py;
     if (a.mode == WA_LOOP) {
@@ -112,21 +158,24 @@ __global__ void __launch_bounds__(kThreads) wa_small_kernel(WaArgs a) {
         const int d = __ldg(a.net_ptr + e + 1) - s;
         net_thread<D>(a.pin_node + s, d, px, py, inv_g, a.gqx, a.gqy, a.n_grad, hpf, waf);
     }
-    const double hp = block_sum((double)hpf, red);
-    const double wa = block_sum((double)waf, red);
+    // per-block partials in FP32 (folded with compensation by the last block
+    // of the warp-per-net launch)
+    const float hp = block_sum_ff(hpf, reinterpret_cast<float *>(red));
+    const float wa = block_sum_ff(waf, reinterpret_cast<float *>(red));
     int off = 0;
 #pragma unroll
     for (int b = 0; b < B; ++b) off += a.bucket_blocks[b];
     if (threadIdx.x == 0) {
-        a.partials[2 * (off + blockIdx.x)] = hp;
-        a.partials[2 * (off + blockIdx.x) + 1] = wa;
+        float *pf = reinterpret_cast<float *>(a.partials);
+        pf[2 * (off + blockIdx.x)] = hp;
+        pf[2 * (off + blockIdx.x) + 1] = wa;
     }
 }
 
 // Nets [n_small, n_nets): one warp per net, any degree.
 __global__ void __launch_bounds__(kThreads) wa_large_kernel(WaArgs a) {
     __shared__ double red[32];
-    const float gamma = a.gamma > 0.f ? a.gamma : (float)a.sc->gamma;
+    const float gamma = a.gamma > 0.f ? a.gamma : a.sc->f_gamma;
     const float inv_g = 1.f / gamma;
     const float *px = a.px, *py = a.py;
     if (a.mode == WA_LOOP) {
@@ -151,32 +200,46 @@ __global__ void __launch_bounds__(kThreads) wa_large_kernel(WaArgs a) {
             const float c0[2] = {v0 ? __ldg(px + n0) : 0.f, v0 ? __ldg(py + n0) : 0.f};
             const float c1[2] = {v1 ? __ldg(px + n1) : 0.f, v1 ? __ldg(py + n1) : 0.f};
             float mx[2], mn[2];
+            {
+                float m4[4];
 #pragma unroll
-            for (int ax = 0; ax < 2; ++ax) {
-                mx[ax] = fmaxf(v0 ? c0[ax] : -3.0e38f, v1 ? c1[ax] : -3.0e38f);
-                mn[ax] = fminf(v0 ? c0[ax] : 3.0e38f, v1 ? c1[ax] : 3.0e38f);
+                for (int ax = 0; ax < 2; ++ax) {
+                    m4[ax] = fmaxf(v0 ? c0[ax] : -3.0e38f, v1 ? c1[ax] : -3.0e38f);
+                    m4[2 + ax] = fmaxf(v0 ? -c0[ax] : -3.0e38f, v1 ? -c1[ax] : -3.0e38f);
+                }
+                warp_max4(m4);
 #pragma unroll
-                for (int o = 16; o > 0; o >>= 1) {
-                    mx[ax] = fmaxf(mx[ax], __shfl_xor_sync(0xffffffffu, mx[ax], o));
-                    mn[ax] = fminf(mn[ax], __shfl_xor_sync(0xffffffffu, mn[ax], o));
+                for (int ax = 0; ax < 2; ++ax) {
+                    mx[ax] = m4[ax];
+                    mn[ax] = -m4[2 + ax];
                 }
             }
-            float ep0[2], em0[2], ep1[2], em1[2], gsum[2][2];
+            float ep0[2], em0[2], ep1[2], em1[2], dp0[2], dm0[2], dp1[2], dm1[2], s8[8], gsum[2][2];
+#pragma unroll
+            for (int ax = 0; ax < 2; ++ax) {
+                dp0[ax] = c0[ax] - mx[ax];
+                dm0[ax] = c0[ax] - mn[ax];
+                dp1[ax] = c1[ax] - mx[ax];
+                dm1[ax] = c1[ax] - mn[ax];
+                ep0[ax] = v0 ? __expf(dp0[ax] * inv_g) : 0.f;
+                em0[ax] = v0 ? __expf(-dm0[ax] * inv_g) : 0.f;
+                ep1[ax] = v1 ? __expf(dp1[ax] * inv_g) : 0.f;
+                em1[ax] = v1 ? __expf(-dm1[ax] * inv_g) : 0.f;
+                s8[4 * ax + 0] = ep0[ax] + ep1[ax];
+                s8[4 * ax + 1] = em0[ax] + em1[ax];
+                s8[4 * ax + 2] = ep0[ax] * dp0[ax] + ep1[ax] * dp1[ax];
+                s8[4 * ax + 3] = em0[ax] * dm0[ax] + em1[ax] * dm1[ax];
+            }
+            warp_sum8(s8);
             float wa_net = 0.f;
 #pragma unroll
             for (int ax = 0; ax < 2; ++ax) {
-                const float dp0 = c0[ax] - mx[ax], dm0 = c0[ax] - mn[ax];
-                const float dp1 = c1[ax] - mx[ax], dm1 = c1[ax] - mn[ax];
-                ep0[ax] = v0 ? __expf(dp0 * inv_g) : 0.f;
-                em0[ax] = v0 ? __expf(-dm0 * inv_g) : 0.f;
-                ep1[ax] = v1 ? __expf(dp1 * inv_g) : 0.f;
-                em1[ax] = v1 ? __expf(-dm1 * inv_g) : 0.f;
-                const float bp = warp_sum(ep0[ax] + ep1[ax]), bm = warp_sum(em0[ax] + em1[ax]);
-                const float cp = warp_sum(ep0[ax] * dp0 + ep1[ax] * dp1);
-                const float cm = warp_sum(em0[ax] * dm0 + em1[ax] * dm1);
-                const float ibp = 1.f / bp, ibm = 1.f / bm, wp = cp * ibp, wm = cm * ibm;
-                gsum[ax][0] = ep0[ax] * ibp * (1.f + (dp0 - wp) * inv_g) - em0[ax] * ibm * (1.f - (dm0 - wm) * inv_g);
-                gsum[ax][1] = ep1[ax] * ibp * (1.f + (dp1 - wp) * inv_g) - em1[ax] * ibm * (1.f - (dm1 - wm) * inv_g);
+                const float ibp = 1.f / s8[4 * ax + 0], ibm = 1.f / s8[4 * ax + 1];
+                const float wp = s8[4 * ax + 2] * ibp, wm = s8[4 * ax + 3] * ibm;
+                gsum[ax][0] = ep0[ax] * ibp * (1.f + (dp0[ax] - wp) * inv_g) -
+                              em0[ax] * ibm * (1.f - (dm0[ax] - wm) * inv_g);
+                gsum[ax][1] = ep1[ax] * ibp * (1.f + (dp1[ax] - wp) * inv_g) -
+                              em1[ax] * ibm * (1.f - (dm1[ax] - wm) * inv_g);
                 wa_net += (mx[ax] - mn[ax]) + wp - wm;
             }
             if (v0 && n0 < a.n_grad) {
@@ -202,12 +265,13 @@ __global__ void __launch_bounds__(kThreads) wa_large_kernel(WaArgs a) {
             ymx = fmaxf(ymx, y);
             ymn = fminf(ymn, y);
         }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            xmx = fmaxf(xmx, __shfl_xor_sync(0xffffffffu, xmx, o));
-            xmn = fminf(xmn, __shfl_xor_sync(0xffffffffu, xmn, o));
-            ymx = fmaxf(ymx, __shfl_xor_sync(0xffffffffu, ymx, o));
-            ymn = fminf(ymn, __shfl_xor_sync(0xffffffffu, ymn, o));
+        {
+            float m4[4] = {xmx, ymx, -xmn, -ymn};
+            warp_max4(m4);
+            xmx = m4[0];
+            ymx = m4[1];
+            xmn = -m4[2];
+            ymn = -m4[3];
         }
         float s8[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};  // bp bm cp cm for x then y
         for (int j = lane; j < d; j += 32) {
@@ -223,8 +287,7 @@ __global__ void __launch_bounds__(kThreads) wa_large_kernel(WaArgs a) {
                 s8[4 * ax + 3] += em * dm;
             }
         }
-#pragma unroll
-        for (int k = 0; k < 8; ++k) s8[k] = warp_sum(s8[k]);
+        warp_sum8(s8);
         AxisTerms t[2];
 #pragma unroll
         for (int ax = 0; ax < 2; ++ax) {
@@ -253,23 +316,18 @@ __global__ void __launch_bounds__(kThreads) wa_large_kernel(WaArgs a) {
             waf += ((xmx - xmn) + t[0].wp - t[0].wm) + ((ymx - ymn) + t[1].wp - t[1].wm);
         }
     }
-    const double hp = block_sum((double)hpf, red);
-    const double wa = block_sum((double)waf, red);
-    double *part = a.partials + 2 * a.small_blocks;
+    const float hp = block_sum_ff(hpf, reinterpret_cast<float *>(red));
+    const float wa = block_sum_ff(waf, reinterpret_cast<float *>(red));
+    float *pf = reinterpret_cast<float *>(a.partials);
     if (threadIdx.x == 0) {
-        part[2 * blockIdx.x] = hp;
-        part[2 * blockIdx.x + 1] = wa;
+        pf[2 * (a.small_blocks + blockIdx.x)] = hp;
+        pf[2 * (a.small_blocks + blockIdx.x) + 1] = wa;
     }
     // the last block of this launch folds both launches' partials
     if (arrive_last(a.counter)) {
         const int nb = a.small_blocks + gridDim.x;
-        double h = 0.0, w = 0.0;
-        for (int i = threadIdx.x; i < nb; i += blockDim.x) {
-            h += __ldcg(a.partials + 2 * i);
-            w += __ldcg(a.partials + 2 * i + 1);
-        }
-        h = block_sum(h, red);
-        w = block_sum(w, red);
+        const double h = block_sum_f(kahan_strided(pf, threadIdx.x, nb, blockDim.x, 2), red);
+        const double w = block_sum_f(kahan_strided(pf + 1, threadIdx.x, nb, blockDim.x, 2), red);
         if (threadIdx.x == 0) {
             if (a.out) {
                 a.out[0] = h;

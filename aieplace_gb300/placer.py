@@ -97,6 +97,13 @@ class Placer:
         check("ap_profile_stages", lib().ap_profile_stages(self._h, int(n_trials), ptr(out), C.byref(n)))
         return [float(v) for v in out[: n.value]]
 
+    def solver_info(self) -> dict:
+        tn, st = C.c_int32(), C.c_int32()
+        tms, sms = np.zeros(2, np.float32), np.zeros(2, np.float32)
+        check("ap_solver_info", lib().ap_solver_info(self._h, C.byref(tn), ptr(tms), C.byref(st), ptr(sms)))
+        return {"tc_tile_n": tn.value, "tc_ms": [float(v) for v in tms], "simt_tile": st.value,
+                "simt_ms": [float(v) for v in sms]}
+
     def run(self) -> int:
         done = C.c_int32()
         check("ap_run", lib().ap_run(self._h, C.byref(done)))
@@ -167,3 +174,73 @@ class Placer:
     def restore(self, blob: bytes):
         buf = np.frombuffer(blob, np.uint8).copy()
         check("ap_restore", lib().ap_restore(self._h, ptr(buf), len(buf)))
+
+
+class BatchPlacer:
+    """Independent placements stepped together (ap_create_batch): one CUDA
+    graph launch advances one trial step of every active instance."""
+
+    def __init__(self, netlists: list[dict], field_solver: str = "fp32", **overrides):
+        n = len(netlists)
+        self._keep = []
+        nls = (Netlist * n)()
+        prms = (Params * n)()
+        self.sizes = []
+        for i, nl in enumerate(netlists):
+            p = default_params()
+            p.bins_x = p.bins_y = int(nl["bins"])
+            p.target_density = float(nl["target_density"])
+            p.field_solver = SOLVERS[field_solver]
+            for k, v in overrides.items():
+                setattr(p, k, v)
+            prms[i] = p
+            a = {k: np.ascontiguousarray(nl[k]) for k in
+                 ("net_ptr", "pin_node", "node_w", "node_h", "node_x", "node_y", "node_fixed")}
+            self._keep.append(a)
+            die = np.asarray(nl["die"], np.float32)
+            nls[i] = Netlist(len(a["node_w"]), len(a["net_ptr"]) - 1, len(a["pin_node"]), ptr(a["net_ptr"]),
+                             ptr(a["pin_node"]), ptr(a["node_w"]), ptr(a["node_h"]), ptr(a["node_x"]),
+                             ptr(a["node_y"]), ptr(a["node_fixed"]), float(die[0]), float(die[1]),
+                             float(die[2]), float(die[3]))
+            self.sizes.append(len(a["node_w"]))
+        h = C.c_void_p()
+        check("ap_create_batch", lib().ap_create_batch(n, C.cast(nls, C.c_void_p), C.cast(prms, C.c_void_p),
+                                                       C.byref(h)))
+        self._h = h
+        self.n = n
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().ap_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def initialize_placement(self, seed: int = 0, sigma: float = 1.0):
+        check("ap_batch_init_seeded", lib().ap_batch_init_seeded(self._h, int(seed), float(sigma)))
+
+    def step(self, n_trials: int):
+        check("ap_batch_step", lib().ap_batch_step(self._h, int(n_trials)))
+
+    def run(self) -> list[int]:
+        it = np.zeros(self.n, np.int32)
+        check("ap_batch_run", lib().ap_batch_run(self._h, ptr(it)))
+        return [int(v) for v in it]
+
+    def stats(self, i: int) -> dict:
+        s = Stats()
+        check("ap_batch_get_stats", lib().ap_batch_get_stats(self._h, int(i), C.byref(s)))
+        return s.as_dict()
+
+    def positions(self, i: int):
+        x = np.zeros(self.sizes[i], np.float32)
+        y = np.zeros(self.sizes[i], np.float32)
+        check("ap_batch_get_positions", lib().ap_batch_get_positions(self._h, int(i), ptr(x), ptr(y)))
+        return x, y

@@ -33,6 +33,22 @@ PRESETS = {
 }
 
 
+def batch_specs(n: int = 64, seed: int = 1, lo: int = 5_000, hi: int = 150_000) -> list[dict]:
+    """The batched workload: cell counts LogUniform[lo, hi], the c1 net and
+    macro statistics, bins the power of two at or above sqrt(cells / 4) clamped to
+    [128, 512], target density 0.7."""
+    rng = np.random.default_rng(seed)
+    specs = []
+    for i in range(n):
+        cells = int(round(float(np.exp(rng.uniform(np.log(lo), np.log(hi))))))
+        bins = int(2 ** np.ceil(np.log2(np.sqrt(cells / 4.0))))
+        bins = min(512, max(128, bins))
+        specs.append(dict(num_cells=cells, num_nets=int(round(1.05 * cells)), num_macros=max(1, cells // 50),
+                          num_pads=0, unit_cells=0, degree_mix=1, locality=0.8, window=64, target_density=0.7,
+                          die_side=0.0, bins=bins))
+    return specs
+
+
 def generate(preset: str | dict, seed: int = 1) -> dict:
     """Returns a dict of numpy arrays: net_ptr, pin_node, node_w/h/x/y, node_fixed,
     die (xl, yl, xh, yh), plus 'bins' and 'target_density' of the preset."""

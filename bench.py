@@ -232,6 +232,60 @@ def profile_mode(args):
                       "overflow": s["overflow"], "iteration": s["iteration"]}))
 
 
+def batch_mode(args):
+    """Batched form: n instances (cell counts LogUniform[5k, 150k], bins 128..512,
+    FP32) as parallel branches of one CUDA graph.  Reports instance-iterations
+    per second of device time over K graph launches and the wall time until
+    every instance is below 10% overflow, next to stepping the instances one
+    after another on their own graphs."""
+    import torch
+
+    import aieplace_gb300 as ap
+    from aieplace_gb300 import build as b
+
+    b.build()
+    specs = ap.synth.batch_specs(args.batch, seed=1)
+    nls = [ap.synth.generate(s, seed=100 + i) for i, s in enumerate(specs)]
+    cells = sum(int((nl["node_fixed"] == 0).sum()) for nl in nls)
+    with ap.BatchPlacer(nls, max_iterations=4000, check_interval=32) as bp:
+        bp.initialize_placement(seed=5, sigma=1.0)
+        bp.step(args.warmup)
+        it0 = sum(bp.stats(i)["iteration"] for i in range(bp.n))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        bp.step(args.steps)
+        el = time.perf_counter() - t0
+        it1 = sum(bp.stats(i)["iteration"] for i in range(bp.n))
+    with ap.BatchPlacer(nls, max_iterations=4000, check_interval=32) as bp:
+        bp.initialize_placement(seed=5, sigma=1.0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        its = bp.run()
+        ttt = time.perf_counter() - t0
+        st = [bp.stats(i) for i in range(bp.n)]
+        over = [s["overflow"] for s in st]
+        missed = [{"instance": i, "cells": specs[i]["num_cells"], "bins": specs[i]["bins"],
+                   "iteration": s["iteration"], "overflow": s["overflow"], "lambda": s["lambda"],
+                   "status": s["status"]} for i, s in enumerate(st) if not s["overflow"] < 0.10]
+    # the same instances one after another, each on its own graph
+    t0 = time.perf_counter()
+    seq_its = 0
+    for i, nl in enumerate(nls[: min(8, len(nls))]):
+        with ap.Placer(nl) as pl:
+            pl.initialize_placement(seed=5 + i, sigma=1.0)
+            pl.step_async(args.steps)
+            torch.cuda.synchronize()
+            seq_its += pl.stats()["iteration"]
+    seq_el = time.perf_counter() - t0
+    print(json.dumps({
+        "metric": "batched instance-iterations/s", "value": (it1 - it0) / el, "unit": "instance-iters/s",
+        "instances": len(nls), "cells_total": cells, "steps": args.steps, "warmup": args.warmup,
+        "graph_launch_ms": 1000 * el / args.steps, "time_to_10pct_all_s": ttt, "iterations": its,
+        "reached": sum(o < 0.10 for o in over), "not_reached": missed,
+        "sequential_instance_iters_per_s_first8": seq_its / seq_el,
+        "bins": [s["bins"] for s in specs], "dtype": "f32", "data": "synthetic"}))
+
+
 def time_to_target(ap, nl, solver, target=0.10, max_iter=4000):
     import torch
 
@@ -258,6 +312,8 @@ def main():
     ap_.add_argument("--solver", default="auto", choices=["auto", "fp32", "bf16x3"])
     ap_.add_argument("--no-cpu-baseline", action="store_true")
     ap_.add_argument("--no-ttt", action="store_true", help="skip the time-to-10%% runs")
+    ap_.add_argument("--batch", type=int, default=0,
+                     help="batched form instead: this many instances (5k-150k cells) in one graph")
     ap_.add_argument("--profile-after", type=int, default=-1,
                      help="profiling mode: run this many iterations, then one eager trial step inside the "
                           "NVTX range 'ap_profile' (for ncu --nvtx-include ap_profile/), print nothing else")
@@ -267,6 +323,8 @@ def main():
         return reference_arm(args)
     if args.profile_after >= 0:
         return profile_mode(args)
+    if args.batch:
+        return batch_mode(args)
 
     import numpy as np
     import torch

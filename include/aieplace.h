@@ -150,6 +150,12 @@ int ap_step_async(ap_handle *h, int32_t n_trials);
  * [3] field solve, [4] field gather + step control.  *n_stages = 5. */
 int ap_profile_stages(ap_handle *h, int32_t n_trials, float *stage_ms, int32_t *n_stages);
 
+/* Tile shapes the autotuner picked at ap_create for this bin count, and the
+ * solve times it measured: tc_tile_n is the N side of the tensor-core tile
+ * (64 or 128; 0 if the tensor-core path is unavailable), simt_tile the FP32
+ * tile side (32 or 64); tc_ms[2] and simt_ms[2] the candidates' times. */
+int ap_solver_info(ap_handle *h, int32_t *tc_tile_n, float *tc_ms, int32_t *simt_tile, float *simt_ms);
+
 /* Iterates until overflow < params.target_overflow or max_iterations;
  * replaces Placer::run (AIEplace.cpp:44-76). */
 int ap_run(ap_handle *h, int32_t *iterations_done);
@@ -210,10 +216,43 @@ int ap_field_solve(ap_handle *h, const float *density, float *ex, float *ey, int
 int ap_field_solve_noalloc(const float *density, float *ex, float *ey, int32_t bins, float bin_ratio,
                            void *cuda_stream);
 
+/* Self-check of the library's integer-arithmetic float<->integer conversions
+ * (used on the hot path in place of conversion instructions) against the
+ * GPU's own conversion instructions.  No counterpart in the reference.
+ * mismatches[5] receives the number of differing results of: round-to-nearest
+ * float->int32, truncating float->int32, int64->float, the gradient
+ * quantiser, small int64->float; each over `samples` (<= 2^32) hashed inputs
+ * including rounding ties.  Runs on the current device, synchronously. */
+int ap_selftest_numerics(int32_t *mismatches, int64_t samples);
+
 /* ---- checkpoint / resume ----------------------------------------------- */
 int ap_snapshot_size(ap_handle *h, size_t *bytes);
 int ap_snapshot(ap_handle *h, void *buf, size_t bytes);
 int ap_restore(ap_handle *h, const void *buf, size_t bytes);
+
+/* ---- batched form ---------------------------------------------------------
+ * Many independent placements stepped together.  The reference places one
+ * design per run (Placer::run, AIEplace.cpp:44-76); small designs cannot fill
+ * a GB300 alone, so a batch captures one trial step of every instance as
+ * parallel branches of one CUDA graph and advances all of them with one graph
+ * launch.  Instances keep their own parameters (bin counts may differ) and
+ * produce exactly the results they produce when stepped alone. */
+typedef struct ap_batch ap_batch;
+
+int ap_create_batch(int32_t n, const ap_netlist *netlists, const ap_params *params, ap_batch **out);
+int ap_batch_destroy(ap_batch *b);
+/* instance i gets ap_init_seeded(seed + i, sigma) */
+int ap_batch_init_seeded(ap_batch *b, uint64_t seed, float sigma);
+/* n_trials graph launches (each one trial step of every active instance) */
+int ap_batch_step(ap_batch *b, int32_t n_trials);
+/* steps until every instance has overflow < its target_overflow (or reached
+ * its max_iterations); converged instances leave the graph, and so does an
+ * instance whose optimiser diverges (its ap_stats.status then reads
+ * AP_ERR_DIVERGED; the others go on).  iterations[i] receives instance i's
+ * accepted iterations (may be NULL). */
+int ap_batch_run(ap_batch *b, int32_t *iterations);
+int ap_batch_get_stats(ap_batch *b, int32_t i, ap_stats *stats);
+int ap_batch_get_positions(ap_batch *b, int32_t i, float *x, float *y);
 
 /* ---- seeded synthetic netlists ------------------------------------------ */
 /* Stands in for the ISPD suites the reference reads through LEF/DEF.  Nodes

@@ -17,6 +17,7 @@
 #endif
 
 #define OR_PI 3.14159265358979323846
+#define OR_LAMBDA_MAX 1e30 /* density penalty cap, the same as the CUDA path */
 
 int or_set_threads(int n) {
 #ifdef _OPENMP
@@ -691,6 +692,10 @@ void or_step(or_placer *o, int n) {
         if (mu < o->p.mu_min) mu = o->p.mu_min;
         if (mu > o->p.mu_max) mu = o->p.mu_max;
         o->lambda *= mu;
+        /* capped where the density term dominates completely: keeps the
+         * CUDA path's FP32 products finite when the target overflow is out
+         * of reach and lambda would otherwise grow 5% per iteration forever */
+        if (o->lambda > OR_LAMBDA_MAX) o->lambda = OR_LAMBDA_MAX;
         o->hpwl_prev = o->hpwl;
         o->iteration++;
     }

@@ -67,6 +67,17 @@ def test_density_map_bit_exact_full_size(ap, oracle_lib):
     assert got.sum() == ref.sum()
 
 
+def test_conversion_helpers_match_hardware(ap):
+    """The hot path rounds and converts with integer arithmetic (the FP64 pipe
+    that executes conversion instructions is narrow on this part); every helper
+    must give the conversion instruction's result bit for bit."""
+    from aieplace_gb300._lib import check, lib, ptr
+
+    m = np.zeros(5, np.int32)
+    check("ap_selftest_numerics", lib().ap_selftest_numerics(ptr(m), 1 << 26))
+    assert m.tolist() == [0, 0, 0, 0, 0]
+
+
 @pytest.mark.parametrize("preset,gamma", [("c0", 4.0), ("c1_small", 0.7), ("c1_small", 25.0)])
 def test_wirelength_gradient(ap, oracle_lib, preset, gamma):
     nl = ap.synth.generate(preset, seed=5)
