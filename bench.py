@@ -373,7 +373,9 @@ def main():
         dist.barrier()
     torch.cuda.synchronize()
     ev0.record(stream)
+    torch.cuda.nvtx.range_push("ap_timed")  # launch lists: ncu --nvtx --nvtx-include ap_timed/
     pl.step_async(args.steps)
+    torch.cuda.nvtx.range_pop()
     ev1.record(stream)
     torch.cuda.synchronize()
     if world > 1:
