@@ -49,7 +49,9 @@ __device__ __forceinline__ double block_max_f(float v, double *smem) {
 constexpr int kScatterThreads = 512;
 constexpr int kScatterPerThread = 4;
 constexpr int kScatterChunk = kScatterThreads * kScatterPerThread;
+constexpr int kScatterWarps = kScatterThreads / 32;
 constexpr int kScatterWindow = 4096;
+constexpr int kScatterWindowSide = 64;  // window columns when the bounding box does not fit
 
 // A node's contribution as a record of 5 int32: the base bin (c0, r0), the
 // spans nc, nr <= 8 and a small-node flag packed in `bin` (non-negative), the
@@ -140,7 +142,7 @@ __device__ __forceinline__ void for_each_overlap(const Grid &g, float x, float y
 
 __global__ void __launch_bounds__(kScatterThreads, 2) scatter_kernel(ScatterArgs a) {
     __shared__ double red[32];
-    __shared__ int box[4];  // bin bounding box of the chunk: c0, c1, r0, r1
+    __shared__ int box[8];  // bin bounding box of the chunk: c0, c1, r0, r1; sums of c0, r0; count; inside
     __shared__ ull win[kScatterWindow];
     const int n = a.update ? a.n_mov : (a.hi - a.lo);
     float alpha = 0.f, mom = 0.f;
@@ -155,6 +157,7 @@ __global__ void __launch_bounds__(kScatterThreads, 2) scatter_kernel(ScatterArgs
     if (threadIdx.x == 0) {
         box[0] = box[2] = 0x7fffffff;
         box[1] = box[3] = -1;
+        box[4] = box[5] = box[6] = box[7] = 0;
     }
     __syncthreads();
     float du = 0.f;  // per-thread partial in FP32; FP64 from the block sum on
@@ -198,6 +201,16 @@ __global__ void __launch_bounds__(kScatterThreads, 2) scatter_kernel(ScatterArgs
             br1 = max(br1, r1);
         }
     }
+    // sums for the chunk's mean bin, from the records (re-evaluated nodes left out)
+    int sc0 = 0, sr0 = 0, cnt = 0;
+#pragma unroll
+    for (int k = 0; k < kScatterPerThread; ++k) {
+        if (rec[k].bin >= 0) {
+            sc0 += rec_c0(rec[k].bin);
+            sr0 += rec_r0(rec[k].bin);
+            ++cnt;
+        }
+    }
     // the chunk's bin bounding box: warp reduction, then one shared atomic per warp
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -205,26 +218,78 @@ __global__ void __launch_bounds__(kScatterThreads, 2) scatter_kernel(ScatterArgs
         bc1 = max(bc1, __shfl_xor_sync(0xffffffffu, bc1, o));
         br0 = min(br0, __shfl_xor_sync(0xffffffffu, br0, o));
         br1 = max(br1, __shfl_xor_sync(0xffffffffu, br1, o));
+        sc0 += __shfl_xor_sync(0xffffffffu, sc0, o);
+        sr0 += __shfl_xor_sync(0xffffffffu, sr0, o);
+        cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
     }
     if ((threadIdx.x & 31) == 0 && bc1 >= 0) {
         atomicMin(box + 0, bc0);
         atomicMax(box + 1, bc1);
         atomicMin(box + 2, br0);
         atomicMax(box + 3, br1);
+        atomicAdd(box + 4, sc0);
+        atomicAdd(box + 5, sr0);
+        atomicAdd(box + 6, cnt);
     }
     __syncthreads();
-    const int wc0 = box[0], wr0 = box[2];
-    const int wc = box[1] - wc0 + 1, wr = box[3] - wr0 + 1;
-    const bool use_win = box[1] >= 0 && (long long)wc * wr <= kScatterWindow;
+    // The window: the chunk's bounding box if it fits kScatterWindow bins, else
+    // a kScatterWindow-bin rectangle about the chunk's mean bin (a dense core
+    // with outliers, as in the first iterations); adds outside it go straight
+    // to the global map.
+    int wc0 = box[0], wr0 = box[2];
+    int wc = box[1] - wc0 + 1, wr = box[3] - wr0 + 1;
+    bool use_win = box[1] >= 0;
+    if (use_win && wc * wr > kScatterWindow) {
+        const int nm = max(box[6], 1);
+        const int mc = box[4] / nm, mr = box[5] / nm;
+        const int tc = min(wc, kScatterWindowSide), tr = min(wr, kScatterWindow / tc);
+        wc0 = min(max(mc - tc / 2, wc0), wc0 + wc - tc);
+        wr0 = min(max(mr - tr / 2, wr0), wr0 + wr - tr);
+        wc = tc;
+        wr = tr;
+        // worth it only if at least half of the chunk's nodes start inside
+        int in = 0;
+#pragma unroll
+        for (int k = 0; k < kScatterPerThread; ++k)
+            in += rec[k].bin >= 0 && (unsigned)(rec_c0(rec[k].bin) - wc0) < (unsigned)wc &&
+                  (unsigned)(rec_r0(rec[k].bin) - wr0) < (unsigned)wr;
+        in = __reduce_add_sync(0xffffffffu, in);
+        if ((threadIdx.x & 31) == 0) atomicAdd(box + 7, in);
+        __syncthreads();
+        use_win = 2 * box[7] >= nm;
+    }
+    const int W = use_win ? wc * wr : 0;
+    // Clustered chunk (e.g. right after initial placement, every node in a few
+    // bins): one private window per warp, and the lanes of a warp that add to
+    // the same slot are summed first (exact: three 21-bit chunks through
+    // redux), so no two adds in flight hit one address.
+    const bool clustered = use_win && W <= kScatterWindow / kScatterWarps;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     if (use_win) {
-        for (int t = threadIdx.x; t < wc * wr; t += kScatterThreads) win[t] = 0ull;
+        const int nw = clustered ? kScatterWarps * W : W;
+        for (int t = threadIdx.x; t < nw; t += kScatterThreads) win[t] = 0ull;
         __syncthreads();
     }
     // shared-space reduction (red.shared.add.u64) into the window
-    const unsigned win_s = (unsigned)__cvta_generic_to_shared(win);
+    const unsigned win_s = (unsigned)__cvta_generic_to_shared(win) + (clustered ? 8u * (unsigned)(warp * W) : 0u);
     auto add_win = [&](int c, int r, long long v) {
-        const unsigned addr = win_s + 8u * (unsigned)((c - wc0) * wr + (r - wr0));
-        asm volatile("red.shared.add.u64 [%0], %1;" ::"r"(addr), "l"(v) : "memory");
+        if ((unsigned)(c - wc0) >= (unsigned)wc || (unsigned)(r - wr0) >= (unsigned)wr) {
+            atomicAdd(a.rho_q + (long long)c * g.my + r, (ull)v);  // outside the window
+            return;
+        }
+        const int slot = (c - wc0) * wr + (r - wr0);
+        if (clustered) {
+            const unsigned peers = __match_any_sync(__activemask(), slot);
+            if (peers != (1u << lane)) {
+                const ull u = (ull)v;
+                const unsigned s0 = __reduce_add_sync(peers, (unsigned)(u & 0x1FFFFFull));
+                const unsigned s1 = __reduce_add_sync(peers, (unsigned)((u >> 21) & 0x1FFFFFull));
+                const int s2 = __reduce_add_sync(peers, (int)(v >> 42));
+                if (lane != __ffs(peers) - 1) return;
+                v = (long long)s0 + (long long)s1 * (1ll << 21) + (long long)s2 * (1ll << 42);
+            }
+        }
+        asm volatile("red.shared.add.u64 [%0], %1;" ::"r"(win_s + 8u * (unsigned)slot), "l"(v) : "memory");
     };
     auto add_glb = [&](int c, int r, long long v) { atomicAdd(a.rho_q + (long long)c * g.my + r, (ull)v); };
 #pragma unroll
@@ -255,7 +320,9 @@ __global__ void __launch_bounds__(kScatterThreads, 2) scatter_kernel(ScatterArgs
         const int step_c = kScatterThreads / wr, step_r = kScatterThreads % wr;
         int c = threadIdx.x / wr, r = threadIdx.x % wr;
         for (int t = threadIdx.x; t < wc * wr; t += kScatterThreads) {
-            const ull v = win[t];
+            ull v = win[t];
+            if (clustered)
+                for (int w = 1; w < kScatterWarps; ++w) v += win[w * W + t];
             if (v) atomicAdd(a.rho_q + (long long)(wc0 + c) * g.my + (wr0 + r), v);
             c += step_c;
             r += step_r;

@@ -51,6 +51,32 @@ def test_density_map_bit_exact(ap, oracle_lib, preset, bins):
     assert np.array_equal(got, ref)
 
 
+@pytest.mark.parametrize("preset,bins,sigma,outliers", [("c1_small", 512, 1.0, 0.0), ("c1_small", 128, 0.3, 0.0),
+                                                         ("c0", 32, 0.5, 0.0), ("c1_small", 512, 4.0, 0.01)])
+def test_density_map_bit_exact_clustered(ap, oracle_lib, preset, bins, sigma, outliers):
+    """Nodes packed around the die centre (the initial placement): the
+    scatter's per-warp windows with same-slot lane aggregation; with a few
+    outliers anywhere on the die, the window about the chunk's mean bin plus
+    global adds for the rest."""
+    nl = ap.synth.generate(preset, seed=5)
+    rng = np.random.default_rng(2)
+    W, H = float(nl["die"][2]), float(nl["die"][3])
+    x = nl["node_x"].copy()
+    y = nl["node_y"].copy()
+    mov = nl["node_fixed"] == 0
+    x[mov] = (W / 2 + sigma * rng.standard_normal(mov.sum())).astype(np.float32)
+    y[mov] = (H / 2 + sigma * rng.standard_normal(mov.sum())).astype(np.float32)
+    far = np.flatnonzero(mov)[rng.random(mov.sum()) < outliers]
+    x[far] = rng.uniform(0, W, far.size).astype(np.float32)
+    y[far] = rng.uniform(0, H, far.size).astype(np.float32)
+    with ap.Placer(nl, bins=bins) as pl:
+        got = pl.compute_overlaps(x, y)
+    g = oracle_lib.grid(W, H, bins)
+    area = (nl["node_w"] * nl["node_h"]) > 0
+    ref = oracle_lib.density_q(g, x, y, nl["node_w"], nl["node_h"], area.astype(np.uint8))
+    assert np.array_equal(got, ref)
+
+
 def test_density_map_bit_exact_full_size(ap, oracle_lib):
     """2M cells / 1024^2 bins: the shipped mixed-precision workload."""
     nl = ap.synth.generate("c2", seed=1)
