@@ -352,41 +352,61 @@ void launch_scatter(const ScatterArgs &a, cudaStream_t st) {
     scatter_kernel<<<blocks, kScatterThreads, 0, st>>>(a);
 }
 
+// gamma(tau) in FP32 (10^e as 2^(e log2 10)): a single-thread FP64 pow at the
+// end of the kernel costs microseconds on this part's narrow FP64 pipe
 __device__ __forceinline__ double gamma_of(const DevScalars *sc, double tau) {
-    double e = (tau - 0.1) * 20.0 / 9.0 - 1.0;
-    e = fmin(fmax(e, -1.0), 1.0);
-    return sc->gamma_base * sc->bin_avg * pow(10.0, e);
+    float e = ((float)tau - 0.1f) * (20.0f / 9.0f) - 1.0f;
+    e = fminf(fmaxf(e, -1.0f), 1.0f);
+    return (double)((float)(sc->gamma_base * sc->bin_avg) * exp2f(e * 3.32192809f));
 }
+
+constexpr int kRhoBatch = 4;
 
 __global__ void __launch_bounds__(kThreads) rho_kernel(RhoArgs a) {
     __shared__ long long red[32];
     long long over = 0, over_abs = 0;
-    // two bins per thread and step: 16-byte loads of the int64 maps
+    // two bins per 16-byte load of the int64 maps; kRhoBatch such pairs per
+    // thread and round, every load of the round issued before any store (the
+    // kernel is bound by memory latency, not bandwidth)
     const int npairs = a.nbins >> 1;
     longlong2 *mov2 = reinterpret_cast<longlong2 *>(a.mov_q);
-    const longlong2 *fs2 = reinterpret_cast<const longlong2 *>(a.fixs_q);
-    const longlong2 *fx2 = reinterpret_cast<const longlong2 *>(a.fix_q);
-    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < npairs; p += gridDim.x * blockDim.x) {
-        const longlong2 mov = mov2[p];
-        mov2[p] = make_longlong2(0, 0);
-        const longlong2 fs = fs2[p], fx = fx2[p];
-        const long long m[2] = {mov.x, mov.y}, s[2] = {fs.x, fs.y}, f[2] = {fx.x, fx.y};
-        float d[2];
+    const longlong2 *__restrict__ fs2 = reinterpret_cast<const longlong2 *>(a.fixs_q);
+    const longlong2 *__restrict__ fx2 = reinterpret_cast<const longlong2 *>(a.fix_q);
+    const int stride = gridDim.x * blockDim.x;
+    for (int p0 = blockIdx.x * blockDim.x + threadIdx.x; p0 < npairs; p0 += kRhoBatch * stride) {
+        longlong2 mv[kRhoBatch], fs[kRhoBatch], fx[kRhoBatch];
 #pragma unroll
-        for (int k = 0; k < 2; ++k) {
-            const long long tot = m[k] + s[k];
-            const long long t = tot - a.cap_q;
-            over += t > 0 ? t : 0;
-            const long long ab = m[k] + f[k] - a.ab_q;
-            over_abs += ab > 0 ? ab : 0;
-            d[k] = ll2f_rn_bits(tot) * a.inv_ab_f;  // same float ops as or_density_float
+        for (int j = 0; j < kRhoBatch; ++j) {
+            const int p = p0 + j * stride;
+            if (p < npairs) {
+                mv[j] = __ldcg(mov2 + p);
+                fs[j] = __ldg(fs2 + p);
+                fx[j] = __ldg(fx2 + p);
+            }
         }
-        if (a.d_f32) reinterpret_cast<float2 *>(a.d_f32)[p] = make_float2(d[0], d[1]);
-        if (a.d_hi) {
-            const __nv_bfloat16 h0 = __float2bfloat16_rn(d[0]), h1 = __float2bfloat16_rn(d[1]);
-            reinterpret_cast<__nv_bfloat162 *>(a.d_hi)[p] = __halves2bfloat162(h0, h1);
-            reinterpret_cast<__nv_bfloat162 *>(a.d_lo)[p] = __floats2bfloat162_rn(
-                d[0] - __bfloat162float(h0), d[1] - __bfloat162float(h1));
+#pragma unroll
+        for (int j = 0; j < kRhoBatch; ++j) {
+            const int p = p0 + j * stride;
+            if (p >= npairs) break;
+            mov2[p] = make_longlong2(0, 0);
+            const long long m[2] = {mv[j].x, mv[j].y}, sq[2] = {fs[j].x, fs[j].y}, f[2] = {fx[j].x, fx[j].y};
+            float d[2];
+#pragma unroll
+            for (int k = 0; k < 2; ++k) {
+                const long long tot = m[k] + sq[k];
+                const long long t = tot - a.cap_q;
+                over += t > 0 ? t : 0;
+                const long long ab = m[k] + f[k] - a.ab_q;
+                over_abs += ab > 0 ? ab : 0;
+                d[k] = ll2f_rn_bits(tot) * a.inv_ab_f;  // same float ops as or_density_float
+            }
+            if (a.d_f32) reinterpret_cast<float2 *>(a.d_f32)[p] = make_float2(d[0], d[1]);
+            if (a.d_hi) {
+                const __nv_bfloat16 h0 = __float2bfloat16_rn(d[0]), h1 = __float2bfloat16_rn(d[1]);
+                reinterpret_cast<__nv_bfloat162 *>(a.d_hi)[p] = __halves2bfloat162(h0, h1);
+                reinterpret_cast<__nv_bfloat162 *>(a.d_lo)[p] = __floats2bfloat162_rn(
+                    d[0] - __bfloat162float(h0), d[1] - __bfloat162float(h1));
+            }
         }
     }
     over = block_sum(over, red);
@@ -406,7 +426,7 @@ __global__ void __launch_bounds__(kThreads) rho_kernel(RhoArgs a) {
         if (threadIdx.x == 0) {
             DevScalars *sc = a.sc;
             const double tau = sc->mov_area_q > 0 ? (double)o / sc->mov_area_q : 0.0;
-            const double tau_abs = ldexp((double)oa, -32);
+            const double tau_abs = (double)oa * 0x1p-32;  // exact power-of-two scaling
             if (a.out) {
                 a.out[0] = tau;
                 a.out[1] = tau_abs;
@@ -427,8 +447,10 @@ __global__ void __launch_bounds__(kThreads) rho_kernel(RhoArgs a) {
 }
 
 void launch_rho(const RhoArgs &a, cudaStream_t st) {
-    int blocks = (a.nbins / 2 + kThreads - 1) / kThreads;
-    if (blocks > 608) blocks = 608;  // 4 blocks per SM (measured faster than one pair per thread)
+    // about one round of kRhoBatch pairs per thread
+    int blocks = (a.nbins / 2 + kRhoBatch * kThreads - 1) / (kRhoBatch * kThreads);
+    if (blocks > 1216) blocks = 1216;
+    if (blocks < 1) blocks = 1;
     rho_kernel<<<blocks, kThreads, 0, st>>>(a);
 }
 
@@ -441,7 +463,9 @@ __device__ void finish_trial(DevScalars *sc, double dv2, double dg2) {
     sc->sum_dv2 = dv2;
     sc->sum_dg2 = dg2;
     sc->evals += 1;
-    const double ahat = dg2 > 0.0 ? sqrt(dv2) / sqrt(dg2) : 0.0;
+    // step and momentum arithmetic in FP32 (single thread; FP64 sqrt/pow here
+    // cost microseconds per trial on the narrow FP64 pipe)
+    const double ahat = dg2 > 0.0 ? (double)(sqrtf((float)dv2) / sqrtf((float)dg2)) : 0.0;
     if (!isfinite(ahat) || !isfinite(dv2) || !isfinite(dg2)) {
         sc->status = 9;
         return;
@@ -460,11 +484,13 @@ __device__ void finish_trial(DevScalars *sc, double dv2, double dg2) {
     sc->alpha = ahat;
     sc->a_k = restart ? 1.0 : sc->a_next;
     if (restart && sc->restart_mode != 2) sc->restarts += 1;
-    sc->a_next = (1.0 + sqrt(4.0 * sc->a_k * sc->a_k + 1.0)) / 2.0;
-    sc->mom = (sc->a_k - 1.0) / sc->a_next;
-    const double pc = (sc->t_hpwl - sc->hpwl_prev) / sc->ref_dh;
-    double mu = pc < 0.0 ? sc->mu_max : pow(sc->mu_max, 1.0 - pc);
-    mu = fmin(fmax(mu, sc->mu_min), sc->mu_max);
+    const float ak = (float)sc->a_k, an = 0.5f * (1.0f + sqrtf(4.0f * ak * ak + 1.0f));
+    sc->a_next = (double)an;
+    sc->mom = (double)((ak - 1.0f) / an);
+    const float pc = (float)(sc->t_hpwl - sc->hpwl_prev) / (float)sc->ref_dh;
+    const float mmax = (float)sc->mu_max, mmin = (float)sc->mu_min;
+    float mu = pc < 0.0f ? mmax : exp2f(log2f(mmax) * (1.0f - pc));
+    mu = fminf(fmaxf(mu, mmin), mmax);
     // capped where the density term dominates completely: keeps the FP32
     // products finite when the target overflow is out of reach (lambda would
     // otherwise grow 5% per iteration until it overflows)
