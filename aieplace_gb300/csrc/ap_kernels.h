@@ -36,7 +36,13 @@ struct WaArgs {
 };
 // launches the four bucket kernels; the last one (warp per net) folds the sums
 void launch_wirelength(const WaArgs &a, cudaStream_t st);
-constexpr int kWaMaxBlocks = 4096;  // per bucket launch (4 x 4096 x 2 partials fit the buffer)
+// Block partials buffer (doubles; the per-block partials are FP32, two per
+// double): holds 2 FP32 per block of the four WA launches at kWaMaxBlocks
+// each, 4 per gather block at kGatherMaxBlocks, 1 per scatter block.
+constexpr int kPartialDoubles = 4 * 8192 + 64;
+// Blocks per bucket launch (grid-stride beyond: one net per thread measured
+// slower -- more block reductions and a longer last-block fold)
+constexpr int kWaMaxBlocks = 4096;
 
 // ---- density scatter (+ Nesterov position update) ---------------------------
 struct ScatterArgs {
@@ -110,6 +116,7 @@ struct GatherArgs {
     const int4 *rec_ov;
 };
 void launch_gather(const GatherArgs &a, cudaStream_t st);
+constexpr int kGatherMaxBlocks = 4096;  // grid-stride beyond (measured faster than one node per thread)
 
 // v_{-1} = v_0 - s g_0, s = coef * bw / max|g_0| (first Lipschitz estimate)
 void launch_perturb(int n_mov, const float *vx, const float *vy, const float *gx, const float *gy,

@@ -573,7 +573,7 @@ int ap_create(const ap_netlist *nl, const ap_params *params, ap_handle **out) {
     A(dalloc(&h->d_sx, N));
     A(dalloc(&h->d_sy, N));
     A(dalloc(&h->d_sc, 1));
-    A(dalloc(&h->d_partials, 4 * 8192 + 64));
+    A(dalloc(&h->d_partials, kPartialDoubles));
     A(dalloc(&h->d_partials_ll, 2 * 4096 + 64));
     A(dalloc(&h->d_counters, 8));
     A(dalloc(&h->d_out, 8));

@@ -654,7 +654,7 @@ __global__ void __launch_bounds__(kThreads) gather_kernel(GatherArgs a) {
 
 void launch_gather(const GatherArgs &a, cudaStream_t st) {
     int blocks = (a.n_mov + kThreads - 1) / kThreads;
-    if (blocks > 4096) blocks = 4096;
+    if (blocks > kGatherMaxBlocks) blocks = kGatherMaxBlocks;
     if (blocks < 1) blocks = 1;
     gather_kernel<<<blocks, kThreads, 0, st>>>(a);
 }
