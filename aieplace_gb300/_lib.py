@@ -25,6 +25,10 @@ EXPORTS = [
     "ap_synth_counts", "ap_synth_generate",
     "ap_create_batch", "ap_batch_destroy", "ap_batch_init_seeded", "ap_batch_step", "ap_batch_run",
     "ap_batch_get_stats", "ap_batch_get_positions",
+    "ap_surrogate_config_default", "ap_surrogate_create", "ap_surrogate_destroy", "ap_surrogate_num_params",
+    "ap_surrogate_get_params", "ap_surrogate_set_params", "ap_surrogate_forward", "ap_surrogate_gradient",
+    "ap_surrogate_reserve", "ap_surrogate_num_samples", "ap_surrogate_collect", "ap_surrogate_train",
+    "ap_surrogate_validate", "ap_attach_surrogate", "ap_surrogate_get_stats",
 ]
 
 AP_OK = 0
@@ -67,6 +71,19 @@ class Stats(C.Structure):
                 "wa": self.wa_wirelength, "overflow": self.overflow,
                 "overflow_abs": self.overflow_abs, "lambda": self.lambda_, "gamma": self.gamma,
                 "alpha": self.alpha, "a_k": self.a_k, "evals": self.evals, "restarts": self.restarts}
+
+
+class SurrogateConfig(C.Structure):
+    _fields_ = [("factor", C.c_int32), ("kernel", C.c_int32 * 4), ("width", C.c_int32), ("seed", C.c_uint64)]
+
+
+class SurrogatePolicy(C.Structure):
+    _fields_ = [("overflow_min", C.c_float), ("judge_every", C.c_int32), ("max_error", C.c_float),
+                ("use_net", C.c_int32)]
+
+
+class SurrogateStats(C.Structure):
+    _fields_ = [("used", C.c_int32), ("judged", C.c_int32), ("fallbacks", C.c_int32), ("last_error", C.c_double)]
 
 
 class SynthConfig(C.Structure):
@@ -120,6 +137,21 @@ def lib():
         L.ap_batch_run.argtypes = [vp, vp]
         L.ap_batch_get_stats.argtypes = [vp, i32, C.POINTER(Stats)]
         L.ap_batch_get_positions.argtypes = [vp, i32, vp, vp]
+        L.ap_surrogate_config_default.argtypes = [C.POINTER(SurrogateConfig)]
+        L.ap_surrogate_create.argtypes = [C.POINTER(SurrogateConfig), C.POINTER(vp)]
+        L.ap_surrogate_destroy.argtypes = [vp]
+        L.ap_surrogate_num_params.argtypes = [vp, C.POINTER(i32)]
+        L.ap_surrogate_get_params.argtypes = [vp, vp, i32]
+        L.ap_surrogate_set_params.argtypes = [vp, vp, i32]
+        L.ap_surrogate_forward.argtypes = [vp, vp, i32, i32, vp]
+        L.ap_surrogate_gradient.argtypes = [vp, vp, vp, i32, i32, i32, C.POINTER(f32), vp]
+        L.ap_surrogate_reserve.argtypes = [vp, i32, i32]
+        L.ap_surrogate_num_samples.argtypes = [vp, C.POINTER(i32)]
+        L.ap_surrogate_collect.argtypes = [vp, vp, i32, i32, C.POINTER(i32)]
+        L.ap_surrogate_train.argtypes = [vp, i32, i32, i32, f32, u64, i32, i32, vp]
+        L.ap_surrogate_validate.argtypes = [vp, i32, i32, vp, vp]
+        L.ap_attach_surrogate.argtypes = [vp, vp, C.POINTER(SurrogatePolicy)]
+        L.ap_surrogate_get_stats.argtypes = [vp, C.POINTER(SurrogateStats)]
         L.ap_synth_counts.argtypes =[C.POINTER(SynthConfig), C.POINTER(i32), C.POINTER(i32), C.POINTER(i32)]
         L.ap_synth_generate.argtypes = [C.POINTER(SynthConfig), vp, vp, vp, vp, vp, vp, vp, vp]
         _lib = L

@@ -16,7 +16,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libaieplace_gb300.so")
-SOURCES = ["capi.cu", "k_wirelength.cu", "k_density.cu", "k_field_simt.cu", "k_field_tc.cu", "synth.cpp"]
+SOURCES = ["capi.cu", "k_wirelength.cu", "k_density.cu", "k_field_simt.cu", "k_field_tc.cu", "k_surrogate.cu",
+           "synth.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -15,6 +15,13 @@ constexpr float kGradScale = 1048576.0f;                // 2^20
 constexpr float kInvGradScale = 1.0f / 1048576.0f;
 constexpr float kGradClamp = 3.99f;                     // |g| 2^20 < 2^22: magic-number rounding is exact
 constexpr double kLambdaMax = 1e30;                     // density penalty cap (the oracle's OR_LAMBDA_MAX)
+
+// field source of a loop trial; launches gated on the mode run when
+// (1 << mode) & mask
+enum { kFieldExact = 0, kFieldSurr = 1, kFieldJudge = 2 };
+constexpr int kGateExact = (1 << kFieldExact) | (1 << kFieldJudge);
+constexpr int kGateSurr = (1 << kFieldSurr) | (1 << kFieldJudge);
+constexpr int kGateJudge = 1 << kFieldJudge;
 constexpr int kThreads = 256;
 
 // FP64 scalars of the optimiser; live in device memory so a whole iteration
@@ -47,6 +54,14 @@ struct DevScalars {
     int restarts;
     int cur;            // buffer index of the accepted state
     int status;
+    // learned-surrogate schedule: the rho kernel's last block picks the field
+    // source of each loop trial (kField*); the judge compares the surrogate
+    // with the exact field and sets surr_ok
+    int field_mode;
+    int surr_attached, surr_ok, surr_judge_every;
+    int surr_used, surr_judged, surr_fallbacks;
+    float surr_tau_min, surr_err_bound;
+    double surr_err;    // last judged relative field error
     // FP32 copies of alpha, mom, lambda, gamma for the per-thread kernels
     // (a double -> float conversion in every thread costs FP64-pipe time);
     // refreshed by publish_f32 wherever the doubles change on the device

@@ -88,6 +88,9 @@ struct RhoArgs {
     unsigned int *counter;
     double *out;                // [2]: tau, tau_abs
     int mode;
+    // graph switch node selecting the field source of a loop trial (0: none);
+    // the last block sets it to the trial's field mode
+    unsigned long long field_switch;
 };
 void launch_rho(const RhoArgs &a, cudaStream_t st);
 
@@ -151,13 +154,16 @@ struct FieldSolver {
 int field_solver_init(FieldSolver &f, int m, float bin_ratio, int want_bf16);
 void field_solver_free(FieldSolver &f);
 // density d (x-major) -> ex, ey; FP32 SIMT contraction
-void field_solve_fp32(FieldSolver &f, const float *d, float *ex, float *ey, cudaStream_t st);
+// gate: the launches run only if gate is null or (1 << *gate) & gate_mask
+// (the loop's surrogate schedule lives in device memory)
+void field_solve_fp32(FieldSolver &f, const float *d, float *ex, float *ey, cudaStream_t st,
+                      const int *gate = nullptr, int gate_mask = 0);
 // Builds the TMA tensor maps of the tcgen05 path with (d_hi, d_lo) as the
 // density input; needs m a multiple of 128.
 int field_solver_bind_bf16(FieldSolver &f, const __nv_bfloat16 *d_hi, const __nv_bfloat16 *d_lo);
 // density as bf16 hi/lo split (the bound buffers) -> ex, ey; tcgen05 BF16x3 contraction
 int field_solve_bf16x3(FieldSolver &f, const __nv_bfloat16 *d_hi, const __nv_bfloat16 *d_lo,
-                       float *ex, float *ey, cudaStream_t st);
+                       float *ex, float *ey, cudaStream_t st, const int *gate = nullptr, int gate_mask = 0);
 // nonzero once a bounded wait in a tcgen05 kernel gave up
 int field_solver_status(FieldSolver &f, unsigned int *out);
 // float -> bf16 hi/lo split (for per-stage API calls)

@@ -13,6 +13,7 @@
 
 #include "../../include/aieplace.h"
 #include "ap_kernels.h"
+#include "ap_surrogate.h"
 
 using namespace ap;
 
@@ -73,6 +74,11 @@ struct ap_handle {
     bool initialized = false;
     cudaGraphExec_t graph = nullptr;  // one trial step (parity lives in device scalars)
     bool graph_ok = false;
+    // attached learned surrogate (not owned) and its per-handle buffers
+    ap_surrogate *surr = nullptr;
+    SurrState surr_state{};
+    cudaStream_t side = nullptr;  // captures the field-switch bodies
+    ap_surrogate_policy policy{0.3f, 8, 0.02f, 1};
 };
 
 namespace {
@@ -80,12 +86,12 @@ namespace {
 int solver_of(const ap_handle *h, int32_t solver) { return solver >= 0 ? solver : h->p.field_solver; }
 
 // density map (bf16 split or fp32 already in place) -> ex, ey
-int run_field(ap_handle *h, int solver, cudaStream_t st) {
+int run_field(ap_handle *h, int solver, cudaStream_t st, const int *gate = nullptr, int gate_mask = 0) {
     if (solver == AP_FIELD_BF16X3) {
-        int r = field_solve_bf16x3(h->fs, h->d_dens_hi, h->d_dens_lo, h->d_ex, h->d_ey, st);
+        int r = field_solve_bf16x3(h->fs, h->d_dens_hi, h->d_dens_lo, h->d_ex, h->d_ey, st, gate, gate_mask);
         if (r != AP_OK) return r;
     } else {
-        field_solve_fp32(h->fs, h->d_dens, h->d_ex, h->d_ey, st);
+        field_solve_fp32(h->fs, h->d_dens, h->d_ex, h->d_ey, st, gate, gate_mask);
     }
     return AP_OK;
 }
@@ -208,12 +214,37 @@ GatherArgs loop_gather_args(ap_handle *h) {
 // One trial step from the accepted state (buffers [cur]) to buffers
 // [1 - cur]; cur lives in device scalars, so one captured graph serves every
 // launch.  The gather's last block accepts the trial or asks for a retry.
+// Field stage of a trial with a surrogate attached.  The rho kernel's last
+// block picks the source (device scalars): exact, surrogate, or both with the
+// surrogate judged.  branch < 0: every launch, each reading the mode from
+// device memory and returning early if it is not selected; branch >= 0: the
+// launches of that source only (one body of the graph's switch node).
+int enqueue_field_surrogate(ap_handle *h, cudaStream_t st, int branch) {
+    const int *gate = &h->d_sc->field_mode;
+    const bool f32 = h->p.field_solver != AP_FIELD_BF16X3;
+    if (branch != kFieldExact)
+        surr_enqueue_field(h->surr->net, h->surr_state, f32 ? h->d_dens : nullptr, f32 ? nullptr : h->d_dens_hi,
+                           f32 ? nullptr : h->d_dens_lo, h->d_ex, h->d_ey, gate, st);
+    if (branch != kFieldSurr) {
+        int r = run_field(h, h->p.field_solver, st, gate, kGateExact);
+        if (r != AP_OK) return r;
+    }
+    if (branch < 0 || branch == kFieldJudge) surr_enqueue_judge(h->surr_state, h->d_ex, h->d_ey, h->d_sc, gate, st);
+    return AP_OK;
+}
+
 int enqueue_iteration(ap_handle *h, cudaStream_t st) {
     launch_scatter(loop_scatter_args(h), st);
     launch_rho(rho_args(h, RHO_LOOP, nullptr), st);
     launch_wirelength(wa_args(h, h->d_px[0], h->d_py[0], 0.f, h->n_mov, WA_LOOP, nullptr), st);
-    int r = run_field(h, h->p.field_solver, st);
-    if (r != AP_OK) return r;
+    int r;
+    if (h->surr) {
+        r = enqueue_field_surrogate(h, st, -1);
+        if (r != AP_OK) return r;
+    } else {
+        r = run_field(h, h->p.field_solver, st);
+        if (r != AP_OK) return r;
+    }
     launch_gather(loop_gather_args(h), st);
     return cudaGetLastError() == cudaSuccess ? AP_OK : AP_ERR_CUDA;
 }
@@ -250,11 +281,52 @@ void destroy_graphs(ap_handle *h) {
     h->graph_ok = false;
 }
 
+// One trial with a surrogate attached, captured with a switch node over the
+// field sources: the rho kernel sets the switch (cudaGraphSetConditional), so
+// only the selected source's kernels launch.
+int capture_trial_switched(ap_handle *h) {
+    cudaStream_t st = h->stream;
+    if (!h->side) CK(cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking));
+    cudaStreamCaptureStatus cs;
+    cudaGraph_t cg = nullptr;
+    CK(cudaStreamGetCaptureInfo(st, &cs, nullptr, &cg, nullptr, nullptr, nullptr));
+    cudaGraphConditionalHandle sw_handle;
+    CK(cudaGraphConditionalHandleCreate(&sw_handle, cg, kFieldExact, cudaGraphCondAssignDefault));
+    launch_scatter(loop_scatter_args(h), st);
+    RhoArgs ra = rho_args(h, RHO_LOOP, nullptr);
+    ra.field_switch = sw_handle;
+    launch_rho(ra, st);
+    launch_wirelength(wa_args(h, h->d_px[0], h->d_py[0], 0.f, h->n_mov, WA_LOOP, nullptr), st);
+    const cudaGraphNode_t *dp = nullptr;
+    size_t nd = 0;
+    CK(cudaStreamGetCaptureInfo(st, &cs, nullptr, nullptr, &dp, nullptr, &nd));
+    std::vector<cudaGraphNode_t> deps(dp, dp + nd);
+    cudaGraphNodeParams np{};
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = sw_handle;
+    np.conditional.type = cudaGraphCondTypeSwitch;
+    np.conditional.size = 3;  // kFieldExact, kFieldSurr, kFieldJudge
+    cudaGraphNode_t sw = nullptr;
+    CK(cudaGraphAddNode(&sw, cg, deps.data(), nullptr, deps.size(), &np));
+    for (int b = 0; b < 3; ++b) {
+        CK(cudaStreamBeginCaptureToGraph(h->side, np.conditional.phGraph_out[b], nullptr, nullptr, 0,
+                                         cudaStreamCaptureModeThreadLocal));
+        const int r = enqueue_field_surrogate(h, h->side, b);
+        cudaGraph_t body = nullptr;
+        const cudaError_t e = cudaStreamEndCapture(h->side, &body);
+        if (r != AP_OK) return r;
+        CK(e);
+    }
+    CK(cudaStreamUpdateCaptureDependencies(st, &sw, nullptr, 1, cudaStreamSetCaptureDependencies));
+    launch_gather(loop_gather_args(h), st);
+    return cudaGetLastError() == cudaSuccess ? AP_OK : AP_ERR_CUDA;
+}
+
 int build_graphs(ap_handle *h) {
     destroy_graphs(h);
     cudaGraph_t gr = nullptr;
     CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-    int r = enqueue_iteration(h, h->stream);
+    int r = h->surr ? capture_trial_switched(h) : enqueue_iteration(h, h->stream);
     cudaError_t e = cudaStreamEndCapture(h->stream, &gr);
     if (r != AP_OK || e != cudaSuccess) {
         if (gr) cudaGraphDestroy(gr);
@@ -321,6 +393,11 @@ int init_optimizer(ap_handle *h) {
     sc.max_backtracks = h->p.max_backtracks;
     sc.restart_mode = h->p.restart_mode;
     sc.cur = 0;
+    sc.surr_attached = h->surr != nullptr;
+    sc.surr_ok = 1;
+    sc.surr_judge_every = h->policy.judge_every;
+    sc.surr_tau_min = h->policy.overflow_min;
+    sc.surr_err_bound = h->policy.max_error;
     CK(cudaMemcpyAsync(h->d_sc, &sc, sizeof(sc), cudaMemcpyHostToDevice, st));
     CK(cudaMemsetAsync(h->d_gqx, 0, sizeof(ull) * h->n_nodes, st));
     CK(cudaMemsetAsync(h->d_gqy, 0, sizeof(ull) * h->n_nodes, st));
@@ -644,6 +721,8 @@ int ap_destroy(ap_handle *h) {
     if (!h) return AP_ERR_INVALID_ARG;
     if (h->stream) cudaStreamSynchronize(h->stream);
     destroy_graphs(h);
+    surr_state_free(h->surr_state);
+    if (h->side) cudaStreamDestroy(h->side);
     field_solver_free(h->fs);
     void *ptrs[] = {h->d_net_ptr, h->d_pin_node, h->d_w,      h->d_h,       h->d_px[0], h->d_px[1],
                     h->d_py[0],   h->d_py[1],    h->d_gx[0],  h->d_gx[1],   h->d_gy[0], h->d_gy[1],
@@ -969,7 +1048,7 @@ int ap_snapshot(ap_handle *h, void *buf, size_t bytes) {
     if (!h->initialized) return AP_ERR_STATE;
     CK(cudaStreamSynchronize(h->stream));
     char *p = (char *)buf;
-    int32_t hdr[4] = {0x41505333, h->n_nodes, h->n_mov, 0};
+    int32_t hdr[4] = {0x41505334, h->n_nodes, h->n_mov, 0};
     memcpy(p, hdr, sizeof(hdr));
     p += sizeof(hdr);
     CK(cudaMemcpy(p, h->d_sc, sizeof(DevScalars), cudaMemcpyDeviceToHost));
@@ -993,7 +1072,7 @@ int ap_restore(ap_handle *h, const void *buf, size_t bytes) {
     const char *p = (const char *)buf;
     int32_t hdr[4];
     memcpy(hdr, p, sizeof(hdr));
-    if (hdr[0] != 0x41505333 || hdr[1] != h->n_nodes || hdr[2] != h->n_mov) return AP_ERR_INVALID_ARG;
+    if (hdr[0] != 0x41505334 || hdr[1] != h->n_nodes || hdr[2] != h->n_mov) return AP_ERR_INVALID_ARG;
     p += sizeof(hdr);
     CK(cudaStreamSynchronize(h->stream));
     CK(cudaMemcpy(h->d_sc, p, sizeof(DevScalars), cudaMemcpyHostToDevice));
@@ -1016,6 +1095,108 @@ int ap_restore(ap_handle *h, const void *buf, size_t bytes) {
     h->initialized = true;
     if (h->p.use_graph && !h->graph_ok) return build_graphs(h);
     return AP_OK;
+}
+
+
+// ---- learned surrogate: attachment, sample collection, statistics ------------
+
+namespace {
+// writes the surrogate schedule fields of the device scalars (read-modify-write)
+int upload_schedule(ap_handle *h) {
+    int r = read_scalars(h);
+    if (r != AP_OK) return r;
+    DevScalars &c = *h->h_sc;
+    c.surr_attached = h->surr != nullptr;
+    c.surr_ok = 1;
+    c.surr_judge_every = h->policy.judge_every;
+    c.surr_tau_min = h->policy.overflow_min;
+    c.surr_err_bound = h->policy.max_error;
+    c.field_mode = kFieldExact;
+    CK(cudaMemcpyAsync(h->d_sc, h->h_sc, sizeof(DevScalars), cudaMemcpyHostToDevice, h->stream));
+    return sync(h);
+}
+}  // namespace
+
+int ap_attach_surrogate(ap_handle *h, ap_surrogate *s, const ap_surrogate_policy *policy) {
+    if (!h) return AP_ERR_INVALID_ARG;
+    if (policy && (policy->judge_every < 1 || !(policy->max_error > 0.f))) return AP_ERR_INVALID_ARG;
+    int r = sync(h);
+    if (r != AP_OK) return r;
+    destroy_graphs(h);
+    surr_state_free(h->surr_state);
+    h->surr = nullptr;
+    if (s) {
+        if (policy) h->policy = *policy;
+        r = surr_state_init(h->surr_state, s->net, h->p.bins_x, h->g.bh / h->g.bw);
+        if (r != AP_OK) return r;
+        h->surr_state.use_net = h->policy.use_net != 0;
+        h->surr = s;
+    }
+    if (!h->initialized) return AP_OK;
+    r = upload_schedule(h);
+    if (r != AP_OK) return r;
+    return h->p.use_graph ? build_graphs(h) : AP_OK;
+}
+
+int ap_surrogate_get_stats(ap_handle *h, ap_surrogate_stats *st) {
+    if (!h || !st) return AP_ERR_INVALID_ARG;
+    int r = read_scalars(h);
+    if (r != AP_OK) return r;
+    st->used = h->h_sc->surr_used;
+    st->judged = h->h_sc->surr_judged;
+    st->fallbacks = h->h_sc->surr_fallbacks;
+    st->last_error = h->h_sc->surr_err;
+    return AP_OK;
+}
+
+int ap_surrogate_collect(ap_handle *h, ap_surrogate *s, int32_t n_trials, int32_t every, int32_t *collected) {
+    if (!h || !s || n_trials < 0 || every < 1) return AP_ERR_INVALID_ARG;
+    if (!h->initialized) return AP_ERR_STATE;
+    const int M = h->p.bins_x;
+    if (!s->d_X || M % s->net.f != 0 || M / s->net.f != s->R) return AP_ERR_INVALID_ARG;
+    int r = sync(h);
+    if (r != AP_OK) return r;
+    SurrState tmp{};
+    SurrState *ss = &h->surr_state;
+    if (h->surr != s) {
+        r = surr_state_init(tmp, s->net, M, h->g.bh / h->g.bw);
+        if (r != AP_OK) return r;
+        ss = &tmp;
+    }
+    // exact trials while collecting: the schedule is off
+    ap_surrogate *attached = h->surr;
+    h->surr = nullptr;
+    r = upload_schedule(h);
+    const bool f32 = h->p.field_solver != AP_FIELD_BF16X3;
+    const size_t RR = (size_t)s->R * s->R;
+    int got = 0;
+    cudaStream_t st = h->stream;
+    for (int t = 1; t <= n_trials && r == AP_OK; ++t) {
+        launch_scatter(loop_scatter_args(h), st);
+        launch_rho(rho_args(h, RHO_LOOP, nullptr), st);
+        launch_wirelength(wa_args(h, h->d_px[0], h->d_py[0], 0.f, h->n_mov, WA_LOOP, nullptr), st);
+        r = run_field(h, h->p.field_solver, st);
+        if (r != AP_OK) break;
+        if (t % every == 0 && s->n < s->cap) {
+            const int slot = s->n;
+            surr_enqueue_input(s->net, *ss, f32 ? h->d_dens : nullptr, f32 ? nullptr : h->d_dens_hi,
+                               f32 ? nullptr : h->d_dens_lo, nullptr, 0, st);
+            surr_enqueue_sample(s->net, *ss, s->d_X + (size_t)slot * s->net.cin0 * RR,
+                                s->d_T + (size_t)slot * s->net.cout * RR, s->d_s + slot, s->d_e2 + slot, h->d_ex,
+                                h->d_ey, st);
+            s->n += 1;
+            ++got;
+        }
+        launch_gather(loop_gather_args(h), st);
+        if (cudaGetLastError() != cudaSuccess) r = AP_ERR_CUDA;
+        if (r == AP_OK && t % 64 == 0) r = sync(h);
+    }
+    if (r == AP_OK) r = sync(h);
+    h->surr = attached;
+    const int r2 = upload_schedule(h);
+    if (ss == &tmp) surr_state_free(tmp);
+    if (collected) *collected = got;
+    return r != AP_OK ? r : r2;
 }
 
 }  // extern "C"

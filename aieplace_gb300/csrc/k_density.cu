@@ -441,6 +441,19 @@ __global__ void __launch_bounds__(kThreads) rho_kernel(RhoArgs a) {
                 sc->gamma = gamma_of(sc, tau);
                 sc->f_gamma = (float)sc->gamma;
             }
+            // field source of this trial: the surrogate while the overflow is
+            // above its threshold and its last judgement passed, the exact
+            // solve judging it every surr_judge_every trials
+            int fm = kFieldExact;
+            if (a.mode == RHO_LOOP && sc->surr_attached && tau > (double)sc->surr_tau_min) {
+                if (sc->evals % sc->surr_judge_every == 0)
+                    fm = kFieldJudge;
+                else if (sc->surr_ok)
+                    fm = kFieldSurr;
+            }
+            sc->field_mode = fm;
+            if (a.field_switch) cudaGraphSetConditional(a.field_switch, (unsigned int)fm);
+            if (fm == kFieldSurr) sc->surr_used += 1;
             *a.counter = 0u;
         }
     }

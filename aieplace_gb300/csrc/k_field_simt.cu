@@ -29,6 +29,8 @@ struct GemmSet {
     const float *A[2];
     const float *B[2];
     float *C[2];
+    const int *gate;  // run only if gate is null or (1 << *gate) & gate_mask
+    int gate_mask;
 };
 
 struct SpectralEpi {
@@ -55,6 +57,7 @@ __device__ __forceinline__ void spectral_store(const SpectralEpi &e, int m, int 
 // D = A B^T on an m x m problem; BM x BM output tile per block, 256 threads.
 template <int BM, bool SPECTRAL>
 __global__ void __launch_bounds__(256) gemm_tn_simt(int m, GemmSet s, SpectralEpi e) {
+    if (s.gate && !((1 << *s.gate) & s.gate_mask)) return;
     constexpr int TM = BM / 16;
     __shared__ __align__(16) float As[BK][BM + 4];
     __shared__ __align__(16) float Bs[BK][BM + 4];
@@ -205,17 +208,18 @@ void field_solver_free(FieldSolver &f) {
     f = FieldSolver();
 }
 
-void field_solve_fp32(FieldSolver &f, const float *d, float *ex, float *ey, cudaStream_t st) {
+void field_solve_fp32(FieldSolver &f, const float *d, float *ex, float *ey, cudaStream_t st, const int *gate,
+                      int gate_mask) {
     const int m = f.m;
     SpectralEpi none{};
-    GemmSet s1{{f.C, nullptr}, {d, nullptr}, {f.t0, nullptr}};
+    GemmSet s1{{f.C, nullptr}, {d, nullptr}, {f.t0, nullptr}, gate, gate_mask};
     gemm<false>(m, s1, 1, none, st, f.simt_bm);
     SpectralEpi epi{f.px, f.py, f.wx, f.wy, 4.0f / ((float)m * (float)m)};
-    GemmSet s2{{f.C, nullptr}, {f.t0, nullptr}, {nullptr, nullptr}};
+    GemmSet s2{{f.C, nullptr}, {f.t0, nullptr}, {nullptr, nullptr}, gate, gate_mask};
     gemm<true>(m, s2, 1, epi, st, f.simt_bm);
-    GemmSet s3{{f.Ct, f.St}, {f.px, f.py}, {f.ux, f.uy}};
+    GemmSet s3{{f.Ct, f.St}, {f.px, f.py}, {f.ux, f.uy}, gate, gate_mask};
     gemm<false>(m, s3, 2, none, st, f.simt_bm);
-    GemmSet s4{{f.St, f.Ct}, {f.ux, f.uy}, {ex, ey}};
+    GemmSet s4{{f.St, f.Ct}, {f.ux, f.uy}, {ex, ey}, gate, gate_mask};
     gemm<false>(m, s4, 2, none, st, f.simt_bm);
 }
 

@@ -60,6 +60,8 @@ struct Epi {
     const float *wx, *wy;
     float scale;
     unsigned int *status;
+    const int *gate;  // run only if gate is null or (1 << *gate) & gate_mask
+    int gate_mask;
 };
 
 // ---- PTX wrappers ----------------------------------------------------------
@@ -191,6 +193,8 @@ __device__ __forceinline__ void store_split(const float (&v)[32], __nv_bfloat16 
 
 template <class T>
 __global__ void __launch_bounds__(THREADS, 1) gemm_bf16x3_kernel(const __grid_constant__ Maps maps, Epi e) {
+    // uniform for the whole grid, before any barrier or TMEM allocation
+    if (e.gate && !((1 << *e.gate) & e.gate_mask)) return;
     constexpr int BN = T::BN, STAGES = T::STAGES, STAGE_BYTES = T::STAGE_BYTES, B_TILE = T::B_TILE;
     constexpr uint32_t TMEM_COLS = T::TMEM_COLS;
     extern __shared__ __align__(1024) uint8_t smem_raw[];
@@ -390,9 +394,12 @@ struct TcState {
 };
 
 template <class T>
-void run_stages(const StageMaps &h, FieldSolver &f, float *ex, float *ey, cudaStream_t st) {
+void run_stages(const StageMaps &h, FieldSolver &f, float *ex, float *ey, cudaStream_t st, const int *gate,
+                int gate_mask) {
     const int m = f.m;
     Epi e{};
+    e.gate = gate;
+    e.gate_mask = gate_mask;
     e.m = m;
     e.status = f.tc_status;
     e.wx = f.wx;
@@ -421,12 +428,13 @@ void run_stages(const StageMaps &h, FieldSolver &f, float *ex, float *ey, cudaSt
     gemm_bf16x3_kernel<T><<<g2, THREADS, T::SMEM_BYTES, st>>>(h.s4, e);
 }
 
-void run_variant(int v, FieldSolver &f, float *ex, float *ey, cudaStream_t st) {
+void run_variant(int v, FieldSolver &f, float *ex, float *ey, cudaStream_t st, const int *gate = nullptr,
+                 int gate_mask = 0) {
     const TcState &s = *reinterpret_cast<const TcState *>(f.tc_maps);
     if (v == 1)
-        run_stages<Tile128>(s.maps[1], f, ex, ey, st);
+        run_stages<Tile128>(s.maps[1], f, ex, ey, st, gate, gate_mask);
     else
-        run_stages<Tile64>(s.maps[0], f, ex, ey, st);
+        run_stages<Tile64>(s.maps[0], f, ex, ey, st, gate, gate_mask);
 }
 
 }  // namespace tc
@@ -486,11 +494,11 @@ int field_solver_bind_bf16(FieldSolver &f, const __nv_bfloat16 *d_hi, const __nv
 }
 
 int field_solve_bf16x3(FieldSolver &f, const __nv_bfloat16 *d_hi, const __nv_bfloat16 *d_lo, float *ex,
-                       float *ey, cudaStream_t st) {
+                       float *ey, cudaStream_t st, const int *gate, int gate_mask) {
     (void)d_hi;
     (void)d_lo;  // bound into the stage-1 tensor maps by field_solver_bind_bf16
     if (!f.tc_ready) return AP_ERR_UNSUPPORTED;
-    tc::run_variant(f.tc_variant, f, ex, ey, st);
+    tc::run_variant(f.tc_variant, f, ex, ey, st, gate, gate_mask);
     return cudaGetLastError() == cudaSuccess ? AP_OK : AP_ERR_CUDA;
 }
 

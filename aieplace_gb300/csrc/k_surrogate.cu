@@ -1,0 +1,991 @@
+// Learned density-to-field surrogate: kernels.
+//
+// No counterpart in the reference (its field solves are exact:
+// AIEplace.cpp:388-934, fft.cpp:204-299).  The surrogate stands in for the
+// exact solve during the early, high-overflow iterations of the ePlace loop:
+//
+//   fine density (M x M)  --pool f x f-->  coarse density (R x R, R = M / f)
+//   coarse density  --exact spectral solve at R (FP32, k_field_simt.cu)-->  coarse field
+//   network input X0 [f^2 + 2][R][R]: the f x f sub-bin densities of each
+//       coarse bin (space-to-depth) and the coarse field scaled by f / s
+//   4-layer conv net (32 channels, ReLU)  -->  Y [2 f^2][R][R]
+//   fine field = bilinear_up(coarse field * f) + s * depth_to_space(Y)
+//
+// s is the RMS of the scaled coarse field (per map), so the network sees and
+// predicts scale-free quantities.  The coarse spectral layer carries the
+// long-range part of the Poisson field (a few 3x3 convolutions cannot); the
+// network learns the fine-resolution residual.
+//
+// Tensors are [C][X][Y] with Y contiguous, like the bin maps (x-major).  Conv
+// kernels are FP32 SIMT: direct convolution with zero padding, one output
+// pixel per thread and all output channels in registers; the weight gradient
+// is reduced over pixel tiles in a fixed order (deterministic).
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "ap_common.cuh"
+#include "ap_surrogate.h"
+
+namespace ap {
+namespace sg {
+
+// ---- helpers --------------------------------------------------------------
+
+// Runs the kernel body only when *gate selects it (nullptr: always).
+__device__ __forceinline__ bool gate_open(const int *gate, int mask) {
+    return gate == nullptr || ((1 << *gate) & mask) != 0;
+}
+
+// bilinear sample of a coarse R x R map at fine index (X, Y), factor f:
+// coarse sample points at bin centres, clamped at the edges
+__device__ __forceinline__ float bilinear_up(const float *c, int R, int f, int X, int Y) {
+    const float u = ((float)X + 0.5f) / (float)f - 0.5f, v = ((float)Y + 0.5f) / (float)f - 0.5f;
+    const float fu = floorf(u), fv = floorf(v);
+    int i0 = (int)fu, j0 = (int)fv;
+    float tu = u - fu, tv = v - fv;
+    if (i0 < 0) { i0 = 0; tu = 0.f; }
+    if (j0 < 0) { j0 = 0; tv = 0.f; }
+    if (i0 >= R - 1) { i0 = R - 1; tu = 0.f; }
+    if (j0 >= R - 1) { j0 = R - 1; tv = 0.f; }
+    const int i1 = min(i0 + 1, R - 1), j1 = min(j0 + 1, R - 1);
+    const float a = c[i0 * R + j0], b = c[i0 * R + j1], d = c[i1 * R + j0], e = c[i1 * R + j1];
+    return (1.f - tu) * ((1.f - tv) * a + tv * b) + tu * ((1.f - tv) * d + tv * e);
+}
+
+// ---- pooling and network input ------------------------------------------
+
+// coarse[I][J] = mean of the f x f fine bins; the fine density is FP32
+// (d_f32) or the BF16 hi/lo split of the tensor-core solver (hi + lo).  The
+// result goes to `coarse` (FP32) or, for the tensor-core coarse solve, to
+// its own hi/lo split (c_hi, c_lo).
+__global__ void pool_kernel(int M, int f, const float *d_f32, const __nv_bfloat16 *d_hi,
+                            const __nv_bfloat16 *d_lo, float *coarse, __nv_bfloat16 *c_hi, __nv_bfloat16 *c_lo,
+                            const int *gate, int mask) {
+    if (!gate_open(gate, mask)) return;
+    const int R = M / f;
+    const float inv = 1.f / (float)(f * f);
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < R * R; q += gridDim.x * blockDim.x) {
+        const int I = q / R, J = q - I * R;
+        float s = 0.f;
+        for (int a = 0; a < f; ++a)
+            for (int b = 0; b < f; ++b) {
+                const size_t k = (size_t)(I * f + a) * M + (J * f + b);
+                s += d_f32 ? d_f32[k] : __bfloat162float(d_hi[k]) + __bfloat162float(d_lo[k]);
+            }
+        const float v = s * inv;
+        if (c_hi) {
+            const __nv_bfloat16 h = __float2bfloat16_rn(v);
+            c_hi[q] = h;
+            c_lo[q] = __float2bfloat16_rn(v - __bfloat162float(h));
+        } else {
+            coarse[q] = v;
+        }
+    }
+}
+
+// Per-map scale s = sqrt(mean((f ex_c)^2 + (f ey_c)^2)) over the coarse map,
+// last-block fold; written to *scale (one float per map of the batch).
+__global__ void scale_kernel(int R, int f, const float *cex, const float *cey, float *partials,
+                             unsigned int *counter, float *scale, const int *gate, int mask) {
+    if (!gate_open(gate, mask)) return;
+    __shared__ double red[32];
+    float acc = 0.f;
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < R * R; q += gridDim.x * blockDim.x)
+        acc += cex[q] * cex[q] + cey[q] * cey[q];
+    const float b = block_sum_ff(acc, reinterpret_cast<float *>(red));
+    if (threadIdx.x == 0) partials[blockIdx.x] = b;
+    if (arrive_last(counter)) {
+        const double t = block_sum_f(kahan_strided(partials, threadIdx.x, gridDim.x, blockDim.x, 1), red);
+        if (threadIdx.x == 0) {
+            const double ms = t * (double)f * (double)f / ((double)R * (double)R);
+            *scale = (float)sqrt(ms) + 1e-20f;
+            *counter = 0u;
+        }
+    }
+}
+
+// X0 [f^2 + 2][R][R]: sub-bin densities (channel a f + b holds fine bin
+// (I f + a, J f + b)), then f ex_c / s and f ey_c / s.
+__global__ void prep_kernel(int M, int f, const float *d_f32, const __nv_bfloat16 *d_hi,
+                            const __nv_bfloat16 *d_lo, const float *cex, const float *cey,
+                            const float *scale, float *x0, const int *gate, int mask) {
+    if (!gate_open(gate, mask)) return;
+    const int R = M / f, RR = R * R, f2 = f * f;
+    const float sc = (float)f / *scale;
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < RR; q += gridDim.x * blockDim.x) {
+        const int I = q / R, J = q - I * R;
+        for (int a = 0; a < f; ++a)
+            for (int b = 0; b < f; ++b) {
+                const size_t k = (size_t)(I * f + a) * M + (J * f + b);
+                x0[(size_t)(a * f + b) * RR + q] =
+                    d_f32 ? d_f32[k] : __bfloat162float(d_hi[k]) + __bfloat162float(d_lo[k]);
+            }
+        x0[(size_t)f2 * RR + q] = cex[q] * sc;
+        x0[(size_t)(f2 + 1) * RR + q] = cey[q] * sc;
+    }
+}
+
+// Training target [2 f^2][R][R]: (E_exact - bilinear_up(f E_c)) / s in the
+// depth-to-space layout of the network output.
+__global__ void target_kernel(int M, int f, const float *ex, const float *ey, const float *cex,
+                              const float *cey, const float *scale, float *tgt) {
+    const int R = M / f, RR = R * R, f2 = f * f;
+    const float inv = 1.f / *scale, ff = (float)f;
+    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < (size_t)M * M;
+         k += (size_t)gridDim.x * blockDim.x) {
+        const int X = (int)(k / M), Y = (int)(k - (size_t)X * M);
+        const int I = X / f, a = X - I * f, J = Y / f, b = Y - J * f;
+        const size_t q = (size_t)I * R + J;
+        tgt[(size_t)(a * f + b) * RR + q] = (ex[k] - ff * bilinear_up(cex, R, f, X, Y)) * inv;
+        tgt[(size_t)(f2 + a * f + b) * RR + q] = (ey[k] - ff * bilinear_up(cey, R, f, X, Y)) * inv;
+    }
+}
+
+// fine field = bilinear_up(f E_c) + s * depth_to_space(Y) (Y may be null:
+// coarse layer only).  Writes (ex, ey), or (jx, jy) on a judged trial (the
+// exact solve then fills ex, ey).
+__global__ void combine_kernel(int M, int f, const float *cex, const float *cey, const float *y,
+                               const float *scale, float *ex, float *ey, float *jx, float *jy, const int *gate,
+                               int mask) {
+    if (!gate_open(gate, mask)) return;
+    if (gate && *gate == kFieldJudge) {
+        ex = jx;
+        ey = jy;
+    }
+    const int R = M / f, RR = R * R, f2 = f * f;
+    const float s = *scale, ff = (float)f;
+    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < (size_t)M * M;
+         k += (size_t)gridDim.x * blockDim.x) {
+        const int X = (int)(k / M), Y = (int)(k - (size_t)X * M);
+        float vx = ff * bilinear_up(cex, R, f, X, Y), vy = ff * bilinear_up(cey, R, f, X, Y);
+        if (y) {
+            const int I = X / f, a = X - I * f, J = Y / f, b = Y - J * f;
+            const size_t q = (size_t)I * R + J;
+            vx += s * y[(size_t)(a * f + b) * RR + q];
+            vy += s * y[(size_t)(f2 + a * f + b) * RR + q];
+        }
+        ex[k] = vx;
+        ey[k] = vy;
+    }
+}
+
+
+// *out = sum over the map of ex^2 + ey^2 (last-block fold)
+__global__ void sumsq_kernel(size_t n, const float *ex, const float *ey, float *partials, unsigned int *counter,
+                             float *out) {
+    __shared__ double red[32];
+    float acc = 0.f;
+    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
+        acc += ex[k] * ex[k] + ey[k] * ey[k];
+    const float bsum = block_sum_ff(acc, reinterpret_cast<float *>(red));
+    if (threadIdx.x == 0) partials[blockIdx.x] = bsum;
+    if (arrive_last(counter)) {
+        const double t = block_sum_f(kahan_strided(partials, threadIdx.x, gridDim.x, blockDim.x, 1), red);
+        if (threadIdx.x == 0) {
+            *out = (float)t;
+            *counter = 0u;
+        }
+    }
+}
+
+// out[0] = sum (y - t)^2, out[1] = sum t^2 (last-block fold)
+__global__ void diff_norms_kernel(size_t n, const float *y, const float *t, float *partials, unsigned int *counter,
+                                  float *out) {
+    __shared__ double red[32];
+    float a = 0.f, b = 0.f;
+    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) {
+        const float d = y[k] - t[k];
+        a += d * d;
+        b += t[k] * t[k];
+    }
+    float *redf = reinterpret_cast<float *>(red);
+    const float ba = block_sum_ff(a, redf), bb = block_sum_ff(b, redf);
+    if (threadIdx.x == 0) {
+        partials[2 * blockIdx.x] = ba;
+        partials[2 * blockIdx.x + 1] = bb;
+    }
+    if (arrive_last(counter)) {
+        const double ta = block_sum_f(kahan_strided(partials, threadIdx.x, gridDim.x, blockDim.x, 2), red);
+        const double tb = block_sum_f(kahan_strided(partials + 1, threadIdx.x, gridDim.x, blockDim.x, 2), red);
+        if (threadIdx.x == 0) {
+            out[0] = (float)ta;
+            out[1] = (float)tb;
+            *counter = 0u;
+        }
+    }
+}
+
+// ---- convolution ----------------------------------------------------------
+// in [B][cin][R][R], W [cout][cin][K][K], bias [cout], out [B][cout][R][R];
+// zero padding, stride 1, cin, cout <= kMaxCh.  The weights sit in shared
+// memory as [cin][K*K][kMaxCh] so that one float4 load feeds four output
+// channels of every lane.
+
+template <int K>
+__global__ void __launch_bounds__(256) conv_fwd_kernel(int B, int R, int cin, int cout, const float *in,
+                                                       const float *W, const float *bias, float *out,
+                                                       int relu, const int *gate, int mask) {
+    if (!gate_open(gate, mask)) return;
+    extern __shared__ float4 smem4[];
+    float *ws = reinterpret_cast<float *>(smem4);
+    constexpr int KK = K * K, H = K / 2;
+    for (int t = threadIdx.x; t < cin * KK * kMaxCh; t += blockDim.x) {
+        const int co = t % kMaxCh, r = t / kMaxCh, ci = r / KK, kk = r - ci * KK;
+        ws[t] = co < cout ? W[((size_t)co * cin + ci) * KK + kk] : 0.f;
+    }
+    __syncthreads();
+    const int RR = R * R;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < B * RR; p += gridDim.x * blockDim.x) {
+        const int b = p / RR, q = p - b * RR, x = q / R, y = q - x * R;
+        float acc[kMaxCh];
+#pragma unroll
+        for (int c = 0; c < kMaxCh; ++c) acc[c] = c < cout ? bias[c] : 0.f;
+        for (int ci = 0; ci < cin; ++ci) {
+            const float *ip = in + ((size_t)b * cin + ci) * RR;
+#pragma unroll
+            for (int kx = 0; kx < K; ++kx) {
+                const int xx = x + kx - H;
+#pragma unroll
+                for (int ky = 0; ky < K; ++ky) {
+                    const int yy = y + ky - H;
+                    const float v = (xx >= 0 && xx < R && yy >= 0 && yy < R) ? __ldg(ip + xx * R + yy) : 0.f;
+                    const float4 *w4 = reinterpret_cast<const float4 *>(ws + (size_t)(ci * KK + kx * K + ky) * kMaxCh);
+#pragma unroll
+                    for (int j = 0; j < kMaxCh / 4; ++j) {
+                        const float4 w = w4[j];
+                        acc[4 * j] += v * w.x;
+                        acc[4 * j + 1] += v * w.y;
+                        acc[4 * j + 2] += v * w.z;
+                        acc[4 * j + 3] += v * w.w;
+                    }
+                }
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < kMaxCh; ++c)
+            if (c < cout) out[((size_t)b * cout + c) * RR + q] = relu ? fmaxf(acc[c], 0.f) : acc[c];
+    }
+}
+
+// dIn[b][ci][x][y] = sum_co sum_k W[co][ci][k] g[b][co][x - kx + H][y - ky + H],
+// g = dOut, masked by out > 0 when the layer has a ReLU.  Weights in shared
+// memory as [cout][K*K][kMaxCh] (input channel fastest).
+template <int K>
+__global__ void __launch_bounds__(256) conv_bwd_data_kernel(int B, int R, int cin, int cout, const float *dout,
+                                                            const float *outv, int relu, const float *W,
+                                                            float *din) {
+    extern __shared__ float4 smem4[];
+    float *ws = reinterpret_cast<float *>(smem4);
+    constexpr int KK = K * K, H = K / 2;
+    for (int t = threadIdx.x; t < cout * KK * kMaxCh; t += blockDim.x) {
+        const int ci = t % kMaxCh, r = t / kMaxCh, co = r / KK, kk = r - co * KK;
+        ws[t] = ci < cin ? W[((size_t)co * cin + ci) * KK + kk] : 0.f;
+    }
+    __syncthreads();
+    const int RR = R * R;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < B * RR; p += gridDim.x * blockDim.x) {
+        const int b = p / RR, q = p - b * RR, x = q / R, y = q - x * R;
+        float acc[kMaxCh];
+#pragma unroll
+        for (int c = 0; c < kMaxCh; ++c) acc[c] = 0.f;
+        for (int co = 0; co < cout; ++co) {
+            const size_t base = ((size_t)b * cout + co) * RR;
+#pragma unroll
+            for (int kx = 0; kx < K; ++kx) {
+                const int xo = x - kx + H;
+#pragma unroll
+                for (int ky = 0; ky < K; ++ky) {
+                    const int yo = y - ky + H;
+                    float g = 0.f;
+                    if (xo >= 0 && xo < R && yo >= 0 && yo < R) {
+                        const size_t o = base + xo * R + yo;
+                        g = __ldg(dout + o);
+                        if (relu && !(__ldg(outv + o) > 0.f)) g = 0.f;
+                    }
+                    const float4 *w4 = reinterpret_cast<const float4 *>(ws + (size_t)(co * KK + kx * K + ky) * kMaxCh);
+#pragma unroll
+                    for (int j = 0; j < kMaxCh / 4; ++j) {
+                        const float4 w = w4[j];
+                        acc[4 * j] += g * w.x;
+                        acc[4 * j + 1] += g * w.y;
+                        acc[4 * j + 2] += g * w.z;
+                        acc[4 * j + 3] += g * w.w;
+                    }
+                }
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < kMaxCh; ++c)
+            if (c < cin) din[((size_t)b * cin + c) * RR + q] = acc[c];
+    }
+}
+
+// Weight and bias gradients of one tile of kTile x kTile output pixels of one
+// image: partial[tile][cout*cin*K*K + cout].  Shared memory: the masked
+// output gradient [kTile^2][kMaxCh] and the input patch [(kTile+K-1)^2][kMaxCh].
+template <int K>
+__global__ void __launch_bounds__(256) conv_bwd_weight_kernel(int B, int R, int cin, int cout, const float *in,
+                                                              const float *dout, const float *outv, int relu,
+                                                              float *partial) {
+    extern __shared__ float4 smem4[];
+    float *gs = reinterpret_cast<float *>(smem4);
+    constexpr int KK = K * K, H = K / 2, P = kTile + K - 1;
+    float *is = gs + kTile * kTile * kMaxCh;
+    const int tiles = R / kTile, tile = blockIdx.x, b = tile / (tiles * tiles);
+    const int tr = tile - b * tiles * tiles, x0 = (tr / tiles) * kTile, y0 = (tr % tiles) * kTile;
+    const int RR = R * R;
+    for (int t = threadIdx.x; t < kTile * kTile * cout; t += blockDim.x) {
+        const int co = t / (kTile * kTile), pp = t - co * kTile * kTile;
+        const int x = x0 + pp / kTile, y = y0 + pp % kTile;
+        const size_t o = ((size_t)b * cout + co) * RR + x * R + y;
+        float g = dout[o];
+        if (relu && !(outv[o] > 0.f)) g = 0.f;
+        gs[pp * kMaxCh + co] = g;
+    }
+    for (int t = threadIdx.x; t < P * P * cin; t += blockDim.x) {
+        const int ci = t / (P * P), pp = t - ci * P * P;
+        const int x = x0 + pp / P - H, y = y0 + pp % P - H;
+        is[pp * kMaxCh + ci] = (x >= 0 && x < R && y >= 0 && y < R) ? in[((size_t)b * cin + ci) * RR + x * R + y] : 0.f;
+    }
+    __syncthreads();
+    const int n_w = cout * cin * KK;
+    float *out = partial + (size_t)tile * (n_w + cout);
+    // (co, ci) pairs, every tap of a pair in registers
+    for (int pr = threadIdx.x; pr < cout * cin; pr += blockDim.x) {
+        const int co = pr / cin, ci = pr - co * cin;
+        float acc[KK];
+#pragma unroll
+        for (int k = 0; k < KK; ++k) acc[k] = 0.f;
+        for (int pp = 0; pp < kTile * kTile; ++pp) {
+            const float g = gs[pp * kMaxCh + co];
+            const int px = pp / kTile, py = pp - px * kTile;
+#pragma unroll
+            for (int kx = 0; kx < K; ++kx)
+#pragma unroll
+                for (int ky = 0; ky < K; ++ky) acc[kx * K + ky] += g * is[((px + kx) * P + py + ky) * kMaxCh + ci];
+        }
+#pragma unroll
+        for (int k = 0; k < KK; ++k) out[((size_t)co * cin + ci) * KK + k] = acc[k];
+    }
+    for (int co = threadIdx.x; co < cout; co += blockDim.x) {
+        float s = 0.f;
+        for (int pp = 0; pp < kTile * kTile; ++pp) s += gs[pp * kMaxCh + co];
+        out[n_w + co] = s;
+    }
+}
+
+// grad[j] = sum over tiles of partial[tile][j], tiles in order
+__global__ void reduce_tiles_kernel(int n_tiles, int n, const float *partial, float *grad) {
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+        float s = 0.f;
+        for (int t = 0; t < n_tiles; ++t) s += partial[(size_t)t * n + j];
+        grad[j] = s;
+    }
+}
+
+// ---- loss and optimiser ---------------------------------------------------
+
+// Mean squared error over the pixels at least `margin` from a map edge:
+// dy = 2 w_b (y - t) / n inside, 0 outside, with per-map weights w_b (null:
+// all 1); partials of the weighted squared error per block.
+__global__ void mse_kernel(int B, int C, int R, int margin, const float *y, const float *t, const float *w,
+                           float *dy, float *partials, unsigned int *counter, float *loss) {
+    __shared__ double red[32];
+    const int RR = R * R, inner = R - 2 * margin;
+    const float inv_n = 1.f / ((float)B * C * inner * inner);
+    float acc = 0.f;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < B * C * RR; k += gridDim.x * blockDim.x) {
+        const int q = k % RR, x = q / R, yy = q - x * R;
+        const bool in = x >= margin && x < R - margin && yy >= margin && yy < R - margin;
+        const float wb = w ? w[k / (C * RR)] : 1.f;
+        const float d = in ? y[k] - t[k] : 0.f;
+        dy[k] = 2.f * wb * d * inv_n;
+        acc += wb * d * d;
+    }
+    const float bsum = block_sum_ff(acc, reinterpret_cast<float *>(red));
+    if (threadIdx.x == 0) partials[blockIdx.x] = bsum;
+    if (arrive_last(counter)) {
+        const double tot = block_sum_f(kahan_strided(partials, threadIdx.x, gridDim.x, blockDim.x, 1), red);
+        if (threadIdx.x == 0) {
+            *loss = (float)(tot * (double)inv_n);
+            *counter = 0u;
+        }
+    }
+}
+
+// Per-map weight of the relative training loss: w_b = 1 / (mean of t^2 over
+// the map's inner pixels + eps), one block per map.  With it every map counts
+// by its relative error, whatever the size of its residual (early maps have
+// residuals hundreds of times larger than late ones).
+__global__ void rel_weight_kernel(int C, int R, int margin, const float *t, float *w) {
+    __shared__ double red[32];
+    const int b = blockIdx.x, RR = R * R, inner = R - 2 * margin;
+    const float *tb = t + (size_t)b * C * RR;
+    float acc = 0.f;
+    for (int k = threadIdx.x; k < C * RR; k += blockDim.x) {
+        const int q = k % RR, x = q / R, yy = q - x * R;
+        if (x >= margin && x < R - margin && yy >= margin && yy < R - margin) acc += tb[k] * tb[k];
+    }
+    const float s = block_sum_ff(acc, reinterpret_cast<float *>(red));
+    if (threadIdx.x == 0) w[b] = 1.f / (s / ((float)C * inner * inner) + 1e-6f);
+}
+
+// Adam (Kingma and Ba, 2015) with bias correction factors c1 = 1 - b1^t,
+// c2 = 1 - b2^t computed on the host.
+__global__ void adam_kernel(int n, float *w, const float *g, float *m, float *v, float lr, float b1, float b2,
+                            float c1, float c2, float eps) {
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+        const float gj = g[j];
+        const float mj = b1 * m[j] + (1.f - b1) * gj, vj = b2 * v[j] + (1.f - b2) * gj * gj;
+        m[j] = mj;
+        v[j] = vj;
+        w[j] -= lr * (mj / c1) / (sqrtf(vj / c2) + eps);
+    }
+}
+
+// Copies B crops of size Rc from the sample store: X [n][cx][R][R] and
+// T [n][ct][R][R] -> xb [B][cx][Rc][Rc], tb [B][ct][Rc][Rc]; crop i is
+// sample sel[3 i] at offset (sel[3 i + 1], sel[3 i + 2]).
+__global__ void crop_kernel(int B, int R, int Rc, int cx, int ct, const float *X, const float *T,
+                            const int *sel, float *xb, float *tb) {
+    const int RRc = Rc * Rc, c_all = cx + ct;
+    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < (size_t)B * c_all * RRc;
+         k += (size_t)gridDim.x * blockDim.x) {
+        const int i = (int)(k / ((size_t)c_all * RRc));
+        const int r = (int)(k - (size_t)i * c_all * RRc), c = r / RRc, q = r - c * RRc;
+        const int x = q / Rc, y = q - x * Rc;
+        const int sidx = sel[3 * i], ox = sel[3 * i + 1], oy = sel[3 * i + 2];
+        const size_t src = (size_t)(ox + x) * R + (oy + y);
+        if (c < cx)
+            xb[((size_t)i * cx + c) * RRc + q] = X[((size_t)sidx * cx + c) * R * R + src];
+        else
+            tb[((size_t)i * ct + (c - cx)) * RRc + q] = T[((size_t)sidx * ct + (c - cx)) * R * R + src];
+    }
+}
+
+// Relative field error of a surrogate field against the exact one over the
+// whole map: sum (s - e)^2 and sum e^2 (both axes), last-block fold into
+// err = sqrt(ratio); the judge then sets the fallback flag.
+__global__ void field_err_kernel(size_t n, const float *sx, const float *sy, const float *ex, const float *ey,
+                                 float *partials, unsigned int *counter, DevScalars *sc, double *err_out,
+                                 const int *gate, int mask) {
+    if (!gate_open(gate, mask)) return;
+    __shared__ double red[32];
+    float a = 0.f, b = 0.f;
+    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) {
+        const float dx = sx[k] - ex[k], dy = sy[k] - ey[k];
+        a += dx * dx + dy * dy;
+        b += ex[k] * ex[k] + ey[k] * ey[k];
+    }
+    float *redf = reinterpret_cast<float *>(red);
+    const float ba = block_sum_ff(a, redf), bb = block_sum_ff(b, redf);
+    if (threadIdx.x == 0) {
+        partials[2 * blockIdx.x] = ba;
+        partials[2 * blockIdx.x + 1] = bb;
+    }
+    if (arrive_last(counter)) {
+        const double ta = block_sum_f(kahan_strided(partials, threadIdx.x, gridDim.x, blockDim.x, 2), red);
+        const double tb = block_sum_f(kahan_strided(partials + 1, threadIdx.x, gridDim.x, blockDim.x, 2), red);
+        if (threadIdx.x == 0) {
+            const double err = tb > 0.0 ? sqrt(ta / tb) : 0.0;
+            if (err_out) *err_out = err;
+            if (sc) {
+                sc->surr_err = err;
+                sc->surr_ok = err <= (double)sc->surr_err_bound;
+                sc->surr_judged += 1;
+                if (!sc->surr_ok) sc->surr_fallbacks += 1;
+            }
+            *counter = 0u;
+        }
+    }
+}
+
+}  // namespace sg
+}  // namespace ap
+
+// ============================================================================
+// Host side
+// ============================================================================
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "../../include/aieplace.h"
+
+namespace ap {
+namespace {
+
+constexpr int kBlocks = 152 * 8;
+
+int grid_for(size_t n) {
+    const size_t b = (n + 255) / 256;
+    return (int)std::max<size_t>(1, std::min<size_t>(b, kBlocks));
+}
+
+template <typename T>
+bool dmalloc(T **p, size_t n) {
+    return cudaMalloc((void **)p, sizeof(T) * (n ? n : 1)) == cudaSuccess;
+}
+
+size_t conv_smem(int c, int k) { return (size_t)c * k * k * kMaxCh * sizeof(float); }
+
+size_t wgrad_smem(int k) {
+    const int P = kTile + k - 1;
+    return (size_t)(kTile * kTile + P * P) * kMaxCh * sizeof(float);
+}
+
+void conv_fwd(const SurrLayer &L, int B, int R, const float *in, const float *params, float *out, cudaStream_t st,
+              const int *gate, int mask) {
+    const int g = grid_for((size_t)B * R * R);
+    if (L.k == 3)
+        sg::conv_fwd_kernel<3><<<g, 256, conv_smem(L.cin, 3), st>>>(B, R, L.cin, L.cout, in, params + L.w_off,
+                                                                      params + L.b_off, out, L.relu, gate, mask);
+    else
+        sg::conv_fwd_kernel<1><<<g, 256, conv_smem(L.cin, 1), st>>>(B, R, L.cin, L.cout, in, params + L.w_off,
+                                                                      params + L.b_off, out, L.relu, gate, mask);
+}
+
+// dOut (w.r.t. this layer's output `outv`) -> weight/bias gradient into
+// grad + w_off, and (din != null) the gradient w.r.t. the layer input
+void conv_bwd(const SurrLayer &L, int B, int R, const float *in, const float *outv, const float *dout,
+              const float *params, float *grad, float *din, float *wpart, cudaStream_t st) {
+    const int tiles = B * (R / kTile) * (R / kTile);
+    const int n = L.cout * L.cin * L.k * L.k + L.cout;
+    if (L.k == 3)
+        sg::conv_bwd_weight_kernel<3><<<tiles, 256, wgrad_smem(3), st>>>(B, R, L.cin, L.cout, in, dout, outv,
+                                                                          L.relu, wpart);
+    else
+        sg::conv_bwd_weight_kernel<1><<<tiles, 256, wgrad_smem(1), st>>>(B, R, L.cin, L.cout, in, dout, outv,
+                                                                          L.relu, wpart);
+    sg::reduce_tiles_kernel<<<grid_for(n), 256, 0, st>>>(tiles, n, wpart, grad + L.w_off);
+    if (!din) return;
+    const int g = grid_for((size_t)B * R * R);
+    if (L.k == 3)
+        sg::conv_bwd_data_kernel<3><<<g, 256, conv_smem(L.cout, 3), st>>>(B, R, L.cin, L.cout, dout, outv, L.relu,
+                                                                           params + L.w_off, din);
+    else
+        sg::conv_bwd_data_kernel<1><<<g, 256, conv_smem(L.cout, 1), st>>>(B, R, L.cin, L.cout, dout, outv, L.relu,
+                                                                           params + L.w_off, din);
+}
+
+bool g_attrs_set = false;
+void set_kernel_attrs() {
+    if (g_attrs_set) return;
+    cudaFuncSetAttribute(sg::conv_bwd_weight_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)wgrad_smem(3));
+    cudaFuncSetAttribute(sg::conv_bwd_weight_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)wgrad_smem(1));
+    g_attrs_set = true;
+}
+
+// network forward over B maps of R x R: a[0] = x, a[l + 1] = layer l (a[4] = y)
+void net_forward(const SurrNet &net, int B, int R, float *const a[kSurrLayers + 1], cudaStream_t st,
+                 const int *gate = nullptr, int mask = 0) {
+    for (int l = 0; l < kSurrLayers; ++l) conv_fwd(net.L[l], B, R, a[l], net.d_params, a[l + 1], st, gate, mask);
+}
+
+}  // namespace
+
+// ---- per-handle state ----------------------------------------------------------
+
+int surr_state_init(SurrState &ss, const SurrNet &net, int M, float bin_ratio) {
+    surr_state_free(ss);
+    if (M % net.f != 0) return AP_ERR_UNSUPPORTED;
+    const int R = M / net.f;
+    if (R % kTile != 0 || R < 32) return AP_ERR_UNSUPPORTED;
+    ss.R = R;
+    ss.M = M;
+    const size_t RR = (size_t)R * R, MM = (size_t)M * M;
+    bool ok = dmalloc(&ss.d_pool, RR) && dmalloc(&ss.d_cex, RR) && dmalloc(&ss.d_cey, RR) && dmalloc(&ss.d_scale, 1) &&
+              dmalloc(&ss.d_x0, RR * net.cin0) && dmalloc(&ss.d_act[0], RR * kMaxCh) &&
+              dmalloc(&ss.d_act[1], RR * kMaxCh) && dmalloc(&ss.d_y, RR * net.cout) && dmalloc(&ss.d_sex, MM) &&
+              dmalloc(&ss.d_sey, MM) && dmalloc(&ss.d_part, 2 * kBlocks) && dmalloc(&ss.d_cnt, 4);
+    if (!ok || cudaMemset(ss.d_cnt, 0, 4 * sizeof(unsigned int)) != cudaSuccess) {
+        surr_state_free(ss);
+        return AP_ERR_CUDA;
+    }
+    // the coarse solve on the tensor cores when R allows 128-row tiles
+    const bool want_tc = R % 128 == 0;
+    int r = field_solver_init(ss.coarse, R, bin_ratio, want_tc ? 1 : 0);
+    if (r != AP_OK) {
+        surr_state_free(ss);
+        return r;
+    }
+    if (want_tc && dmalloc(&ss.d_phi, RR) && dmalloc(&ss.d_plo, RR) &&
+        cudaMemset(ss.d_phi, 0, sizeof(__nv_bfloat16) * RR) == cudaSuccess &&
+        cudaMemset(ss.d_plo, 0, sizeof(__nv_bfloat16) * RR) == cudaSuccess &&
+        field_solver_bind_bf16(ss.coarse, ss.d_phi, ss.d_plo) == AP_OK)
+        ss.tc = 1;
+    return AP_OK;
+}
+
+void surr_state_free(SurrState &ss) {
+    if (ss.R) field_solver_free(ss.coarse);
+    void *p[] = {ss.d_pool, ss.d_cex, ss.d_cey, ss.d_scale, ss.d_x0, ss.d_act[0], ss.d_act[1], ss.d_y,
+                 ss.d_sex, ss.d_sey, ss.d_part, ss.d_cnt, ss.d_phi, ss.d_plo};
+    for (void *q : p)
+        if (q) cudaFree(q);
+    ss = SurrState{};
+}
+
+void surr_enqueue_input(const SurrNet &net, SurrState &ss, const float *d_f32, const __nv_bfloat16 *d_hi,
+                        const __nv_bfloat16 *d_lo, const int *gate, int mask, cudaStream_t st, bool with_net_input) {
+    const int R = ss.R, M = ss.M, f = net.f;
+    const int g = grid_for((size_t)R * R);
+    if (ss.tc) {
+        sg::pool_kernel<<<g, 256, 0, st>>>(M, f, d_f32, d_hi, d_lo, nullptr, ss.d_phi, ss.d_plo, gate, mask);
+        field_solve_bf16x3(ss.coarse, ss.d_phi, ss.d_plo, ss.d_cex, ss.d_cey, st, gate, mask);
+    } else {
+        sg::pool_kernel<<<g, 256, 0, st>>>(M, f, d_f32, d_hi, d_lo, ss.d_pool, nullptr, nullptr, gate, mask);
+        field_solve_fp32(ss.coarse, ss.d_pool, ss.d_cex, ss.d_cey, st, gate, mask);
+    }
+    sg::scale_kernel<<<g, 256, 0, st>>>(R, f, ss.d_cex, ss.d_cey, ss.d_part, ss.d_cnt + 0, ss.d_scale, gate, mask);
+    if (with_net_input)
+        sg::prep_kernel<<<g, 256, 0, st>>>(M, f, d_f32, d_hi, d_lo, ss.d_cex, ss.d_cey, ss.d_scale, ss.d_x0, gate,
+                                           mask);
+}
+
+void surr_enqueue_field(const SurrNet &net, SurrState &ss, const float *d_f32, const __nv_bfloat16 *d_hi,
+                        const __nv_bfloat16 *d_lo, float *ex, float *ey, const int *gate, cudaStream_t st) {
+    const int mask = kGateSurr;
+    surr_enqueue_input(net, ss, d_f32, d_hi, d_lo, gate, mask, st, ss.use_net != 0);
+    const float *y = nullptr;
+    if (ss.use_net) {
+        float *const a[kSurrLayers + 1] = {ss.d_x0, ss.d_act[0], ss.d_act[1], ss.d_act[0], ss.d_y};
+        net_forward(net, 1, ss.R, a, st, gate, mask);
+        y = ss.d_y;
+    }
+    sg::combine_kernel<<<grid_for((size_t)ss.M * ss.M), 256, 0, st>>>(ss.M, net.f, ss.d_cex, ss.d_cey, y,
+                                                                      ss.d_scale, ex, ey, ss.d_sex, ss.d_sey,
+                                                                      gate, mask);
+}
+
+void surr_enqueue_judge(SurrState &ss, const float *ex, const float *ey, DevScalars *sc, const int *gate,
+                        cudaStream_t st) {
+    const size_t n = (size_t)ss.M * ss.M;
+    sg::field_err_kernel<<<grid_for(n), 256, 0, st>>>(n, ss.d_sex, ss.d_sey, ex, ey, ss.d_part, ss.d_cnt + 1, sc,
+                                                      nullptr, gate, kGateJudge);
+}
+
+void surr_enqueue_sample(const SurrNet &net, SurrState &ss, float *X, float *T, float *s_slot, float *e2_slot,
+                         const float *ex, const float *ey, cudaStream_t st) {
+    const size_t RR = (size_t)ss.R * ss.R, MM = (size_t)ss.M * ss.M;
+    cudaMemcpyAsync(X, ss.d_x0, sizeof(float) * RR * net.cin0, cudaMemcpyDeviceToDevice, st);
+    sg::target_kernel<<<grid_for(MM), 256, 0, st>>>(ss.M, net.f, ex, ey, ss.d_cex, ss.d_cey, ss.d_scale, T);
+    cudaMemcpyAsync(s_slot, ss.d_scale, sizeof(float), cudaMemcpyDeviceToDevice, st);
+    sg::sumsq_kernel<<<grid_for(MM), 256, 0, st>>>(MM, ex, ey, ss.d_part, ss.d_cnt + 2, e2_slot);
+}
+
+}  // namespace ap
+
+// ---- C ABI: the network --------------------------------------------------------
+namespace {
+
+using ap::kMaxCh;
+using ap::kSurrLayers;
+using ap::kTile;
+
+// xoshiro256** (Blackman and Vigna), seeded through splitmix64
+struct Rng {
+    uint64_t s[4];
+    explicit Rng(uint64_t seed) {
+        for (int i = 0; i < 4; ++i) {
+            seed += 0x9E3779B97F4A7C15ull;
+            uint64_t z = seed;
+            z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+            z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+            s[i] = z ^ (z >> 31);
+        }
+    }
+    static uint64_t rotl(uint64_t x, int k) { return (x << k) | (x >> (64 - k)); }
+    uint64_t next() {
+        const uint64_t r = rotl(s[1] * 5, 7) * 9, t = s[1] << 17;
+        s[2] ^= s[0];
+        s[3] ^= s[1];
+        s[1] ^= s[2];
+        s[0] ^= s[3];
+        s[2] ^= t;
+        s[3] = rotl(s[3], 45);
+        return r;
+    }
+    double uniform() { return (double)(next() >> 11) * (1.0 / 9007199254740992.0); }
+    double normal() {  // Box-Muller
+        double u = uniform(), v = uniform();
+        if (u < 1e-300) u = 1e-300;
+        return sqrt(-2.0 * log(u)) * cos(6.283185307179586 * v);
+    }
+    int below(int n) { return (int)(next() % (uint64_t)n); }
+};
+
+void free_scratch(ap_surrogate *s) {
+    for (float *&p : s->d_a)
+        if (p) cudaFree(p), p = nullptr;
+    for (float *&p : s->d_g)
+        if (p) cudaFree(p), p = nullptr;
+    float **fp[] = {&s->d_tb, &s->d_wpart, &s->d_lpart, &s->d_loss, &s->d_w};
+    for (float **p : fp)
+        if (*p) cudaFree(*p), *p = nullptr;
+    if (s->d_sel) cudaFree(s->d_sel), s->d_sel = nullptr;
+    if (s->d_cnt) cudaFree(s->d_cnt), s->d_cnt = nullptr;
+    s->tB = s->tR = 0;
+}
+
+// scratch for B maps of R x R (activations, gradients, targets, partials)
+int ensure_scratch(ap_surrogate *s, int B, int R) {
+    if (s->tB >= B && s->tR == R) return AP_OK;
+    free_scratch(s);
+    const size_t RR = (size_t)R * R;
+    const ap::SurrNet &n = s->net;
+    bool ok = ap::dmalloc(&s->d_a[0], (size_t)B * n.cin0 * RR);
+    for (int l = 1; l <= kSurrLayers; ++l) ok = ok && ap::dmalloc(&s->d_a[l], (size_t)B * kMaxCh * RR);
+    ok = ok && ap::dmalloc(&s->d_g[0], (size_t)B * kMaxCh * RR) && ap::dmalloc(&s->d_g[1], (size_t)B * kMaxCh * RR);
+    const size_t tiles = (size_t)B * (R / kTile) * (R / kTile);
+    ok = ok && ap::dmalloc(&s->d_tb, (size_t)B * n.cout * RR) &&
+         ap::dmalloc(&s->d_wpart, tiles * (kMaxCh * kMaxCh * 9 + kMaxCh)) && ap::dmalloc(&s->d_lpart, 2 * ap::kBlocks) &&
+         ap::dmalloc(&s->d_loss, 2) && ap::dmalloc(&s->d_sel, 3 * (size_t)B) && ap::dmalloc(&s->d_cnt, 4) &&
+         ap::dmalloc(&s->d_w, B);
+    if (!ok || cudaMemset(s->d_cnt, 0, 4 * sizeof(unsigned int)) != cudaSuccess) {
+        free_scratch(s);
+        return AP_ERR_CUDA;
+    }
+    s->tB = B;
+    s->tR = R;
+    return AP_OK;
+}
+
+// forward + loss + backward on s->d_a[0] (inputs) and s->d_tb (targets);
+// gradient into net.d_grad, loss into s->d_loss
+void train_pass(ap_surrogate *s, int B, int R, int margin, bool relative, cudaStream_t st) {
+    ap::SurrNet &net = s->net;
+    float *const *a = s->d_a;
+    ap::net_forward(net, B, R, a, st);
+    const size_t ny = (size_t)B * net.cout * R * R;
+    if (relative) ap::sg::rel_weight_kernel<<<B, 256, 0, st>>>(net.cout, R, margin, s->d_tb, s->d_w);
+    ap::sg::mse_kernel<<<ap::grid_for(ny), 256, 0, st>>>(B, net.cout, R, margin, a[kSurrLayers], s->d_tb,
+                                                         relative ? s->d_w : nullptr, s->d_g[0], s->d_lpart,
+                                                         s->d_cnt, s->d_loss);
+    int cur = 0;
+    for (int l = kSurrLayers - 1; l >= 0; --l) {
+        float *din = l > 0 ? s->d_g[1 - cur] : nullptr;
+        ap::conv_bwd(net.L[l], B, R, a[l], a[l + 1], s->d_g[cur], net.d_params, net.d_grad, din, s->d_wpart, st);
+        cur = 1 - cur;
+    }
+}
+
+#define CKS(call)                                         \
+    do {                                                  \
+        if ((call) != cudaSuccess) return AP_ERR_CUDA;    \
+    } while (0)
+
+}  // namespace
+
+extern "C" {
+
+int ap_surrogate_config_default(ap_surrogate_config *cfg) {
+    if (!cfg) return AP_ERR_INVALID_ARG;
+    cfg->factor = 2;
+    cfg->kernel[0] = 3;
+    cfg->kernel[1] = 1;
+    cfg->kernel[2] = 1;
+    cfg->kernel[3] = 3;
+    cfg->width = 32;
+    cfg->seed = 1;
+    return AP_OK;
+}
+
+int ap_surrogate_create(const ap_surrogate_config *cfg, ap_surrogate **out) {
+    if (!cfg || !out) return AP_ERR_INVALID_ARG;
+    *out = nullptr;
+    const int f = cfg->factor;
+    if (f < 1 || f > 4 || cfg->width < 1 || cfg->width > kMaxCh) return AP_ERR_INVALID_ARG;
+    if (2 * f * f > kMaxCh || f * f + 2 > kMaxCh) return AP_ERR_INVALID_ARG;
+    for (int l = 0; l < kSurrLayers; ++l)
+        if (cfg->kernel[l] != 1 && cfg->kernel[l] != 3) return AP_ERR_INVALID_ARG;
+    ap::set_kernel_attrs();
+    ap_surrogate *s = new ap_surrogate();
+    ap::SurrNet &n = s->net;
+    n.f = f;
+    n.cin0 = f * f + 2;
+    n.cout = 2 * f * f;
+    n.width = cfg->width;
+    size_t off = 0;
+    for (int l = 0; l < kSurrLayers; ++l) {
+        ap::SurrLayer &L = n.L[l];
+        L.cin = l == 0 ? n.cin0 : n.width;
+        L.cout = l == kSurrLayers - 1 ? n.cout : n.width;
+        L.k = cfg->kernel[l];
+        L.relu = l < kSurrLayers - 1;
+        L.w_off = off;
+        off += (size_t)L.cout * L.cin * L.k * L.k;
+        L.b_off = off;
+        off += L.cout;
+    }
+    n.n_params = (int)off;
+    // He-normal hidden layers, zero output layer (the untrained net adds nothing)
+    std::vector<float> p(off, 0.f);
+    Rng rng(cfg->seed);
+    for (int l = 0; l < kSurrLayers - 1; ++l) {
+        const ap::SurrLayer &L = n.L[l];
+        const double sd = sqrt(2.0 / (double)(L.cin * L.k * L.k));
+        for (size_t i = 0; i < (size_t)L.cout * L.cin * L.k * L.k; ++i) p[L.w_off + i] = (float)(sd * rng.normal());
+    }
+    bool ok = ap::dmalloc(&n.d_params, off) && ap::dmalloc(&n.d_grad, off) && ap::dmalloc(&n.d_m, off) &&
+              ap::dmalloc(&n.d_v, off);
+    ok = ok && cudaMemcpy(n.d_params, p.data(), sizeof(float) * off, cudaMemcpyHostToDevice) == cudaSuccess &&
+         cudaMemset(n.d_m, 0, sizeof(float) * off) == cudaSuccess &&
+         cudaMemset(n.d_v, 0, sizeof(float) * off) == cudaSuccess;
+    if (!ok) {
+        ap_surrogate_destroy(s);
+        return AP_ERR_CUDA;
+    }
+    *out = s;
+    return AP_OK;
+}
+
+int ap_surrogate_destroy(ap_surrogate *s) {
+    if (!s) return AP_ERR_INVALID_ARG;
+    cudaDeviceSynchronize();
+    free_scratch(s);
+    float *p[] = {s->net.d_params, s->net.d_grad, s->net.d_m, s->net.d_v, s->d_X, s->d_T, s->d_s, s->d_e2};
+    for (float *q : p)
+        if (q) cudaFree(q);
+    delete s;
+    return AP_OK;
+}
+
+int ap_surrogate_num_params(ap_surrogate *s, int32_t *n) {
+    if (!s || !n) return AP_ERR_INVALID_ARG;
+    *n = s->net.n_params;
+    return AP_OK;
+}
+
+int ap_surrogate_get_params(ap_surrogate *s, float *params, int32_t n) {
+    if (!s || !params || n != s->net.n_params) return AP_ERR_INVALID_ARG;
+    CKS(cudaMemcpy(params, s->net.d_params, sizeof(float) * n, cudaMemcpyDeviceToHost));
+    return AP_OK;
+}
+
+int ap_surrogate_set_params(ap_surrogate *s, const float *params, int32_t n) {
+    if (!s || !params || n != s->net.n_params) return AP_ERR_INVALID_ARG;
+    CKS(cudaMemcpy(s->net.d_params, params, sizeof(float) * n, cudaMemcpyHostToDevice));
+    CKS(cudaMemset(s->net.d_m, 0, sizeof(float) * n));
+    CKS(cudaMemset(s->net.d_v, 0, sizeof(float) * n));
+    s->net.adam_t = 0;
+    return AP_OK;
+}
+
+int ap_surrogate_forward(ap_surrogate *s, const float *x, int32_t batch, int32_t res, float *y) {
+    if (!s || !x || !y || batch < 1 || res < kTile || res % kTile) return AP_ERR_INVALID_ARG;
+    int r = ensure_scratch(s, batch, res);
+    if (r != AP_OK) return r;
+    const size_t RR = (size_t)res * res;
+    CKS(cudaMemcpy(s->d_a[0], x, sizeof(float) * batch * s->net.cin0 * RR, cudaMemcpyHostToDevice));
+    ap::net_forward(s->net, batch, res, s->d_a, 0);
+    CKS(cudaGetLastError());
+    CKS(cudaMemcpy(y, s->d_a[kSurrLayers], sizeof(float) * batch * s->net.cout * RR, cudaMemcpyDeviceToHost));
+    return AP_OK;
+}
+
+int ap_surrogate_gradient(ap_surrogate *s, const float *x, const float *t, int32_t batch, int32_t res,
+                          int32_t margin, float *loss, float *grad) {
+    if (!s || !x || !t || !loss || !grad || batch < 1 || res < kTile || res % kTile || margin < 0 ||
+        2 * margin >= res)
+        return AP_ERR_INVALID_ARG;
+    int r = ensure_scratch(s, batch, res);
+    if (r != AP_OK) return r;
+    const size_t RR = (size_t)res * res;
+    CKS(cudaMemcpy(s->d_a[0], x, sizeof(float) * batch * s->net.cin0 * RR, cudaMemcpyHostToDevice));
+    CKS(cudaMemcpy(s->d_tb, t, sizeof(float) * batch * s->net.cout * RR, cudaMemcpyHostToDevice));
+    train_pass(s, batch, res, margin, false, 0);
+    CKS(cudaGetLastError());
+    CKS(cudaMemcpy(loss, s->d_loss, sizeof(float), cudaMemcpyDeviceToHost));
+    CKS(cudaMemcpy(grad, s->net.d_grad, sizeof(float) * s->net.n_params, cudaMemcpyDeviceToHost));
+    return AP_OK;
+}
+
+int ap_surrogate_reserve(ap_surrogate *s, int32_t n, int32_t res) {
+    if (!s || n < 1 || res < 32 || res % kTile) return AP_ERR_INVALID_ARG;
+    float *p[] = {s->d_X, s->d_T, s->d_s, s->d_e2};
+    for (float *q : p)
+        if (q) cudaFree(q);
+    s->d_X = s->d_T = s->d_s = s->d_e2 = nullptr;
+    s->cap = s->n = 0;
+    const size_t RR = (size_t)res * res;
+    if (!ap::dmalloc(&s->d_X, (size_t)n * s->net.cin0 * RR) || !ap::dmalloc(&s->d_T, (size_t)n * s->net.cout * RR) ||
+        !ap::dmalloc(&s->d_s, n) || !ap::dmalloc(&s->d_e2, n))
+        return AP_ERR_CUDA;
+    s->cap = n;
+    s->R = res;
+    return AP_OK;
+}
+
+int ap_surrogate_num_samples(ap_surrogate *s, int32_t *n) {
+    if (!s || !n) return AP_ERR_INVALID_ARG;
+    *n = s->n;
+    return AP_OK;
+}
+
+int ap_surrogate_train(ap_surrogate *s, int32_t steps, int32_t batch, int32_t crop, float lr, uint64_t seed,
+                       int32_t first, int32_t count, float *loss_per_step) {
+    if (!s || steps < 0 || batch < 1 || crop < kTile || crop % kTile || crop > s->R || !(lr > 0.f) || first < 0 ||
+        count < 1 || first + count > s->n)
+        return AP_ERR_INVALID_ARG;
+    int r = ensure_scratch(s, batch, crop);
+    if (r != AP_OK) return r;
+    ap::SurrNet &net = s->net;
+    Rng rng(seed);
+    std::vector<int> sel(3 * (size_t)batch);
+    const int margin = 2;  // pixels a crop's zero padding can reach through the two 3x3 layers
+    const float b1 = 0.9f, b2 = 0.999f;
+    for (int it = 0; it < steps; ++it) {
+        for (int i = 0; i < batch; ++i) {
+            sel[3 * i] = first + rng.below(count);
+            sel[3 * i + 1] = rng.below(s->R - crop + 1);
+            sel[3 * i + 2] = rng.below(s->R - crop + 1);
+        }
+        CKS(cudaMemcpy(s->d_sel, sel.data(), sizeof(int) * sel.size(), cudaMemcpyHostToDevice));
+        const size_t n_el = (size_t)batch * (net.cin0 + net.cout) * crop * crop;
+        ap::sg::crop_kernel<<<ap::grid_for(n_el), 256>>>(batch, s->R, crop, net.cin0, net.cout, s->d_X, s->d_T,
+                                                         s->d_sel, s->d_a[0], s->d_tb);
+        train_pass(s, batch, crop, margin, true, 0);
+        net.adam_t += 1;
+        const float c1 = 1.f - powf(b1, (float)net.adam_t), c2 = 1.f - powf(b2, (float)net.adam_t);
+        ap::sg::adam_kernel<<<ap::grid_for(net.n_params), 256>>>(net.n_params, net.d_params, net.d_grad, net.d_m,
+                                                                 net.d_v, lr, b1, b2, c1, c2, 1e-8f);
+        CKS(cudaGetLastError());
+        if (loss_per_step) CKS(cudaMemcpy(loss_per_step + it, s->d_loss, sizeof(float), cudaMemcpyDeviceToHost));
+    }
+    CKS(cudaDeviceSynchronize());
+    return AP_OK;
+}
+
+int ap_surrogate_validate(ap_surrogate *s, int32_t first, int32_t count, double *err_net, double *err_coarse) {
+    if (!s || !err_net || !err_coarse || first < 0 || count < 1 || first + count > s->n) return AP_ERR_INVALID_ARG;
+    const int R = s->R;
+    int r = ensure_scratch(s, 1, R);
+    if (r != AP_OK) return r;
+    ap::SurrNet &net = s->net;
+    const size_t RR = (size_t)R * R, ny = (size_t)net.cout * RR;
+    std::vector<float> sc(s->n), e2(s->n);
+    CKS(cudaMemcpy(sc.data(), s->d_s, sizeof(float) * s->n, cudaMemcpyDeviceToHost));
+    CKS(cudaMemcpy(e2.data(), s->d_e2, sizeof(float) * s->n, cudaMemcpyDeviceToHost));
+    for (int i = first; i < first + count; ++i) {
+        CKS(cudaMemcpy(s->d_a[0], s->d_X + (size_t)i * net.cin0 * RR, sizeof(float) * net.cin0 * RR,
+                       cudaMemcpyDeviceToDevice));
+        ap::net_forward(net, 1, R, s->d_a, 0);
+        ap::sg::diff_norms_kernel<<<ap::grid_for(ny), 256>>>(ny, s->d_a[kSurrLayers], s->d_T + (size_t)i * ny,
+                                                             s->d_lpart, s->d_cnt + 1, s->d_loss);
+        float nm[2];
+        CKS(cudaMemcpy(nm, s->d_loss, 2 * sizeof(float), cudaMemcpyDeviceToHost));
+        // t = (E - base) / s, so s |t| = |E - base| and s |y - t| = |E - (base + s y)|;
+        // |E| = sqrt(e2): errors relative to the exact field over the fine map
+        const double en = sqrt((double)e2[i]) / (double)sc[i];
+        err_coarse[i - first] = en > 0 ? sqrt((double)nm[1]) / en : 0.0;
+        err_net[i - first] = en > 0 ? sqrt((double)nm[0]) / en : 0.0;
+    }
+    return AP_OK;
+}
+
+}  // extern "C"

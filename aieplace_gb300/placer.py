@@ -20,7 +20,8 @@ import ctypes as C
 
 import numpy as np
 
-from ._lib import AP_FIELD_BF16X3, AP_FIELD_FP32, Netlist, Params, Stats, check, lib, ptr
+from ._lib import (AP_FIELD_BF16X3, AP_FIELD_FP32, Netlist, Params, Stats, SurrogatePolicy, SurrogateStats, check,
+                   lib, ptr)
 
 SOLVERS = {"fp32": AP_FIELD_FP32, "bf16x3": AP_FIELD_BF16X3}
 
@@ -162,6 +163,23 @@ class Placer:
         sv = -1 if solver is None else SOLVERS[solver]
         check("ap_field_solve", lib().ap_field_solve(self._h, ptr(d), ptr(ex), ptr(ey), sv))
         return ex, ey
+
+    # ---- learned surrogate (no counterpart in the reference) ---------------
+    def attach_surrogate(self, surrogate, overflow_min: float = 0.3, judge_every: int = 8,
+                         max_error: float = 0.02, use_net: bool = True):
+        """The loop takes its field from `surrogate` while the overflow exceeds
+        overflow_min; every judge_every-th trial the exact solve runs too and
+        the surrogate is dropped until the next judgement if its relative
+        field error exceeds max_error.  surrogate=None detaches."""
+        self._surrogate = surrogate  # keep it alive while attached
+        pol = SurrogatePolicy(float(overflow_min), int(judge_every), float(max_error), int(bool(use_net)))
+        sh = None if surrogate is None else surrogate._h
+        check("ap_attach_surrogate", lib().ap_attach_surrogate(self._h, sh, C.byref(pol)))
+
+    def surrogate_stats(self) -> dict:
+        s = SurrogateStats()
+        check("ap_surrogate_get_stats", lib().ap_surrogate_get_stats(self._h, C.byref(s)))
+        return {"used": s.used, "judged": s.judged, "fallbacks": s.fallbacks, "last_error": s.last_error}
 
     # ---- checkpoint / resume ----------------------------------------------
     def snapshot(self) -> bytes:

@@ -254,6 +254,72 @@ int ap_batch_run(ap_batch *b, int32_t *iterations);
 int ap_batch_get_stats(ap_batch *b, int32_t i, ap_stats *stats);
 int ap_batch_get_positions(ap_batch *b, int32_t i, float *x, float *y);
 
+/* ---- learned density-to-field surrogate ------------------------------------
+ * No counterpart in the reference (its field solves are exact).  A surrogate
+ * stands in for the exact solve of an M x M map during the early,
+ * high-overflow trials of the loop:
+ *   coarse grid R = M / factor: the density is pooled factor x factor, the
+ *   field is solved exactly at R (FP32), and a 4-layer conv net (32 hidden
+ *   channels, ReLU) maps the factor^2 sub-bin densities of each coarse bin
+ *   plus the coarse field (scaled by its RMS) to the fine-resolution residual
+ *   field (2 factor^2 output channels, depth-to-space).
+ * Training runs on the GPU with the library's own forward/backward kernels
+ * (FP32, Adam, deterministic) on (density, field) pairs that the exact solver
+ * produces during loop runs (ap_surrogate_collect).  Parameters are one flat
+ * FP32 vector: per layer the weights [cout][cin][k][k], then the biases.
+ * R must be a multiple of 16.  Tensors are [batch][channel][x][y], y fastest. */
+typedef struct ap_surrogate ap_surrogate;
+
+typedef struct ap_surrogate_config {
+    int32_t factor;     /* pooling factor f (M = f R); 1..4 */
+    int32_t kernel[4];  /* kernel size of each layer, 1 or 3 */
+    int32_t width;      /* hidden channels, <= 32 (32 in the shipped form) */
+    uint64_t seed;      /* weight initialisation (He normal; last layer zero) */
+} ap_surrogate_config;
+
+typedef struct ap_surrogate_policy {
+    float overflow_min;  /* surrogate used while the trial's overflow exceeds this (0.3) */
+    int32_t judge_every; /* every n-th trial the exact solve runs and judges the surrogate (8) */
+    float max_error;     /* relative field error above which the exact solve takes over (0.02) */
+    int32_t use_net;     /* 0: coarse spectral layer only (the ablation), 1: with the net */
+} ap_surrogate_policy;
+
+typedef struct ap_surrogate_stats {
+    int32_t used;        /* trials whose field came from the surrogate */
+    int32_t judged;      /* trials that ran both and compared */
+    int32_t fallbacks;   /* judgements above max_error */
+    double last_error;   /* last judged relative field error */
+} ap_surrogate_stats;
+
+int ap_surrogate_config_default(ap_surrogate_config *cfg);
+int ap_surrogate_create(const ap_surrogate_config *cfg, ap_surrogate **out);
+int ap_surrogate_destroy(ap_surrogate *s);
+int ap_surrogate_num_params(ap_surrogate *s, int32_t *n);
+int ap_surrogate_get_params(ap_surrogate *s, float *params, int32_t n);
+int ap_surrogate_set_params(ap_surrogate *s, const float *params, int32_t n);
+/* network forward on host tensors: x [batch][f^2 + 2][res][res] -> y [batch][2 f^2][res][res] */
+int ap_surrogate_forward(ap_surrogate *s, const float *x, int32_t batch, int32_t res, float *y);
+/* loss = mean over pixels >= margin from the edges of (y - t)^2 and its
+ * gradient with respect to every parameter (grad: num_params floats) */
+int ap_surrogate_gradient(ap_surrogate *s, const float *x, const float *t, int32_t batch, int32_t res,
+                          int32_t margin, float *loss, float *grad);
+/* sample store on the device for n samples at coarse resolution res */
+int ap_surrogate_reserve(ap_surrogate *s, int32_t n, int32_t res);
+int ap_surrogate_num_samples(ap_surrogate *s, int32_t *n);
+/* runs n_trials exact loop trials of h, storing every `every`-th trial's
+ * (network input, residual target) pair; *collected receives the count */
+int ap_surrogate_collect(ap_handle *h, ap_surrogate *s, int32_t n_trials, int32_t every, int32_t *collected);
+/* Adam on random crop x crop patches (batch per step) of samples
+ * [first, first + count); loss_per_step may be NULL */
+int ap_surrogate_train(ap_surrogate *s, int32_t steps, int32_t batch, int32_t crop, float lr, uint64_t seed,
+                       int32_t first, int32_t count, float *loss_per_step);
+/* per-sample relative field error (over the whole fine map) with the net
+ * and with the coarse layer alone */
+int ap_surrogate_validate(ap_surrogate *s, int32_t first, int32_t count, double *err_net, double *err_coarse);
+/* attaches (s != NULL) or detaches (s == NULL) a surrogate to the loop of h */
+int ap_attach_surrogate(ap_handle *h, ap_surrogate *s, const ap_surrogate_policy *policy);
+int ap_surrogate_get_stats(ap_handle *h, ap_surrogate_stats *stats);
+
 /* ---- seeded synthetic netlists ------------------------------------------ */
 /* Stands in for the ISPD suites the reference reads through LEF/DEF.  Nodes
  * are ordered: movable cells, fixed macros, IO pads. */

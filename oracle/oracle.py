@@ -90,6 +90,13 @@ def lib():
         L.or_destroy.argtypes = [C.c_void_p]
         L.or_set_threads.restype = C.c_int
         L.or_set_threads.argtypes = [C.c_int]
+        L.or_surr_num_params.argtypes = [C.c_int, C.c_int, C.c_int, _i32p]
+        L.or_surr_forward.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _i32p, _f64p, _f64p, _f64p]
+        L.or_surr_loss_grad.restype = C.c_double
+        L.or_surr_loss_grad.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _i32p, _f64p, _f64p, _f64p,
+                                        C.c_int, _f64p]
+        L.or_surr_pool.argtypes = [C.c_int, C.c_int, _f64p, _f64p]
+        L.or_surr_combine.argtypes = [C.c_int, C.c_int, _f64p, _f64p, C.c_void_p, C.c_double, _f64p, _f64p]
         _lib = L
     return _lib
 
@@ -256,3 +263,51 @@ def _f32(a):
 
 def _i32(a):
     return np.ascontiguousarray(a, dtype=np.int32)
+
+
+# ---- learned surrogate network (surrogate.c) -----------------------------------
+
+def surr_num_params(cin0: int, width: int, cout: int, kernels) -> int:
+    k = np.ascontiguousarray(kernels, np.int32)
+    return lib().or_surr_num_params(cin0, width, cout, k)
+
+
+def surr_forward(x, params, width: int, cout: int, kernels):
+    """x [B][cin0][R][R] -> y [B][cout][R][R], FP64."""
+    x = np.ascontiguousarray(x, np.float64)
+    B, cin0, R, _ = x.shape
+    y = np.zeros((B, cout, R, R), np.float64)
+    lib().or_surr_forward(B, R, cin0, width, cout, np.ascontiguousarray(kernels, np.int32),
+                          np.ascontiguousarray(params, np.float64), x, y)
+    return y
+
+
+def surr_loss_grad(x, t, params, width: int, kernels, margin: int):
+    x = np.ascontiguousarray(x, np.float64)
+    t = np.ascontiguousarray(t, np.float64)
+    B, cin0, R, _ = x.shape
+    cout = t.shape[1]
+    p = np.ascontiguousarray(params, np.float64)
+    g = np.zeros_like(p)
+    loss = lib().or_surr_loss_grad(B, R, cin0, width, cout, np.ascontiguousarray(kernels, np.int32), p, x, t,
+                                   margin, g)
+    return loss, g
+
+
+def surr_pool(d, f: int):
+    d = np.ascontiguousarray(d, np.float64)
+    M = d.shape[0]
+    out = np.zeros((M // f, M // f), np.float64)
+    lib().or_surr_pool(M, f, d, out)
+    return out
+
+
+def surr_combine(cex, cey, y, s: float, f: int):
+    cex = np.ascontiguousarray(cex, np.float64)
+    cey = np.ascontiguousarray(cey, np.float64)
+    M = cex.shape[0] * f
+    ex = np.zeros((M, M), np.float64)
+    ey = np.zeros((M, M), np.float64)
+    yp = None if y is None else np.ascontiguousarray(y, np.float64)
+    lib().or_surr_combine(M, f, cex, cey, None if yp is None else yp.ctypes.data, float(s), ex, ey)
+    return ex, ey
