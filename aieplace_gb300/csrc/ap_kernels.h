@@ -12,9 +12,10 @@ namespace ap {
 enum { WA_OUT_ONLY = 0, WA_LOOP = 1, WA_INIT = 2 };
 
 // Nets are bucketed by degree: [2], [3,4], [5,8] (one thread per net, pins in
-// registers) and > 8 (one warp per net); bucket b spans nets
-// [bucket_lo[b], bucket_lo[b+1]).
-constexpr int kWaBuckets = 4;
+// registers), [9,16] (16 lanes per net), [17,32], [33,64] (a warp, one or two
+// pins per lane in registers) and > 64 (a warp looping over the pins); bucket
+// b spans nets [bucket_lo[b], bucket_lo[b+1]).
+constexpr int kWaBuckets = 7;
 
 struct WaArgs {
     const int *net_ptr;    // [n_nets + 1], nets in bucket order

@@ -67,7 +67,7 @@ struct ap_handle {
     unsigned int *d_counters = nullptr;
     double *d_out = nullptr;
     double *h_out = nullptr;  // pinned [4]
-    int bucket_lo[kWaBuckets + 1] = {0, 0, 0, 0, 0};
+    int bucket_lo[kWaBuckets + 1] = {};
     FieldSolver fs{};
     cudaStream_t stream = nullptr;
     bool own_stream = false;
@@ -555,10 +555,12 @@ int ap_create(const ap_netlist *nl, const ap_params *params, ap_handle **out) {
         }
     for (int i = 0; i < N; ++i)
         if (h->ext2int[(size_t)i] != i) h->identity = false;
-    // nets of degree >= 2 in degree buckets [2], [3,4], [5,8], [9,...); within a
-    // bucket by their lowest internal node index, so neighbouring threads
-    // gather and accumulate neighbouring nodes
-    auto bucket_of = [](int d) { return d <= 2 ? 0 : (d <= 4 ? 1 : (d <= 8 ? 2 : 3)); };
+    // nets of degree >= 2 in degree buckets [2], [3,4], [5,8], [9,16], [17,32],
+    // [33,64], [65,...); within a bucket by their lowest internal node index, so
+    // neighbouring threads gather and accumulate neighbouring nodes
+    auto bucket_of = [](int d) {
+        return d <= 2 ? 0 : d <= 4 ? 1 : d <= 8 ? 2 : d <= 16 ? 3 : d <= 32 ? 4 : d <= 64 ? 5 : 6;
+    };
     std::vector<int> order, first((size_t)nl->num_nets, 0);
     for (int e = 0; e < nl->num_nets; ++e) {
         if (nl->net_ptr[e + 1] - nl->net_ptr[e] < 2) continue;

@@ -15,6 +15,8 @@
 // which keeps FP32 exact where the reference form cancels (x_i/g ~ 1e4).
 // Each pin's gradient is rounded to 2^-20 and accumulated per node in int64,
 // so the sum over a node's nets is the same whatever order the atomics land in.
+#include <algorithm>
+
 #include "ap_common.cuh"
 #include "ap_kernels.h"
 
@@ -26,50 +28,132 @@ struct AxisTerms {
     float inv_bp, inv_bm, wp, wm;  // 1/b+, 1/b-, shifted WA+ - x_max, WA- - x_min
 };
 
-// Warp sums of 8 values at once (transposed butterfly): halving exchanges at
-// offsets 16, 8, 4 leave lane L with a partial of quantity (L >> 2) & 7,
-// offsets 2, 1 finish it, and 8 broadcasts hand every lane every total --
-// 17 shuffles instead of 40.  Fixed order, so the same on every run.
-__device__ __forceinline__ void warp_sum8(float v[8]) {
-    const int lane = threadIdx.x & 31;
-    const bool a = lane & 16, b = lane & 8, c = lane & 4;
+// Sums of 8 values at once over an aligned group of G lanes (transposed
+// butterfly): halving exchanges at offsets G/2, G/4, G/8 leave lane-in-group
+// l with a partial of quantity (l / (G/8)) & 7, the remaining offsets finish
+// it, and 8 broadcasts hand every lane of the group every total -- 3 + log2(G/8)
+// + 8 shuffles instead of 8 log2(G).  Fixed order, so the same on every run.
+// `mask`: the group's lanes; `base`: its first lane.
+template <int G>
+__device__ __forceinline__ void group_sum8(float v[8], int l, unsigned mask, int base) {
+    static_assert(G >= 8 && G <= 32, "group of 8..32 lanes");
+    const bool a = l & (G / 2), b = l & (G / 4), c = l & (G / 8);
     float u[4];
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
         const float send = a ? v[k] : v[k + 4];
-        u[k] = (a ? v[k + 4] : v[k]) + __shfl_xor_sync(0xffffffffu, send, 16);
+        u[k] = (a ? v[k + 4] : v[k]) + __shfl_xor_sync(mask, send, G / 2);
     }
     float t[2];
 #pragma unroll
     for (int k = 0; k < 2; ++k) {
         const float send = b ? u[k] : u[k + 2];
-        t[k] = (b ? u[k + 2] : u[k]) + __shfl_xor_sync(0xffffffffu, send, 8);
+        t[k] = (b ? u[k + 2] : u[k]) + __shfl_xor_sync(mask, send, G / 4);
     }
-    float s = (c ? t[1] : t[0]) + __shfl_xor_sync(0xffffffffu, c ? t[0] : t[1], 4);
-    s += __shfl_xor_sync(0xffffffffu, s, 2);
-    s += __shfl_xor_sync(0xffffffffu, s, 1);
-    // lane L holds quantity q = 4 a + 2 b + c = (L >> 2) & 7
+    float sum = (c ? t[1] : t[0]) + __shfl_xor_sync(mask, c ? t[0] : t[1], G / 8);
 #pragma unroll
-    for (int q = 0; q < 8; ++q) v[q] = __shfl_sync(0xffffffffu, s, 4 * q);
+    for (int o = G / 16; o > 0; o >>= 1) sum += __shfl_xor_sync(mask, sum, o);
+#pragma unroll
+    for (int q = 0; q < 8; ++q) v[q] = __shfl_sync(mask, sum, base + q * (G / 8));
 }
 
-// Warp maxima of 4 values at once, the same scheme: 10 shuffles instead of 20.
-__device__ __forceinline__ void warp_max4(float v[4]) {
-    const int lane = threadIdx.x & 31;
-    const bool a = lane & 16, b = lane & 8;
+// Maxima of 4 values at once over an aligned group of G lanes, the same scheme.
+template <int G>
+__device__ __forceinline__ void group_max4(float v[4], int l, unsigned mask, int base) {
+    const bool a = l & (G / 2), b = l & (G / 4);
     float u[2];
 #pragma unroll
     for (int k = 0; k < 2; ++k) {
         const float send = a ? v[k] : v[k + 2];
-        u[k] = fmaxf(a ? v[k + 2] : v[k], __shfl_xor_sync(0xffffffffu, send, 16));
+        u[k] = fmaxf(a ? v[k + 2] : v[k], __shfl_xor_sync(mask, send, G / 2));
     }
-    float s = fmaxf(b ? u[1] : u[0], __shfl_xor_sync(0xffffffffu, b ? u[0] : u[1], 8));
-    s = fmaxf(s, __shfl_xor_sync(0xffffffffu, s, 4));
-    s = fmaxf(s, __shfl_xor_sync(0xffffffffu, s, 2));
-    s = fmaxf(s, __shfl_xor_sync(0xffffffffu, s, 1));
-    // lane L holds quantity q = 2 a + b = (L >> 3) & 3
+    float m = fmaxf(b ? u[1] : u[0], __shfl_xor_sync(mask, b ? u[0] : u[1], G / 4));
 #pragma unroll
-    for (int q = 0; q < 4; ++q) v[q] = __shfl_sync(0xffffffffu, s, 8 * q);
+    for (int o = G / 8; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(mask, m, o));
+#pragma unroll
+    for (int q = 0; q < 4; ++q) v[q] = __shfl_sync(mask, m, base + q * (G / 4));
+}
+
+// One net of degree d <= G P by an aligned group of G lanes, P pins per lane
+// in registers (pin j on lane j mod G): one load pass, each exponential once.
+template <int G, int P>
+__device__ __forceinline__ void net_group(const WaArgs &a, int s, int d, int l, unsigned mask, int base,
+                                          const float *px, const float *py, float inv_g, float &hpf, float &waf) {
+    bool v[P];
+    int nd[P];
+    float c[P][2];
+#pragma unroll
+    for (int p = 0; p < P; ++p) {
+        const int j = l + p * G;
+        v[p] = j < d;
+        nd[p] = v[p] ? __ldg(a.pin_node + s + j) : 0;
+        c[p][0] = v[p] ? __ldg(px + nd[p]) : 0.f;
+        c[p][1] = v[p] ? __ldg(py + nd[p]) : 0.f;
+    }
+    float m4[4] = {-3.0e38f, -3.0e38f, -3.0e38f, -3.0e38f};  // max x, max y, -min x, -min y
+#pragma unroll
+    for (int p = 0; p < P; ++p)
+        if (v[p]) {
+            m4[0] = fmaxf(m4[0], c[p][0]);
+            m4[1] = fmaxf(m4[1], c[p][1]);
+            m4[2] = fmaxf(m4[2], -c[p][0]);
+            m4[3] = fmaxf(m4[3], -c[p][1]);
+        }
+    group_max4<G>(m4, l, mask, base);
+    const float mx[2] = {m4[0], m4[1]}, mn[2] = {-m4[2], -m4[3]};
+    float ep[P][2], em[P][2], s8[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) s8[k] = 0.f;
+#pragma unroll
+    for (int ax = 0; ax < 2; ++ax)
+#pragma unroll
+        for (int p = 0; p < P; ++p) {
+            const float dp = c[p][ax] - mx[ax], dm = c[p][ax] - mn[ax];
+            ep[p][ax] = v[p] ? __expf(dp * inv_g) : 0.f;
+            em[p][ax] = v[p] ? __expf(-dm * inv_g) : 0.f;
+            s8[4 * ax + 0] += ep[p][ax];
+            s8[4 * ax + 1] += em[p][ax];
+            s8[4 * ax + 2] += ep[p][ax] * dp;
+            s8[4 * ax + 3] += em[p][ax] * dm;
+        }
+    group_sum8<G>(s8, l, mask, base);
+    float g[P][2], wa_net = 0.f;
+#pragma unroll
+    for (int ax = 0; ax < 2; ++ax) {
+        const float ibp = 1.f / s8[4 * ax + 0], ibm = 1.f / s8[4 * ax + 1];
+        const float wp = s8[4 * ax + 2] * ibp, wm = s8[4 * ax + 3] * ibm;
+#pragma unroll
+        for (int p = 0; p < P; ++p) {
+            const float dp = c[p][ax] - mx[ax], dm = c[p][ax] - mn[ax];
+            g[p][ax] = ep[p][ax] * ibp * (1.f + (dp - wp) * inv_g) - em[p][ax] * ibm * (1.f - (dm - wm) * inv_g);
+        }
+        wa_net += (mx[ax] - mn[ax]) + wp - wm;
+    }
+#pragma unroll
+    for (int p = 0; p < P; ++p)
+        if (v[p] && nd[p] < a.n_grad) {
+            atomicAdd(a.gqx + nd[p], grad_q(g[p][0]));
+            atomicAdd(a.gqy + nd[p], grad_q(g[p][1]));
+        }
+    if (l == 0) {
+        hpf += (mx[0] - mn[0]) + (mx[1] - mn[1]);
+        waf += wa_net;
+    }
+}
+
+// Nets of sub-bucket [lo, hi) by groups of G lanes; the launch's blocks
+// [b0, b0 + nb) serve this sub-bucket.
+template <int G, int P>
+__device__ __forceinline__ void net_groups(const WaArgs &a, int lo, int hi, int b0, int nb, const float *px,
+                                           const float *py, float inv_g, float &hpf, float &waf) {
+    constexpr int per_block = kThreads / G;
+    const int lane = threadIdx.x & 31, l = lane & (G - 1), base = lane - l;
+    const unsigned mask = G == 32 ? 0xffffffffu : (((1u << G) - 1u) << base);
+    const int group = ((int)blockIdx.x - b0) * per_block + (int)threadIdx.x / G, n_groups = nb * per_block;
+    for (int e = lo + group; e < hi; e += n_groups) {
+        const int s = __ldg(a.net_ptr + e), d = __ldg(a.net_ptr + e + 1) - s;
+        net_group<G, P>(a, s, d, l, mask, base, px, py, inv_g, hpf, waf);
+    }
 }
 
 // One net with d <= D pins held in registers by one thread.
@@ -152,10 +236,13 @@ __global__ void __launch_bounds__(kThreads) wa_small_kernel(WaArgs a) {
     // per-thread partials in FP32 (a thread owns a few nets), FP64 from the
     // block sum on: the FP64 pipe of this part is narrow
     float hpf = 0.f, waf = 0.f;
-    const int hi = a.bucket_lo[B + 1];
-    for (int e = a.bucket_lo[B] + blockIdx.x * blockDim.x + threadIdx.x; e < hi; e += gridDim.x * blockDim.x) {
-        const int s = __ldg(a.net_ptr + e);
-        const int d = __ldg(a.net_ptr + e + 1) - s;
+    const int lo = a.bucket_lo[B], hi = a.bucket_lo[B + 1];
+    // every net of the 2-pin bucket has degree 2: its pins sit at a computed
+    // offset, one dependent load fewer per net
+    const int s0 = D == 2 && lo < hi ? __ldg(a.net_ptr + lo) : 0;
+    for (int e = lo + blockIdx.x * blockDim.x + threadIdx.x; e < hi; e += gridDim.x * blockDim.x) {
+        const int s = D == 2 ? s0 + 2 * (e - lo) : __ldg(a.net_ptr + e);
+        const int d = D == 2 ? 2 : __ldg(a.net_ptr + e + 1) - s;
         net_thread<D>(a.pin_node + s, d, px, py, inv_g, a.gqx, a.gqy, a.n_grad, hpf, waf);
     }
     // per-block partials in FP32 (folded with compensation by the last block
@@ -172,7 +259,70 @@ __global__ void __launch_bounds__(kThreads) wa_small_kernel(WaArgs a) {
     }
 }
 
-// Nets [n_small, n_nets): one warp per net, any degree.
+// General path of one net of any degree by a warp: three passes over the pins
+// (extrema; sums; gradients), pins lane, lane + 32, ...
+__device__ __forceinline__ void net_warp_loop(const WaArgs &a, int s, int d, const float *px, const float *py,
+                                              float inv_g, float &hpf, float &waf) {
+    const int lane = threadIdx.x & 31;
+    float m4[4] = {-3.0e38f, -3.0e38f, -3.0e38f, -3.0e38f};  // max x, max y, -min x, -min y
+    for (int j = lane; j < d; j += 32) {
+        const int n = __ldg(a.pin_node + s + j);
+        const float x = __ldg(px + n), y = __ldg(py + n);
+        m4[0] = fmaxf(m4[0], x);
+        m4[1] = fmaxf(m4[1], y);
+        m4[2] = fmaxf(m4[2], -x);
+        m4[3] = fmaxf(m4[3], -y);
+    }
+    group_max4<32>(m4, lane, 0xffffffffu, 0);
+    const float xmx = m4[0], ymx = m4[1], xmn = -m4[2], ymn = -m4[3];
+    float s8[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};  // bp bm cp cm for x then y
+    for (int j = lane; j < d; j += 32) {
+        const int n = __ldg(a.pin_node + s + j);
+        const float c2[2] = {__ldg(px + n), __ldg(py + n)};
+#pragma unroll
+        for (int ax = 0; ax < 2; ++ax) {
+            const float dp = c2[ax] - (ax ? ymx : xmx), dm = c2[ax] - (ax ? ymn : xmn);
+            const float ep = __expf(dp * inv_g), em = __expf(-dm * inv_g);
+            s8[4 * ax + 0] += ep;
+            s8[4 * ax + 1] += em;
+            s8[4 * ax + 2] += ep * dp;
+            s8[4 * ax + 3] += em * dm;
+        }
+    }
+    group_sum8<32>(s8, lane, 0xffffffffu, 0);
+    AxisTerms t[2];
+#pragma unroll
+    for (int ax = 0; ax < 2; ++ax) {
+        t[ax].inv_bp = 1.f / s8[4 * ax + 0];
+        t[ax].inv_bm = 1.f / s8[4 * ax + 1];
+        t[ax].wp = s8[4 * ax + 2] * t[ax].inv_bp;
+        t[ax].wm = s8[4 * ax + 3] * t[ax].inv_bm;
+    }
+    for (int j = lane; j < d; j += 32) {
+        const int n = __ldg(a.pin_node + s + j);
+        if (n >= a.n_grad) continue;
+        const float c2[2] = {__ldg(px + n), __ldg(py + n)};
+        float g[2];
+#pragma unroll
+        for (int ax = 0; ax < 2; ++ax) {
+            const float dp = c2[ax] - (ax ? ymx : xmx), dm = c2[ax] - (ax ? ymn : xmn);
+            const float ep = __expf(dp * inv_g), em = __expf(-dm * inv_g);
+            g[ax] = ep * t[ax].inv_bp * (1.f + (dp - t[ax].wp) * inv_g) -
+                    em * t[ax].inv_bm * (1.f - (dm - t[ax].wm) * inv_g);
+        }
+        atomicAdd(a.gqx + n, grad_q(g[0]));
+        atomicAdd(a.gqy + n, grad_q(g[1]));
+    }
+    if (lane == 0) {
+        hpf += (xmx - xmn) + (ymx - ymn);
+        waf += ((xmx - xmn) + t[0].wp - t[0].wm) + ((ymx - ymn) + t[1].wp - t[1].wm);
+    }
+}
+
+// Nets of degree > 8 (buckets 3..6): blocks [0, b3) take degrees 9..16 with
+// 16 lanes per net, then 17..32 with a warp (one pin per lane), 33..64 with a
+// warp (two pins per lane), and above 64 with a warp looping over the pins --
+// the lane group fits the net, so few lanes idle.
 __global__ void __launch_bounds__(kThreads) wa_large_kernel(WaArgs a) {
     __shared__ double red[32];
     const float gamma = a.gamma > 0.f ? a.gamma : a.sc->f_gamma;
@@ -183,137 +333,23 @@ __global__ void __launch_bounds__(kThreads) wa_large_kernel(WaArgs a) {
         px = a.pxs[t];
         py = a.pys[t];
     }
-    const int lane = threadIdx.x & 31;
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int nwarps = (gridDim.x * blockDim.x) >> 5;
     // per-thread partials in FP32 (a thread owns a few nets), FP64 from the
     // block sum on: the FP64 pipe of this part is narrow
     float hpf = 0.f, waf = 0.f;
-    for (int e = a.bucket_lo[3] + warp; e < a.bucket_lo[4]; e += nwarps) {
-        const int s = __ldg(a.net_ptr + e), d = __ldg(a.net_ptr + e + 1) - s;
-        if (d <= 64) {
-            // pins lane and lane + 32 held in registers: one load pass, each
-            // exponential evaluated once
-            const bool v0 = lane < d, v1 = lane + 32 < d;
-            const int n0 = v0 ? __ldg(a.pin_node + s + lane) : 0;
-            const int n1 = v1 ? __ldg(a.pin_node + s + lane + 32) : 0;
-            const float c0[2] = {v0 ? __ldg(px + n0) : 0.f, v0 ? __ldg(py + n0) : 0.f};
-            const float c1[2] = {v1 ? __ldg(px + n1) : 0.f, v1 ? __ldg(py + n1) : 0.f};
-            float mx[2], mn[2];
-            {
-                float m4[4];
-#pragma unroll
-                for (int ax = 0; ax < 2; ++ax) {
-                    m4[ax] = fmaxf(v0 ? c0[ax] : -3.0e38f, v1 ? c1[ax] : -3.0e38f);
-                    m4[2 + ax] = fmaxf(v0 ? -c0[ax] : -3.0e38f, v1 ? -c1[ax] : -3.0e38f);
-                }
-                warp_max4(m4);
-#pragma unroll
-                for (int ax = 0; ax < 2; ++ax) {
-                    mx[ax] = m4[ax];
-                    mn[ax] = -m4[2 + ax];
-                }
-            }
-            float ep0[2], em0[2], ep1[2], em1[2], dp0[2], dm0[2], dp1[2], dm1[2], s8[8], gsum[2][2];
-#pragma unroll
-            for (int ax = 0; ax < 2; ++ax) {
-                dp0[ax] = c0[ax] - mx[ax];
-                dm0[ax] = c0[ax] - mn[ax];
-                dp1[ax] = c1[ax] - mx[ax];
-                dm1[ax] = c1[ax] - mn[ax];
-                ep0[ax] = v0 ? __expf(dp0[ax] * inv_g) : 0.f;
-                em0[ax] = v0 ? __expf(-dm0[ax] * inv_g) : 0.f;
-                ep1[ax] = v1 ? __expf(dp1[ax] * inv_g) : 0.f;
-                em1[ax] = v1 ? __expf(-dm1[ax] * inv_g) : 0.f;
-                s8[4 * ax + 0] = ep0[ax] + ep1[ax];
-                s8[4 * ax + 1] = em0[ax] + em1[ax];
-                s8[4 * ax + 2] = ep0[ax] * dp0[ax] + ep1[ax] * dp1[ax];
-                s8[4 * ax + 3] = em0[ax] * dm0[ax] + em1[ax] * dm1[ax];
-            }
-            warp_sum8(s8);
-            float wa_net = 0.f;
-#pragma unroll
-            for (int ax = 0; ax < 2; ++ax) {
-                const float ibp = 1.f / s8[4 * ax + 0], ibm = 1.f / s8[4 * ax + 1];
-                const float wp = s8[4 * ax + 2] * ibp, wm = s8[4 * ax + 3] * ibm;
-                gsum[ax][0] = ep0[ax] * ibp * (1.f + (dp0[ax] - wp) * inv_g) -
-                              em0[ax] * ibm * (1.f - (dm0[ax] - wm) * inv_g);
-                gsum[ax][1] = ep1[ax] * ibp * (1.f + (dp1[ax] - wp) * inv_g) -
-                              em1[ax] * ibm * (1.f - (dm1[ax] - wm) * inv_g);
-                wa_net += (mx[ax] - mn[ax]) + wp - wm;
-            }
-            if (v0 && n0 < a.n_grad) {
-                atomicAdd(a.gqx + n0, grad_q(gsum[0][0]));
-                atomicAdd(a.gqy + n0, grad_q(gsum[1][0]));
-            }
-            if (v1 && n1 < a.n_grad) {
-                atomicAdd(a.gqx + n1, grad_q(gsum[0][1]));
-                atomicAdd(a.gqy + n1, grad_q(gsum[1][1]));
-            }
-            if (lane == 0) {
-                hpf += (mx[0] - mn[0]) + (mx[1] - mn[1]);
-                waf += wa_net;
-            }
-            continue;
-        }
-        float xmx = -3.0e38f, xmn = 3.0e38f, ymx = -3.0e38f, ymn = 3.0e38f;
-        for (int j = lane; j < d; j += 32) {
-            const int n = __ldg(a.pin_node + s + j);
-            const float x = __ldg(px + n), y = __ldg(py + n);
-            xmx = fmaxf(xmx, x);
-            xmn = fminf(xmn, x);
-            ymx = fmaxf(ymx, y);
-            ymn = fminf(ymn, y);
-        }
-        {
-            float m4[4] = {xmx, ymx, -xmn, -ymn};
-            warp_max4(m4);
-            xmx = m4[0];
-            ymx = m4[1];
-            xmn = -m4[2];
-            ymn = -m4[3];
-        }
-        float s8[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};  // bp bm cp cm for x then y
-        for (int j = lane; j < d; j += 32) {
-            const int n = __ldg(a.pin_node + s + j);
-            const float c2[2] = {__ldg(px + n), __ldg(py + n)};
-#pragma unroll
-            for (int ax = 0; ax < 2; ++ax) {
-                const float dp = c2[ax] - (ax ? ymx : xmx), dm = c2[ax] - (ax ? ymn : xmn);
-                const float ep = __expf(dp * inv_g), em = __expf(-dm * inv_g);
-                s8[4 * ax + 0] += ep;
-                s8[4 * ax + 1] += em;
-                s8[4 * ax + 2] += ep * dp;
-                s8[4 * ax + 3] += em * dm;
-            }
-        }
-        warp_sum8(s8);
-        AxisTerms t[2];
-#pragma unroll
-        for (int ax = 0; ax < 2; ++ax) {
-            t[ax].inv_bp = 1.f / s8[4 * ax + 0];
-            t[ax].inv_bm = 1.f / s8[4 * ax + 1];
-            t[ax].wp = s8[4 * ax + 2] * t[ax].inv_bp;
-            t[ax].wm = s8[4 * ax + 3] * t[ax].inv_bm;
-        }
-        for (int j = lane; j < d; j += 32) {
-            const int n = __ldg(a.pin_node + s + j);
-            if (n >= a.n_grad) continue;
-            const float c2[2] = {__ldg(px + n), __ldg(py + n)};
-            float g[2];
-#pragma unroll
-            for (int ax = 0; ax < 2; ++ax) {
-                const float dp = c2[ax] - (ax ? ymx : xmx), dm = c2[ax] - (ax ? ymn : xmn);
-                const float ep = __expf(dp * inv_g), em = __expf(-dm * inv_g);
-                g[ax] = ep * t[ax].inv_bp * (1.f + (dp - t[ax].wp) * inv_g) -
-                        em * t[ax].inv_bm * (1.f - (dm - t[ax].wm) * inv_g);
-            }
-            atomicAdd(a.gqx + n, grad_q(g[0]));
-            atomicAdd(a.gqy + n, grad_q(g[1]));
-        }
-        if (lane == 0) {
-            hpf += (xmx - xmn) + (ymx - ymn);
-            waf += ((xmx - xmn) + t[0].wp - t[0].wm) + ((ymx - ymn) + t[1].wp - t[1].wm);
+    int b0 = 0;
+    const int bid = blockIdx.x;
+    if (bid < b0 + a.bucket_blocks[3]) {
+        net_groups<16, 1>(a, a.bucket_lo[3], a.bucket_lo[4], b0, a.bucket_blocks[3], px, py, inv_g, hpf, waf);
+    } else if (bid < (b0 += a.bucket_blocks[3]) + a.bucket_blocks[4]) {
+        net_groups<32, 1>(a, a.bucket_lo[4], a.bucket_lo[5], b0, a.bucket_blocks[4], px, py, inv_g, hpf, waf);
+    } else if (bid < (b0 += a.bucket_blocks[4]) + a.bucket_blocks[5]) {
+        net_groups<32, 2>(a, a.bucket_lo[5], a.bucket_lo[6], b0, a.bucket_blocks[5], px, py, inv_g, hpf, waf);
+    } else {
+        b0 += a.bucket_blocks[5];
+        const int warp = ((bid - b0) * kThreads + (int)threadIdx.x) >> 5, nwarps = (a.bucket_blocks[6] * kThreads) >> 5;
+        for (int e = a.bucket_lo[6] + warp; e < a.bucket_lo[7]; e += nwarps) {
+            const int s = __ldg(a.net_ptr + e), d = __ldg(a.net_ptr + e + 1) - s;
+            net_warp_loop(a, s, d, px, py, inv_g, hpf, waf);
         }
     }
     const float hp = block_sum_ff(hpf, reinterpret_cast<float *>(red));
@@ -354,12 +390,18 @@ void launch_wirelength(const WaArgs &a0, cudaStream_t st) {
         return b < 1 ? 1 : (b > kWaMaxBlocks ? kWaMaxBlocks : b);
     };
     for (int b = 0; b < 3; ++b) a.bucket_blocks[b] = grid(a.bucket_lo[b + 1] - a.bucket_lo[b]);
-    a.bucket_blocks[3] = grid((a.bucket_lo[4] - a.bucket_lo[3]) * 32);
+    // large-net sub-buckets: lanes per net 16, 32, 32, 32; <= kWaMaxBlocks in all
+    const int lanes[4] = {16, 32, 32, 32};
+    int large = 0;
+    for (int b = 3; b < kWaBuckets; ++b) {
+        a.bucket_blocks[b] = std::min(grid((a.bucket_lo[b + 1] - a.bucket_lo[b]) * lanes[b - 3]), kWaMaxBlocks / 4);
+        large += a.bucket_blocks[b];
+    }
     a.small_blocks = a.bucket_blocks[0] + a.bucket_blocks[1] + a.bucket_blocks[2];
     wa_small_kernel<2, 0><<<a.bucket_blocks[0], kThreads, 0, st>>>(a);
     wa_small_kernel<4, 1><<<a.bucket_blocks[1], kThreads, 0, st>>>(a);
     wa_small_kernel<8, 2><<<a.bucket_blocks[2], kThreads, 0, st>>>(a);
-    wa_large_kernel<<<a.bucket_blocks[3], kThreads, 0, st>>>(a);
+    wa_large_kernel<<<large, kThreads, 0, st>>>(a);
 }
 
 }  // namespace ap

@@ -119,6 +119,31 @@ def test_wirelength_gradient(ap, oracle_lib, preset, gamma):
     assert abs(wa - rwa) <= 1e-5 * rwa
 
 
+def test_wirelength_gradient_every_degree_bucket(ap, oracle_lib):
+    """Nets of degree 2..8 (thread per net), 9..16 (16 lanes), 17..32 and
+    33..64 (a warp, pins in registers) and 65..300 (a warp looping): the
+    synthetic netlists have none above 64, so these are added here."""
+    nl = dict(ap.synth.generate("c0", seed=2))
+    rng = np.random.default_rng(8)
+    n = len(nl["node_w"])
+    ptr = list(nl["net_ptr"])
+    pins = list(nl["pin_node"])
+    for d in (9, 12, 16, 17, 24, 32, 33, 48, 64, 65, 100, 200, 300):
+        pins += list(rng.choice(n, size=min(d, n), replace=False))
+        ptr.append(len(pins))
+    nl["net_ptr"] = np.array(ptr, np.int32)
+    nl["pin_node"] = np.array(pins, np.int32)
+    x, y = spread_positions(nl, rng, margin=0.0)
+    with ap.Placer(nl, bins=32) as pl:
+        gx, gy, wa, hp = pl.compute_all_partials(x, y, 2.0)
+    rx, ry, rwa, rhp = oracle_lib.wa_grad(nl["net_ptr"], nl["pin_node"], x, y, 2.0)
+    scale = max(np.abs(rx).max(), np.abs(ry).max())
+    assert np.abs(gx - rx).max() <= 1e-4 * scale
+    assert np.abs(gy - ry).max() <= 1e-4 * scale
+    assert abs(hp - rhp) <= 1e-6 * rhp
+    assert abs(wa - rwa) <= 1e-5 * rwa
+
+
 @pytest.mark.parametrize("m", [32, 128, 512])
 def test_field_fp32_against_oracle(ap, oracle_lib, m):
     rng = np.random.default_rng(m)
