@@ -146,8 +146,8 @@ struct FieldSolver {
     int tc_ready;
     unsigned int *tc_status; // device error flag of the tcgen05 kernels
     // tile autotuner results
-    int tc_variant;          // 0: 128 x 64 tiles, 1: 128 x 128 tiles
-    float tc_tune_ms[2];     // measured solve time of each variant
+    int tc_variant;          // 0: 128 x 64 tiles, 1: 128 x 128, 2: 128 x 64 with 2 stages (2 CTAs per SM)
+    float tc_tune_ms[3];     // measured solve time of each variant
     int simt_bm;             // FP32 path tile (32 or 64); 0 = size rule
     float simt_tune_ms[2];   // measured solve time with 32 / 64 tiles
 };

@@ -794,13 +794,11 @@ int ap_step(ap_handle *h, int32_t n_iter) {
     return sync(h);
 }
 
-int ap_solver_info(ap_handle *h, int32_t *tc_tile_n, float *tc_ms, int32_t *simt_tile, float *simt_ms) {
+int ap_solver_info(ap_handle *h, int32_t *tc_variant, float *tc_ms, int32_t *simt_tile, float *simt_ms) {
     if (!h) return AP_ERR_INVALID_ARG;
-    if (tc_tile_n) *tc_tile_n = h->fs.tc_ready ? (h->fs.tc_variant ? 128 : 64) : 0;
-    if (tc_ms) {
-        tc_ms[0] = h->fs.tc_tune_ms[0];
-        tc_ms[1] = h->fs.tc_tune_ms[1];
-    }
+    if (tc_variant) *tc_variant = h->fs.tc_ready ? h->fs.tc_variant : -1;
+    if (tc_ms)
+        for (int v = 0; v < 3; ++v) tc_ms[v] = h->fs.tc_tune_ms[v];
     if (simt_tile) *simt_tile = h->fs.simt_bm;
     if (simt_ms) {
         simt_ms[0] = h->fs.simt_tune_ms[0];

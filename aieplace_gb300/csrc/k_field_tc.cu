@@ -45,6 +45,8 @@ struct TileCfg {
 };
 using Tile64 = TileCfg<64, 4>;    // 48 KB stages
 using Tile128 = TileCfg<128, 3>;  // 64 KB stages
+using Tile64x2 = TileCfg<64, 2>;  // 2 stages, ~97 KB: two CTAs per SM
+constexpr int kTcVariants = 3;
 
 enum { EPI_SPLIT = 0, EPI_SPECTRAL = 1, EPI_F32 = 2 };
 
@@ -433,6 +435,8 @@ void run_variant(int v, FieldSolver &f, float *ex, float *ey, cudaStream_t st, c
     const TcState &s = *reinterpret_cast<const TcState *>(f.tc_maps);
     if (v == 1)
         run_stages<Tile128>(s.maps[1], f, ex, ey, st, gate, gate_mask);
+    else if (v == 2)
+        run_stages<Tile64x2>(s.maps[0], f, ex, ey, st, gate, gate_mask);
     else
         run_stages<Tile64>(s.maps[0], f, ex, ey, st, gate, gate_mask);
 }
@@ -440,8 +444,10 @@ void run_variant(int v, FieldSolver &f, float *ex, float *ey, cudaStream_t st, c
 }  // namespace tc
 
 // Builds the tensor maps of both tile shapes, then times one full solve of
-// each (3 warm, 5 timed, CUDA events) and keeps the faster: the tile
-// autotuner of the tensor-core path.  The scratch outputs are overwritten.
+// each variant (128 x 64 tiles with 4 pipeline stages, 128 x 128 with 3,
+// 128 x 64 with 2 so that two CTAs share an SM; 3 warm, 5 timed, CUDA
+// events) and keeps the fastest: the tile autotuner of the tensor-core path.
+// The scratch outputs are overwritten.
 int field_solver_bind_bf16(FieldSolver &f, const __nv_bfloat16 *d_hi, const __nv_bfloat16 *d_lo) {
     using namespace tc;
     if (f.m < BM || (f.m % BM) != 0 || !f.C_hi) return AP_ERR_UNSUPPORTED;
@@ -456,7 +462,9 @@ int field_solver_bind_bf16(FieldSolver &f, const __nv_bfloat16 *d_hi, const __nv
     if (cudaFuncSetAttribute(gemm_bf16x3_kernel<Tile64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              Tile64::SMEM_BYTES) != cudaSuccess ||
         cudaFuncSetAttribute(gemm_bf16x3_kernel<Tile128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             Tile128::SMEM_BYTES) != cudaSuccess)
+                             Tile128::SMEM_BYTES) != cudaSuccess ||
+        cudaFuncSetAttribute(gemm_bf16x3_kernel<Tile64x2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             Tile64x2::SMEM_BYTES) != cudaSuccess)
         return AP_ERR_CUDA;
     // the input map holds whatever the caller's buffer holds; timing does not depend on values
     if (cudaMemset((void *)d_hi, 0, sizeof(__nv_bfloat16) * (size_t)f.m * f.m) != cudaSuccess ||
@@ -466,7 +474,7 @@ int field_solver_bind_bf16(FieldSolver &f, const __nv_bfloat16 *d_hi, const __nv
     if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) return AP_ERR_CUDA;
     float best = 1e30f;
     f.tc_variant = 0;
-    for (int v = 0; v < 2; ++v) {
+    for (int v = 0; v < kTcVariants; ++v) {
         for (int w = 0; w < 3; ++w) run_variant(v, f, f.ux, f.uy, 0);
         cudaEventRecord(e0, 0);
         for (int t = 0; t < 5; ++t) run_variant(v, f, f.ux, f.uy, 0);

@@ -99,10 +99,10 @@ class Placer:
         return [float(v) for v in out[: n.value]]
 
     def solver_info(self) -> dict:
-        tn, st = C.c_int32(), C.c_int32()
-        tms, sms = np.zeros(2, np.float32), np.zeros(2, np.float32)
-        check("ap_solver_info", lib().ap_solver_info(self._h, C.byref(tn), ptr(tms), C.byref(st), ptr(sms)))
-        return {"tc_tile_n": tn.value, "tc_ms": [float(v) for v in tms], "simt_tile": st.value,
+        tv, st = C.c_int32(), C.c_int32()
+        tms, sms = np.zeros(3, np.float32), np.zeros(2, np.float32)
+        check("ap_solver_info", lib().ap_solver_info(self._h, C.byref(tv), ptr(tms), C.byref(st), ptr(sms)))
+        return {"tc_variant": tv.value, "tc_ms": [float(v) for v in tms], "simt_tile": st.value,
                 "simt_ms": [float(v) for v in sms]}
 
     def run(self) -> int:

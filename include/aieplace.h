@@ -151,10 +151,11 @@ int ap_step_async(ap_handle *h, int32_t n_trials);
 int ap_profile_stages(ap_handle *h, int32_t n_trials, float *stage_ms, int32_t *n_stages);
 
 /* Tile shapes the autotuner picked at ap_create for this bin count, and the
- * solve times it measured: tc_tile_n is the N side of the tensor-core tile
- * (64 or 128; 0 if the tensor-core path is unavailable), simt_tile the FP32
- * tile side (32 or 64); tc_ms[2] and simt_ms[2] the candidates' times. */
-int ap_solver_info(ap_handle *h, int32_t *tc_tile_n, float *tc_ms, int32_t *simt_tile, float *simt_ms);
+ * solve times it measured: tc_variant is the tensor-core candidate (0: 128 x 64
+ * tiles, 4 pipeline stages; 1: 128 x 128, 3 stages; 2: 128 x 64, 2 stages, two
+ * CTAs per SM; -1 if the tensor-core path is unavailable), simt_tile the FP32
+ * tile side (32 or 64); tc_ms[3] and simt_ms[2] the candidates' times. */
+int ap_solver_info(ap_handle *h, int32_t *tc_variant, float *tc_ms, int32_t *simt_tile, float *simt_ms);
 
 /* Iterates until overflow < params.target_overflow or max_iterations;
  * replaces Placer::run (AIEplace.cpp:44-76). */
