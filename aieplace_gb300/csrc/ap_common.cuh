@@ -159,9 +159,27 @@ __device__ __forceinline__ float i64_to_float(long long q) {
 
 // per-pin WA contribution in the int64 accumulators' fixed point: g 2^20
 // rounded to nearest by the magic-number FMA (|g 2^20| < 2^22)
-__device__ __forceinline__ ull grad_q(float g) {
+__device__ __forceinline__ int grad_q32(float g) {
     const float c = fminf(fmaxf(g, -kGradClamp), kGradClamp);
-    return (ull)(long long)(__float_as_int(fmaf(c, kGradScale, 12582912.0f)) - 0x4B400000);
+    return __float_as_int(fmaf(c, kGradScale, 12582912.0f)) - 0x4B400000;
+}
+__device__ __forceinline__ ull grad_q(float g) { return (ull)(long long)grad_q32(g); }
+
+// Both axes of a node's WA gradient in one int64 accumulator, y 2^32 + x: the
+// int64 sum is exact and order independent, and its halves decode exactly
+// while |sum x| and |sum y| stay below 2^31 -- at most kPackMaxPins pins of
+// |q| <= 3.99 2^20.  Nodes with more pins (flagged by the top bit of their
+// pin_node entries) use one accumulator per axis.
+constexpr int kPackMaxPins = 512;
+constexpr int kPinHeavy = (int)0x80000000u;
+constexpr int kPinNode = 0x7fffffff;
+__device__ __forceinline__ ull pack_q(int qx, int qy) {
+    return (ull)((long long)qy * 4294967296ll + (long long)qx);
+}
+__device__ __forceinline__ void unpack_q(ull p, long long &sx, long long &sy) {
+    const int lo = (int)(unsigned)p;
+    sx = lo;
+    sy = ((long long)p - (long long)lo) >> 32;
 }
 
 // The bins a node touches under the reference rules (Grid.cpp:38-110,

@@ -19,7 +19,7 @@ constexpr int kWaBuckets = 7;
 
 struct WaArgs {
     const int *net_ptr;    // [n_nets + 1], nets in bucket order
-    const int *pin_node;   // internal node ids
+    const int *pin_node;   // internal node ids (| kPinHeavy: node of more than kPackMaxPins pins)
     int n_small, n_nets;
     int bucket_lo[kWaBuckets + 1];
     int bucket_blocks[kWaBuckets];  // grid of each bucket's launch (filled by the launcher)
@@ -27,7 +27,8 @@ struct WaArgs {
     const float *pxs[2], *pys[2];  // WA_LOOP: the trial point is buffer [1 - sc->cur]
     float gamma;           // > 0 overrides sc->gamma
     DevScalars *sc;
-    ull *gqx, *gqy;        // int64 fixed-point gradient accumulators
+    ull *gq;               // int64 fixed-point gradient accumulators, both axes packed (pack_q)
+    ull *gqx, *gqy;        // the same, one per axis, for nodes of more than kPackMaxPins pins
     int n_grad;            // nodes [0, n_grad) receive gradient
     double *partials;      // 2 per block over all bucket launches
     unsigned int *counter;
@@ -106,7 +107,8 @@ struct GatherArgs {
     float *vx[2], *vy[2];   // evaluation point [at], comparison point [1 - at]
     const float *w, *h;
     const float *ex, *ey;   // field per bin
-    ull *gqx, *gqy;         // WA gradient accumulators (cleared after reading)
+    ull *gq;                // WA gradient accumulators, packed (cleared after reading)
+    ull *gqx, *gqy;         // per-axis accumulators of nodes of more than kPackMaxPins pins
     const float *pins;      // pin count per movable node
     const float *charge;    // area / bin area
     float *gx[2], *gy[2];   // preconditioned gradient: output [at], comparison [1 - at]

@@ -54,7 +54,8 @@ struct ap_handle {
     float *d_pins = nullptr, *d_charge = nullptr;
     int *d_rec_bin = nullptr;  // per movable node: bin record of the trial point
     int4 *d_rec_ov = nullptr;
-    ull *d_gqx = nullptr, *d_gqy = nullptr;
+    ull *d_gq = nullptr;                     // packed WA gradient accumulators (pack_q)
+    ull *d_gqx = nullptr, *d_gqy = nullptr;  // per axis, nodes of more than kPackMaxPins pins
     ull *d_mov_q = nullptr;
     long long *d_fix_q = nullptr, *d_fixs_q = nullptr;
     float *d_dens = nullptr, *d_ex = nullptr, *d_ey = nullptr;
@@ -159,6 +160,7 @@ WaArgs wa_args(ap_handle *h, const float *px, const float *py, float gamma, int 
     }
     a.gamma = gamma;
     a.sc = h->d_sc;
+    a.gq = h->d_gq;
     a.gqx = h->d_gqx;
     a.gqy = h->d_gqy;
     a.n_grad = n_grad;
@@ -184,6 +186,7 @@ GatherArgs gather_args(ap_handle *h, int at, int mode) {
     a.h = h->d_h;
     a.ex = h->d_ex;
     a.ey = h->d_ey;
+    a.gq = h->d_gq;
     a.gqx = h->d_gqx;
     a.gqy = h->d_gqy;
     a.pins = h->d_pins;
@@ -399,6 +402,7 @@ int init_optimizer(ap_handle *h) {
     sc.surr_tau_min = h->policy.overflow_min;
     sc.surr_err_bound = h->policy.max_error;
     CK(cudaMemcpyAsync(h->d_sc, &sc, sizeof(sc), cudaMemcpyHostToDevice, st));
+    CK(cudaMemsetAsync(h->d_gq, 0, sizeof(ull) * h->n_nodes, st));
     CK(cudaMemsetAsync(h->d_gqx, 0, sizeof(ull) * h->n_nodes, st));
     CK(cudaMemsetAsync(h->d_gqy, 0, sizeof(ull) * h->n_nodes, st));
     CK(cudaMemsetAsync(h->d_mov_q, 0, sizeof(ull) * (size_t)h->p.bins_x * h->p.bins_y, st));
@@ -589,6 +593,9 @@ int ap_create(const ap_netlist *nl, const ap_params *params, ap_handle **out) {
     }
     h->n_nets = (int)order.size();
     h->n_pins = (int)pin_node.size();
+    // pins of nodes past the packed accumulators' range carry the heavy flag
+    for (int &q : pin_node)
+        if (pins[(size_t)q] > (float)kPackMaxPins) q |= kPinHeavy;
     // node arrays in internal order
     std::vector<float> w((size_t)N), hh((size_t)N), x((size_t)N), y((size_t)N), charge((size_t)N);
     for (int i = 0; i < N; ++i) {
@@ -639,6 +646,7 @@ int ap_create(const ap_netlist *nl, const ap_params *params, ap_handle **out) {
     A(dalloc(&h->d_charge, N));
     A(dalloc(&h->d_rec_bin, std::max(1, h->n_mov)));
     A(dalloc(&h->d_rec_ov, std::max(1, h->n_mov)));
+    A(dalloc(&h->d_gq, N));
     A(dalloc(&h->d_gqx, N));
     A(dalloc(&h->d_gqy, N));
     A(dalloc(&h->d_mov_q, nb));
@@ -677,6 +685,7 @@ int ap_create(const ap_netlist *nl, const ap_params *params, ap_handle **out) {
     A(cudaMemcpy(h->d_charge, charge.data(), sizeof(float) * N, cudaMemcpyHostToDevice));
     A(cudaMemset(h->d_mov_q, 0, sizeof(ull) * nb));
     A(cudaMemset(h->d_counters, 0, sizeof(unsigned int) * 8));
+    A(cudaMemset(h->d_gq, 0, sizeof(ull) * N));
     A(cudaMemset(h->d_gqx, 0, sizeof(ull) * N));
     A(cudaMemset(h->d_gqy, 0, sizeof(ull) * N));
     if (!ok) {
@@ -732,7 +741,7 @@ int ap_destroy(ap_handle *h) {
                     h->d_pins,    h->d_charge,   h->d_gqx,    h->d_gqy,
                     h->d_mov_q,   h->d_fix_q,    h->d_fixs_q, h->d_dens,    h->d_ex,    h->d_ey,
                     h->d_dens_hi, h->d_dens_lo,  h->d_sx,     h->d_sy,      h->d_sc,    h->d_partials,
-                    h->d_partials_ll, h->d_counters, h->d_out, h->d_rec_bin, h->d_rec_ov};
+                    h->d_partials_ll, h->d_counters, h->d_out, h->d_rec_bin, h->d_rec_ov, h->d_gq};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     if (h->h_sc) cudaFreeHost(h->h_sc);
@@ -973,22 +982,30 @@ int ap_wirelength_grad(ap_handle *h, const float *x, const float *y, float gamma
     if (!h || !x || !y || !gx || !gy || !(gamma > 0.f)) return AP_ERR_INVALID_ARG;
     int r = stage_positions(h, x, y);
     if (r != AP_OK) return r;
-    CK(cudaMemsetAsync(h->d_gqx, 0, sizeof(ull) * h->n_nodes, h->stream));
-    CK(cudaMemsetAsync(h->d_gqy, 0, sizeof(ull) * h->n_nodes, h->stream));
+    const size_t N = (size_t)h->n_nodes;
+    CK(cudaMemsetAsync(h->d_gq, 0, sizeof(ull) * N, h->stream));
+    CK(cudaMemsetAsync(h->d_gqx, 0, sizeof(ull) * N, h->stream));
+    CK(cudaMemsetAsync(h->d_gqy, 0, sizeof(ull) * N, h->stream));
     launch_wirelength(wa_args(h, h->d_sx, h->d_sy, gamma, h->n_nodes, WA_OUT_ONLY, h->d_out), h->stream);
     CK(cudaGetLastError());
-    std::vector<long long> qx((size_t)h->n_nodes), qy((size_t)h->n_nodes);
-    CK(cudaMemcpyAsync(qx.data(), h->d_gqx, sizeof(ull) * h->n_nodes, cudaMemcpyDeviceToHost, h->stream));
-    CK(cudaMemcpyAsync(qy.data(), h->d_gqy, sizeof(ull) * h->n_nodes, cudaMemcpyDeviceToHost, h->stream));
+    std::vector<unsigned long long> q(N), qx(N), qy(N);
+    CK(cudaMemcpyAsync(q.data(), h->d_gq, sizeof(ull) * N, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaMemcpyAsync(qx.data(), h->d_gqx, sizeof(ull) * N, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaMemcpyAsync(qy.data(), h->d_gqy, sizeof(ull) * N, cudaMemcpyDeviceToHost, h->stream));
     CK(cudaMemcpyAsync(h->h_out, h->d_out, sizeof(double) * 2, cudaMemcpyDeviceToHost, h->stream));
-    CK(cudaMemsetAsync(h->d_gqx, 0, sizeof(ull) * h->n_nodes, h->stream));
-    CK(cudaMemsetAsync(h->d_gqy, 0, sizeof(ull) * h->n_nodes, h->stream));
+    CK(cudaMemsetAsync(h->d_gq, 0, sizeof(ull) * N, h->stream));
+    CK(cudaMemsetAsync(h->d_gqx, 0, sizeof(ull) * N, h->stream));
+    CK(cudaMemsetAsync(h->d_gqy, 0, sizeof(ull) * N, h->stream));
     r = sync(h);
     if (r != AP_OK) return r;
-    for (int i = 0; i < h->n_nodes; ++i) {
-        const int e = h->int2ext[(size_t)i];
-        gx[e] = (float)ldexp((double)qx[(size_t)i], -20);  // kGradScale = 2^20
-        gy[e] = (float)ldexp((double)qy[(size_t)i], -20);
+    for (size_t i = 0; i < N; ++i) {
+        // packed halves (y 2^32 + x, x the signed low word) plus the per-axis sums
+        const long long lo = (long long)(int32_t)(uint32_t)q[i];
+        const long long sx = lo + (long long)qx[i];
+        const long long sy = (((long long)q[i] - lo) >> 32) + (long long)qy[i];
+        const int e = h->int2ext[i];
+        gx[e] = (float)ldexp((double)sx, -20);  // kGradScale = 2^20
+        gy[e] = (float)ldexp((double)sy, -20);
     }
     if (hpwl) *hpwl = h->h_out[0];
     if (wa) *wa = h->h_out[1];
@@ -1088,6 +1105,7 @@ int ap_restore(ap_handle *h, const void *buf, size_t bytes) {
         CK(cudaMemcpy(a, p, sizeof(float) * M, cudaMemcpyHostToDevice));
         p += sizeof(float) * M;
     }
+    CK(cudaMemset(h->d_gq, 0, sizeof(ull) * N));
     CK(cudaMemset(h->d_gqx, 0, sizeof(ull) * N));
     CK(cudaMemset(h->d_gqy, 0, sizeof(ull) * N));
     CK(cudaMemset(h->d_mov_q, 0, sizeof(ull) * (size_t)h->p.bins_x * h->p.bins_y));

@@ -586,16 +586,27 @@ __global__ void __launch_bounds__(kThreads) gather_kernel(GatherArgs a) {
             a.fy[i] = fy;
             continue;
         }
-        const float wlx = i64_to_float((long long)a.gqx[i]) * kInvGradScale;
-        const float wly = i64_to_float((long long)a.gqy[i]) * kInvGradScale;
+        long long qx, qy;
+        unpack_q(a.gq[i], qx, qy);
+        const float pc = a.pins[i];
+        const bool heavy = pc > (float)kPackMaxPins;
+        if (heavy) {
+            qx += (long long)a.gqx[i];
+            qy += (long long)a.gqy[i];
+        }
+        const float wlx = i64_to_float(qx) * kInvGradScale;
+        const float wly = i64_to_float(qy) * kInvGradScale;
         if (a.mode == GATHER_INIT_NORMS) {
             s2 += fabsf(wlx) + fabsf(wly);
             s3 += fabsf(fx) + fabsf(fy);
             continue;
         }
-        a.gqx[i] = 0ull;
-        a.gqy[i] = 0ull;
-        const float hd = fmaxf(1.f, a.pins[i] + lam * a.charge[i]);
+        a.gq[i] = 0ull;
+        if (heavy) {
+            a.gqx[i] = 0ull;
+            a.gqy[i] = 0ull;
+        }
+        const float hd = fmaxf(1.f, pc + lam * a.charge[i]);
         const float ihd = __frcp_rn(hd);
         const float gx = (wlx - lam * fx) * ihd, gy = (wly - lam * fy) * ihd;
         gx_out[i] = gx;

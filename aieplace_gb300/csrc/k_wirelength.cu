@@ -14,7 +14,9 @@
 //   WA+ = x_max + sum a+ (x - x_max) / b+,  WA- = x_min + sum a- (x - x_min) / b-,
 // which keeps FP32 exact where the reference form cancels (x_i/g ~ 1e4).
 // Each pin's gradient is rounded to 2^-20 and accumulated per node in int64,
-// so the sum over a node's nets is the same whatever order the atomics land in.
+// so the sum over a node's nets is the same whatever order the atomics land in;
+// both axes share one 64-bit atomic (pack_q) unless the node has more than
+// kPackMaxPins pins.
 #include <algorithm>
 
 #include "ap_common.cuh"
@@ -27,6 +29,17 @@ namespace {
 struct AxisTerms {
     float inv_bp, inv_bm, wp, wm;  // 1/b+, 1/b-, shifted WA+ - x_max, WA- - x_min
 };
+
+// one pin's gradient into its node's accumulators; `raw` is the pin_node entry
+__device__ __forceinline__ void add_grad(ull *gq, ull *gqx, ull *gqy, int raw, float gx, float gy) {
+    const int n = raw & kPinNode;
+    if (raw >= 0) {
+        atomicAdd(gq + n, pack_q(grad_q32(gx), grad_q32(gy)));
+    } else {
+        atomicAdd(gqx + n, grad_q(gx));
+        atomicAdd(gqy + n, grad_q(gy));
+    }
+}
 
 // Sums of 8 values at once over an aligned group of G lanes (transposed
 // butterfly): halving exchanges at offsets G/2, G/4, G/8 leave lane-in-group
@@ -86,9 +99,9 @@ __device__ __forceinline__ void net_group(const WaArgs &a, int s, int d, int l, 
     for (int p = 0; p < P; ++p) {
         const int j = l + p * G;
         v[p] = j < d;
-        nd[p] = v[p] ? __ldg(a.pin_node + s + j) : 0;
-        c[p][0] = v[p] ? __ldg(px + nd[p]) : 0.f;
-        c[p][1] = v[p] ? __ldg(py + nd[p]) : 0.f;
+        nd[p] = v[p] ? __ldg(a.pin_node + s + j) : 0;  // raw entry (heavy flag)
+        c[p][0] = v[p] ? __ldg(px + (nd[p] & kPinNode)) : 0.f;
+        c[p][1] = v[p] ? __ldg(py + (nd[p] & kPinNode)) : 0.f;
     }
     float m4[4] = {-3.0e38f, -3.0e38f, -3.0e38f, -3.0e38f};  // max x, max y, -min x, -min y
 #pragma unroll
@@ -131,10 +144,7 @@ __device__ __forceinline__ void net_group(const WaArgs &a, int s, int d, int l, 
     }
 #pragma unroll
     for (int p = 0; p < P; ++p)
-        if (v[p] && nd[p] < a.n_grad) {
-            atomicAdd(a.gqx + nd[p], grad_q(g[p][0]));
-            atomicAdd(a.gqy + nd[p], grad_q(g[p][1]));
-        }
+        if (v[p] && (nd[p] & kPinNode) < a.n_grad) add_grad(a.gq, a.gqx, a.gqy, nd[p], g[p][0], g[p][1]);
     if (l == 0) {
         hpf += (mx[0] - mn[0]) + (mx[1] - mn[1]);
         waf += wa_net;
@@ -159,17 +169,17 @@ __device__ __forceinline__ void net_groups(const WaArgs &a, int lo, int hi, int 
 // One net with d <= D pins held in registers by one thread.
 template <int D>
 __device__ __forceinline__ void net_thread(const int *__restrict__ pins, int d, const float *__restrict__ px,
-                                           const float *__restrict__ py, float inv_g, ull *gqx, ull *gqy,
-                                           int n_grad, float &hp_acc, float &wa_acc) {
+                                           const float *__restrict__ py, float inv_g, ull *gq, ull *gqx,
+                                           ull *gqy, int n_grad, float &hp_acc, float &wa_acc) {
     int node[D];
     float xs[D], ys[D];
     float xmx = -3.0e38f, xmn = 3.0e38f, ymx = -3.0e38f, ymn = 3.0e38f;
 #pragma unroll
     for (int j = 0; j < D; ++j) {
         if (j < d) {
-            node[j] = __ldg(pins + j);
-            xs[j] = __ldg(px + node[j]);
-            ys[j] = __ldg(py + node[j]);
+            node[j] = __ldg(pins + j);  // raw entry (heavy flag)
+            xs[j] = __ldg(px + (node[j] & kPinNode));
+            ys[j] = __ldg(py + (node[j] & kPinNode));
             xmx = fmaxf(xmx, xs[j]);
             xmn = fminf(xmn, xs[j]);
             ymx = fmaxf(ymx, ys[j]);
@@ -208,9 +218,8 @@ __device__ __forceinline__ void net_thread(const int *__restrict__ pins, int d, 
                                 em[j] * ibm * (1.f - ((c - cmn) - wm) * inv_g);
                 if (axis == 0) {
                     gxs[j] = g;
-                } else if (node[j] < n_grad) {
-                    atomicAdd(gqx + node[j], grad_q(gxs[j]));
-                    atomicAdd(gqy + node[j], grad_q(g));
+                } else if ((node[j] & kPinNode) < n_grad) {
+                    add_grad(gq, gqx, gqy, node[j], gxs[j], g);
                 }
             }
         }
@@ -243,7 +252,7 @@ __global__ void __launch_bounds__(kThreads) wa_small_kernel(WaArgs a) {
     for (int e = lo + blockIdx.x * blockDim.x + threadIdx.x; e < hi; e += gridDim.x * blockDim.x) {
         const int s = D == 2 ? s0 + 2 * (e - lo) : __ldg(a.net_ptr + e);
         const int d = D == 2 ? 2 : __ldg(a.net_ptr + e + 1) - s;
-        net_thread<D>(a.pin_node + s, d, px, py, inv_g, a.gqx, a.gqy, a.n_grad, hpf, waf);
+        net_thread<D>(a.pin_node + s, d, px, py, inv_g, a.gq, a.gqx, a.gqy, a.n_grad, hpf, waf);
     }
     // per-block partials in FP32 (folded with compensation by the last block
     // of the warp-per-net launch)
@@ -266,7 +275,7 @@ __device__ __forceinline__ void net_warp_loop(const WaArgs &a, int s, int d, con
     const int lane = threadIdx.x & 31;
     float m4[4] = {-3.0e38f, -3.0e38f, -3.0e38f, -3.0e38f};  // max x, max y, -min x, -min y
     for (int j = lane; j < d; j += 32) {
-        const int n = __ldg(a.pin_node + s + j);
+        const int n = __ldg(a.pin_node + s + j) & kPinNode;
         const float x = __ldg(px + n), y = __ldg(py + n);
         m4[0] = fmaxf(m4[0], x);
         m4[1] = fmaxf(m4[1], y);
@@ -277,7 +286,7 @@ __device__ __forceinline__ void net_warp_loop(const WaArgs &a, int s, int d, con
     const float xmx = m4[0], ymx = m4[1], xmn = -m4[2], ymn = -m4[3];
     float s8[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};  // bp bm cp cm for x then y
     for (int j = lane; j < d; j += 32) {
-        const int n = __ldg(a.pin_node + s + j);
+        const int n = __ldg(a.pin_node + s + j) & kPinNode;
         const float c2[2] = {__ldg(px + n), __ldg(py + n)};
 #pragma unroll
         for (int ax = 0; ax < 2; ++ax) {
@@ -299,7 +308,7 @@ __device__ __forceinline__ void net_warp_loop(const WaArgs &a, int s, int d, con
         t[ax].wm = s8[4 * ax + 3] * t[ax].inv_bm;
     }
     for (int j = lane; j < d; j += 32) {
-        const int n = __ldg(a.pin_node + s + j);
+        const int raw = __ldg(a.pin_node + s + j), n = raw & kPinNode;
         if (n >= a.n_grad) continue;
         const float c2[2] = {__ldg(px + n), __ldg(py + n)};
         float g[2];
@@ -310,8 +319,7 @@ __device__ __forceinline__ void net_warp_loop(const WaArgs &a, int s, int d, con
             g[ax] = ep * t[ax].inv_bp * (1.f + (dp - t[ax].wp) * inv_g) -
                     em * t[ax].inv_bm * (1.f - (dm - t[ax].wm) * inv_g);
         }
-        atomicAdd(a.gqx + n, grad_q(g[0]));
-        atomicAdd(a.gqy + n, grad_q(g[1]));
+        add_grad(a.gq, a.gqx, a.gqy, raw, g[0], g[1]);
     }
     if (lane == 0) {
         hpf += (xmx - xmn) + (ymx - ymn);

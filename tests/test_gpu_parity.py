@@ -144,6 +144,62 @@ def test_wirelength_gradient_every_degree_bucket(ap, oracle_lib):
     assert abs(wa - rwa) <= 1e-5 * rwa
 
 
+def with_hub_nodes(ap, seed=3):
+    """c0 plus 600 two-pin nets on one movable node and 700 on one fixed node:
+    more pins than one packed two-axis accumulator holds (512), so those two
+    nodes take the per-axis accumulators."""
+    nl = dict(ap.synth.generate("c0", seed=seed))
+    rng = np.random.default_rng(seed)
+    n = len(nl["node_w"])
+    fixed = np.flatnonzero(nl["node_fixed"])
+    mov = np.flatnonzero(nl["node_fixed"] == 0)
+    hubs = [(int(mov[n // 7 % len(mov)]), 600)] + ([(int(fixed[0]), 700)] if len(fixed) else [])
+    ptr = list(nl["net_ptr"])
+    pins = list(nl["pin_node"])
+    for hub, k in hubs:
+        for o in rng.choice(np.setdiff1d(np.arange(n), [hub]), size=k):
+            pins += [hub, int(o)]
+            ptr.append(len(pins))
+    nl["net_ptr"] = np.array(ptr, np.int32)
+    nl["pin_node"] = np.array(pins, np.int32)
+    return nl, [h for h, _ in hubs]
+
+
+def test_wirelength_gradient_hub_nodes(ap, oracle_lib):
+    nl, hubs = with_hub_nodes(ap)
+    rng = np.random.default_rng(4)
+    x, y = spread_positions(nl, rng, margin=0.0)
+    with ap.Placer(nl, bins=32) as pl:
+        gx, gy, wa, hp = pl.compute_all_partials(x, y, 2.0)
+    rx, ry, rwa, rhp = oracle_lib.wa_grad(nl["net_ptr"], nl["pin_node"], x, y, 2.0)
+    scale = max(np.abs(rx).max(), np.abs(ry).max())
+    assert np.abs(gx - rx).max() <= 1e-4 * scale
+    assert np.abs(gy - ry).max() <= 1e-4 * scale
+    for hub in hubs:  # the per-axis accumulators: hundreds of pins in one sum
+        assert abs(rx[hub]) + abs(ry[hub]) > 10.0
+        assert abs(gx[hub] - rx[hub]) <= 1e-5 * (abs(rx[hub]) + 1.0)
+        assert abs(gy[hub] - ry[hub]) <= 1e-5 * (abs(ry[hub]) + 1.0)
+    assert abs(hp - rhp) <= 1e-6 * rhp
+
+
+def test_loop_hub_nodes_first_iterations_like_oracle(ap, oracle_lib):
+    """The loop's gather reads the hub's per-axis accumulators: its first
+    iterations follow the FP64 oracle loop (positions within 1e-3 of the die)."""
+    nl, hubs = with_hub_nodes(ap)
+    ref = oracle_lib.Placer(nl, 32, 1.0)
+    ref.init(nl["node_x"], nl["node_y"])
+    with ap.Placer(nl, bins=32, target_density=1.0) as pl:
+        pl.initialize_placement(nl["node_x"], nl["node_y"])
+        for _ in range(3):
+            pl.perform_iteration(1)
+            ref.step(1)
+            x, y = pl.positions()
+            rx, ry = ref.positions()
+            tol = 1e-3 * float(nl["die"][2])
+            assert np.abs(x - rx).max() <= tol and np.abs(y - ry).max() <= tol
+            assert abs(x[hubs[0]] - rx[hubs[0]]) <= tol and abs(y[hubs[0]] - ry[hubs[0]]) <= tol
+
+
 @pytest.mark.parametrize("m", [32, 128, 512])
 def test_field_fp32_against_oracle(ap, oracle_lib, m):
     rng = np.random.default_rng(m)
