@@ -8,13 +8,20 @@
 // one FP32 accumulator in tensor memory: A_hi B_hi + A_hi B_lo + A_lo B_hi
 // (the "bf16x3" split; the dropped A_lo B_lo term is 2^-16 relative).
 //
-// Kernel layout (one 128 x 64 output tile per CTA, 4 warps):
+// Kernel layout (a 128 x BN output tile per cluster of S CTAs, 4 warps each;
+// the S CTAs split K):
 //   warp 0 lane 0   TMA producer: 4-stage ring of {A_hi, A_lo, B_hi, B_lo}
 //                   128B-swizzled K-major tiles, mbarrier complete_tx
 //   warp 1 lane 0   MMA issuer: tcgen05.mma.cta_group::1.kind::f16, M=128,
 //                   N=64, K=16; tcgen05.commit frees stages / signals the end
 //   warps 0-3       epilogue: tcgen05.ld 32x32b (warp w owns TMEM lanes
-//                   32w..32w+31 = output rows), fused stage epilogue, stores
+//                   32w..32w+31 = output rows); CTA r of the cluster finishes
+//                   rows [r 128/S, (r+1) 128/S): once every CTA of the cluster
+//                   is past its K loop (cluster barrier), every CTA stores its partial
+//                   of those rows into CTA r's shared memory (distributed
+//                   shared memory, slot = source rank); cluster barrier; CTA
+//                   r sums its S slots in rank order, applies the stage
+//                   epilogue and stores a warp per row, coalesced
 // Every mbarrier wait is bounded; a wait that gives up sets the solver's
 // status word and the CTA drains and exits without further issue.
 #include <cuda.h>
@@ -57,6 +64,7 @@ struct Maps {
 struct Epi {
     int m;
     int mode;
+    int split;  // S: CTAs per cluster splitting K (the cluster's x extent)
     __nv_bfloat16 *o_hi[2], *o_lo[2];  // EPI_SPLIT; EPI_SPECTRAL: [0] = Px, [1] = Py
     float *o_f32[2];                   // EPI_F32
     const float *wx, *wy;
@@ -123,6 +131,42 @@ __device__ __forceinline__ void tma_prefetch(const CUtensorMap *map) {
     asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)map) : "memory");
 }
 
+__device__ __forceinline__ void cluster_sync() {
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+// shared::cluster address of the same offset in CTA `rank` of the cluster
+__device__ __forceinline__ uint32_t map_rank(uint32_t local, int rank) {
+    uint32_t r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(local), "r"(rank));
+    return r;
+}
+
+__device__ __forceinline__ void st_shared_f4(uint32_t addr, float4 v) {
+    asm volatile("st.shared.v4.f32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "f"(v.x), "f"(v.y), "f"(v.z), "f"(v.w)
+                 : "memory");
+}
+
+__device__ __forceinline__ void st_cluster_f4(uint32_t addr, float4 v) {
+    asm volatile("st.shared::cluster.v4.f32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "f"(v.x), "f"(v.y), "f"(v.z),
+                 "f"(v.w)
+                 : "memory");
+}
+
+// explicit shared-space loads: a generic load could alias the epilogue's
+// global stores and would wait for them
+__device__ __forceinline__ float2 ld_shared_f2(uint32_t addr) {
+    float2 v;
+    asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(addr));
+    return v;
+}
+
+__device__ __forceinline__ float4 ld_shared_f4(uint32_t addr) {
+    float4 v;
+    asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];" : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "r"(addr));
+    return v;
+}
+
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
@@ -175,21 +219,68 @@ __device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
     return *reinterpret_cast<const uint32_t *>(&v);
 }
 
-// 32 FP32 values of one output row -> hi/lo BF16 rows (64 bytes each)
-__device__ __forceinline__ void store_split(const float (&v)[32], __nv_bfloat16 *hi, __nv_bfloat16 *lo) {
-    uint32_t h[16], l[16];
+// VEC FP32 values -> hi/lo BF16 (VEC = 2 or 4 consecutive outputs)
+template <int VEC>
+__device__ __forceinline__ void store_split_vec(const float (&v)[VEC], __nv_bfloat16 *hi, __nv_bfloat16 *lo) {
+    uint32_t h[VEC / 2], l[VEC / 2];
 #pragma unroll
-    for (int i = 0; i < 16; ++i) {
+    for (int i = 0; i < VEC / 2; ++i) {
         const __nv_bfloat16 a = __float2bfloat16_rn(v[2 * i]), b = __float2bfloat16_rn(v[2 * i + 1]);
         const __nv_bfloat162 hp = __halves2bfloat162(a, b);
         h[i] = *reinterpret_cast<const uint32_t *>(&hp);
         l[i] = pack_bf16(v[2 * i] - __bfloat162float(a), v[2 * i + 1] - __bfloat162float(b));
     }
-    uint4 *ph = reinterpret_cast<uint4 *>(hi), *pl = reinterpret_cast<uint4 *>(lo);
+    if (VEC == 4) {
+        *reinterpret_cast<uint2 *>(hi) = make_uint2(h[0], h[VEC / 2 - 1]);
+        *reinterpret_cast<uint2 *>(lo) = make_uint2(l[0], l[VEC / 2 - 1]);
+    } else {
+        *reinterpret_cast<uint32_t *>(hi) = h[0];
+        *reinterpret_cast<uint32_t *>(lo) = l[0];
+    }
+}
+
+// Output pointers of one CTA's stage epilogue, resolved before the row loop:
+// indexing the parameter block by blockIdx.z inside the loop made the compiler
+// copy it to local memory.
+struct EpiOut {
+    int m, mode;
+    float *f32;
+    __nv_bfloat16 *hi0, *lo0, *hi1, *lo1;
+    float scale;
+};
+
+// Stage epilogue of VEC consecutive outputs (row, col..col+VEC-1); a warp
+// covers one row's BN columns, so each store instruction writes one
+// contiguous 128-512 byte segment.  wx, wy: the row's and the columns'
+// spectral frequencies (EPI_SPECTRAL).
+template <int VEC>
+__device__ __forceinline__ void epi_store(const EpiOut &o, int row, int col, const float (&v)[VEC], float wx,
+                                          const float (&wy)[VEC]) {
+    const size_t off = (size_t)row * o.m + col;
+    if (o.mode == EPI_F32) {
+        if (VEC == 4)
+            *reinterpret_cast<float4 *>(o.f32 + off) = make_float4(v[0], v[1], v[VEC - 2], v[VEC - 1]);
+        else
+            *reinterpret_cast<float2 *>(o.f32 + off) = make_float2(v[0], v[1]);
+    } else if (o.mode == EPI_SPLIT) {
+        store_split_vec<VEC>(v, o.hi0 + off, o.lo0 + off);
+    } else {
+        // spectral scaling of fft.cpp:217-273: halve row/column 0, 4/(Mx My),
+        // phi = a / (wx^2 + wy^2), Px = phi wx, Py = phi wy (straight-line
+        // 2-ulp division: the IEEE divide's slow path is a call)
+        const float rs = row == 0 ? 0.5f * o.scale : o.scale;
+        float px[VEC], py[VEC];
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
-        ph[i] = make_uint4(h[4 * i], h[4 * i + 1], h[4 * i + 2], h[4 * i + 3]);
-        pl[i] = make_uint4(l[4 * i], l[4 * i + 1], l[4 * i + 2], l[4 * i + 3]);
+        for (int i = 0; i < VEC; ++i) {
+            float c = v[i] * rs;
+            if (col + i == 0) c *= 0.5f;
+            const float den = wx * wx + wy[i] * wy[i];
+            c = den > 0.f ? __fdividef(c, den) : 0.f;
+            px[i] = c * wx;
+            py[i] = c * wy[i];
+        }
+        store_split_vec<VEC>(px, o.hi0 + off, o.lo0 + off);
+        store_split_vec<VEC>(py, o.hi1 + off, o.lo1 + off);
     }
 }
 
@@ -209,8 +300,10 @@ __global__ void __launch_bounds__(THREADS, 1) gemm_bf16x3_kernel(const __grid_co
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int z = blockIdx.z;
-    const int n0 = blockIdx.x * BN, m0 = blockIdx.y * BM;
-    const int nk = e.m / BK;
+    // cluster of S CTAs along x: rank r accumulates k-blocks [r nk, (r+1) nk)
+    const int S = e.split, rank = (int)blockIdx.x % S;
+    const int n0 = ((int)blockIdx.x / S) * BN, m0 = blockIdx.y * BM;
+    const int nk = e.m / BK / S, kb0 = rank * nk;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < STAGES; ++s) {
@@ -247,10 +340,11 @@ __global__ void __launch_bounds__(THREADS, 1) gemm_bf16x3_kernel(const __grid_co
             if (*abort_flag) break;
             uint8_t *st = smem + s * STAGE_BYTES;
             mbar_expect_tx(full + s, STAGE_BYTES);
-            tma_load_2d(&maps.a_hi[z], full + s, st, kb * BK, m0);
-            tma_load_2d(&maps.a_lo[z], full + s, st + A_TILE, kb * BK, m0);
-            tma_load_2d(&maps.b_hi[z], full + s, st + 2 * A_TILE, kb * BK, n0);
-            tma_load_2d(&maps.b_lo[z], full + s, st + 2 * A_TILE + B_TILE, kb * BK, n0);
+            const int kx = (kb0 + kb) * BK;
+            tma_load_2d(&maps.a_hi[z], full + s, st, kx, m0);
+            tma_load_2d(&maps.a_lo[z], full + s, st + A_TILE, kx, m0);
+            tma_load_2d(&maps.b_hi[z], full + s, st + 2 * A_TILE, kx, n0);
+            tma_load_2d(&maps.b_lo[z], full + s, st + 2 * A_TILE + B_TILE, kx, n0);
             issued = kb + 1;
         }
     } else if (warp == 1 && lane == 0) {
@@ -281,45 +375,115 @@ __global__ void __launch_bounds__(THREADS, 1) gemm_bf16x3_kernel(const __grid_co
     // ---- epilogue ----------------------------------------------------------
     const bool ok = mbar_wait(done, 0, e.status) && !*abort_flag;
     tc_fence_after();
+    // The pipeline buffers are free once the accumulator is complete (every
+    // issued load landed and was read): they hold the FP32 staging slots,
+    // slot q (source rank) x 128/S rows, row stride BN + 4 floats (16-byte
+    // rows, conflict-free v4 stores).
+    constexpr int LD = BN + 4, VEC = BN / 32;
+    static_assert(BM * LD * 4 <= STAGES * STAGE_BYTES, "staging tile fits the pipeline buffers");
+    const uint32_t stg = smem_u32(smem);
+    const int RS = BM / S;  // rows finished per CTA
+    // a peer's pipeline buffers are free only once its accumulator is
+    // complete too: no partial goes out before every CTA of the cluster is
+    // past its K loop
+    if (S > 1) cluster_sync();
     if (ok) {
-        const int row = m0 + warp * 32 + lane;
+        const int row = warp * 32 + lane, dst = row / RS, lr = row - dst * RS;
+        const uint32_t la = stg + (uint32_t)(((rank * RS + lr) * LD) * 4);
+        const uint32_t ra = dst == rank ? la : map_rank(la, dst);
 #pragma unroll
         for (int c0 = 0; c0 < BN; c0 += 32) {
             uint32_t r[32];
             tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, r);
-            float v[32];
 #pragma unroll
-            for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
-            const size_t off = (size_t)row * e.m + n0 + c0;
-            if (e.mode == EPI_F32) {
-                float4 *o = reinterpret_cast<float4 *>(e.o_f32[z] + off);
-#pragma unroll
-                for (int i = 0; i < 8; ++i) o[i] = make_float4(v[4 * i], v[4 * i + 1], v[4 * i + 2], v[4 * i + 3]);
-            } else if (e.mode == EPI_SPLIT) {
-                store_split(v, e.o_hi[z] + off, e.o_lo[z] + off);
-            } else {
-                // spectral scaling of fft.cpp:217-273: halve row/column 0,
-                // 4/(Mx My), phi = a / (wx^2 + wy^2), Px = phi wx, Py = phi wy
-                const int u = row;
-                const float wx = e.wx[u];
-                float px[32], py[32];
-#pragma unroll
-                for (int i = 0; i < 32; ++i) {
-                    const int vv = n0 + c0 + i;
-                    const float wy = e.wy[vv];
-                    float c = v[i] * e.scale;
-                    if (u == 0) c *= 0.5f;
-                    if (vv == 0) c *= 0.5f;
-                    const float den = wx * wx + wy * wy;
-                    c = den > 0.f ? c / den : 0.f;
-                    px[i] = c * wx;
-                    py[i] = c * wy;
-                }
-                store_split(px, e.o_hi[0] + off, e.o_lo[0] + off);
-                store_split(py, e.o_hi[1] + off, e.o_lo[1] + off);
+            for (int i = 0; i < 8; ++i) {
+                const float4 v = make_float4(__uint_as_float(r[4 * i]), __uint_as_float(r[4 * i + 1]),
+                                             __uint_as_float(r[4 * i + 2]), __uint_as_float(r[4 * i + 3]));
+                const uint32_t off = (uint32_t)((c0 + 4 * i) * 4);
+                if (dst == rank)
+                    st_shared_f4(la + off, v);
+                else
+                    st_cluster_f4(ra + off, v);
             }
         }
     }
+    // every CTA of the cluster arrives on every path (an aborted CTA too);
+    // release/acquire makes the peers' slot stores visible
+    if (S > 1)
+        cluster_sync();
+    else
+        __syncthreads();
+    if (ok) {
+        // this CTA's rows, the S slots summed in rank order; a warp per row,
+        // VEC columns per lane.  Pointers and frequencies go to registers
+        // first: the loop reads nothing but shared memory.
+        EpiOut o;
+        o.m = e.m;
+        o.mode = e.mode;
+        o.scale = e.scale;
+        o.f32 = z ? e.o_f32[1] : e.o_f32[0];
+        const bool two = e.mode == EPI_SPECTRAL;  // Px and Py
+        o.hi0 = (z && !two) ? e.o_hi[1] : e.o_hi[0];
+        o.lo0 = (z && !two) ? e.o_lo[1] : e.o_lo[0];
+        o.hi1 = e.o_hi[1];
+        o.lo1 = e.o_lo[1];
+        float wy[VEC], wx_lane = 0.f;
+#pragma unroll
+        for (int i = 0; i < VEC; ++i) wy[i] = 0.f;
+        if (two) {
+#pragma unroll
+            for (int i = 0; i < VEC; ++i) wy[i] = __ldg(e.wy + n0 + lane * VEC + i);
+            // lane k holds the frequency of this warp's k-th row (<= 32 rows)
+            const int lr = warp + (THREADS / 32) * lane;
+            if (lr < RS) wx_lane = __ldg(e.wx + m0 + rank * RS + lr);
+        }
+        // rows lr = warp + 4 k; four rows a batch, every slot load of the
+        // batch issued before the first add (one load in flight per row
+        // measured ~250 cycles a row)
+        constexpr int NR = 4, W = THREADS / 32;
+        static_assert(BM % (NR * W * 4) == 0, "rows per warp a multiple of the batch for S <= 4");
+        for (int k0 = 0; warp + k0 * W < RS; k0 += NR) {
+            float p[4][NR][VEC];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                if (q < S) {
+#pragma unroll
+                    for (int j = 0; j < NR; ++j) {
+                        const int lr = warp + (k0 + j) * W;
+                        const uint32_t a = stg + (uint32_t)((((q * RS + lr) * LD) + lane * VEC) * 4);
+                        if (VEC == 4) {
+                            const float4 t = ld_shared_f4(a);
+                            p[q][j][0] = t.x;
+                            p[q][j][1] = t.y;
+                            p[q][j][VEC - 2] = t.z;
+                            p[q][j][VEC - 1] = t.w;
+                        } else {
+                            const float2 t = ld_shared_f2(a);
+                            p[q][j][0] = t.x;
+                            p[q][j][VEC - 1] = t.y;
+                        }
+                    }
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < NR; ++j) {
+                const int lr = warp + (k0 + j) * W;
+                float acc[VEC];
+#pragma unroll
+                for (int i = 0; i < VEC; ++i) acc[i] = 0.f;
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+                    if (q < S) {
+#pragma unroll
+                        for (int i = 0; i < VEC; ++i) acc[i] += p[q][j][i];
+                    }
+                const float wx = __shfl_sync(0xffffffffu, wx_lane, (k0 + j) & 31);
+                epi_store<VEC>(o, m0 + rank * RS + lr, n0 + lane * VEC, acc, wx, wy);
+            }
+        }
+    }
+    // (no second cluster barrier: peers write this CTA's slots only before
+    // the one above, whose release orders those stores ahead of its arrival)
     tc_fence_before();
     __syncthreads();
     if (threadIdx.x == 0 && issued > 0) {
@@ -395,10 +559,46 @@ struct TcState {
     StageMaps maps[2];  // [0] 128 x 64 tiles, [1] 128 x 128 tiles
 };
 
+// CTAs per cluster splitting K: doubled (up to 4) while the k-blocks divide
+// and the launch still fits one wave of `per_sm` CTAs per SM -- small grids
+// (few output tiles) then use more SMs
+int pick_split(int tiles, int nk, int per_sm) {
+    static int sms = 0;
+    if (sms <= 0) {
+        int dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0)
+            sms = 148;
+    }
+    int s = 1;
+    while (s < 4 && nk % (2 * s) == 0 && tiles * 2 * s <= sms * per_sm) s *= 2;
+    return s;
+}
+
+template <class T>
+void launch_stage(const Maps &maps, Epi e, int m, int batch, int per_sm, cudaStream_t st) {
+    const int tiles = (m / T::BN) * (m / BM) * batch;
+    e.split = pick_split(tiles, m / BK, per_sm);
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3((m / T::BN) * e.split, m / BM, batch);
+    cfg.blockDim = dim3(THREADS);
+    cfg.dynamicSmemBytes = T::SMEM_BYTES;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = e.split;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = e.split > 1 ? 1 : 0;
+    cudaLaunchKernelEx(&cfg, gemm_bf16x3_kernel<T>, maps, e);
+}
+
 template <class T>
 void run_stages(const StageMaps &h, FieldSolver &f, float *ex, float *ey, cudaStream_t st, const int *gate,
                 int gate_mask) {
     const int m = f.m;
+    const int per_sm = T::SMEM_BYTES * 2 <= 227 * 1024 ? 2 : 1;
     Epi e{};
     e.gate = gate;
     e.gate_mask = gate_mask;
@@ -407,27 +607,26 @@ void run_stages(const StageMaps &h, FieldSolver &f, float *ex, float *ey, cudaSt
     e.wx = f.wx;
     e.wy = f.wy;
     e.scale = 4.0f / ((float)m * (float)m);
-    const dim3 g1(m / T::BN, m / BM, 1), g2(m / T::BN, m / BM, 2);
     e.mode = EPI_SPLIT;
     e.o_hi[0] = f.b_t_hi;
     e.o_lo[0] = f.b_t_lo;
-    gemm_bf16x3_kernel<T><<<g1, THREADS, T::SMEM_BYTES, st>>>(h.s1, e);
+    launch_stage<T>(h.s1, e, m, 1, per_sm, st);
     e.mode = EPI_SPECTRAL;
     e.o_hi[0] = f.b_px_hi;
     e.o_lo[0] = f.b_px_lo;
     e.o_hi[1] = f.b_py_hi;
     e.o_lo[1] = f.b_py_lo;
-    gemm_bf16x3_kernel<T><<<g1, THREADS, T::SMEM_BYTES, st>>>(h.s2, e);
+    launch_stage<T>(h.s2, e, m, 1, per_sm, st);
     e.mode = EPI_SPLIT;
     e.o_hi[0] = f.b_ux_hi;
     e.o_lo[0] = f.b_ux_lo;
     e.o_hi[1] = f.b_uy_hi;
     e.o_lo[1] = f.b_uy_lo;
-    gemm_bf16x3_kernel<T><<<g2, THREADS, T::SMEM_BYTES, st>>>(h.s3, e);
+    launch_stage<T>(h.s3, e, m, 2, per_sm, st);
     e.mode = EPI_F32;
     e.o_f32[0] = ex;
     e.o_f32[1] = ey;
-    gemm_bf16x3_kernel<T><<<g2, THREADS, T::SMEM_BYTES, st>>>(h.s4, e);
+    launch_stage<T>(h.s4, e, m, 2, per_sm, st);
 }
 
 void run_variant(int v, FieldSolver &f, float *ex, float *ey, cudaStream_t st, const int *gate = nullptr,
