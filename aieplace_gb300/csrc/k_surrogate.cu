@@ -267,6 +267,114 @@ __global__ void __launch_bounds__(256) conv_fwd_kernel(int B, int R, int cin, in
     }
 }
 
+// Inference forward of the (K0, 1, 1, 1) architecture in one launch: the
+// arithmetic of four conv_fwd_kernel launches in the same order (bias first,
+// then input channel, kx, ky; ReLU on the hidden layers), so the output is
+// bit-identical, without the three hidden maps in global memory.  Block: an
+// 8 x 32 pixel tile, one pixel per thread (two pixels a thread measured
+// slower: 233 registers left one block per SM); shared memory holds the
+// input tile with its halo and every layer's weights as [input][kMaxCh] rows
+// (one float4 load feeds four output channels).
+struct FusedNet {
+    int cin0, width, cout;
+    size_t w_off[kSurrLayers], b_off[kSurrLayers];
+};
+
+constexpr int kFuseTX = 8, kFuseTY = 32;
+
+__host__ __device__ constexpr int fused_halo(int k) { return (kFuseTX + k - 1) * (kFuseTY + k - 1); }
+
+template <int K0>
+__global__ void __launch_bounds__(256, 2) net_fwd_fused_kernel(int R, FusedNet fn, const float *x0,
+                                                                const float *params, float *y, const int *gate,
+                                                                int mask) {
+    if (!gate_open(gate, mask)) return;
+    extern __shared__ float4 smem4[];
+    constexpr int KK = K0 * K0, H = K0 / 2, HX = kFuseTX + K0 - 1, HY = kFuseTY + K0 - 1;
+    const int cin0 = fn.cin0, width = fn.width, cout = fn.cout;
+    float *w0 = reinterpret_cast<float *>(smem4);      // [cin0 KK][kMaxCh]
+    float *wh = w0 + cin0 * KK * kMaxCh;               // 3 x [kMaxCh][kMaxCh] (layers 1-3)
+    float *bs = wh + 3 * kMaxCh * kMaxCh;              // 4 x [kMaxCh]
+    float *xin = bs + 4 * kMaxCh;                      // [cin0][HX][HY]
+    const int b = blockIdx.z, X0 = blockIdx.y * kFuseTX, Y0 = blockIdx.x * kFuseTY, RR = R * R;
+    for (int t = threadIdx.x; t < cin0 * KK * kMaxCh; t += blockDim.x) {
+        const int co = t % kMaxCh, r = t / kMaxCh, ci = r / KK, kk = r - ci * KK;
+        w0[t] = co < width ? params[fn.w_off[0] + ((size_t)co * cin0 + ci) * KK + kk] : 0.f;
+    }
+    for (int t = threadIdx.x; t < 3 * kMaxCh * kMaxCh; t += blockDim.x) {
+        const int l = 1 + t / (kMaxCh * kMaxCh), r = t % (kMaxCh * kMaxCh), ci = r / kMaxCh, co = r % kMaxCh;
+        const int cin = width, co_n = l == kSurrLayers - 1 ? cout : width;
+        const size_t wo = l == 1 ? fn.w_off[1] : l == 2 ? fn.w_off[2] : fn.w_off[3];
+        wh[t] = (co < co_n && ci < cin) ? params[wo + (size_t)co * cin + ci] : 0.f;
+    }
+    for (int t = threadIdx.x; t < 4 * kMaxCh; t += blockDim.x) {
+        const int l = t / kMaxCh, co = t % kMaxCh, co_n = l == kSurrLayers - 1 ? cout : width;
+        const size_t bo = l == 0 ? fn.b_off[0] : l == 1 ? fn.b_off[1] : l == 2 ? fn.b_off[2] : fn.b_off[3];
+        bs[t] = co < co_n ? params[bo + co] : 0.f;
+    }
+    const float *xb = x0 + (size_t)b * cin0 * RR;
+    for (int t = threadIdx.x; t < cin0 * HX * HY; t += blockDim.x) {
+        const int ci = t / (HX * HY), r = t - ci * (HX * HY), hx = r / HY, hy = r - hx * HY;
+        const int xx = X0 + hx - H, yy = Y0 + hy - H;
+        xin[t] = (xx >= 0 && xx < R && yy >= 0 && yy < R) ? __ldg(xb + (size_t)ci * RR + xx * R + yy) : 0.f;
+    }
+    __syncthreads();
+    const int lx = threadIdx.x / kFuseTY, ly = threadIdx.x % kFuseTY;  // rows lx and lx + 8
+    float a0[kMaxCh], h0[kMaxCh];
+#pragma unroll
+    for (int c = 0; c < kMaxCh; ++c) a0[c] = bs[c];
+    const float4 *w04 = reinterpret_cast<const float4 *>(w0);
+    for (int ci = 0; ci < cin0; ++ci) {
+        const float *xc = xin + ci * (HX * HY);
+#pragma unroll
+        for (int kx = 0; kx < K0; ++kx)
+#pragma unroll
+            for (int ky = 0; ky < K0; ++ky) {
+                const float v0 = xc[(lx + kx) * HY + ly + ky];
+                const float4 *w4 = w04 + (ci * KK + kx * K0 + ky) * (kMaxCh / 4);
+#pragma unroll
+                for (int j = 0; j < kMaxCh / 4; ++j) {
+                    const float4 w = w4[j];
+                    a0[4 * j] += v0 * w.x;
+                    a0[4 * j + 1] += v0 * w.y;
+                    a0[4 * j + 2] += v0 * w.z;
+                    a0[4 * j + 3] += v0 * w.w;
+                }
+            }
+    }
+#pragma unroll
+    for (int l = 1; l < kSurrLayers; ++l) {
+#pragma unroll
+        for (int c = 0; c < kMaxCh; ++c) {
+            h0[c] = fmaxf(a0[c], 0.f);  // every layer before the last has a ReLU
+            a0[c] = bs[l * kMaxCh + c];
+        }
+        const float4 *w4l = reinterpret_cast<const float4 *>(wh + (l - 1) * kMaxCh * kMaxCh);
+#pragma unroll
+        for (int ci = 0; ci < kMaxCh; ++ci) {
+            if (ci < width) {
+#pragma unroll
+                for (int j = 0; j < kMaxCh / 4; ++j) {
+                    const float4 w = w4l[ci * (kMaxCh / 4) + j];
+                    a0[4 * j] += h0[ci] * w.x;
+                    a0[4 * j + 1] += h0[ci] * w.y;
+                    a0[4 * j + 2] += h0[ci] * w.z;
+                    a0[4 * j + 3] += h0[ci] * w.w;
+                }
+            }
+        }
+    }
+    const int xg = X0 + lx, yg = Y0 + ly;
+    if (yg < R) {
+        float *yb = y + (size_t)b * cout * RR;
+#pragma unroll
+        for (int c = 0; c < kMaxCh; ++c)
+            if (c < cout) {
+                yb[(size_t)c * RR + xg * R + yg] = a0[c];
+            }
+    }
+}
+
 // dIn[b][ci][x][y] = sum_co sum_k W[co][ci][k] g[b][co][x - kx + H][y - ky + H],
 // g = dOut, masked by out > 0 when the layer has a ReLU.  Weights in shared
 // memory as [cout][K*K][kMaxCh] (input channel fastest).
@@ -570,9 +678,19 @@ void conv_bwd(const SurrLayer &L, int B, int R, const float *in, const float *ou
                                                                            params + L.w_off, din);
 }
 
+size_t fused_smem(int cin0, int k0) {
+    return ((size_t)cin0 * k0 * k0 * kMaxCh + 3 * kMaxCh * kMaxCh + 4 * kMaxCh +
+            (size_t)cin0 * sg::fused_halo(k0)) *
+           sizeof(float);
+}
+
 bool g_attrs_set = false;
 void set_kernel_attrs() {
     if (g_attrs_set) return;
+    cudaFuncSetAttribute(sg::net_fwd_fused_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)fused_smem(kMaxCh, 3));
+    cudaFuncSetAttribute(sg::net_fwd_fused_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)fused_smem(kMaxCh, 1));
     cudaFuncSetAttribute(sg::conv_bwd_weight_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)wgrad_smem(3));
     cudaFuncSetAttribute(sg::conv_bwd_weight_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -584,6 +702,33 @@ void set_kernel_attrs() {
 void net_forward(const SurrNet &net, int B, int R, float *const a[kSurrLayers + 1], cudaStream_t st,
                  const int *gate = nullptr, int mask = 0) {
     for (int l = 0; l < kSurrLayers; ++l) conv_fwd(net.L[l], B, R, a[l], net.d_params, a[l + 1], st, gate, mask);
+}
+
+// Inference forward x -> y: one fused launch when every layer after the first
+// is 1 x 1 (the hidden maps stay in registers), else the per-layer kernels
+// through the scratch maps a[1..3].  Both give the same bits.
+void net_infer(const SurrNet &net, int B, int R, const float *x, float *const a[kSurrLayers + 1], float *y,
+               cudaStream_t st, const int *gate = nullptr, int mask = 0) {
+    bool fuse = true;
+    for (int l = 1; l < kSurrLayers; ++l) fuse = fuse && net.L[l].k == 1;
+    if (fuse) {
+        sg::FusedNet fn{net.cin0, net.width, net.cout, {}, {}};
+        for (int l = 0; l < kSurrLayers; ++l) {
+            fn.w_off[l] = net.L[l].w_off;
+            fn.b_off[l] = net.L[l].b_off;
+        }
+        const dim3 g((R + sg::kFuseTY - 1) / sg::kFuseTY, R / sg::kFuseTX, B);
+        if (net.L[0].k == 3)
+            sg::net_fwd_fused_kernel<3><<<g, 256, fused_smem(net.cin0, 3), st>>>(R, fn, x, net.d_params, y, gate,
+                                                                                  mask);
+        else
+            sg::net_fwd_fused_kernel<1><<<g, 256, fused_smem(net.cin0, 1), st>>>(R, fn, x, net.d_params, y, gate,
+                                                                                  mask);
+        return;
+    }
+    conv_fwd(net.L[0], B, R, x, net.d_params, a[1], st, gate, mask);
+    for (int l = 1; l < kSurrLayers; ++l)
+        conv_fwd(net.L[l], B, R, a[l], net.d_params, l == kSurrLayers - 1 ? y : a[l + 1], st, gate, mask);
 }
 
 }  // namespace
@@ -654,7 +799,7 @@ void surr_enqueue_field(const SurrNet &net, SurrState &ss, const float *d_f32, c
     const float *y = nullptr;
     if (ss.use_net) {
         float *const a[kSurrLayers + 1] = {ss.d_x0, ss.d_act[0], ss.d_act[1], ss.d_act[0], ss.d_y};
-        net_forward(net, 1, ss.R, a, st, gate, mask);
+        net_infer(net, 1, ss.R, ss.d_x0, a, ss.d_y, st, gate, mask);
         y = ss.d_y;
     }
     sg::combine_kernel<<<grid_for((size_t)ss.M * ss.M), 256, 0, st>>>(ss.M, net.f, ss.d_cex, ss.d_cey, y,
@@ -882,7 +1027,7 @@ int ap_surrogate_forward(ap_surrogate *s, const float *x, int32_t batch, int32_t
     if (r != AP_OK) return r;
     const size_t RR = (size_t)res * res;
     CKS(cudaMemcpy(s->d_a[0], x, sizeof(float) * batch * s->net.cin0 * RR, cudaMemcpyHostToDevice));
-    ap::net_forward(s->net, batch, res, s->d_a, 0);
+    ap::net_infer(s->net, batch, res, s->d_a[0], s->d_a, s->d_a[kSurrLayers], 0);
     CKS(cudaGetLastError());
     CKS(cudaMemcpy(y, s->d_a[kSurrLayers], sizeof(float) * batch * s->net.cout * RR, cudaMemcpyDeviceToHost));
     return AP_OK;
@@ -974,7 +1119,7 @@ int ap_surrogate_validate(ap_surrogate *s, int32_t first, int32_t count, double 
     for (int i = first; i < first + count; ++i) {
         CKS(cudaMemcpy(s->d_a[0], s->d_X + (size_t)i * net.cin0 * RR, sizeof(float) * net.cin0 * RR,
                        cudaMemcpyDeviceToDevice));
-        ap::net_forward(net, 1, R, s->d_a, 0);
+        ap::net_infer(net, 1, R, s->d_a[0], s->d_a, s->d_a[kSurrLayers], 0);
         ap::sg::diff_norms_kernel<<<ap::grid_for(ny), 256>>>(ny, s->d_a[kSurrLayers], s->d_T + (size_t)i * ny,
                                                              s->d_lpart, s->d_cnt + 1, s->d_loss);
         float nm[2];

@@ -339,6 +339,25 @@ def test_field_bf16x3_full_size_vs_fp32(ap):
     assert np.abs(ex2 - 2 * ex).max() <= 1e-6 * np.abs(ex).max()
 
 
+@pytest.mark.parametrize("m", [256, 1024])
+def test_field_bf16x3_repeatable(ap, m):
+    """The split-K clusters sum their partials in a fixed order through
+    distributed shared memory: repeated solves of one map are bit-identical
+    (a CTA writing a peer's buffers too early would show up here)."""
+    rng = np.random.default_rng(m)
+    d = density_like(m, rng)
+    nl = ap.synth.generate("c0", seed=1)
+    with ap.Placer(nl, bins=m) as pl:
+        ex0, ey0 = pl.compute_electric_fields(d, "bf16x3")
+        for _ in range(12):
+            ex, ey = pl.compute_electric_fields(d, "bf16x3")
+            np.testing.assert_array_equal(ex, ex0)
+            np.testing.assert_array_equal(ey, ey0)
+        fx, fy = pl.compute_electric_fields(d, "fp32")
+    assert np.abs(ex0 - fx).max() <= 1e-4 * np.abs(fx).max()
+    assert np.abs(ey0 - fy).max() <= 1e-4 * np.abs(fy).max()
+
+
 def test_loop_bf16x3_matches_fp32_loop(ap):
     """Same netlist, both solvers: the mixed-precision loop reaches the target
     with HPWL within 1% of the plain FP32 loop."""

@@ -34,7 +34,7 @@ def random_params(s, rng, scale=0.15):
     return (scale * rng.standard_normal(s.num_params)).astype(np.float32)
 
 
-@pytest.mark.parametrize("kernels", [(3, 1, 1, 3), (1, 3, 3, 1)])
+@pytest.mark.parametrize("kernels", [(3, 1, 1, 3), (1, 3, 3, 1), (3, 1, 1, 1), (1, 1, 1, 1)])
 def test_forward_and_gradient_match_oracle(ap, oracle_lib, kernels):
     rng = np.random.default_rng(7)
     f, R, B, margin = 2, 32, 2, 2
@@ -54,6 +54,22 @@ def test_forward_and_gradient_match_oracle(ap, oracle_lib, kernels):
         assert abs(loss - lr) <= 1e-5 * lr
         assert np.abs(g - gr).max() <= 1e-3 * np.abs(gr).max()
         assert float(g @ gr) / (np.linalg.norm(g) * np.linalg.norm(gr)) >= 0.99999
+
+
+@pytest.mark.parametrize("kernels,width,f,R", [((3, 1, 1, 1), 32, 4, 64), ((3, 1, 1, 1), 16, 2, 48),
+                                                ((1, 1, 1, 1), 24, 1, 32)])
+def test_fused_forward_matches_layer_by_layer(ap, kernels, width, f, R):
+    """Inference runs (K0, 1, 1, 1) nets as one fused launch; training runs the
+    layers one by one (it keeps the hidden maps).  Same arithmetic in the same
+    order: with the fused output as the training target, the training
+    forward's loss is exactly zero."""
+    rng = np.random.default_rng(R)
+    with ap.Surrogate(factor=f, kernels=kernels, width=width) as s:
+        s.set_params(random_params(s, rng))
+        x = rng.standard_normal((2, s.cin, R, R)).astype(np.float32)
+        y = s.forward(x)
+        loss, _ = s.gradient(x, y, 0)
+        assert loss == 0.0
 
 
 def collect_run(ap, s, n, every, seed):
