@@ -301,6 +301,46 @@ def test_loop_c0_reaches_target_like_oracle(ap, oracle_lib):
     assert abs(s["iteration"] - rs["iteration"]) <= 0.2 * rs["iteration"], (s, rs)
 
 
+_ORACLE_RUNS = {}
+
+
+def clustered_start(nl, seed):
+    """Movable cells at the die centre plus N(0, 1 site), seeded."""
+    rng = np.random.default_rng(seed)
+    W, H = float(nl["die"][2]), float(nl["die"][3])
+    x0, y0 = nl["node_x"].copy(), nl["node_y"].copy()
+    mov = nl["node_fixed"] == 0
+    x0[mov] = (W / 2 + rng.standard_normal(mov.sum())).astype(np.float32)
+    y0[mov] = (H / 2 + rng.standard_normal(mov.sum())).astype(np.float32)
+    return x0, y0
+
+
+@pytest.mark.parametrize("solver", ["fp32", "bf16x3"])
+@pytest.mark.parametrize("seed", [1, 2])
+def test_loop_final_hpwl_and_overflow_match_oracle(ap, oracle_lib, solver, seed):
+    """20k cells, 128^2 bins, target density 0.7, run to overflow < 0.10 from
+    the same seeded start: the GPU loop's final HPWL within 0.5% and final
+    overflow within 0.005 of the FP64 oracle loop's (measured: 0.015-0.083%
+    and < 0.0015).  On the 576-cell case the stopping iteration is too
+    sensitive for this bound (see test_loop_c0_reaches_target_like_oracle)."""
+    nl = ap.synth.generate("c1_small", seed=seed)
+    x0, y0 = clustered_start(nl, seed)
+    if seed not in _ORACLE_RUNS:
+        ref = oracle_lib.Placer(nl, 128, 0.7)
+        ref.init(x0, y0)
+        while ref.stats()["overflow"] >= 0.10 and ref.stats()["iteration"] < 4000:
+            ref.step(1)
+        _ORACLE_RUNS[seed] = ref.stats()
+    rs = _ORACLE_RUNS[seed]
+    with ap.Placer(nl, bins=128, target_density=0.7, check_interval=1, field_solver=solver) as pl:
+        pl.initialize_placement(x0, y0)
+        pl.run()
+        s = pl.stats()
+    assert s["overflow"] < 0.10 and rs["overflow"] < 0.10
+    assert abs(s["hpwl"] - rs["hpwl"]) <= 0.005 * rs["hpwl"], (s, rs)
+    assert abs(s["overflow"] - rs["overflow"]) <= 0.005, (s, rs)
+
+
 def density_like(m, rng):
     """A placement-like density: ~0.8 background, a dense cluster, an empty macro."""
     d = (0.8 + 0.1 * rng.standard_normal((m, m))).astype(np.float32)
