@@ -312,6 +312,24 @@ def time_to_target(ap, nl, solver, target=0.10, max_iter=4000, surrogate=None, u
     return out
 
 
+def c4_block(ap):
+    """The learned surrogate's own workload: 200k cells, 512^2 bins, the
+    surrogate on the 256^2-pooled density (factor 2), trained here as for
+    C2; time to 10% overflow of the plain, mixed and mixed + surrogate forms."""
+    nl = ap.synth.generate("c1", seed=1)
+    out = {"workload": "c1: 200000 movable cells, 4000 fixed macros, 210000 nets, 512x512 bins, target "
+                       "density 0.7, seed 1; surrogate factor 2 (256x256 coarse grid)",
+           "plain": time_to_target(ap, nl, "fp32"), "mixed": time_to_target(ap, nl, "bf16x3")}
+    surr, info = train_surrogate(ap, "c1", "bf16x3")
+    out["surrogate_training"] = info
+    out["mixed_surrogate"] = time_to_target(ap, nl, "bf16x3", surrogate=surr, use_net=True)
+    out["mixed_surrogate_coarse_only"] = time_to_target(ap, nl, "bf16x3", surrogate=surr, use_net=False)
+    surr.close()
+    for k in ("mixed", "mixed_surrogate", "mixed_surrogate_coarse_only"):
+        out[k]["speedup_vs_plain"] = out["plain"]["seconds"] / out[k]["seconds"]
+    return out
+
+
 def train_surrogate(ap, preset: str, solver: str):
     """The learned surrogate of the mixed+surrogate form, trained here on the GPU
     by the library's own kernels: 140 (density, field) pairs from the exact
@@ -351,6 +369,8 @@ def main():
     ap_.add_argument("--solver", default="auto", choices=["auto", "fp32", "bf16x3"])
     ap_.add_argument("--no-cpu-baseline", action="store_true")
     ap_.add_argument("--no-ttt", action="store_true", help="skip the time-to-10%% runs")
+    ap_.add_argument("--no-c4", action="store_true",
+                     help="skip the surrogate's own workload (200k cells, 512^2 bins, 256^2 coarse grid)")
     ap_.add_argument("--batch", type=int, default=0,
                      help="batched form instead: this many instances (5k-150k cells) in one graph")
     ap_.add_argument("--profile-after", type=int, default=-1,
@@ -500,6 +520,8 @@ def main():
                 plain_s = ttt["plain"]["seconds"]
                 for k in ("mixed", "mixed_surrogate", "mixed_surrogate_coarse_only"):
                     ttt[k]["speedup_vs_plain"] = plain_s / ttt[k]["seconds"]
+            if solver == "bf16x3" and not args.no_c4:
+                ttt["c4"] = c4_block(ap)
         if not args.no_cpu_baseline:
             cpu = cpu_baseline(nl)
         line = {
