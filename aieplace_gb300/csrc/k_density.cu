@@ -260,9 +260,11 @@ __global__ void __launch_bounds__(kScatterThreads, 2) scatter_kernel(ScatterArgs
     }
     const int W = use_win ? wc * wr : 0;
     // Clustered chunk (e.g. right after initial placement, every node in a few
-    // bins): one private window per warp, and the lanes of a warp that add to
-    // the same slot are summed first (exact: three 21-bit chunks through
-    // redux), so no two adds in flight hit one address.
+    // bins): one private window per warp.  In every window the lanes of a warp
+    // that add to the same slot are summed first (exact: three 21-bit chunks
+    // through redux), so no two adds of one instruction hit one address: in
+    // the first hundreds of iterations this took the scatter from 264 to
+    // 170 us (2M cells), at 6% extra cost mid-run.
     const bool clustered = use_win && W <= kScatterWindow / kScatterWarps;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     if (use_win) {
@@ -278,7 +280,7 @@ __global__ void __launch_bounds__(kScatterThreads, 2) scatter_kernel(ScatterArgs
             return;
         }
         const int slot = (c - wc0) * wr + (r - wr0);
-        if (clustered) {
+        {
             const unsigned peers = __match_any_sync(__activemask(), slot);
             if (peers != (1u << lane)) {
                 const ull u = (ull)v;
