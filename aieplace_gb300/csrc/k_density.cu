@@ -140,19 +140,54 @@ __device__ __forceinline__ void for_each_overlap(const Grid &g, float x, float y
     }
 }
 
-__global__ void __launch_bounds__(kScatterThreads, 2) scatter_kernel(ScatterArgs a) {
+// Update mode, first of the two launches: the Nesterov step of every movable
+// node from the accepted state (buffers [cur]) to the trial point (buffers
+// [1 - cur]) and the node's bin record there, one node per thread -- a
+// streaming pass; block sums of |u' - u|^2 folded by the last block.  Split
+// from the bin adds, which need few threads per SM's worth of registers and
+// shared memory, so that this part runs at full occupancy.
+__global__ void __launch_bounds__(kThreads) update_kernel(ScatterArgs a) {
     __shared__ double red[32];
+    const float alpha = a.sc->f_alpha, mom = a.sc->f_mom;
+    const int cur = a.sc->cur, nxt = 1 - cur;
+    const Grid g = a.g;
+    float du = 0.f;  // per-thread partial in FP32; FP64 from the block sum on
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n_mov; i += gridDim.x * blockDim.x) {
+        const float w = __ldg(a.w + i), h = __ldg(a.h + i);
+        const float xhi = fmaxf(a.die_w - w, 0.f), yhi = fmaxf(a.die_h - h, 0.f);
+        const float ux = a.ux[cur][i], uy = a.uy[cur][i];
+        const float nux = clampf(a.vx[cur][i] - alpha * a.gx[cur][i], 0.f, xhi);
+        const float nuy = clampf(a.vy[cur][i] - alpha * a.gy[cur][i], 0.f, yhi);
+        const float x = clampf(nux + mom * (nux - ux), 0.f, xhi);
+        const float y = clampf(nuy + mom * (nuy - uy), 0.f, yhi);
+        a.ux[nxt][i] = nux;
+        a.uy[nxt][i] = nuy;
+        a.vx[nxt][i] = x;
+        a.vy[nxt][i] = y;
+        du += (nux - ux) * (nux - ux) + (nuy - uy) * (nuy - uy);
+        int c0, c1, r0, r1;
+        const NodeRec r = make_rec(g, x, y, w, h, c0, c1, r0, r1);
+        a.rec_bin[i] = r.bin;
+        a.rec_ov[i] = make_int4(r.xr, r.wq, r.yr, r.hq);
+    }
+    float *pf = reinterpret_cast<float *>(a.partials);
+    const float dub = block_sum_ff(du, reinterpret_cast<float *>(red));
+    if (threadIdx.x == 0) pf[blockIdx.x] = dub;
+    if (arrive_last(a.counter)) {
+        const double t = block_sum_f(kahan_strided(pf, threadIdx.x, gridDim.x, blockDim.x, 1), red);
+        if (threadIdx.x == 0) {
+            a.sc->t_du = t;
+            *a.counter = 0u;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kScatterThreads, 2) scatter_kernel(ScatterArgs a) {
     __shared__ int box[8];  // bin bounding box of the chunk: c0, c1, r0, r1; sums of c0, r0; count; inside
     __shared__ ull win[kScatterWindow];
     const int n = a.update ? a.n_mov : (a.hi - a.lo);
-    float alpha = 0.f, mom = 0.f;
-    int cur = 0;
-    if (a.update) {
-        alpha = a.sc->f_alpha;
-        mom = a.sc->f_mom;
-        cur = a.sc->cur;
-    }
-    const int nxt = 1 - cur;
+    // update mode: the trial point and its records come from update_kernel
+    const int nxt = a.update ? 1 - a.sc->cur : 0;
     const Grid g = a.g;
     if (threadIdx.x == 0) {
         box[0] = box[2] = 0x7fffffff;
@@ -160,7 +195,6 @@ __global__ void __launch_bounds__(kScatterThreads, 2) scatter_kernel(ScatterArgs
         box[4] = box[5] = box[6] = box[7] = 0;
     }
     __syncthreads();
-    float du = 0.f;  // per-thread partial in FP32; FP64 from the block sum on
     NodeRec rec[kScatterPerThread];
     int bc0 = 0x7fffffff, bc1 = -1, br0 = 0x7fffffff, br1 = -1;
     const int base = blockIdx.x * kScatterChunk;
@@ -169,30 +203,27 @@ __global__ void __launch_bounds__(kScatterThreads, 2) scatter_kernel(ScatterArgs
         const int i = base + k * kScatterThreads + threadIdx.x;
         rec[k].bin = kRecNone;
         if (i >= n) continue;
-        const int node = a.update ? i : a.lo + i;
-        const float w = __ldg(a.w + node), h = __ldg(a.h + node);
-        float x, y;
-        if (a.update) {
-            const float xhi = fmaxf(a.die_w - w, 0.f), yhi = fmaxf(a.die_h - h, 0.f);
-            const float ux = a.ux[cur][i], uy = a.uy[cur][i];
-            const float nux = clampf(a.vx[cur][i] - alpha * a.gx[cur][i], 0.f, xhi);
-            const float nuy = clampf(a.vy[cur][i] - alpha * a.gy[cur][i], 0.f, yhi);
-            x = clampf(nux + mom * (nux - ux), 0.f, xhi);
-            y = clampf(nuy + mom * (nuy - uy), 0.f, yhi);
-            a.ux[nxt][i] = nux;
-            a.uy[nxt][i] = nuy;
-            a.vx[nxt][i] = x;
-            a.vy[nxt][i] = y;
-            du += (nux - ux) * (nux - ux) + (nuy - uy) * (nuy - uy);
-        } else {
-            x = __ldg(a.px + node);
-            y = __ldg(a.py + node);
-        }
         int c0, c1, r0, r1;
-        rec[k] = make_rec(g, x, y, w, h, c0, c1, r0, r1);
-        if (a.update && a.rec_bin) {
-            a.rec_bin[i] = rec[k].bin;
-            a.rec_ov[i] = make_int4(rec[k].xr, rec[k].wq, rec[k].yr, rec[k].hq);
+        if (a.update) {
+            const int bin = a.rec_bin[i];
+            const int4 o = a.rec_ov[i];
+            rec[k] = NodeRec{bin, o.x, o.y, o.z, o.w};
+            c1 = r1 = -1;
+            if (bin >= 0) {
+                c0 = rec_c0(bin);
+                r0 = rec_r0(bin);
+                c1 = (bin & kRecSmall) ? c0 : c0 + rec_nc(bin) - 1;
+                r1 = (bin & kRecSmall) ? r0 : r0 + rec_nr(bin) - 1;
+            } else if (bin == kRecFull) {
+                bool small;
+                if (!bin_range(g, a.vx[nxt][i], a.vy[nxt][i], __ldg(a.w + i), __ldg(a.h + i), c0, c1, r0, r1,
+                               small))
+                    c1 = r1 = -1;
+            }
+        } else {
+            const int node = a.lo + i;
+            rec[k] = make_rec(g, __ldg(a.px + node), __ldg(a.py + node), __ldg(a.w + node), __ldg(a.h + node), c0,
+                              c1, r0, r1);
         }
         if (c1 >= 0) {
             bc0 = min(bc0, c0);
@@ -334,23 +365,18 @@ __global__ void __launch_bounds__(kScatterThreads, 2) scatter_kernel(ScatterArgs
             }
         }
     }
-    if (!a.update) return;
-    float *pf = reinterpret_cast<float *>(a.partials);
-    const float dub = block_sum_ff(du, reinterpret_cast<float *>(red));
-    if (threadIdx.x == 0) pf[blockIdx.x] = dub;
-    if (arrive_last(a.counter)) {
-        const double t = block_sum_f(kahan_strided(pf, threadIdx.x, gridDim.x, blockDim.x, 1), red);
-        if (threadIdx.x == 0) {
-            a.sc->t_du = t;
-            *a.counter = 0u;
-        }
-    }
 }
 
 void launch_scatter(const ScatterArgs &a, cudaStream_t st) {
     const int n = a.update ? a.n_mov : (a.hi - a.lo);
     if (n <= 0) return;
-    const int blocks = (n + kScatterChunk - 1) / kScatterChunk;  // <= 8192 partials for 16M nodes
+    if (a.update) {
+        // one node per thread up to 8192 blocks (the partials buffer), grid-stride beyond
+        int ub = (n + kThreads - 1) / kThreads;
+        if (ub > 8192) ub = 8192;
+        update_kernel<<<ub, kThreads, 0, st>>>(a);
+    }
+    const int blocks = (n + kScatterChunk - 1) / kScatterChunk;
     scatter_kernel<<<blocks, kScatterThreads, 0, st>>>(a);
 }
 

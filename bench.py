@@ -39,7 +39,7 @@ sys.path.insert(0, os.path.join(HERE, "oracle"))
 
 METRIC = "Nesterov iters/s & time-to-10% overflow, 2M cells: mixed+surrogate vs plain"
 UNIT = "iters/s"
-KERNELS_PER_TRIAL = 11  # scatter, rho, 4x WA (degree buckets), 4x field, gather
+KERNELS_PER_TRIAL = 12  # update, scatter, rho, 4x WA (degree buckets), 4x field, gather
 STAGES = ["scatter+update", "density+overflow", "wirelength", "field", "gather+control"]
 
 
