@@ -214,6 +214,18 @@ __device__ __forceinline__ long long overlap_1d(long long lo_bin, long long span
     return (hi_bin < hi ? hi_bin : hi) - (lo_bin > lo ? lo_bin : lo);
 }
 
+// The same integer in 32-bit arithmetic, for bin records, whose values and
+// sums are checked to fit when the record is made
+__device__ __forceinline__ int overlap_1d32(int lo_bin, int span, int lo, int len) {
+    return min(lo_bin + span, lo + len) - max(lo_bin, lo);
+}
+
+// float of a non-negative 32-bit fixed-point value: exact below 2^22, else as
+// i64_to_float
+__device__ __forceinline__ float i32_to_float(int q) {
+    return q < 4194304 ? i2f_small(q) : i64_to_float((long long)q);
+}
+
 template <typename T>
 __device__ __forceinline__ T warp_sum(T v) {
 #pragma unroll

@@ -58,8 +58,10 @@ constexpr int kScatterWindowSide = 64;  // window columns when the bounding box 
 // node's fixed-point x and y relative to the base bin's corner and its
 // fixed-point width and height.  Column c0 + j overlaps the node by
 // overlap_1d(j bw, bw, xr, wq) -- the same integer as from absolute
-// coordinates.  Nodes that span more bins, or whose extents do not fit int32,
-// are re-evaluated in full (kRecFull).  Bin counts are at most 4096 per axis.
+// coordinates, evaluated in 32-bit arithmetic (a record is made only when its
+// values and their sums fit int32).  Nodes that span more bins, or whose
+// extents do not fit, are re-evaluated in full (kRecFull).  Bin counts are at
+// most 4096 per axis.
 constexpr int kRecNone = -1, kRecFull = -2;
 constexpr int kRecSmall = 1 << 30, kRecMaxSpan = 8;
 
@@ -95,8 +97,11 @@ __device__ __forceinline__ NodeRec make_rec(const Grid &g, float x, float y, flo
         return r;
     }
     const long long xr = to_q(x) - (long long)c0 * g.bw_q, yr = to_q(y) - (long long)r0 * g.bh_q;
+    // every integer of emit_rec / the gather's record path must fit int32:
+    // xr + wq, yr + hq and (span + 1) bin widths
     if (c1 - c0 >= kRecMaxSpan || r1 - r0 >= kRecMaxSpan || !fits_i32(xr) || !fits_i32(yr) || !fits_i32(wq) ||
-        !fits_i32(hq)) {
+        !fits_i32(hq) || !fits_i32(xr + wq) || !fits_i32(yr + hq) || g.bw_q * (kRecMaxSpan + 1) > 2147483647ll ||
+        g.bh_q * (kRecMaxSpan + 1) > 2147483647ll) {
         r.bin = kRecFull;
         return r;
     }
@@ -119,8 +124,9 @@ __device__ __forceinline__ void emit_rec(const Grid &g, int bin, int xr, int wq,
     }
     const int nc = rec_nc(bin), nr = rec_nr(bin);
     for (int j = 0; j < nc; ++j) {
-        const long long ow = overlap_1d((long long)j * g.bw_q, g.bw_q, xr, wq);
-        for (int k = 0; k < nr; ++k) add(c0 + j, r0 + k, ow * overlap_1d((long long)k * g.bh_q, g.bh_q, yr, hq));
+        const int bw = (int)g.bw_q, bh = (int)g.bh_q;  // record bins: (span + 1) widths fit int32
+        const int ow = overlap_1d32(j * bw, bw, xr, wq);
+        for (int k = 0; k < nr; ++k) add(c0 + j, r0 + k, (long long)ow * overlap_1d32(k * bh, bh, yr, hq));
     }
 }
 
@@ -577,10 +583,10 @@ __global__ void __launch_bounds__(kThreads) gather_kernel(GatherArgs a) {
             } else {
                 const int nc = rec_nc(rb), nr = rec_nr(rb);
                 for (int j = 0; j < nc; ++j) {
-                    const float fw = i64_to_float(overlap_1d((long long)j * g.bw_q, g.bw_q, o.x, o.y));
+                    const float fw = i32_to_float(overlap_1d32(j * (int)g.bw_q, (int)g.bw_q, o.x, o.y));
                     const int bc = (c0r + j) * g.my + r0r;
                     for (int k = 0; k < nr; ++k) {
-                        const float fh = i64_to_float(overlap_1d((long long)k * g.bh_q, g.bh_q, o.z, o.w));
+                        const float fh = i32_to_float(overlap_1d32(k * (int)g.bh_q, (int)g.bh_q, o.z, o.w));
                         const float wt = (fw * fh) * g.inv_ab;
                         fx += wt * __ldg(a.ex + bc + k);
                         fy += wt * __ldg(a.ey + bc + k);
