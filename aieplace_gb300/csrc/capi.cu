@@ -362,6 +362,31 @@ int read_scalars(ap_handle *h) {
     return sync(h);
 }
 
+// Positions of the accepted buffer (device scalar `cur`) <-> staging arrays,
+// on the device, so the host needs no round trip to learn `cur`:
+// to_cur = 1: s -> [cur] for the first n nodes, else [cur] -> s.
+__global__ void stage_cur_kernel(int n, int to_cur, const DevScalars *sc, float *x0, float *y0, float *x1, float *y1,
+                                 float *sx, float *sy) {
+    const int cur = sc->cur;
+    float *x = cur ? x1 : x0, *y = cur ? y1 : y0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        if (to_cur) {
+            x[i] = sx[i];
+            y[i] = sy[i];
+        } else {
+            sx[i] = x[i];
+            sy[i] = y[i];
+        }
+    }
+}
+
+void stage_cur(ap_handle *h, int n, int to_cur) {
+    if (n <= 0) return;
+    const int blocks = std::min((n + kThreads - 1) / kThreads, 4096);
+    stage_cur_kernel<<<blocks, kThreads, 0, h->stream>>>(n, to_cur, h->d_sc, h->d_px[0], h->d_py[0], h->d_px[1],
+                                                         h->d_py[1], h->d_sx, h->d_sy);
+}
+
 void fill_stats(const ap_handle *h, ap_stats *s) {
     const DevScalars &c = *h->h_sc;
     s->iteration = c.iteration;
@@ -903,6 +928,28 @@ int ap_step_host(ap_handle *h, const float *x_in, const float *y_in, float *x_ou
     if (!h) return AP_ERR_INVALID_ARG;
     if (!h->initialized) return AP_ERR_STATE;
     const bool direct = h->identity && h->die_xl == 0.f && h->die_yl == 0.f;
+    if (direct && h->p.max_backtracks == 0) {
+        // Without backtracking every trial is accepted: one trial is the
+        // iteration, and positions move through the staging arrays by device
+        // kernels that read `cur` themselves -- one host round trip per call.
+        if (x_in && y_in) {
+            CK(cudaMemcpyAsync(h->d_sx, x_in, sizeof(float) * h->n_mov, cudaMemcpyHostToDevice, h->stream));
+            CK(cudaMemcpyAsync(h->d_sy, y_in, sizeof(float) * h->n_mov, cudaMemcpyHostToDevice, h->stream));
+            stage_cur(h, h->n_mov, 1);
+        }
+        int r = launch_trials(h, 1);
+        if (r != AP_OK) return r;
+        if (x_out && y_out) {
+            stage_cur(h, h->n_nodes, 0);
+            CK(cudaMemcpyAsync(x_out, h->d_sx, sizeof(float) * h->n_nodes, cudaMemcpyDeviceToHost, h->stream));
+            CK(cudaMemcpyAsync(y_out, h->d_sy, sizeof(float) * h->n_nodes, cudaMemcpyDeviceToHost, h->stream));
+        }
+        CK(cudaGetLastError());
+        r = read_scalars(h);
+        if (r != AP_OK) return r;
+        if (stats) fill_stats(h, stats);
+        return h->h_sc->status;
+    }
     int r = read_scalars(h);
     if (r != AP_OK) return r;
     if (x_in && y_in) {
