@@ -36,7 +36,11 @@ struct DevScalars {
     double a_k;
     double a_next;      // a_{k+1} for the current iteration
     double lambda;
-    double gamma;
+    // WA smoothing of the next evaluation.  A loop trial's WA uses gamma(tau)
+    // of the previous evaluation (one-evaluation lag), so the WA launches do
+    // not wait for the trial's own density: rho writes gamma_next, the
+    // gather's last block makes it current.
+    double gamma, gamma_next;
     double hpwl, hpwl_prev, wa;      // accepted point
     double tau, tau_abs;             // accepted point
     double t_hpwl, t_wa, t_tau, t_tau_abs, t_du;  // last trial

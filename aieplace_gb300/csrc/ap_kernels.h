@@ -71,6 +71,10 @@ struct ScatterArgs {
     int4 *rec_ov;
 };
 void launch_scatter(const ScatterArgs &a, cudaStream_t st);
+// the two launches of launch_scatter: the position update and records (update
+// mode only), then the bin adds
+void launch_update(const ScatterArgs &a, cudaStream_t st);
+void launch_scatter_bins(const ScatterArgs &a, cudaStream_t st);
 
 // ---- density map -> solver input + overflow ---------------------------------
 enum { RHO_OUT_ONLY = 0, RHO_LOOP = 1, RHO_INIT = 2 };

@@ -79,6 +79,9 @@ struct ap_handle {
     ap_surrogate *surr = nullptr;
     SurrState surr_state{};
     cudaStream_t side = nullptr;  // captures the field-switch bodies
+    // the WA launches of a trial run beside scatter -> rho -> field
+    cudaStream_t wa_stream = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     ap_surrogate_policy policy{0.3f, 8, 0.02f, 1};
 };
 
@@ -236,11 +239,29 @@ int enqueue_field_surrogate(ap_handle *h, cudaStream_t st, int branch) {
     return AP_OK;
 }
 
+// The WA launches of a trial on their own stream, after the position update
+// and joined before the gather (fork_wa / join_wa): the WA gradient needs the
+// trial point and the previous evaluation's gamma, not this trial's density.
+int fork_wa(ap_handle *h, cudaStream_t st) {
+    CK(cudaEventRecord(h->ev_fork, st));
+    CK(cudaStreamWaitEvent(h->wa_stream, h->ev_fork, 0));
+    launch_wirelength(wa_args(h, h->d_px[0], h->d_py[0], 0.f, h->n_mov, WA_LOOP, nullptr), h->wa_stream);
+    CK(cudaEventRecord(h->ev_join, h->wa_stream));
+    return AP_OK;
+}
+
+int join_wa(ap_handle *h, cudaStream_t st) {
+    CK(cudaStreamWaitEvent(st, h->ev_join, 0));
+    return AP_OK;
+}
+
 int enqueue_iteration(ap_handle *h, cudaStream_t st) {
-    launch_scatter(loop_scatter_args(h), st);
+    const ScatterArgs sa = loop_scatter_args(h);
+    launch_update(sa, st);
+    int r = fork_wa(h, st);
+    if (r != AP_OK) return r;
+    launch_scatter_bins(sa, st);
     launch_rho(rho_args(h, RHO_LOOP, nullptr), st);
-    launch_wirelength(wa_args(h, h->d_px[0], h->d_py[0], 0.f, h->n_mov, WA_LOOP, nullptr), st);
-    int r;
     if (h->surr) {
         r = enqueue_field_surrogate(h, st, -1);
         if (r != AP_OK) return r;
@@ -248,6 +269,8 @@ int enqueue_iteration(ap_handle *h, cudaStream_t st) {
         r = run_field(h, h->p.field_solver, st);
         if (r != AP_OK) return r;
     }
+    r = join_wa(h, st);
+    if (r != AP_OK) return r;
     launch_gather(loop_gather_args(h), st);
     return cudaGetLastError() == cudaSuccess ? AP_OK : AP_ERR_CUDA;
 }
@@ -295,11 +318,14 @@ int capture_trial_switched(ap_handle *h) {
     CK(cudaStreamGetCaptureInfo(st, &cs, nullptr, &cg, nullptr, nullptr, nullptr));
     cudaGraphConditionalHandle sw_handle;
     CK(cudaGraphConditionalHandleCreate(&sw_handle, cg, kFieldExact, cudaGraphCondAssignDefault));
-    launch_scatter(loop_scatter_args(h), st);
+    const ScatterArgs sa = loop_scatter_args(h);
+    launch_update(sa, st);
+    const int fr = fork_wa(h, st);
+    if (fr != AP_OK) return fr;
+    launch_scatter_bins(sa, st);
     RhoArgs ra = rho_args(h, RHO_LOOP, nullptr);
     ra.field_switch = sw_handle;
     launch_rho(ra, st);
-    launch_wirelength(wa_args(h, h->d_px[0], h->d_py[0], 0.f, h->n_mov, WA_LOOP, nullptr), st);
     const cudaGraphNode_t *dp = nullptr;
     size_t nd = 0;
     CK(cudaStreamGetCaptureInfo(st, &cs, nullptr, nullptr, &dp, nullptr, &nd));
@@ -321,6 +347,8 @@ int capture_trial_switched(ap_handle *h) {
         CK(e);
     }
     CK(cudaStreamUpdateCaptureDependencies(st, &sw, nullptr, 1, cudaStreamSetCaptureDependencies));
+    const int jr = join_wa(h, st);
+    if (jr != AP_OK) return jr;
     launch_gather(loop_gather_args(h), st);
     return cudaGetLastError() == cudaSuccess ? AP_OK : AP_ERR_CUDA;
 }
@@ -693,6 +721,9 @@ int ap_create(const ap_netlist *nl, const ap_params *params, ap_handle **out) {
     A(cudaMallocHost((void **)&h->h_out, sizeof(double) * 8));
     A(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
     h->own_stream = true;
+    A(cudaStreamCreateWithFlags(&h->wa_stream, cudaStreamNonBlocking));
+    A(cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming));
+    A(cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming));
     if (!ok) {
         ap_destroy(h);
         return AP_ERR_CUDA;
@@ -759,6 +790,9 @@ int ap_destroy(ap_handle *h) {
     destroy_graphs(h);
     surr_state_free(h->surr_state);
     if (h->side) cudaStreamDestroy(h->side);
+    if (h->wa_stream) cudaStreamDestroy(h->wa_stream);
+    if (h->ev_fork) cudaEventDestroy(h->ev_fork);
+    if (h->ev_join) cudaEventDestroy(h->ev_join);
     field_solver_free(h->fs);
     void *ptrs[] = {h->d_net_ptr, h->d_pin_node, h->d_w,      h->d_h,       h->d_px[0], h->d_px[1],
                     h->d_py[0],   h->d_py[1],    h->d_gx[0],  h->d_gx[1],   h->d_gy[0], h->d_gy[1],
@@ -1112,7 +1146,7 @@ int ap_snapshot(ap_handle *h, void *buf, size_t bytes) {
     if (!h->initialized) return AP_ERR_STATE;
     CK(cudaStreamSynchronize(h->stream));
     char *p = (char *)buf;
-    int32_t hdr[4] = {0x41505334, h->n_nodes, h->n_mov, 0};
+    int32_t hdr[4] = {0x41505335, h->n_nodes, h->n_mov, 0};
     memcpy(p, hdr, sizeof(hdr));
     p += sizeof(hdr);
     CK(cudaMemcpy(p, h->d_sc, sizeof(DevScalars), cudaMemcpyDeviceToHost));
@@ -1136,7 +1170,7 @@ int ap_restore(ap_handle *h, const void *buf, size_t bytes) {
     const char *p = (const char *)buf;
     int32_t hdr[4];
     memcpy(hdr, p, sizeof(hdr));
-    if (hdr[0] != 0x41505334 || hdr[1] != h->n_nodes || hdr[2] != h->n_mov) return AP_ERR_INVALID_ARG;
+    if (hdr[0] != 0x41505335 || hdr[1] != h->n_nodes || hdr[2] != h->n_mov) return AP_ERR_INVALID_ARG;
     p += sizeof(hdr);
     CK(cudaStreamSynchronize(h->stream));
     CK(cudaMemcpy(h->d_sc, p, sizeof(DevScalars), cudaMemcpyHostToDevice));

@@ -373,17 +373,24 @@ __global__ void __launch_bounds__(kScatterThreads, 2) scatter_kernel(ScatterArgs
     }
 }
 
-void launch_scatter(const ScatterArgs &a, cudaStream_t st) {
+void launch_update(const ScatterArgs &a, cudaStream_t st) {
+    if (!a.update || a.n_mov <= 0) return;
+    // one node per thread up to 8192 blocks (the partials buffer), grid-stride beyond
+    int ub = (a.n_mov + kThreads - 1) / kThreads;
+    if (ub > 8192) ub = 8192;
+    update_kernel<<<ub, kThreads, 0, st>>>(a);
+}
+
+void launch_scatter_bins(const ScatterArgs &a, cudaStream_t st) {
     const int n = a.update ? a.n_mov : (a.hi - a.lo);
     if (n <= 0) return;
-    if (a.update) {
-        // one node per thread up to 8192 blocks (the partials buffer), grid-stride beyond
-        int ub = (n + kThreads - 1) / kThreads;
-        if (ub > 8192) ub = 8192;
-        update_kernel<<<ub, kThreads, 0, st>>>(a);
-    }
     const int blocks = (n + kScatterChunk - 1) / kScatterChunk;
     scatter_kernel<<<blocks, kScatterThreads, 0, st>>>(a);
+}
+
+void launch_scatter(const ScatterArgs &a, cudaStream_t st) {
+    launch_update(a, st);
+    launch_scatter_bins(a, st);
 }
 
 // gamma(tau) in FP32 (10^e as 2^(e log2 10)): a single-thread FP64 pow at the
@@ -472,7 +479,11 @@ __global__ void __launch_bounds__(kThreads) rho_kernel(RhoArgs a) {
             if (a.mode != RHO_OUT_ONLY) {
                 sc->t_tau = tau;
                 sc->t_tau_abs = tau_abs;
-                sc->gamma = gamma_of(sc, tau);
+                sc->gamma_next = gamma_of(sc, tau);
+            }
+            if (a.mode == RHO_INIT) {
+                // the first evaluation's WA uses its own overflow
+                sc->gamma = sc->gamma_next;
                 sc->f_gamma = (float)sc->gamma;
             }
             // field source of this trial: the surrogate while the overflow is
@@ -702,6 +713,9 @@ __global__ void __launch_bounds__(kThreads) gather_kernel(GatherArgs a) {
                 sc->mom = 0.0;
                 if (!isfinite(sc->alpha)) sc->status = 9;
             } else {
+                // the next evaluation's WA smoothing: this trial's gamma(tau),
+                // whether the trial is accepted or not
+                sc->gamma = sc->gamma_next;
                 finish_trial(sc, t0, t1);
             }
             publish_f32(sc);

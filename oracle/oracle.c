@@ -435,8 +435,13 @@ static double gamma_of(const or_placer *o, double tau) {
     return o->p.gamma_base_bins * 0.5 * (o->bw + o->bh) * pow(10.0, e);
 }
 
-/* density, overflow, (gamma), WA gradient + HPWL, field, gather at (x, y) */
-static void evaluate(or_placer *o, int update_gamma) {
+/* density, overflow, WA gradient + HPWL, field, gather at (x, y).
+ * gamma_mode 0: keep gamma; 1: gamma(tau) of this point before the WA terms
+ * (the first evaluation); 2: the WA terms with the current gamma, then
+ * gamma(tau) of this point for the next evaluation (loop trials: a
+ * one-evaluation lag, so that the GPU's WA launches need not wait for the
+ * trial's density). */
+static void evaluate(or_placer *o, int gamma_mode) {
     const int nb = o->p.mx * o->p.my, n = o->n_nodes;
     for (int b = 0; b < nb; ++b) o->rho[b] = 0.0;
     for (int i = 0; i < o->n_mov; ++i) node_overlaps(o, o->x[i], o->y[i], o->w[i], o->h[i], add_cb, o->rho);
@@ -451,7 +456,7 @@ static void evaluate(or_placer *o, int update_gamma) {
     }
     o->tau = over / o->mov_area;
     o->tau_abs = over_abs;
-    if (update_gamma) o->gamma = gamma_of(o, o->tau);
+    if (gamma_mode == 1) o->gamma = gamma_of(o, o->tau);
     for (int i = 0; i < n; ++i) {
         o->xf[i] = (float)o->x[i];
         o->yf[i] = (float)o->y[i];
@@ -489,6 +494,7 @@ static void evaluate(or_placer *o, int update_gamma) {
         o->wa = wa;
         o->hpwl = hp;
     }
+    if (gamma_mode == 2) o->gamma = gamma_of(o, o->tau);
     or_field_solve(o->p.mx, o->p.my, o->bh / o->bw, o->d, NULL, o->ex, o->ey);
 #pragma omp parallel for schedule(static)
     for (int i = 0; i < o->n_mov; ++i) {
@@ -658,7 +664,7 @@ void or_step(or_placer *o, int n) {
                 o->x[i] = clampd(nux + mom * (nux - o->ux[i]), 0.0, o->die_w - o->w[i]);
                 o->y[i] = clampd(nuy + mom * (nuy - o->uy[i]), 0.0, o->die_h - o->h[i]);
             }
-            evaluate(o, 1);
+            evaluate(o, 2);
             precond_grad(o, o->gpx, o->gpy);
             o->evals++;
             ahat = lipschitz_step(o, o->x, o->y, o->vpx, o->vpy, o->gpx, o->gpy, o->gx, o->gy);
