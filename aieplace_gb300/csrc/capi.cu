@@ -363,7 +363,7 @@ int build_graphs(ap_handle *h) {
         if (gr) cudaGraphDestroy(gr);
         return r != AP_OK ? r : AP_ERR_CUDA;
     }
-    e = cudaGraphInstantiate(&h->graph, gr, 0);
+    e = cudaGraphInstantiate(&h->graph, gr, cudaGraphInstantiateFlagUseNodePriority);
     cudaGraphDestroy(gr);
     if (e != cudaSuccess) return AP_ERR_CUDA;
     h->graph_ok = true;
@@ -719,9 +719,13 @@ int ap_create(const ap_netlist *nl, const ap_params *params, ap_handle **out) {
     A(dalloc(&h->d_out, 8));
     A(cudaMallocHost((void **)&h->h_sc, sizeof(DevScalars)));
     A(cudaMallocHost((void **)&h->h_out, sizeof(double) * 8));
-    A(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+    // the density chain (scatter -> rho -> field) is the trial's critical
+    // path; the WA launches beside it yield the SMs to it
+    int prio_low = 0, prio_high = 0;
+    A(cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high));
+    A(cudaStreamCreateWithPriority(&h->stream, cudaStreamNonBlocking, prio_high));
     h->own_stream = true;
-    A(cudaStreamCreateWithFlags(&h->wa_stream, cudaStreamNonBlocking));
+    A(cudaStreamCreateWithPriority(&h->wa_stream, cudaStreamNonBlocking, prio_low));
     A(cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming));
     A(cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming));
     if (!ok) {
@@ -1339,7 +1343,7 @@ int batch_build_graph(ap_batch *b) {
         if (gr) cudaGraphDestroy(gr);
         return r != AP_OK ? r : AP_ERR_CUDA;
     }
-    e = cudaGraphInstantiate(&b->graph, gr, 0);
+    e = cudaGraphInstantiate(&b->graph, gr, cudaGraphInstantiateFlagUseNodePriority);
     cudaGraphDestroy(gr);
     return e == cudaSuccess ? AP_OK : AP_ERR_CUDA;
 }
