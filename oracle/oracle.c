@@ -465,10 +465,14 @@ static void evaluate(or_placer *o, int gamma_mode) {
     {
         int32_t np = o->net_ptr[o->n_nets];
         double *px = dalloc((size_t)np), *py = dalloc((size_t)np);
-        double wa = 0, hp = 0;
-#pragma omp parallel for schedule(dynamic, 512) reduction(+ : wa, hp)
+        /* per-net terms summed in net order afterwards: the same sum for any
+         * thread count and schedule (HPWL drives the lambda update, so a
+         * run-dependent last bit would move the loop's trajectory) */
+        double *hpn = dalloc((size_t)o->n_nets + 1), *wan = dalloc((size_t)o->n_nets + 1);
+#pragma omp parallel for schedule(dynamic, 512)
         for (int e = 0; e < o->n_nets; ++e) {
             int s = o->net_ptr[e], dg = o->net_ptr[e + 1] - s;
+            hpn[e] = wan[e] = 0.0;
             if (dg < 2) continue;
             double bxl[64], byl[64];
             double *bx = dg <= 64 ? bxl : dalloc((size_t)dg), *by = dg <= 64 ? byl : dalloc((size_t)dg);
@@ -479,11 +483,18 @@ static void evaluate(or_placer *o, int gamma_mode) {
                 xmx = fmax(xmx, bx[j]); xmn = fmin(xmn, bx[j]);
                 ymx = fmax(ymx, by[j]); ymn = fmin(ymn, by[j]);
             }
-            hp += (xmx - xmn) + (ymx - ymn);
-            wa += wa_net_axis(dg, bx, o->gamma, px + s);
-            wa += wa_net_axis(dg, by, o->gamma, py + s);
+            hpn[e] = (xmx - xmn) + (ymx - ymn);
+            wan[e] = wa_net_axis(dg, bx, o->gamma, px + s);
+            wan[e] += wa_net_axis(dg, by, o->gamma, py + s);
             if (dg > 64) { free(bx); free(by); }
         }
+        double wa = 0, hp = 0;
+        for (int e = 0; e < o->n_nets; ++e) {
+            hp += hpn[e];
+            wa += wan[e];
+        }
+        free(hpn);
+        free(wan);
         for (int i = 0; i < n; ++i) o->wlx[i] = o->wly[i] = 0;
         for (int32_t q = 0; q < np; ++q) {
             o->wlx[o->pin_node[q]] += px[q];
