@@ -249,6 +249,35 @@ def test_loop_deterministic_and_resumable(ap):
     np.testing.assert_array_equal(runs[0][0], runs[1][0])
 
 
+@pytest.mark.parametrize("use_graph", [1, 0])
+def test_caller_stream_matches_own_stream(ap, use_graph):
+    """A trial step forks its wirelength launches onto a library stream and
+    joins before the gather; on a caller's stream (ap_set_stream), captured in
+    a graph or launched eagerly, the loop gives the same bits as on the
+    handle's own stream."""
+    import torch
+
+    nl = ap.synth.generate("c1_small", seed=4)
+    runs = []
+    for caller in (False, True):
+        with ap.Placer(nl, bins=128, use_graph=use_graph) as pl:
+            s = torch.cuda.Stream()
+            if caller:
+                pl.set_stream(s.cuda_stream)
+            pl.initialize_placement(seed=3, sigma=1.0)
+            pl.step_async(60)
+            if caller:
+                ev = torch.cuda.Event()
+                ev.record(s)  # everything of the steps precedes an event on the caller's stream
+                ev.synchronize()
+            runs.append((pl.positions(), pl.stats()))
+    (x0, y0), s0 = runs[0]
+    (x1, y1), s1 = runs[1]
+    np.testing.assert_array_equal(x0, x1)
+    np.testing.assert_array_equal(y0, y1)
+    assert s0["hpwl"] == s1["hpwl"] and s0["iteration"] == s1["iteration"]
+
+
 def test_step_host_matches_device_step(ap):
     nl = ap.synth.generate("c0", seed=1)
     with ap.Placer(nl, bins=32) as a, ap.Placer(nl, bins=32) as b:
