@@ -44,6 +44,7 @@ struct DevScalars {
     double hpwl, hpwl_prev, wa;      // accepted point
     double tau, tau_abs;             // accepted point
     double t_hpwl, t_wa, t_tau, t_tau_abs, t_du;  // last trial
+    double t_dv2;  // last trial: |v_trial - v_accepted|^2 (the position update's sum)
     double du_prev, tau_prev;        // restart tests
     double sum_dv2, sum_dg2, sum_gwl, sum_f;
     double gmax;
@@ -267,6 +268,26 @@ __device__ __forceinline__ double block_sum_f(float v, double *smem /* >= 32 */)
     }
     __syncthreads();
     return d;
+}
+
+// NV block sums entirely in FP32 with one barrier pair (each value in the
+// same shuffle tree as block_sum_ff); valid in thread 0.  smem holds 32 * NV
+// floats; the caller passes a barrier before reusing it.
+template <int NV>
+__device__ __forceinline__ void block_sums_ff(float (&v)[NV], float *smem) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) v[k] = warp_sum(v[k]);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) smem[32 * k + wid] = v[k];
+    }
+    __syncthreads();
+    if (wid == 0) {
+        const int nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+        for (int k = 0; k < NV; ++k) v[k] = warp_sum(lane < nw ? smem[32 * k + lane] : 0.f);
+    }
 }
 
 // Block sum entirely in FP32 (fixed shuffle tree); valid in thread 0.

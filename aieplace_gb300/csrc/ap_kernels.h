@@ -40,7 +40,8 @@ struct WaArgs {
 void launch_wirelength(const WaArgs &a, cudaStream_t st);
 // Block partials buffer (doubles; the per-block partials are FP32, two per
 // double): holds 2 FP32 per block of the four WA launches at kWaMaxBlocks
-// each, 4 per gather block at kGatherMaxBlocks, 1 per scatter block.
+// each, 4 per gather block at kGatherMaxBlocks, 2 per update block (at most
+// 8192 blocks).
 constexpr int kPartialDoubles = 4 * 8192 + 64;
 // Blocks per bucket launch (grid-stride beyond: one net per thread measured
 // slower -- more block reductions and a longer last-block fold)

@@ -1150,7 +1150,7 @@ int ap_snapshot(ap_handle *h, void *buf, size_t bytes) {
     if (!h->initialized) return AP_ERR_STATE;
     CK(cudaStreamSynchronize(h->stream));
     char *p = (char *)buf;
-    int32_t hdr[4] = {0x41505335, h->n_nodes, h->n_mov, 0};
+    int32_t hdr[4] = {0x41505336, h->n_nodes, h->n_mov, 0};
     memcpy(p, hdr, sizeof(hdr));
     p += sizeof(hdr);
     CK(cudaMemcpy(p, h->d_sc, sizeof(DevScalars), cudaMemcpyDeviceToHost));
@@ -1174,7 +1174,7 @@ int ap_restore(ap_handle *h, const void *buf, size_t bytes) {
     const char *p = (const char *)buf;
     int32_t hdr[4];
     memcpy(hdr, p, sizeof(hdr));
-    if (hdr[0] != 0x41505335 || hdr[1] != h->n_nodes || hdr[2] != h->n_mov) return AP_ERR_INVALID_ARG;
+    if (hdr[0] != 0x41505336 || hdr[1] != h->n_nodes || hdr[2] != h->n_mov) return AP_ERR_INVALID_ARG;
     p += sizeof(hdr);
     CK(cudaStreamSynchronize(h->stream));
     CK(cudaMemcpy(h->d_sc, p, sizeof(DevScalars), cudaMemcpyHostToDevice));

@@ -153,17 +153,20 @@ __device__ __forceinline__ void for_each_overlap(const Grid &g, float x, float y
 // from the bin adds, which need few threads per SM's worth of registers and
 // shared memory, so that this part runs at full occupancy.
 __global__ void __launch_bounds__(kThreads) update_kernel(ScatterArgs a) {
-    __shared__ double red[32];
+    __shared__ double red[32];  // 64 floats: two block sums
     const float alpha = a.sc->f_alpha, mom = a.sc->f_mom;
     const int cur = a.sc->cur, nxt = 1 - cur;
     const Grid g = a.g;
-    float du = 0.f;  // per-thread partial in FP32; FP64 from the block sum on
+    // per-thread partials in FP32 (|u_new - u|^2 for the speed restart and
+    // |v_new - v|^2 for the step-length estimate); FP64 from the block sums on
+    float du = 0.f, dv = 0.f;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n_mov; i += gridDim.x * blockDim.x) {
         const float w = __ldg(a.w + i), h = __ldg(a.h + i);
         const float xhi = fmaxf(a.die_w - w, 0.f), yhi = fmaxf(a.die_h - h, 0.f);
         const float ux = a.ux[cur][i], uy = a.uy[cur][i];
-        const float nux = clampf(a.vx[cur][i] - alpha * a.gx[cur][i], 0.f, xhi);
-        const float nuy = clampf(a.vy[cur][i] - alpha * a.gy[cur][i], 0.f, yhi);
+        const float vx = a.vx[cur][i], vy = a.vy[cur][i];
+        const float nux = clampf(vx - alpha * a.gx[cur][i], 0.f, xhi);
+        const float nuy = clampf(vy - alpha * a.gy[cur][i], 0.f, yhi);
         const float x = clampf(nux + mom * (nux - ux), 0.f, xhi);
         const float y = clampf(nuy + mom * (nuy - uy), 0.f, yhi);
         a.ux[nxt][i] = nux;
@@ -171,18 +174,25 @@ __global__ void __launch_bounds__(kThreads) update_kernel(ScatterArgs a) {
         a.vx[nxt][i] = x;
         a.vy[nxt][i] = y;
         du += (nux - ux) * (nux - ux) + (nuy - uy) * (nuy - uy);
+        dv += (x - vx) * (x - vx) + (y - vy) * (y - vy);
         int c0, c1, r0, r1;
         const NodeRec r = make_rec(g, x, y, w, h, c0, c1, r0, r1);
         a.rec_bin[i] = r.bin;
         a.rec_ov[i] = make_int4(r.xr, r.wq, r.yr, r.hq);
     }
     float *pf = reinterpret_cast<float *>(a.partials);
-    const float dub = block_sum_ff(du, reinterpret_cast<float *>(red));
-    if (threadIdx.x == 0) pf[blockIdx.x] = dub;
+    float bs[2] = {du, dv};
+    block_sums_ff<2>(bs, reinterpret_cast<float *>(red));
+    if (threadIdx.x == 0) {
+        pf[2 * blockIdx.x] = bs[0];
+        pf[2 * blockIdx.x + 1] = bs[1];
+    }
     if (arrive_last(a.counter)) {
-        const double t = block_sum_f(kahan_strided(pf, threadIdx.x, gridDim.x, blockDim.x, 1), red);
+        const double t = block_sum_f(kahan_strided(pf, threadIdx.x, gridDim.x, blockDim.x, 2), red);
+        const double t2 = block_sum_f(kahan_strided(pf + 1, threadIdx.x, gridDim.x, blockDim.x, 2), red);
         if (threadIdx.x == 0) {
             a.sc->t_du = t;
+            a.sc->t_dv2 = t2;
             *a.counter = 0u;
         }
     }
@@ -575,7 +585,7 @@ __device__ void finish_trial(DevScalars *sc, double dv2, double dg2) {
 }
 
 __global__ void __launch_bounds__(kThreads) gather_kernel(GatherArgs a) {
-    __shared__ double red[32];
+    __shared__ double red[64];  // 128 floats: four block sums
     const Grid g = a.g;
     const float lam = a.sc->f_lambda;
     const int at = a.mode == GATHER_STEP ? 1 - a.sc->cur : a.at;
@@ -587,7 +597,6 @@ __global__ void __launch_bounds__(kThreads) gather_kernel(GatherArgs a) {
     float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
     const bool use_rec = a.mode == GATHER_STEP && a.rec_bin != nullptr;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n_mov; i += gridDim.x * blockDim.x) {
-        const float x = vx[i], y = vy[i];
         float fx = 0.f, fy = 0.f;
         int c0, c1, r0, r1;
         bool small;
@@ -615,8 +624,9 @@ __global__ void __launch_bounds__(kThreads) gather_kernel(GatherArgs a) {
                     }
                 }
             }
-        } else if (rb == kRecFull && bin_range(g, x, y, __ldg(a.w + i), __ldg(a.h + i), c0, c1, r0, r1, small)) {
-            const float w = __ldg(a.w + i), h = __ldg(a.h + i);
+        } else if (rb == kRecFull && bin_range(g, vx[i], vy[i], __ldg(a.w + i), __ldg(a.h + i), c0, c1, r0, r1,
+                                               small)) {
+            const float x = vx[i], y = vy[i], w = __ldg(a.w + i), h = __ldg(a.h + i);
             const long long xq = to_q(x), yq = to_q(y), wq = to_q(w), hq = to_q(h);
             if (small) {
                 const long long b = (long long)c0 * g.my + r0;
@@ -670,9 +680,12 @@ __global__ void __launch_bounds__(kThreads) gather_kernel(GatherArgs a) {
         if (a.mode == GATHER_INIT_GRAD) {
             s2 = fmaxf(s2, fmaxf(fabsf(gx), fabsf(gy)));
         } else {
-            const float dx = x - vpx[i], dy = y - vpy[i];
+            // |v - v_prev|^2 of a loop trial comes from the position update
+            if (a.mode != GATHER_STEP) {
+                const float dx = vx[i] - vpx[i], dy = vy[i] - vpy[i];
+                s0 += dx * dx + dy * dy;
+            }
             const float ddx = gx - gpx[i], ddy = gy - gpy[i];
-            s0 += dx * dx + dy * dy;
             s1 += ddx * ddx + ddy * ddy;
         }
     }
@@ -680,22 +693,24 @@ __global__ void __launch_bounds__(kThreads) gather_kernel(GatherArgs a) {
     const bool is_max = a.mode == GATHER_INIT_GRAD;
     // per-block partials in FP32; the last block sums them with compensation
     // and only its warp 0 adds in FP64 (the FP64 pipe of this part is narrow)
-    float *redf = reinterpret_cast<float *>(red);
-    const float b0 = block_sum_ff(s0, redf);
-    const float b1 = block_sum_ff(s1, redf);
-    const float b2 = is_max ? (float)block_max_f(s2, red) : block_sum_ff(s2, redf);
-    const float b3 = block_sum_ff(s3, redf);
+    float bs[4] = {s0, s1, s2, s3};
+    if (is_max)
+        bs[2] = (float)block_max_f(s2, red);  // s0, s1, s3 are zero in this mode
+    else
+        block_sums_ff<4>(bs, reinterpret_cast<float *>(red));
     float *pf = reinterpret_cast<float *>(a.partials);
     if (threadIdx.x == 0) {
         float *p = pf + 4 * blockIdx.x;
-        p[0] = b0;
-        p[1] = b1;
-        p[2] = b2;
-        p[3] = b3;
+        p[0] = bs[0];
+        p[1] = bs[1];
+        p[2] = bs[2];
+        p[3] = bs[3];
     }
     if (arrive_last(a.counter)) {
         const int nb = (int)gridDim.x;
-        const double t0 = block_sum_f(kahan_strided(pf + 0, threadIdx.x, nb, blockDim.x, 4), red);
+        const double t0 = a.mode == GATHER_STEP
+                              ? 0.0
+                              : block_sum_f(kahan_strided(pf + 0, threadIdx.x, nb, blockDim.x, 4), red);
         const double t1 = block_sum_f(kahan_strided(pf + 1, threadIdx.x, nb, blockDim.x, 4), red);
         double t2;
         if (is_max) {
@@ -727,7 +742,7 @@ __global__ void __launch_bounds__(kThreads) gather_kernel(GatherArgs a) {
                 // the next evaluation's WA smoothing: this trial's gamma(tau),
                 // whether the trial is accepted or not
                 sc->gamma = sc->gamma_next;
-                finish_trial(sc, t0, t1);
+                finish_trial(sc, sc->t_dv2, t1);
             }
             publish_f32(sc);
             *a.counter = 0u;
