@@ -584,7 +584,7 @@ __device__ void finish_trial(DevScalars *sc, double dv2, double dg2) {
     sc->iteration += 1;
 }
 
-__global__ void __launch_bounds__(kThreads) gather_kernel(GatherArgs a) {
+__global__ void __launch_bounds__(kThreads, 4) gather_kernel(GatherArgs a) {
     __shared__ double red[64];  // 128 floats: four block sums
     const Grid g = a.g;
     const float lam = a.sc->f_lambda;
@@ -600,11 +600,27 @@ __global__ void __launch_bounds__(kThreads) gather_kernel(GatherArgs a) {
         float fx = 0.f, fy = 0.f;
         int c0, c1, r0, r1;
         bool small;
+        // every load that does not depend on the field is issued here, ahead
+        // of the field gather: loads after its data-dependent loop would wait
+        // for it, and loads under the record's branch for the record
         const int rb = use_rec ? __ldg(a.rec_bin + i) : kRecFull;
+        const int4 o = use_rec ? __ldg(a.rec_ov + i) : make_int4(0, 0, 0, 0);  // xr, wq, yr, hq
+        ull gqv = 0ull;
+        float pc = 0.f, chg = 0.f, gpxv = 0.f, gpyv = 0.f;
+        if (a.mode != GATHER_FORCE_ONLY) {
+            gqv = a.gq[i];
+            pc = __ldg(a.pins + i);
+        }
+        if (a.mode == GATHER_STEP || a.mode == GATHER_INIT_GRAD || a.mode == GATHER_INIT_PREV) {
+            chg = __ldg(a.charge + i);
+            if (a.mode != GATHER_INIT_GRAD) {
+                gpxv = __ldg(gpx + i);
+                gpyv = __ldg(gpy + i);
+            }
+        }
         if (rb >= 0) {
             // the scatter's record at this point: the weights of the path
             // below, in the same order, without the bin arithmetic
-            const int4 o = __ldg(a.rec_ov + i);  // xr, wq, yr, hq
             const int c0r = rec_c0(rb), r0r = rec_r0(rb);
             if (rb & kRecSmall) {
                 const int b = c0r * g.my + r0r;
@@ -653,8 +669,7 @@ __global__ void __launch_bounds__(kThreads) gather_kernel(GatherArgs a) {
             continue;
         }
         long long qx, qy;
-        unpack_q(a.gq[i], qx, qy);
-        const float pc = a.pins[i];
+        unpack_q(gqv, qx, qy);
         const bool heavy = pc > (float)kPackMaxPins;
         if (heavy) {
             qx += (long long)a.gqx[i];
@@ -672,7 +687,7 @@ __global__ void __launch_bounds__(kThreads) gather_kernel(GatherArgs a) {
             a.gqx[i] = 0ull;
             a.gqy[i] = 0ull;
         }
-        const float hd = fmaxf(1.f, pc + lam * a.charge[i]);
+        const float hd = fmaxf(1.f, pc + lam * chg);
         const float ihd = __frcp_rn(hd);
         const float gx = (wlx - lam * fx) * ihd, gy = (wly - lam * fy) * ihd;
         gx_out[i] = gx;
@@ -685,7 +700,7 @@ __global__ void __launch_bounds__(kThreads) gather_kernel(GatherArgs a) {
                 const float dx = vx[i] - vpx[i], dy = vy[i] - vpy[i];
                 s0 += dx * dx + dy * dy;
             }
-            const float ddx = gx - gpx[i], ddy = gy - gpy[i];
+            const float ddx = gx - gpxv, ddy = gy - gpyv;
             s1 += ddx * ddx + ddy * ddy;
         }
     }
