@@ -68,16 +68,17 @@ def stage_model(nl):
     m2 = int(nl["bins"]) ** 2
     m3 = int(nl["bins"]) ** 3
     return {
-        # read v, g, u, w, h; write u', v'; int64 map written once
-        "scatter+update": ("hbm", 48 * n_mov + 8 * m2),
+        # update: read v, g, u, w, h, write u', v' and the 20-byte bin record;
+        # bin adds: read the record; int64 map written once
+        "scatter+update": ("hbm", 88 * n_mov + 8 * m2),
         # read mov, fixed, fixed-scaled maps; clear mov; write solver input
         "density+overflow": ("hbm", 36 * m2),
         # net_ptr, pin_node, node positions, int64 gradient per movable node
         "wirelength": ("hbm", 4 * (e + 1) + 4 * p + 8 * n_nodes + 16 * n_mov),
         # 6 dense m x m x m contractions (useful FLOPs)
         "field": ("tensor", 12 * m3),
-        # v, w, h, int64 grad read+clear, pins, charge, v_prev, g_prev, g out; field maps
-        "gather+control": ("hbm", 88 * n_mov + 8 * m2),
+        # bin record, int64 WA gradient read+clear, pins, charge, g_prev, g out; field maps
+        "gather+control": ("hbm", 60 * n_mov + 8 * m2),
     }
 
 
