@@ -160,25 +160,34 @@ __global__ void __launch_bounds__(kThreads) update_kernel(ScatterArgs a) {
     // per-thread partials in FP32 (|u_new - u|^2 for the speed restart and
     // |v_new - v|^2 for the step-length estimate); FP64 from the block sums on
     float du = 0.f, dv = 0.f;
+    // distinct arrays: the loads of a node need not wait for the stores of
+    // the thread's previous node (grid-stride over one wave of blocks)
+    const float *__restrict__ uxc = a.ux[cur], *__restrict__ uyc = a.uy[cur];
+    const float *__restrict__ vxc = a.vx[cur], *__restrict__ vyc = a.vy[cur];
+    const float *__restrict__ gxc = a.gx[cur], *__restrict__ gyc = a.gy[cur];
+    float *__restrict__ uxn = a.ux[nxt], *__restrict__ uyn = a.uy[nxt];
+    float *__restrict__ vxn = a.vx[nxt], *__restrict__ vyn = a.vy[nxt];
+    int *__restrict__ rbin = a.rec_bin;
+    int4 *__restrict__ rov = a.rec_ov;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n_mov; i += gridDim.x * blockDim.x) {
         const float w = __ldg(a.w + i), h = __ldg(a.h + i);
         const float xhi = fmaxf(a.die_w - w, 0.f), yhi = fmaxf(a.die_h - h, 0.f);
-        const float ux = a.ux[cur][i], uy = a.uy[cur][i];
-        const float vx = a.vx[cur][i], vy = a.vy[cur][i];
-        const float nux = clampf(vx - alpha * a.gx[cur][i], 0.f, xhi);
-        const float nuy = clampf(vy - alpha * a.gy[cur][i], 0.f, yhi);
+        const float ux = uxc[i], uy = uyc[i];
+        const float vx = vxc[i], vy = vyc[i];
+        const float nux = clampf(vx - alpha * gxc[i], 0.f, xhi);
+        const float nuy = clampf(vy - alpha * gyc[i], 0.f, yhi);
         const float x = clampf(nux + mom * (nux - ux), 0.f, xhi);
         const float y = clampf(nuy + mom * (nuy - uy), 0.f, yhi);
-        a.ux[nxt][i] = nux;
-        a.uy[nxt][i] = nuy;
-        a.vx[nxt][i] = x;
-        a.vy[nxt][i] = y;
+        uxn[i] = nux;
+        uyn[i] = nuy;
+        vxn[i] = x;
+        vyn[i] = y;
         du += (nux - ux) * (nux - ux) + (nuy - uy) * (nuy - uy);
         dv += (x - vx) * (x - vx) + (y - vy) * (y - vy);
         int c0, c1, r0, r1;
         const NodeRec r = make_rec(g, x, y, w, h, c0, c1, r0, r1);
-        a.rec_bin[i] = r.bin;
-        a.rec_ov[i] = make_int4(r.xr, r.wq, r.yr, r.hq);
+        rbin[i] = r.bin;
+        rov[i] = make_int4(r.xr, r.wq, r.yr, r.hq);
     }
     float *pf = reinterpret_cast<float *>(a.partials);
     float bs[2] = {du, dv};
@@ -385,9 +394,19 @@ __global__ void __launch_bounds__(kScatterThreads, 2) scatter_kernel(ScatterArgs
 
 void launch_update(const ScatterArgs &a, cudaStream_t st) {
     if (!a.update || a.n_mov <= 0) return;
-    // one node per thread up to 8192 blocks (the partials buffer), grid-stride beyond
+    // one wave of resident blocks (at most 8192, the partials buffer),
+    // grid-stride beyond: fewer block sums and last-block folds
+    static int wave = 0;
+    if (wave <= 0) {
+        int dev = 0, sms = 0, per_sm = 0;
+        if (cudaGetDevice(&dev) == cudaSuccess &&
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess &&
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, update_kernel, kThreads, 0) == cudaSuccess)
+            wave = sms * per_sm;
+        if (wave <= 0 || wave > 8192) wave = 1216;
+    }
     int ub = (a.n_mov + kThreads - 1) / kThreads;
-    if (ub > 8192) ub = 8192;
+    if (ub > wave) ub = wave;
     update_kernel<<<ub, kThreads, 0, st>>>(a);
 }
 
