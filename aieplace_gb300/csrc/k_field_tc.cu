@@ -72,6 +72,7 @@ struct Epi {
     unsigned int *status;
     const int *gate;  // run only if gate is null or (1 << *gate) & gate_mask
     int gate_mask;
+    int pdl;  // launched as a programmatic dependent of the previous stage
 };
 
 // ---- PTX wrappers ----------------------------------------------------------
@@ -328,6 +329,11 @@ __global__ void __launch_bounds__(THREADS, 1) gemm_bf16x3_kernel(const __grid_co
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
+    // A programmatic dependent (stages 2-4) starts as SMs free up while the
+    // previous stage finishes, and has its barriers and TMEM set up by then;
+    // the previous stage's outputs are this stage's data, so nothing is
+    // loaded or stored before that grid has completed.
+    if (e.pdl) asm volatile("griddepcontrol.wait;" ::: "memory");
 
     int issued = 0;  // producer: k-blocks whose loads were issued
     if (warp == 0 && lane == 0) {
@@ -374,6 +380,8 @@ __global__ void __launch_bounds__(THREADS, 1) gemm_bf16x3_kernel(const __grid_co
 
     // ---- epilogue ----------------------------------------------------------
     const bool ok = mbar_wait(done, 0, e.status) && !*abort_flag;
+    // the next stage may be scheduled once every CTA of this one is here
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     tc_fence_after();
     // The pipeline buffers are free once the accumulator is complete (every
     // issued load landed and was read): they hold the FP32 staging slots,
@@ -584,13 +592,22 @@ void launch_stage(const Maps &maps, Epi e, int m, int batch, int per_sm, cudaStr
     cfg.blockDim = dim3(THREADS);
     cfg.dynamicSmemBytes = T::SMEM_BYTES;
     cfg.stream = st;
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeClusterDimension;
-    at[0].val.clusterDim.x = e.split;
-    at[0].val.clusterDim.y = 1;
-    at[0].val.clusterDim.z = 1;
+    cudaLaunchAttribute at[2];
+    unsigned int na = 0;
+    if (e.split > 1) {
+        at[na].id = cudaLaunchAttributeClusterDimension;
+        at[na].val.clusterDim.x = e.split;
+        at[na].val.clusterDim.y = 1;
+        at[na].val.clusterDim.z = 1;
+        ++na;
+    }
+    if (e.pdl) {
+        at[na].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        at[na].val.programmaticStreamSerializationAllowed = 1;
+        ++na;
+    }
     cfg.attrs = at;
-    cfg.numAttrs = e.split > 1 ? 1 : 0;
+    cfg.numAttrs = na;
     cudaLaunchKernelEx(&cfg, gemm_bf16x3_kernel<T>, maps, e);
 }
 
@@ -611,6 +628,7 @@ void run_stages(const StageMaps &h, FieldSolver &f, float *ex, float *ey, cudaSt
     e.o_hi[0] = f.b_t_hi;
     e.o_lo[0] = f.b_t_lo;
     launch_stage<T>(h.s1, e, m, 1, per_sm, st);
+    e.pdl = 1;  // stages 2-4 overlap their set-up with the previous stage's end
     e.mode = EPI_SPECTRAL;
     e.o_hi[0] = f.b_px_hi;
     e.o_lo[0] = f.b_px_lo;
