@@ -36,6 +36,15 @@ __device__ __forceinline__ bool gate_open(const int *gate, int mask) {
     return gate == nullptr || ((1 << *gate) & mask) != 0;
 }
 
+// 4-byte asynchronous copy global -> shared (zero-filled when !valid; the
+// source is then not read): every copy of a staging loop is in flight at once
+__device__ __forceinline__ void cp_async4(float *dst, const float *src, bool valid) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"((unsigned)__cvta_generic_to_shared(dst)),
+                 "l"(src), "r"(valid ? 4 : 0)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
 // bilinear sample of a coarse R x R map at fine index (X, Y), factor f:
 // coarse sample points at bin centres, clamped at the edges
 __device__ __forceinline__ float bilinear_up(const float *c, int R, int f, int X, int Y) {
@@ -297,27 +306,34 @@ __global__ void __launch_bounds__(256, 2) net_fwd_fused_kernel(int R, FusedNet f
     float *bs = wh + 3 * kMaxCh * kMaxCh;              // 4 x [kMaxCh]
     float *xin = bs + 4 * kMaxCh;                      // [cin0][HX][HY]
     const int b = blockIdx.z, X0 = blockIdx.y * kFuseTX, Y0 = blockIdx.x * kFuseTY, RR = R * R;
+    // staging by asynchronous copies (zero fill for unused slots and the
+    // halo outside the map): the loads of the whole loop are in flight together
     for (int t = threadIdx.x; t < cin0 * KK * kMaxCh; t += blockDim.x) {
         const int co = t % kMaxCh, r = t / kMaxCh, ci = r / KK, kk = r - ci * KK;
-        w0[t] = co < width ? params[fn.w_off[0] + ((size_t)co * cin0 + ci) * KK + kk] : 0.f;
+        const bool ok = co < width;
+        cp_async4(w0 + t, params + (ok ? fn.w_off[0] + ((size_t)co * cin0 + ci) * KK + kk : 0), ok);
     }
     for (int t = threadIdx.x; t < 3 * kMaxCh * kMaxCh; t += blockDim.x) {
         const int l = 1 + t / (kMaxCh * kMaxCh), r = t % (kMaxCh * kMaxCh), ci = r / kMaxCh, co = r % kMaxCh;
         const int cin = width, co_n = l == kSurrLayers - 1 ? cout : width;
         const size_t wo = l == 1 ? fn.w_off[1] : l == 2 ? fn.w_off[2] : fn.w_off[3];
-        wh[t] = (co < co_n && ci < cin) ? params[wo + (size_t)co * cin + ci] : 0.f;
+        const bool ok = co < co_n && ci < cin;
+        cp_async4(wh + t, params + (ok ? wo + (size_t)co * cin + ci : 0), ok);
     }
     for (int t = threadIdx.x; t < 4 * kMaxCh; t += blockDim.x) {
         const int l = t / kMaxCh, co = t % kMaxCh, co_n = l == kSurrLayers - 1 ? cout : width;
         const size_t bo = l == 0 ? fn.b_off[0] : l == 1 ? fn.b_off[1] : l == 2 ? fn.b_off[2] : fn.b_off[3];
-        bs[t] = co < co_n ? params[bo + co] : 0.f;
+        const bool ok = co < co_n;
+        cp_async4(bs + t, params + (ok ? bo + co : 0), ok);
     }
     const float *xb = x0 + (size_t)b * cin0 * RR;
     for (int t = threadIdx.x; t < cin0 * HX * HY; t += blockDim.x) {
         const int ci = t / (HX * HY), r = t - ci * (HX * HY), hx = r / HY, hy = r - hx * HY;
         const int xx = X0 + hx - H, yy = Y0 + hy - H;
-        xin[t] = (xx >= 0 && xx < R && yy >= 0 && yy < R) ? __ldg(xb + (size_t)ci * RR + xx * R + yy) : 0.f;
+        const bool ok = xx >= 0 && xx < R && yy >= 0 && yy < R;
+        cp_async4(xin + t, xb + (ok ? (size_t)ci * RR + xx * R + yy : 0), ok);
     }
+    cp_async_wait_all();
     __syncthreads();
     const int lx = threadIdx.x / kFuseTY, ly = threadIdx.x % kFuseTY;  // rows lx and lx + 8
     float a0[kMaxCh], h0[kMaxCh];
