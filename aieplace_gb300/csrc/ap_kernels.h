@@ -70,6 +70,9 @@ struct ScatterArgs {
     // or a sentinel; overlaps ow0, ow1, oh0, oh1) for the gather at the same point
     int *rec_bin;
     int4 *rec_ov;
+    // update mode, optional: the trial point also written here (movable
+    // nodes), for a copy to the host that overlaps the rest of the trial
+    float *trial_x, *trial_y;
 };
 void launch_scatter(const ScatterArgs &a, cudaStream_t st);
 // the two launches of launch_scatter: the position update and records (update

@@ -82,6 +82,10 @@ struct ap_handle {
     // the WA launches of a trial run beside scatter -> rho -> field
     cudaStream_t wa_stream = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    // host step: the trial point's copy to the host runs on copy_stream from
+    // the position update on (ev_upd), joined before the call returns (ev_copy)
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t ev_upd = nullptr, ev_copy = nullptr;
     ap_surrogate_policy policy{0.3f, 8, 0.02f, 1};
 };
 
@@ -255,9 +259,16 @@ int join_wa(ap_handle *h, cudaStream_t st) {
     return AP_OK;
 }
 
-int enqueue_iteration(ap_handle *h, cudaStream_t st) {
-    const ScatterArgs sa = loop_scatter_args(h);
+// One trial; with `trial_x` set, the position update also writes the trial
+// point there and `after_update` is recorded behind it (the host step's copy
+// of the result starts from that event).
+int enqueue_iteration(ap_handle *h, cudaStream_t st, float *trial_x = nullptr, float *trial_y = nullptr,
+                      cudaEvent_t after_update = nullptr) {
+    ScatterArgs sa = loop_scatter_args(h);
+    sa.trial_x = trial_x;
+    sa.trial_y = trial_y;
     launch_update(sa, st);
+    if (after_update) CK(cudaEventRecord(after_update, st));
     int r = fork_wa(h, st);
     if (r != AP_OK) return r;
     launch_scatter_bins(sa, st);
@@ -399,6 +410,24 @@ __global__ void stage_cur_kernel(int n, int to_cur, const DevScalars *sc, float 
     float *x = cur ? x1 : x0, *y = cur ? y1 : y0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         if (to_cur) {
+            x[i] = sx[i];
+            y[i] = sy[i];
+        } else {
+            sx[i] = x[i];
+            sy[i] = y[i];
+        }
+    }
+}
+
+// Host step input: movable nodes from the staging arrays into buffers [cur],
+// and the fixed nodes' positions the other way (the staging arrays then hold
+// the whole result once the position update has written the trial point).
+__global__ void stage_in_kernel(int n_mov, int n_nodes, const DevScalars *sc, float *x0, float *y0, float *x1,
+                                float *y1, float *sx, float *sy) {
+    const int cur = sc->cur;
+    float *x = cur ? x1 : x0, *y = cur ? y1 : y0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n_nodes; i += gridDim.x * blockDim.x) {
+        if (i < n_mov) {
             x[i] = sx[i];
             y[i] = sy[i];
         } else {
@@ -728,6 +757,9 @@ int ap_create(const ap_netlist *nl, const ap_params *params, ap_handle **out) {
     A(cudaStreamCreateWithPriority(&h->wa_stream, cudaStreamNonBlocking, prio_low));
     A(cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming));
     A(cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming));
+    A(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
+    A(cudaEventCreateWithFlags(&h->ev_upd, cudaEventDisableTiming));
+    A(cudaEventCreateWithFlags(&h->ev_copy, cudaEventDisableTiming));
     if (!ok) {
         ap_destroy(h);
         return AP_ERR_CUDA;
@@ -797,6 +829,9 @@ int ap_destroy(ap_handle *h) {
     if (h->wa_stream) cudaStreamDestroy(h->wa_stream);
     if (h->ev_fork) cudaEventDestroy(h->ev_fork);
     if (h->ev_join) cudaEventDestroy(h->ev_join);
+    if (h->copy_stream) cudaStreamDestroy(h->copy_stream);
+    if (h->ev_upd) cudaEventDestroy(h->ev_upd);
+    if (h->ev_copy) cudaEventDestroy(h->ev_copy);
     field_solver_free(h->fs);
     void *ptrs[] = {h->d_net_ptr, h->d_pin_node, h->d_w,      h->d_h,       h->d_px[0], h->d_px[1],
                     h->d_py[0],   h->d_py[1],    h->d_gx[0],  h->d_gx[1],   h->d_gy[0], h->d_gy[1],
@@ -973,8 +1008,29 @@ int ap_step_host(ap_handle *h, const float *x_in, const float *y_in, float *x_ou
         if (x_in && y_in) {
             CK(cudaMemcpyAsync(h->d_sx, x_in, sizeof(float) * h->n_mov, cudaMemcpyHostToDevice, h->stream));
             CK(cudaMemcpyAsync(h->d_sy, y_in, sizeof(float) * h->n_mov, cudaMemcpyHostToDevice, h->stream));
-            stage_cur(h, h->n_mov, 1);
         }
+        if (x_out && y_out && !h->surr) {
+            // the accepted point is the trial point (no backtracking): its copy
+            // to the host runs beside the rest of the trial, from the update on
+            // (launched eagerly: the copies' host pointers change every call)
+            const int blocks = std::min((h->n_nodes + kThreads - 1) / kThreads, 4096);
+            stage_in_kernel<<<blocks, kThreads, 0, h->stream>>>(x_in && y_in ? h->n_mov : 0, h->n_nodes, h->d_sc,
+                                                                h->d_px[0], h->d_py[0], h->d_px[1], h->d_py[1],
+                                                                h->d_sx, h->d_sy);
+            int r = enqueue_iteration(h, h->stream, h->d_sx, h->d_sy, h->ev_upd);
+            if (r != AP_OK) return r;
+            CK(cudaStreamWaitEvent(h->copy_stream, h->ev_upd, 0));
+            CK(cudaMemcpyAsync(x_out, h->d_sx, sizeof(float) * h->n_nodes, cudaMemcpyDeviceToHost, h->copy_stream));
+            CK(cudaMemcpyAsync(y_out, h->d_sy, sizeof(float) * h->n_nodes, cudaMemcpyDeviceToHost, h->copy_stream));
+            CK(cudaEventRecord(h->ev_copy, h->copy_stream));
+            CK(cudaStreamWaitEvent(h->stream, h->ev_copy, 0));
+            CK(cudaGetLastError());
+            r = read_scalars(h);
+            if (r != AP_OK) return r;
+            if (stats) fill_stats(h, stats);
+            return h->h_sc->status;
+        }
+        if (x_in && y_in) stage_cur(h, h->n_mov, 1);
         int r = launch_trials(h, 1);
         if (r != AP_OK) return r;
         if (x_out && y_out) {

@@ -182,6 +182,10 @@ __global__ void __launch_bounds__(kThreads) update_kernel(ScatterArgs a) {
         uyn[i] = nuy;
         vxn[i] = x;
         vyn[i] = y;
+        if (a.trial_x) {
+            a.trial_x[i] = x;
+            a.trial_y[i] = y;
+        }
         du += (nux - ux) * (nux - ux) + (nuy - uy) * (nuy - uy);
         dv += (x - vx) * (x - vx) + (y - vy) * (y - vy);
         int c0, c1, r0, r1;
