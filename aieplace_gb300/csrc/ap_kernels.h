@@ -73,11 +73,18 @@ struct ScatterArgs {
     // update mode, optional: the trial point also written here (movable
     // nodes), for a copy to the host that overlaps the rest of the trial
     float *trial_x, *trial_y;
+    // update mode, optional: the accepted point read from here instead of
+    // buffers [cur] (a host step's input)
+    const float *in_x, *in_y;
+    // update mode: nodes [upd_lo, upd_hi) when upd_hi > 0 (one chunk of a
+    // host step's input); block partials from slot part_base on; no_fold: a
+    // later launch folds the sums
+    int upd_lo, upd_hi, part_base, no_fold;
 };
 void launch_scatter(const ScatterArgs &a, cudaStream_t st);
 // the two launches of launch_scatter: the position update and records (update
 // mode only), then the bin adds
-void launch_update(const ScatterArgs &a, cudaStream_t st);
+int launch_update(const ScatterArgs &a, cudaStream_t st);  // returns the blocks launched
 void launch_scatter_bins(const ScatterArgs &a, cudaStream_t st);
 
 // ---- density map -> solver input + overflow ---------------------------------

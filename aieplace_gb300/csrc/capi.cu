@@ -86,6 +86,11 @@ struct ap_handle {
     // the position update on (ev_upd), joined before the call returns (ev_copy)
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t ev_upd = nullptr, ev_copy = nullptr;
+    // host step input: copied in chunks on copy_in (ev_in[k] behind chunk k)
+    // into d_ix / d_iy, each chunk's position update waiting for its copy
+    cudaStream_t copy_in = nullptr;
+    cudaEvent_t ev_start = nullptr, ev_in[4] = {nullptr, nullptr, nullptr, nullptr};
+    float *d_ix = nullptr, *d_iy = nullptr;
     ap_surrogate_policy policy{0.3f, 8, 0.02f, 1};
 };
 
@@ -259,16 +264,9 @@ int join_wa(ap_handle *h, cudaStream_t st) {
     return AP_OK;
 }
 
-// One trial; with `trial_x` set, the position update also writes the trial
-// point there and `after_update` is recorded behind it (the host step's copy
-// of the result starts from that event).
-int enqueue_iteration(ap_handle *h, cudaStream_t st, float *trial_x = nullptr, float *trial_y = nullptr,
-                      cudaEvent_t after_update = nullptr) {
-    ScatterArgs sa = loop_scatter_args(h);
-    sa.trial_x = trial_x;
-    sa.trial_y = trial_y;
-    launch_update(sa, st);
-    if (after_update) CK(cudaEventRecord(after_update, st));
+// The trial after its position update.
+int enqueue_after_update(ap_handle *h, cudaStream_t st) {
+    const ScatterArgs sa = loop_scatter_args(h);
     int r = fork_wa(h, st);
     if (r != AP_OK) return r;
     launch_scatter_bins(sa, st);
@@ -284,6 +282,11 @@ int enqueue_iteration(ap_handle *h, cudaStream_t st, float *trial_x = nullptr, f
     if (r != AP_OK) return r;
     launch_gather(loop_gather_args(h), st);
     return cudaGetLastError() == cudaSuccess ? AP_OK : AP_ERR_CUDA;
+}
+
+int enqueue_iteration(ap_handle *h, cudaStream_t st) {
+    launch_update(loop_scatter_args(h), st);
+    return enqueue_after_update(h, st);
 }
 
 // Density/overflow + WA + field at buffer `at` (no position update).
@@ -419,21 +422,16 @@ __global__ void stage_cur_kernel(int n, int to_cur, const DevScalars *sc, float 
     }
 }
 
-// Host step input: movable nodes from the staging arrays into buffers [cur],
-// and the fixed nodes' positions the other way (the staging arrays then hold
-// the whole result once the position update has written the trial point).
-__global__ void stage_in_kernel(int n_mov, int n_nodes, const DevScalars *sc, float *x0, float *y0, float *x1,
-                                float *y1, float *sx, float *sy) {
+// Host step: the fixed nodes' positions (nodes [first, first + n)) from
+// buffers [cur] into the staging arrays, which hold the whole result once the
+// position update has written the trial point of the movable nodes.
+__global__ void stage_in_kernel(int n, int first, const DevScalars *sc, const float *x0, const float *y0,
+                                const float *x1, const float *y1, float *sx, float *sy) {
     const int cur = sc->cur;
-    float *x = cur ? x1 : x0, *y = cur ? y1 : y0;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n_nodes; i += gridDim.x * blockDim.x) {
-        if (i < n_mov) {
-            x[i] = sx[i];
-            y[i] = sy[i];
-        } else {
-            sx[i] = x[i];
-            sy[i] = y[i];
-        }
+    const float *x = cur ? x1 : x0, *y = cur ? y1 : y0;
+    for (int i = first + blockIdx.x * blockDim.x + threadIdx.x; i < first + n; i += gridDim.x * blockDim.x) {
+        sx[i] = x[i];
+        sy[i] = y[i];
     }
 }
 
@@ -760,6 +758,11 @@ int ap_create(const ap_netlist *nl, const ap_params *params, ap_handle **out) {
     A(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
     A(cudaEventCreateWithFlags(&h->ev_upd, cudaEventDisableTiming));
     A(cudaEventCreateWithFlags(&h->ev_copy, cudaEventDisableTiming));
+    A(cudaStreamCreateWithFlags(&h->copy_in, cudaStreamNonBlocking));
+    A(cudaEventCreateWithFlags(&h->ev_start, cudaEventDisableTiming));
+    for (cudaEvent_t &e : h->ev_in) A(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    A(dalloc(&h->d_ix, std::max(1, h->n_mov)));
+    A(dalloc(&h->d_iy, std::max(1, h->n_mov)));
     if (!ok) {
         ap_destroy(h);
         return AP_ERR_CUDA;
@@ -832,6 +835,10 @@ int ap_destroy(ap_handle *h) {
     if (h->copy_stream) cudaStreamDestroy(h->copy_stream);
     if (h->ev_upd) cudaEventDestroy(h->ev_upd);
     if (h->ev_copy) cudaEventDestroy(h->ev_copy);
+    if (h->copy_in) cudaStreamDestroy(h->copy_in);
+    if (h->ev_start) cudaEventDestroy(h->ev_start);
+    for (cudaEvent_t e : h->ev_in)
+        if (e) cudaEventDestroy(e);
     field_solver_free(h->fs);
     void *ptrs[] = {h->d_net_ptr, h->d_pin_node, h->d_w,      h->d_h,       h->d_px[0], h->d_px[1],
                     h->d_py[0],   h->d_py[1],    h->d_gx[0],  h->d_gx[1],   h->d_gy[0], h->d_gy[1],
@@ -839,7 +846,8 @@ int ap_destroy(ap_handle *h) {
                     h->d_pins,    h->d_charge,   h->d_gqx,    h->d_gqy,
                     h->d_mov_q,   h->d_fix_q,    h->d_fixs_q, h->d_dens,    h->d_ex,    h->d_ey,
                     h->d_dens_hi, h->d_dens_lo,  h->d_sx,     h->d_sy,      h->d_sc,    h->d_partials,
-                    h->d_partials_ll, h->d_counters, h->d_out, h->d_rec_bin, h->d_rec_ov, h->d_gq};
+                    h->d_partials_ll, h->d_counters, h->d_out, h->d_rec_bin, h->d_rec_ov, h->d_gq,
+                    h->d_ix,      h->d_iy};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     if (h->h_sc) cudaFreeHost(h->h_sc);
@@ -1005,19 +1013,49 @@ int ap_step_host(ap_handle *h, const float *x_in, const float *y_in, float *x_ou
         // Without backtracking every trial is accepted: one trial is the
         // iteration, and positions move through the staging arrays by device
         // kernels that read `cur` themselves -- one host round trip per call.
-        if (x_in && y_in) {
-            CK(cudaMemcpyAsync(h->d_sx, x_in, sizeof(float) * h->n_mov, cudaMemcpyHostToDevice, h->stream));
-            CK(cudaMemcpyAsync(h->d_sy, y_in, sizeof(float) * h->n_mov, cudaMemcpyHostToDevice, h->stream));
-        }
         if (x_out && y_out && !h->surr) {
-            // the accepted point is the trial point (no backtracking): its copy
-            // to the host runs beside the rest of the trial, from the update on
-            // (launched eagerly: the copies' host pointers change every call)
-            const int blocks = std::min((h->n_nodes + kThreads - 1) / kThreads, 4096);
-            stage_in_kernel<<<blocks, kThreads, 0, h->stream>>>(x_in && y_in ? h->n_mov : 0, h->n_nodes, h->d_sc,
-                                                                h->d_px[0], h->d_py[0], h->d_px[1], h->d_py[1],
-                                                                h->d_sx, h->d_sy);
-            int r = enqueue_iteration(h, h->stream, h->d_sx, h->d_sy, h->ev_upd);
+            // The accepted point is the trial point (no backtracking).  The
+            // input arrives in chunks, each chunk's position update starting
+            // once its copy has landed; the update writes the trial point to
+            // the staging arrays, whose copy back runs beside the rest of the
+            // trial.  Launched eagerly: the host pointers change every call.
+            cudaStream_t st = h->stream;
+            const bool in = x_in && y_in;
+            const int nc = in && h->n_mov >= 65536 ? 4 : 1;
+            if (in) {
+                CK(cudaEventRecord(h->ev_start, st));  // after the stream's earlier work
+                CK(cudaStreamWaitEvent(h->copy_in, h->ev_start, 0));
+            }
+            if (h->n_nodes > h->n_mov) {  // fixed nodes' positions into the staging arrays
+                const int nf = h->n_nodes - h->n_mov, blocks = std::min((nf + kThreads - 1) / kThreads, 4096);
+                stage_in_kernel<<<blocks, kThreads, 0, st>>>(nf, h->n_mov, h->d_sc, h->d_px[0], h->d_py[0],
+                                                             h->d_px[1], h->d_py[1], h->d_sx, h->d_sy);
+            }
+            ScatterArgs sa = loop_scatter_args(h);
+            sa.trial_x = h->d_sx;
+            sa.trial_y = h->d_sy;
+            if (in) {
+                sa.in_x = h->d_ix;
+                sa.in_y = h->d_iy;
+            }
+            int base = 0;
+            for (int k = 0; k < nc; ++k) {
+                const int lo = (int)((long long)h->n_mov * k / nc), hi = (int)((long long)h->n_mov * (k + 1) / nc);
+                if (in) {
+                    const size_t b = sizeof(float) * (size_t)(hi - lo);
+                    CK(cudaMemcpyAsync(h->d_ix + lo, x_in + lo, b, cudaMemcpyHostToDevice, h->copy_in));
+                    CK(cudaMemcpyAsync(h->d_iy + lo, y_in + lo, b, cudaMemcpyHostToDevice, h->copy_in));
+                    CK(cudaEventRecord(h->ev_in[k], h->copy_in));
+                    CK(cudaStreamWaitEvent(st, h->ev_in[k], 0));
+                }
+                sa.upd_lo = lo;
+                sa.upd_hi = hi;  // chunks are non-empty: nc > 1 only for n_mov >= 65536
+                sa.part_base = base;
+                sa.no_fold = k < nc - 1;
+                base += launch_update(sa, st);
+            }
+            CK(cudaEventRecord(h->ev_upd, st));
+            int r = enqueue_after_update(h, st);
             if (r != AP_OK) return r;
             CK(cudaStreamWaitEvent(h->copy_stream, h->ev_upd, 0));
             CK(cudaMemcpyAsync(x_out, h->d_sx, sizeof(float) * h->n_nodes, cudaMemcpyDeviceToHost, h->copy_stream));
@@ -1030,7 +1068,11 @@ int ap_step_host(ap_handle *h, const float *x_in, const float *y_in, float *x_ou
             if (stats) fill_stats(h, stats);
             return h->h_sc->status;
         }
-        if (x_in && y_in) stage_cur(h, h->n_mov, 1);
+        if (x_in && y_in) {
+            CK(cudaMemcpyAsync(h->d_sx, x_in, sizeof(float) * h->n_mov, cudaMemcpyHostToDevice, h->stream));
+            CK(cudaMemcpyAsync(h->d_sy, y_in, sizeof(float) * h->n_mov, cudaMemcpyHostToDevice, h->stream));
+            stage_cur(h, h->n_mov, 1);
+        }
         int r = launch_trials(h, 1);
         if (r != AP_OK) return r;
         if (x_out && y_out) {

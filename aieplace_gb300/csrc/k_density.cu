@@ -163,13 +163,14 @@ __global__ void __launch_bounds__(kThreads) update_kernel(ScatterArgs a) {
     // distinct arrays: the loads of a node need not wait for the stores of
     // the thread's previous node (grid-stride over one wave of blocks)
     const float *__restrict__ uxc = a.ux[cur], *__restrict__ uyc = a.uy[cur];
-    const float *__restrict__ vxc = a.vx[cur], *__restrict__ vyc = a.vy[cur];
+    const float *__restrict__ vxc = a.in_x ? a.in_x : a.vx[cur], *__restrict__ vyc = a.in_y ? a.in_y : a.vy[cur];
     const float *__restrict__ gxc = a.gx[cur], *__restrict__ gyc = a.gy[cur];
     float *__restrict__ uxn = a.ux[nxt], *__restrict__ uyn = a.uy[nxt];
     float *__restrict__ vxn = a.vx[nxt], *__restrict__ vyn = a.vy[nxt];
     int *__restrict__ rbin = a.rec_bin;
     int4 *__restrict__ rov = a.rec_ov;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n_mov; i += gridDim.x * blockDim.x) {
+    const int lo = a.upd_hi > 0 ? a.upd_lo : 0, hi = a.upd_hi > 0 ? a.upd_hi : a.n_mov;
+    for (int i = lo + blockIdx.x * blockDim.x + threadIdx.x; i < hi; i += gridDim.x * blockDim.x) {
         const float w = __ldg(a.w + i), h = __ldg(a.h + i);
         const float xhi = fmaxf(a.die_w - w, 0.f), yhi = fmaxf(a.die_h - h, 0.f);
         const float ux = uxc[i], uy = uyc[i];
@@ -197,12 +198,16 @@ __global__ void __launch_bounds__(kThreads) update_kernel(ScatterArgs a) {
     float bs[2] = {du, dv};
     block_sums_ff<2>(bs, reinterpret_cast<float *>(red));
     if (threadIdx.x == 0) {
-        pf[2 * blockIdx.x] = bs[0];
-        pf[2 * blockIdx.x + 1] = bs[1];
+        pf[2 * (a.part_base + blockIdx.x)] = bs[0];
+        pf[2 * (a.part_base + blockIdx.x) + 1] = bs[1];
     }
+    if (a.no_fold) return;  // uniform: an earlier chunk of a chunked update
     if (arrive_last(a.counter)) {
-        const double t = block_sum_f(kahan_strided(pf, threadIdx.x, gridDim.x, blockDim.x, 2), red);
-        const double t2 = block_sum_f(kahan_strided(pf + 1, threadIdx.x, gridDim.x, blockDim.x, 2), red);
+        // the partials of this launch and of the chunks before it (launched
+        // earlier on the same stream, so complete)
+        const int nb = a.part_base + (int)gridDim.x;
+        const double t = block_sum_f(kahan_strided(pf, threadIdx.x, nb, blockDim.x, 2), red);
+        const double t2 = block_sum_f(kahan_strided(pf + 1, threadIdx.x, nb, blockDim.x, 2), red);
         if (threadIdx.x == 0) {
             a.sc->t_du = t;
             a.sc->t_dv2 = t2;
@@ -396,8 +401,8 @@ __global__ void __launch_bounds__(kScatterThreads, 2) scatter_kernel(ScatterArgs
     }
 }
 
-void launch_update(const ScatterArgs &a, cudaStream_t st) {
-    if (!a.update || a.n_mov <= 0) return;
+int launch_update(const ScatterArgs &a, cudaStream_t st) {
+    if (!a.update || a.n_mov <= 0) return 0;
     // one wave of resident blocks (at most 8192, the partials buffer),
     // grid-stride beyond: fewer block sums and last-block folds
     static int wave = 0;
@@ -409,9 +414,12 @@ void launch_update(const ScatterArgs &a, cudaStream_t st) {
             wave = sms * per_sm;
         if (wave <= 0 || wave > 8192) wave = 1216;
     }
-    int ub = (a.n_mov + kThreads - 1) / kThreads;
+    const int n = a.upd_hi > 0 ? a.upd_hi - a.upd_lo : a.n_mov;
+    int ub = (n + kThreads - 1) / kThreads;
     if (ub > wave) ub = wave;
+    if (ub < 1) ub = 1;  // an empty chunk still writes its partials (zero) and may fold
     update_kernel<<<ub, kThreads, 0, st>>>(a);
+    return ub;
 }
 
 void launch_scatter_bins(const ScatterArgs &a, cudaStream_t st) {

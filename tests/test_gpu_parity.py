@@ -295,6 +295,29 @@ def test_step_host_matches_device_step(ap):
         assert s["iteration"] == 10
 
 
+def test_step_host_output_only_and_in_place(ap):
+    # no input (the device state steps on), and one buffer as input and output
+    nl = ap.synth.generate("c0", seed=2)
+    with ap.Placer(nl, bins=32) as a, ap.Placer(nl, bins=32) as b:
+        a.initialize_placement(nl["node_x"], nl["node_y"])
+        b.initialize_placement(nl["node_x"], nl["node_y"])
+        xo, yo = np.zeros(b.num_nodes, np.float32), np.zeros(b.num_nodes, np.float32)
+        for _ in range(3):
+            a.perform_iteration(1)
+            b.step_host(None, None, xo, yo)
+        ax, ay = a.positions()
+        np.testing.assert_array_equal(ax, xo)
+        np.testing.assert_array_equal(ay, yo)
+        x, y = b.positions()
+        for _ in range(3):
+            a.perform_iteration(1)
+            s = b.step_host(x, y, x, y)
+        ax, ay = a.positions()
+        np.testing.assert_array_equal(ax, x)
+        np.testing.assert_array_equal(ay, y)
+        assert s["iteration"] == 6
+
+
 def test_errors_are_status_codes(ap):
     from aieplace_gb300 import APError
 
