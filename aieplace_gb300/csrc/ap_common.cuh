@@ -121,6 +121,13 @@ __device__ __forceinline__ int f2i_rz_bits(float s) {
     return (b >> 31) ? -(int)r : (int)r;
 }
 
+// Truncation toward zero for -1 < s < 2^23 (= (int)s there): s clamped at 0
+// (truncation maps (-1, 0] to 0), then 2^23 added rounding toward zero, which
+// drops the fraction and leaves the integer in the low mantissa bits.
+__device__ __forceinline__ int f2i_rz_small(float s) {
+    return __float_as_int(__fadd_rz(fmaxf(s, 0.0f), 8388608.0f)) - 0x4B000000;
+}
+
 // Round-to-nearest-even int64 -> float from integer arithmetic (= (float)v).
 __device__ __forceinline__ float ll2f_rn_bits(long long v) {
     if (v == 0) return 0.0f;
@@ -198,17 +205,18 @@ __device__ __forceinline__ bool bin_range(const Grid &g, float x, float y, float
     const float qx = __fdiv_rn(x, g.bw), qy = __fdiv_rn(y, g.bh);
     if (small) {
         if (!(qx > -1.0f) || !(qx < (float)g.mx) || !(qy > -1.0f) || !(qy < (float)g.my)) return false;
-        c0 = c1 = f2i_rz_bits(qx);
-        r0 = r1 = f2i_rz_bits(qy);
+        c0 = c1 = f2i_rz_small(qx);  // bin counts <= 4096: in range
+        r0 = r1 = f2i_rz_small(qy);
         return true;
     }
     if (!(qx > -1.0f) || !(qy > -1.0f)) return false;
     const float qx1 = __fdiv_rn(__fadd_rn(x, w), g.bw), qy1 = __fdiv_rn(__fadd_rn(y, h), g.bh);
     if (qx1 != qx1 || qy1 != qy1) return false;
-    c0 = qx >= (float)g.mx ? g.mx : f2i_rz_bits(qx);
-    r0 = qy >= (float)g.my ? g.my : f2i_rz_bits(qy);
-    c1 = qx1 >= (float)g.mx ? g.mx - 1 : f2i_rz_bits(qx1);
-    r1 = qy1 >= (float)g.my ? g.my - 1 : f2i_rz_bits(qy1);
+    // each conversion is taken only for -1 < q < bins <= 4096 (qx1 >= qx)
+    c0 = qx >= (float)g.mx ? g.mx : f2i_rz_small(qx);
+    r0 = qy >= (float)g.my ? g.my : f2i_rz_small(qy);
+    c1 = qx1 >= (float)g.mx ? g.mx - 1 : f2i_rz_small(qx1);
+    r1 = qy1 >= (float)g.my ? g.my - 1 : f2i_rz_small(qy1);
     if (c1 > g.mx - 1) c1 = g.mx - 1;
     if (r1 > g.my - 1) r1 = g.my - 1;
     return c0 <= c1 && r0 <= r1;

@@ -853,23 +853,27 @@ __global__ void numerics_selftest_kernel(long long n, ull seed, int *mism) {
         if ((long long)grad_q(c) != (long long)__float2int_rn(c * kGradScale)) atomicAdd(mism + 3, 1);
         const long long q = (long long)(lo % 8388607u) - 4194303ll;  // |q| < 2^22
         if (__float_as_uint(i64_to_float(q)) != __float_as_uint(__ll2float_rn(q))) atomicAdd(mism + 4, 1);
+        // (-1, 2^23): [1, 2^23) with every exponent, or (-1, 1)
+        const float t = __uint_as_float((lo & 0x007FFFFFu) | ((127u + (hi >> 12) % 23u) << 23));
+        const float u = (hi & 0x800u) ? t : __fmul_rn(t, 1.0f / 4194304.0f) - 1.0f;
+        if (u > -1.0f && f2i_rz_small(u) != __float2int_rz(u)) atomicAdd(mism + 5, 1);
     }
 }
 
 }  // namespace ap
 
 /* Self-check of the conversion helpers; no counterpart in the reference.
- * mismatches[0..4]: f2i_rn_bits, f2i_rz_bits, ll2f_rn_bits, grad_q,
- * i64_to_float, each over `samples` hashed inputs. */
+ * mismatches[0..5]: f2i_rn_bits, f2i_rz_bits, ll2f_rn_bits, grad_q,
+ * i64_to_float, f2i_rz_small, each over `samples` hashed inputs. */
 extern "C" int ap_selftest_numerics(int32_t *mismatches, int64_t samples) {
     if (!mismatches || samples <= 0 || samples > (1ll << 32)) return 1;  // AP_ERR_INVALID_ARG
     int *d = nullptr;
-    if (cudaMalloc(&d, 5 * sizeof(int)) != cudaSuccess) return 4;  // AP_ERR_CUDA
+    if (cudaMalloc(&d, 6 * sizeof(int)) != cudaSuccess) return 4;  // AP_ERR_CUDA
     int rc = 0;
-    if (cudaMemset(d, 0, 5 * sizeof(int)) != cudaSuccess) rc = 4;
+    if (cudaMemset(d, 0, 6 * sizeof(int)) != cudaSuccess) rc = 4;
     if (!rc) {
         ap::numerics_selftest_kernel<<<152 * 8, ap::kThreads>>>(samples, 0x243F6A8885A308D3ull, d);
-        if (cudaGetLastError() != cudaSuccess || cudaMemcpy(mismatches, d, 5 * sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
+        if (cudaGetLastError() != cudaSuccess || cudaMemcpy(mismatches, d, 6 * sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
             rc = 4;
     }
     cudaFree(d);

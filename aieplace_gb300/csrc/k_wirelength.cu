@@ -328,8 +328,9 @@ __device__ __forceinline__ void net_warp_loop(const WaArgs &a, int s, int d, con
 }
 
 // Nets of degree > 8 (buckets 3..6): blocks [0, b3) take degrees 9..16 with
-// 16 lanes per net, then 17..32 with a warp (one pin per lane), 33..64 with a
-// warp (two pins per lane), and above 64 with a warp looping over the pins --
+// 16 lanes per net, then 17..32 with a warp (one pin per lane), 33..64 with
+// 16 lanes (four pins per lane: two nets per warp share each shuffle
+// reduction), and above 64 with a warp looping over the pins --
 // the lane group fits the net, so few lanes idle.
 __global__ void __launch_bounds__(kThreads) wa_large_kernel(WaArgs a) {
     __shared__ double red[32];
@@ -351,7 +352,7 @@ __global__ void __launch_bounds__(kThreads) wa_large_kernel(WaArgs a) {
     } else if (bid < (b0 += a.bucket_blocks[3]) + a.bucket_blocks[4]) {
         net_groups<32, 1>(a, a.bucket_lo[4], a.bucket_lo[5], b0, a.bucket_blocks[4], px, py, inv_g, hpf, waf);
     } else if (bid < (b0 += a.bucket_blocks[4]) + a.bucket_blocks[5]) {
-        net_groups<32, 2>(a, a.bucket_lo[5], a.bucket_lo[6], b0, a.bucket_blocks[5], px, py, inv_g, hpf, waf);
+        net_groups<16, 4>(a, a.bucket_lo[5], a.bucket_lo[6], b0, a.bucket_blocks[5], px, py, inv_g, hpf, waf);
     } else {
         b0 += a.bucket_blocks[5];
         const int warp = ((bid - b0) * kThreads + (int)threadIdx.x) >> 5, nwarps = (a.bucket_blocks[6] * kThreads) >> 5;
@@ -398,8 +399,8 @@ void launch_wirelength(const WaArgs &a0, cudaStream_t st) {
         return b < 1 ? 1 : (b > kWaMaxBlocks ? kWaMaxBlocks : b);
     };
     for (int b = 0; b < 3; ++b) a.bucket_blocks[b] = grid(a.bucket_lo[b + 1] - a.bucket_lo[b]);
-    // large-net sub-buckets: lanes per net 16, 32, 32, 32; <= kWaMaxBlocks in all
-    const int lanes[4] = {16, 32, 32, 32};
+    // large-net sub-buckets: lanes per net 16, 32, 16, 32; <= kWaMaxBlocks in all
+    const int lanes[4] = {16, 32, 16, 32};
     int large = 0;
     for (int b = 3; b < kWaBuckets; ++b) {
         a.bucket_blocks[b] = std::min(grid((a.bucket_lo[b + 1] - a.bucket_lo[b]) * lanes[b - 3]), kWaMaxBlocks / 4);

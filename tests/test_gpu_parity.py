@@ -99,9 +99,9 @@ def test_conversion_helpers_match_hardware(ap):
     must give the conversion instruction's result bit for bit."""
     from aieplace_gb300._lib import check, lib, ptr
 
-    m = np.zeros(5, np.int32)
+    m = np.zeros(6, np.int32)
     check("ap_selftest_numerics", lib().ap_selftest_numerics(ptr(m), 1 << 26))
-    assert m.tolist() == [0, 0, 0, 0, 0]
+    assert m.tolist() == [0, 0, 0, 0, 0, 0]
 
 
 @pytest.mark.parametrize("preset,gamma", [("c0", 4.0), ("c1_small", 0.7), ("c1_small", 25.0)])
