@@ -19,7 +19,7 @@ EXPORTS = [
     "ap_set_stream", "ap_init_positions", "ap_init_seeded", "ap_step", "ap_step_async",
     "ap_profile_stages", "ap_solver_info", "ap_run", "ap_step_host",
     "ap_get_positions", "ap_get_stats", "ap_hpwl", "ap_overflow", "ap_wirelength_grad",
-    "ap_density_map", "ap_field_solve", "ap_field_solve_noalloc", "ap_selftest_numerics",
+    "ap_density_map", "ap_field_solve", "ap_node_force", "ap_debug_inject", "ap_field_solve_noalloc", "ap_selftest_numerics",
     "ap_snapshot_size", "ap_snapshot",
     "ap_restore",
     "ap_synth_counts", "ap_synth_generate",
@@ -123,6 +123,8 @@ def lib():
         L.ap_hpwl.argtypes = [vp, C.POINTER(C.c_double)]
         L.ap_overflow.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_double)]
         L.ap_wirelength_grad.argtypes = [vp, vp, vp, f32, vp, vp, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        L.ap_node_force.argtypes = [vp, vp, vp, vp, vp, f32, f32, vp, vp, vp, vp]
+        L.ap_debug_inject.argtypes = [vp, i32, C.c_int64]
         L.ap_density_map.argtypes = [vp, vp, vp, vp]
         L.ap_field_solve.argtypes = [vp, vp, vp, vp, i32]
         L.ap_field_solve_noalloc.argtypes = [vp, vp, vp, i32, f32, vp]

@@ -36,7 +36,10 @@ def _compile(src: str, verbose_ptxas: bool) -> str:
         if verbose_ptxas:
             cmd[1:1] = ["-Xptxas", "-v"]
     else:
-        cmd = [nvcc(), "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-x", "c++", "-c", path, "-o", obj]
+        # no floating-point contraction: host code gives the same results on
+        # x86 and Arm (the netlist generator's draws in particular)
+        cmd = [nvcc(), "-O3", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off", "-x", "c++", "-c", path,
+               "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"compile of {src} failed:\n{r.stdout}\n{r.stderr}")

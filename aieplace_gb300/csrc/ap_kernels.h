@@ -113,7 +113,7 @@ void launch_rho(const RhoArgs &a, cudaStream_t st);
 
 // ---- field gather + preconditioned gradient + optimiser scalars -------------
 enum { GATHER_STEP = 0, GATHER_INIT_NORMS = 1, GATHER_INIT_GRAD = 2, GATHER_INIT_PREV = 3,
-       GATHER_FORCE_ONLY = 4 };
+       GATHER_FORCE_ONLY = 4, GATHER_NODE_OUT = 5 };
 
 struct GatherArgs {
     Grid g;
@@ -127,16 +127,25 @@ struct GatherArgs {
     const float *pins;      // pin count per movable node
     const float *charge;    // area / bin area
     float *gx[2], *gy[2];   // preconditioned gradient: output [at], comparison [1 - at]
-    float *fx, *fy;         // GATHER_FORCE_ONLY output: overlap-weighted field per node
+    float *fx, *fy;         // GATHER_FORCE_ONLY / NODE_OUT output: overlap-weighted field per node
+    // GATHER_NODE_OUT (the per-node stage entry point): the preconditioned
+    // gradient at the density weight `lambda` into gxo, gyo (if non-null);
+    // the bin records of the evaluation point (launch_records) are read as in
+    // a loop trial
+    float lambda;
+    float *gxo, *gyo;
     DevScalars *sc;
     double *partials;       // 4 * grid
     unsigned int *counter;
     int mode;
-    // GATHER_STEP, optional: the bin records the scatter wrote at this point
+    // GATHER_STEP / NODE_OUT, optional: the bin records of this point
     const int *rec_bin;
     const int4 *rec_ov;
 };
 void launch_gather(const GatherArgs &a, cudaStream_t st);
+// bin records (as the position update writes them) of movable nodes at (x, y)
+void launch_records(const Grid &g, int n_mov, const float *x, const float *y, const float *w, const float *h,
+                    int *rec_bin, int4 *rec_ov, cudaStream_t st);
 constexpr int kGatherMaxBlocks = 4096;  // partials capacity; launched as one wave of resident blocks
 
 // v_{-1} = v_0 - s g_0, s = coef * bw / max|g_0| (first Lipschitz estimate)
@@ -167,6 +176,10 @@ struct FieldSolver {
     float tc_tune_ms[3];     // measured solve time of each variant
     int simt_bm;             // FP32 path tile (32 or 64); 0 = size rule
     float simt_tune_ms[2];   // measured solve time with 32 / 64 tiles
+    // failure injection (ap_debug_inject): the tcgen05 kernels issue no loads
+    // and bound each wait by fault_wait_ns, so their waits run out
+    int fault_stall;
+    unsigned long long fault_wait_ns;
 };
 
 int field_solver_init(FieldSolver &f, int m, float bin_ratio, int want_bf16);
@@ -184,6 +197,7 @@ int field_solve_bf16x3(FieldSolver &f, const __nv_bfloat16 *d_hi, const __nv_bfl
                        float *ex, float *ey, cudaStream_t st, const int *gate = nullptr, int gate_mask = 0);
 // nonzero once a bounded wait in a tcgen05 kernel gave up
 int field_solver_status(FieldSolver &f, unsigned int *out);
+int field_solver_clear_status(FieldSolver &f);
 // float -> bf16 hi/lo split (for per-stage API calls)
 void launch_split_bf16(int n, const float *src, __nv_bfloat16 *hi, __nv_bfloat16 *lo, cudaStream_t st);
 

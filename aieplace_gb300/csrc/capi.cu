@@ -1230,6 +1230,86 @@ int ap_field_solve(ap_handle *h, const float *density, float *ex, float *ey, int
     return sync(h);
 }
 
+int ap_node_force(ap_handle *h, const float *x, const float *y, const float *ex, const float *ey, float gamma,
+                  float lambda, float *fx, float *fy, float *gx, float *gy) {
+    if (!h || !x || !y || !ex || !ey || !fx || !fy || (!gx) != (!gy)) return AP_ERR_INVALID_ARG;
+    const bool grad = gx != nullptr;
+    if (grad && (!(gamma > 0.f) || !(lambda >= 0.f) || !std::isfinite(lambda))) return AP_ERR_INVALID_ARG;
+    int r = stage_positions(h, x, y);
+    if (r != AP_OK) return r;
+    const size_t nb = (size_t)h->p.bins_x * h->p.bins_y, N = (size_t)h->n_nodes, M = (size_t)h->n_mov;
+    CK(cudaMemcpyAsync(h->d_ex, ex, sizeof(float) * nb, cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->d_ey, ey, sizeof(float) * nb, cudaMemcpyHostToDevice, h->stream));
+    // the bin records of this point, as a loop trial's position update makes
+    // them, so that the gather below runs the loop's record path
+    launch_records(h->g, h->n_mov, h->d_sx, h->d_sy, h->d_w, h->d_h, h->d_rec_bin, h->d_rec_ov, h->stream);
+    float *d_g = nullptr;
+    if (grad) {
+        CK(cudaMallocAsync((void **)&d_g, sizeof(float) * 2 * std::max<size_t>(M, 1), h->stream));
+        CK(cudaMemsetAsync(h->d_gq, 0, sizeof(ull) * N, h->stream));
+        CK(cudaMemsetAsync(h->d_gqx, 0, sizeof(ull) * N, h->stream));
+        CK(cudaMemsetAsync(h->d_gqy, 0, sizeof(ull) * N, h->stream));
+        launch_wirelength(wa_args(h, h->d_sx, h->d_sy, gamma, h->n_mov, WA_OUT_ONLY, h->d_out), h->stream);
+    }
+    GatherArgs a = gather_args(h, 0, GATHER_NODE_OUT);
+    a.vx[0] = a.vx[1] = h->d_sx;
+    a.vy[0] = a.vy[1] = h->d_sy;
+    a.rec_bin = h->d_rec_bin;
+    a.rec_ov = h->d_rec_ov;
+    a.fx = h->d_ix;  // host-step input staging, n_mov floats each
+    a.fy = h->d_iy;
+    a.lambda = lambda;
+    a.gxo = grad ? d_g : nullptr;
+    a.gyo = grad ? d_g + M : nullptr;
+    launch_gather(a, h->stream);
+    const cudaError_t le = cudaGetLastError();
+    std::vector<float> hf(2 * std::max<size_t>(M, 1)), hg(grad ? 2 * std::max<size_t>(M, 1) : 0);
+    cudaError_t ce = cudaSuccess;
+    if (M) {
+        if (ce == cudaSuccess) ce = cudaMemcpyAsync(hf.data(), h->d_ix, sizeof(float) * M, cudaMemcpyDeviceToHost, h->stream);
+        if (ce == cudaSuccess) ce = cudaMemcpyAsync(hf.data() + M, h->d_iy, sizeof(float) * M, cudaMemcpyDeviceToHost, h->stream);
+        if (grad && ce == cudaSuccess)
+            ce = cudaMemcpyAsync(hg.data(), d_g, sizeof(float) * 2 * M, cudaMemcpyDeviceToHost, h->stream);
+    }
+    if (d_g) cudaFreeAsync(d_g, h->stream);
+    CK(le);
+    CK(ce);
+    r = sync(h);
+    if (r != AP_OK) return r;
+    for (size_t i = 0; i < N; ++i) {
+        const int e = h->int2ext[i];
+        const bool mov = i < M;
+        fx[e] = mov ? hf[i] : 0.f;
+        fy[e] = mov ? hf[M + i] : 0.f;
+        if (grad) {
+            gx[e] = mov ? hg[i] : 0.f;
+            gy[e] = mov ? hg[M + i] : 0.f;
+        }
+    }
+    return AP_OK;
+}
+
+int ap_debug_inject(ap_handle *h, int32_t kind, int64_t wait_ns) {
+    if (!h) return AP_ERR_INVALID_ARG;
+    if (kind != AP_FAULT_NONE && kind != AP_FAULT_TC_STALL) return AP_ERR_INVALID_ARG;
+    if (kind == AP_FAULT_TC_STALL && (wait_ns < 1000000 || wait_ns > 2000000000)) return AP_ERR_INVALID_ARG;
+    if (kind == AP_FAULT_TC_STALL && !h->fs.tc_ready) return AP_ERR_UNSUPPORTED;
+    // nothing of this handle may be in flight while the solver changes
+    CK(cudaStreamSynchronize(h->stream));
+    if (h->wa_stream) CK(cudaStreamSynchronize(h->wa_stream));
+    h->fs.fault_stall = kind == AP_FAULT_TC_STALL;
+    h->fs.fault_wait_ns = kind == AP_FAULT_TC_STALL ? (unsigned long long)wait_ns : 0ull;
+    if (kind == AP_FAULT_NONE) {
+        const int r = field_solver_clear_status(h->fs);
+        if (r != AP_OK) return r;
+    }
+    // the trial graph holds the solver's launch parameters
+    const bool rebuild = h->graph_ok;
+    destroy_graphs(h);
+    if (rebuild && h->initialized && h->p.use_graph) return build_graphs(h);
+    return AP_OK;
+}
+
 // ---- snapshots ------------------------------------------------------------
 // layout: magic, n_nodes, n_mov, 0, DevScalars, px[2][N], py[2][N], ux[2], uy[2], gx[2], gy[2]
 
@@ -1275,8 +1355,31 @@ int ap_restore(ap_handle *h, const void *buf, size_t bytes) {
     if (hdr[0] != 0x41505336 || hdr[1] != h->n_nodes || hdr[2] != h->n_mov) return AP_ERR_INVALID_ARG;
     p += sizeof(hdr);
     CK(cudaStreamSynchronize(h->stream));
-    CK(cudaMemcpy(h->d_sc, p, sizeof(DevScalars), cudaMemcpyHostToDevice));
+    // The optimiser state comes from the snapshot; the handle's configuration
+    // (loop constants, surrogate attachment and policy) stays the handle's.
+    // A snapshot taken with another surrogate attachment restarts the
+    // surrogate schedule and its counters.
+    DevScalars sc;
+    memcpy(&sc, p, sizeof(DevScalars));
     p += sizeof(DevScalars);
+    sc.max_backtracks = h->p.max_backtracks;
+    sc.restart_mode = h->p.restart_mode;
+    sc.mu_max = h->p.lambda_mu_max;
+    sc.mu_min = h->p.lambda_mu_min;
+    sc.gamma_base = h->p.gamma_base_bins;
+    sc.init_density_weight = h->p.init_density_weight;
+    const int attached = h->surr != nullptr;
+    if (sc.surr_attached != attached) {
+        sc.surr_ok = 1;
+        sc.surr_used = sc.surr_judged = sc.surr_fallbacks = 0;
+        sc.surr_err = 0.0;
+    }
+    sc.surr_attached = attached;
+    sc.surr_judge_every = h->policy.judge_every;
+    sc.surr_tau_min = h->policy.overflow_min;
+    sc.surr_err_bound = h->policy.max_error;
+    sc.field_mode = kFieldExact;
+    CK(cudaMemcpy(h->d_sc, &sc, sizeof(DevScalars), cudaMemcpyHostToDevice));
     const size_t N = (size_t)h->n_nodes, M = (size_t)h->n_mov;
     float *arrs_n[4] = {h->d_px[0], h->d_px[1], h->d_py[0], h->d_py[1]};
     for (float *a : arrs_n) {

@@ -618,7 +618,7 @@ __device__ void finish_trial(DevScalars *sc, double dv2, double dg2) {
 __global__ void __launch_bounds__(kThreads, 4) gather_kernel(GatherArgs a) {
     __shared__ double red[64];  // 128 floats: four block sums
     const Grid g = a.g;
-    const float lam = a.sc->f_lambda;
+    const float lam = a.mode == GATHER_NODE_OUT ? a.lambda : a.sc->f_lambda;
     const int at = a.mode == GATHER_STEP ? 1 - a.sc->cur : a.at;
     const float *vx = a.vx[at], *vy = a.vy[at], *vpx = a.vx[1 - at], *vpy = a.vy[1 - at];
     float *gx_out = a.gx[at], *gy_out = a.gy[at];
@@ -626,7 +626,7 @@ __global__ void __launch_bounds__(kThreads, 4) gather_kernel(GatherArgs a) {
     // per-thread partials in FP32 (a thread owns a couple of nodes); FP64 from
     // the block sums on -- the FP64 pipe of this part is narrow
     float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
-    const bool use_rec = a.mode == GATHER_STEP && a.rec_bin != nullptr;
+    const bool use_rec = (a.mode == GATHER_STEP || a.mode == GATHER_NODE_OUT) && a.rec_bin != nullptr;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n_mov; i += gridDim.x * blockDim.x) {
         float fx = 0.f, fy = 0.f;
         int c0, c1, r0, r1;
@@ -642,9 +642,10 @@ __global__ void __launch_bounds__(kThreads, 4) gather_kernel(GatherArgs a) {
             gqv = a.gq[i];
             pc = __ldg(a.pins + i);
         }
-        if (a.mode == GATHER_STEP || a.mode == GATHER_INIT_GRAD || a.mode == GATHER_INIT_PREV) {
+        if (a.mode == GATHER_STEP || a.mode == GATHER_INIT_GRAD || a.mode == GATHER_INIT_PREV ||
+            a.mode == GATHER_NODE_OUT) {
             chg = __ldg(a.charge + i);
-            if (a.mode != GATHER_INIT_GRAD) {
+            if (a.mode != GATHER_INIT_GRAD && a.mode != GATHER_NODE_OUT) {
                 gpxv = __ldg(gpx + i);
                 gpyv = __ldg(gpy + i);
             }
@@ -694,10 +695,10 @@ __global__ void __launch_bounds__(kThreads, 4) gather_kernel(GatherArgs a) {
                 }
             }
         }
-        if (a.mode == GATHER_FORCE_ONLY) {
+        if (a.mode == GATHER_FORCE_ONLY || a.mode == GATHER_NODE_OUT) {
             a.fx[i] = fx;
             a.fy[i] = fy;
-            continue;
+            if (a.mode == GATHER_FORCE_ONLY) continue;
         }
         long long qx, qy;
         unpack_q(gqv, qx, qy);
@@ -721,6 +722,13 @@ __global__ void __launch_bounds__(kThreads, 4) gather_kernel(GatherArgs a) {
         const float hd = fmaxf(1.f, pc + lam * chg);
         const float ihd = __frcp_rn(hd);
         const float gx = (wlx - lam * fx) * ihd, gy = (wly - lam * fy) * ihd;
+        if (a.mode == GATHER_NODE_OUT) {
+            if (a.gxo) {
+                a.gxo[i] = gx;
+                a.gyo[i] = gy;
+            }
+            continue;
+        }
         gx_out[i] = gx;
         gy_out[i] = gy;
         if (a.mode == GATHER_INIT_GRAD) {
@@ -735,7 +743,7 @@ __global__ void __launch_bounds__(kThreads, 4) gather_kernel(GatherArgs a) {
             s1 += ddx * ddx + ddy * ddy;
         }
     }
-    if (a.mode == GATHER_FORCE_ONLY) return;
+    if (a.mode == GATHER_FORCE_ONLY || a.mode == GATHER_NODE_OUT) return;
     const bool is_max = a.mode == GATHER_INIT_GRAD;
     // per-block partials in FP32; the last block sums them with compensation
     // and only its warp 0 adds in FP64 (the FP64 pipe of this part is narrow)
@@ -812,6 +820,27 @@ void launch_gather(const GatherArgs &a, cudaStream_t st) {
     if (blocks > wave) blocks = wave;
     if (blocks < 1) blocks = 1;
     gather_kernel<<<blocks, kThreads, 0, st>>>(a);
+}
+
+// Bin records of movable nodes at given positions, as update_kernel writes
+// them at a trial point (the per-node stage entry point reads them through
+// the gather's record path).
+__global__ void records_kernel(Grid g, int n_mov, const float *x, const float *y, const float *w, const float *h,
+                               int *rec_bin, int4 *rec_ov) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n_mov; i += gridDim.x * blockDim.x) {
+        int c0, c1, r0, r1;
+        const NodeRec r = make_rec(g, x[i], y[i], w[i], h[i], c0, c1, r0, r1);
+        rec_bin[i] = r.bin;
+        rec_ov[i] = make_int4(r.xr, r.wq, r.yr, r.hq);
+    }
+}
+
+void launch_records(const Grid &g, int n_mov, const float *x, const float *y, const float *w, const float *h,
+                    int *rec_bin, int4 *rec_ov, cudaStream_t st) {
+    if (n_mov <= 0) return;
+    int blocks = (n_mov + kThreads - 1) / kThreads;
+    if (blocks > 4096) blocks = 4096;
+    records_kernel<<<blocks, kThreads, 0, st>>>(g, n_mov, x, y, w, h, rec_bin, rec_ov);
 }
 
 __global__ void perturb_kernel(int n, const float *vx, const float *vy, const float *gx, const float *gy,

@@ -279,14 +279,47 @@ constexpr int kNoAllocMaxDevices = 64;
 
 static __device__ __align__(256) float g_field_scratch[kNoAllocFloats];
 
-// Per device: the device address of g_field_scratch (host code may not use the
-// symbol itself as an address) and the grid whose tables it currently holds.
+// Per device: which context's copy of g_field_scratch holds the tables of
+// which grid.  A context that is destroyed and recreated (cudaDeviceReset)
+// gets a fresh, zeroed copy of the array, so the key includes the context's
+// unique id; without a way to read that id the tables are refilled on every
+// call.
 struct NoAllocState {
+    unsigned long long ctx_id;  // 0: nothing cached
     float *base;
     int m;
     float ratio;
 };
 static NoAllocState g_noalloc_state[kNoAllocMaxDevices];
+
+typedef int (*PfnCtxGetCurrent)(void **ctx);
+typedef int (*PfnCtxGetId)(void *ctx, unsigned long long *id);
+
+// Unique id of the calling thread's current context (driver entry points
+// looked up through the runtime, so the library needs no libcuda link), or
+// 0 if it cannot be read.
+unsigned long long current_context_id() {
+    static PfnCtxGetCurrent get_cur = nullptr;
+    static PfnCtxGetId get_id = nullptr;
+    static bool looked_up = false;
+    if (!looked_up) {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_cur = (PfnCtxGetCurrent)p;
+        p = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = (PfnCtxGetId)p;
+        looked_up = true;
+    }
+    if (!get_cur || !get_id) return 0ull;
+    void *ctx = nullptr;
+    unsigned long long id = 0ull;
+    if (get_cur(&ctx) != 0 || !ctx || get_id(ctx, &id) != 0) return 0ull;
+    return id;
+}
 
 __global__ void noalloc_tables_kernel(float *C, float *Ct, float *St, float *wx, float *wy, int m, float ratio) {
     const double pi = 3.14159265358979323846;
@@ -310,32 +343,35 @@ __global__ void noalloc_tables_kernel(float *C, float *Ct, float *St, float *wx,
 }  // namespace ap
 
 // Same result as ap_field_solve with the FP32 solver, on caller-owned device
-// buffers and without allocating.  The first call on a device (and the first
-// call after the bin count or ratio changes) looks up the scratch address with
-// cudaGetSymbolAddress and fills the transform tables; make that first call
-// before any stream capture.  All calls share the one scratch array: calls
-// whose GPU work overlaps (other streams, other threads) race on it.
+// buffers and without allocating.  Every call looks the scratch address up
+// with cudaGetSymbolAddress (host code may not use the symbol as an address);
+// the first call on a device, the first after the bin count or bin_ratio
+// changes and the first in a new context fill the transform tables, so make
+// that first call before any stream capture.  All calls share the one
+// scratch array: calls whose GPU work overlaps (other streams, other threads)
+// race on it.  The density is read in 16-byte vectors, so it must start on a
+// 16-byte boundary; ex and ey must be float-aligned.
 extern "C" int ap_field_solve_noalloc(const float *density, float *ex, float *ey, int32_t bins, float bin_ratio,
                                       void *stream) {
     using namespace ap;
     if (!density || !ex || !ey) return AP_ERR_INVALID_ARG;
+    if (((uintptr_t)density & 15u) != 0 || ((uintptr_t)ex & 3u) != 0 || ((uintptr_t)ey & 3u) != 0)
+        return AP_ERR_INVALID_ARG;
     if (bins < 32 || bins > kNoAllocMaxBins || (bins % 32) != 0) return AP_ERR_INVALID_ARG;
-    if (!(bin_ratio > 0.f)) return AP_ERR_INVALID_ARG;
+    if (!(bin_ratio > 0.f) || !(bin_ratio < 1e30f)) return AP_ERR_INVALID_ARG;
     int dev = -1;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNoAllocMaxDevices) return AP_ERR_NO_DEVICE;
     cudaStream_t st = (cudaStream_t)stream;
+    void *p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_field_scratch) != cudaSuccess || !p) return AP_ERR_CUDA;
+    const unsigned long long ctx = current_context_id();
     NoAllocState &s = g_noalloc_state[dev];
-    if (!s.base) {
-        void *p = nullptr;
-        if (cudaGetSymbolAddress(&p, g_field_scratch) != cudaSuccess || !p) return AP_ERR_CUDA;
-        s.base = (float *)p;
-        s.m = 0;
-    }
+    const bool fresh = ctx == 0ull || s.ctx_id != ctx || s.base != (float *)p || s.m != bins || s.ratio != bin_ratio;
     const size_t mm = (size_t)bins * bins;
     FieldSolver f{};
     f.m = bins;
     f.bin_ratio = bin_ratio;
-    f.C = s.base;
+    f.C = (float *)p;
     f.Ct = f.C + mm;
     f.St = f.Ct + mm;
     f.t0 = f.St + mm;
@@ -345,10 +381,13 @@ extern "C" int ap_field_solve_noalloc(const float *density, float *ex, float *ey
     f.uy = f.ux + mm;
     f.wx = f.uy + mm;
     f.wy = f.wx + bins;
-    if (s.m != bins || s.ratio != bin_ratio) {
+    if (fresh) {
+        s.ctx_id = 0ull;  // set again only once the fill is enqueued
         noalloc_tables_kernel<<<(int)((mm + 255) / 256), 256, 0, st>>>(f.C, f.Ct, f.St, f.wx, f.wy, bins,
                                                                       bin_ratio);
         if (cudaGetLastError() != cudaSuccess) return AP_ERR_CUDA;
+        s.ctx_id = ctx;
+        s.base = (float *)p;
         s.m = bins;
         s.ratio = bin_ratio;
     }

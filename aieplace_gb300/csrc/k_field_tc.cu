@@ -73,6 +73,11 @@ struct Epi {
     const int *gate;  // run only if gate is null or (1 << *gate) & gate_mask
     int gate_mask;
     int pdl;  // launched as a programmatic dependent of the previous stage
+    // failure injection (tests of the timeout path): the load issuer issues
+    // nothing, so the MMA issuer's wait for data runs out after wait_ns with
+    // no copy in flight
+    int skip_loads;
+    unsigned long long wait_ns;  // bound on any single mbarrier wait
 };
 
 // ---- PTX wrappers ----------------------------------------------------------
@@ -106,14 +111,16 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
     return ok != 0;
 }
 
-// Bounded wait: false (and the status flag set) if the phase did not complete in time.
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, unsigned int *status) {
+// Bounded wait: false (and the status flag set) if the phase did not complete
+// within wait_ns.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, unsigned int *status,
+                                          unsigned long long wait_ns) {
     if (mbar_try_wait(bar, parity)) return true;
     const unsigned long long t0 = global_ns();
     for (;;) {
         for (int i = 0; i < 64; ++i)
             if (mbar_try_wait(bar, parity)) return true;
-        if (global_ns() - t0 > WAIT_NS) {
+        if (global_ns() - t0 > wait_ns) {
             atomicOr(status, 1u);
             return false;
         }
@@ -337,9 +344,10 @@ __global__ void __launch_bounds__(THREADS, 1) gemm_bf16x3_kernel(const __grid_co
 
     int issued = 0;  // producer: k-blocks whose loads were issued
     if (warp == 0 && lane == 0) {
-        for (int kb = 0; kb < nk; ++kb) {
+        const int nk_issue = e.skip_loads ? 0 : nk;
+        for (int kb = 0; kb < nk_issue; ++kb) {
             const int s = kb % STAGES, round = kb / STAGES;
-            if (round > 0 && !mbar_wait(empty + s, (round - 1) & 1, e.status)) {
+            if (round > 0 && !mbar_wait(empty + s, (round - 1) & 1, e.status, e.wait_ns)) {
                 *abort_flag = 1;
                 break;
             }
@@ -357,7 +365,7 @@ __global__ void __launch_bounds__(THREADS, 1) gemm_bf16x3_kernel(const __grid_co
         constexpr uint32_t idesc = idesc_bf16(BM, BN);
         for (int kb = 0; kb < nk; ++kb) {
             const int s = kb % STAGES, round = kb / STAGES;
-            if (!mbar_wait(full + s, round & 1, e.status)) {
+            if (!mbar_wait(full + s, round & 1, e.status, e.wait_ns)) {
                 *abort_flag = 1;
                 break;
             }
@@ -379,7 +387,10 @@ __global__ void __launch_bounds__(THREADS, 1) gemm_bf16x3_kernel(const __grid_co
     __syncwarp();
 
     // ---- epilogue ----------------------------------------------------------
-    const bool ok = mbar_wait(done, 0, e.status) && !*abort_flag;
+    // twice the bound of the K loop's waits: an MMA issuer whose wait for data
+    // ran out commits `done` before any wait on `done` can give up, so no
+    // thread leaves with that arrival still pending
+    const bool ok = mbar_wait(done, 0, e.status, 2 * e.wait_ns) && !*abort_flag;
     // the next stage may be scheduled once every CTA of this one is here
     asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     tc_fence_after();
@@ -497,7 +508,7 @@ __global__ void __launch_bounds__(THREADS, 1) gemm_bf16x3_kernel(const __grid_co
     if (threadIdx.x == 0 && issued > 0) {
         // after an abort, let every issued load land before the CTA exits
         for (int kb = issued - 1; kb >= 0 && kb >= issued - STAGES; --kb)
-            mbar_wait(full + (kb % STAGES), (kb / STAGES) & 1, e.status);
+            mbar_wait(full + (kb % STAGES), (kb / STAGES) & 1, e.status, e.wait_ns);
     }
     __syncthreads();
     if (warp == 0) {
@@ -621,6 +632,8 @@ void run_stages(const StageMaps &h, FieldSolver &f, float *ex, float *ey, cudaSt
     e.gate_mask = gate_mask;
     e.m = m;
     e.status = f.tc_status;
+    e.skip_loads = f.fault_stall;
+    e.wait_ns = f.fault_stall ? f.fault_wait_ns : WAIT_NS;
     e.wx = f.wx;
     e.wy = f.wy;
     e.scale = 4.0f / ((float)m * (float)m);
@@ -725,6 +738,11 @@ int field_solve_bf16x3(FieldSolver &f, const __nv_bfloat16 *d_hi, const __nv_bfl
     if (!f.tc_ready) return AP_ERR_UNSUPPORTED;
     tc::run_variant(f.tc_variant, f, ex, ey, st, gate, gate_mask);
     return cudaGetLastError() == cudaSuccess ? AP_OK : AP_ERR_CUDA;
+}
+
+int field_solver_clear_status(FieldSolver &f) {
+    if (!f.tc_status) return AP_OK;
+    return cudaMemset(f.tc_status, 0, sizeof(unsigned int)) == cudaSuccess ? AP_OK : AP_ERR_CUDA;
 }
 
 int field_solver_status(FieldSolver &f, unsigned int *out) {

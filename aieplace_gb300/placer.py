@@ -164,6 +164,25 @@ class Placer:
         check("ap_field_solve", lib().ap_field_solve(self._h, ptr(d), ptr(ex), ptr(ey), sv))
         return ex, ey
 
+    def compute_node_forces(self, x, y, ex, ey, gamma: float | None = None, lam: float | None = None):
+        """nudgeNode's per-node force at (x, y) on the field maps (ex, ey),
+        and, when gamma and lam are given, the preconditioned gradient
+        (dWA - lam F) / max(1, pins + lam area / bin area).  Returns (fx, fy)
+        or (fx, fy, gx, gy)."""
+        x = np.ascontiguousarray(x, np.float32)
+        y = np.ascontiguousarray(y, np.float32)
+        ex = np.ascontiguousarray(ex, np.float32).reshape(-1)
+        ey = np.ascontiguousarray(ey, np.float32).reshape(-1)
+        n = self.num_nodes
+        fx, fy = np.zeros(n, np.float32), np.zeros(n, np.float32)
+        grad = gamma is not None and lam is not None
+        gx = np.zeros(n, np.float32) if grad else None
+        gy = np.zeros(n, np.float32) if grad else None
+        check("ap_node_force", lib().ap_node_force(
+            self._h, ptr(x), ptr(y), ptr(ex), ptr(ey), float(gamma or 0.0), float(lam or 0.0), ptr(fx), ptr(fy),
+            ptr(gx) if grad else None, ptr(gy) if grad else None))
+        return (fx, fy, gx, gy) if grad else (fx, fy)
+
     # ---- learned surrogate (no counterpart in the reference) ---------------
     def attach_surrogate(self, surrogate, overflow_min: float = 0.3, judge_every: int = 8,
                          max_error: float = 0.02, use_net: bool = True):

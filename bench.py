@@ -20,8 +20,10 @@ layer alone).
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
 --impl reference times the CPU restatement of the reference path (oracle/,
-FP64, OpenMP) on this host's cores: the reference ships no GPU code and its
-own CPU loop (host C++ behind XRT) does not build outside the VCK5000 flow.
+FP64, OpenMP, field solve by fast transforms) on this host's cores: the
+reference ships no GPU code and its own CPU loop (host C++ behind XRT) does
+not build outside the VCK5000 flow.  That process loads only oracle/
+libraries (the netlist comes from oracle/libsynth.so).
 """
 from __future__ import annotations
 
@@ -167,21 +169,34 @@ def cpu_baseline(nl, budget_s: float = 20.0):
             break
     return {"value": n / el, "unit": UNIT, "cores": cores, "kind": "port",
             "sample": f"FP64 oracle loop on the full workload: init (2 evaluations, untimed) + {n} "
-                      f"iteration(s) in {el:.1f} s on {cores} threads"}
+                      f"iteration(s) in {el:.1f} s on {cores} threads; field solve by fast transforms "
+                      f"(O(M^2 log M))"}
+
+
+def load_presets():
+    """The workload presets (aieplace_gb300/presets.py, data only), read
+    without importing the product package."""
+    import importlib.util
+
+    spec = importlib.util.spec_from_file_location("ap_presets", os.path.join(HERE, "aieplace_gb300", "presets.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod.PRESETS
 
 
 def reference_arm(args):
+    """The reference path's CPU implementation on this host's cores: the FP64
+    oracle loop (oracle/, OpenMP; its field solve by fast transforms like the
+    reference's Ooura/RePlAce solver).  The netlist comes from the standalone
+    generator library (oracle/libsynth.so): this process loads no library of
+    the GPU product."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    import aieplace_gb300 as ap
-    from aieplace_gb300 import build as b
-
-    b.build()
-    nl = ap.synth.generate(args.preset, seed=1)
     import oracle
 
     oracle.build(with_ref=False)
+    nl = oracle.synth_generate(load_presets()[args.preset], seed=1)
     cores = oracle.set_threads(os.cpu_count() or 1)
     pl = oracle.Placer(nl, int(nl["bins"]), float(nl["target_density"]))
     pl.init(nl["node_x"], nl["node_y"])
@@ -208,7 +223,8 @@ def reference_arm(args):
         "config": workload_desc(nl, args.preset),
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
                          "sample": f"{done} of {args.steps} requested FP64 iterations of the full workload "
-                                   f"(bounded to ~{budget:.0f} s)"},
+                                   f"(bounded to ~{budget:.0f} s); field solve by fast transforms "
+                                   f"(O(M^2 log M))"},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)

@@ -200,6 +200,21 @@ int ap_density_map(ap_handle *h, const float *x, const float *y, int64_t *rho_q)
  * field per bin; the solver is params.field_solver or `solver` if >= 0. */
 int ap_field_solve(ap_handle *h, const float *density, float *ex, float *ey, int32_t solver);
 
+/* Per-node field force and preconditioned gradient at given positions, on
+ * caller field maps: the stage of a loop trial between the field solve and
+ * the position update, evaluated by the loop's own gather kernel (through
+ * the bin records a trial's position update makes).  Replaces the
+ * per-component force of Placer::nudgeNode (AIEplace.cpp:1004-1046), which
+ * the reference turns into a fixed-rate step.  x, y: all nodes, netlist
+ * order; ex, ey: field per bin, x-major bins_x*bins_y (as ap_field_solve
+ * returns).  fx, fy receive F_i = sum over the bins b the node overlaps of
+ * (overlap_ib / bin area) * E_b, for movable nodes (0 for fixed nodes).  gx,
+ * gy (both NULL to skip) receive the preconditioned gradient
+ * (dWA/dx_i - lambda F_i) / max(1, pins_i + lambda * area_i / bin area),
+ * the WA gradient taken at smoothing gamma (die units). */
+int ap_node_force(ap_handle *h, const float *x, const float *y, const float *ex, const float *ey, float gamma,
+                  float lambda, float *fx, float *fy, float *gx, float *gy);
+
 /* Allocation-free field solve.  No counterpart in the reference.  For callers
  * that cannot allocate device memory -- a host framework that owns every
  * device allocation and hands out only its own buffers, a fixed memory
@@ -209,8 +224,12 @@ int ap_field_solve(ap_handle *h, const float *density, float *ex, float *ey, int
  * array in the library's static device memory, sized for bins <= 256 (2.1 MB,
  * held on every GPU that loads the library until the process exits).  bins
  * must be a multiple of 32 in [32, 256]; other sizes return
- * AP_ERR_INVALID_ARG.  The first call on a device, and the first after bins
- * or bin_ratio change, looks the scratch address up and fills its transform
+ * AP_ERR_INVALID_ARG.  bin_ratio is bin height / bin width (ap_create uses
+ * (die height / bins_y) / (die width / bins_x)); it scales the y frequencies.
+ * density must start on a 16-byte boundary (it is read in 16-byte vectors)
+ * and ex, ey on a 4-byte boundary; otherwise AP_ERR_INVALID_ARG and nothing
+ * is launched.  The first call on a device, the first after bins or
+ * bin_ratio change and the first in a new CUDA context fill the transform
  * tables: make that call before any stream capture.  All calls share the one
  * scratch array, so calls whose GPU work overlaps race on it.  Work is
  * enqueued on `cuda_stream` (a cudaStream_t, NULL = legacy default stream). */
@@ -226,6 +245,18 @@ int ap_field_solve_noalloc(const float *density, float *ex, float *ey, int32_t b
  * over `samples` (<= 2^32) hashed inputs
  * including rounding ties.  Runs on the current device, synchronously. */
 int ap_selftest_numerics(int32_t *mismatches, int64_t samples);
+
+/* Failure injection for tests of the error paths.  No counterpart in the
+ * reference.  Nothing is faulted: AP_FAULT_TC_STALL makes the tensor-core
+ * solve's load issuer issue no copies and bounds each of its kernels' waits
+ * by wait_ns (1 ms .. 2 s), so the MMA issuer's wait for data that never
+ * arrives runs out, every CTA leaves through the abort path with no copy in
+ * flight (TMEM freed, cluster barriers met), and the next synchronising call
+ * of the handle returns AP_ERR_TIMEOUT; the GPU context stays usable.
+ * AP_FAULT_NONE removes the injection and clears the handle's timeout status.
+ * Needs the tensor-core solver (AP_ERR_UNSUPPORTED otherwise). */
+enum { AP_FAULT_NONE = 0, AP_FAULT_TC_STALL = 1 };
+int ap_debug_inject(ap_handle *h, int32_t kind, int64_t wait_ns);
 
 /* ---- checkpoint / resume ----------------------------------------------- */
 int ap_snapshot_size(ap_handle *h, size_t *bytes);

@@ -213,6 +213,46 @@ void or_density_q(const or_grid *g, int n_nodes, const float *x, const float *y,
     }
 }
 
+/* Placer::nudgeNode's per-component force (AIEplace.cpp:1004-1046): the
+ * field of every bin the node overlaps, weighted by overlap / bin area, with
+ * the overlaps of or_density_q (fixed point, so the weights are exact) and
+ * FP64 sums.  fx, fy are overwritten; nodes with include[i] == 0 get 0. */
+void or_node_force(const or_grid *g, int n_nodes, const float *x, const float *y, const float *w,
+                   const float *h, const uint8_t *include, const double *ex, const double *ey, double *fx,
+                   double *fy) {
+    const double inv_ab = 1.0 / (double)(g->bw_q * g->bh_q);
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < n_nodes; ++i) {
+        double sx = 0.0, sy = 0.0;
+        int c0, c1, r0, r1, small;
+        if ((!include || include[i]) && bin_range(g, x[i], y[i], w[i], h[i], &c0, &c1, &r0, &r1, &small)) {
+            const int64_t xq = llrintf(x[i] * 65536.0f), yq = llrintf(y[i] * 65536.0f);
+            const int64_t wq = llrintf(w[i] * 65536.0f), hq = llrintf(h[i] * 65536.0f);
+            if (small) {
+                const int64_t b = (int64_t)c0 * g->my + r0;
+                const double wt = (double)(wq * hq) * inv_ab;
+                sx = wt * ex[b];
+                sy = wt * ey[b];
+            } else {
+                for (int c = c0; c <= c1; ++c) {
+                    int64_t lo = (int64_t)c * g->bw_q, hi = lo + g->bw_q;
+                    int64_t ow = (hi < xq + wq ? hi : xq + wq) - (lo > xq ? lo : xq);
+                    for (int r = r0; r <= r1; ++r) {
+                        int64_t lo2 = (int64_t)r * g->bh_q, hi2 = lo2 + g->bh_q;
+                        int64_t oh = (hi2 < yq + hq ? hi2 : yq + hq) - (lo2 > yq ? lo2 : yq);
+                        const int64_t b = (int64_t)c * g->my + r;
+                        const double wt = (double)(ow * oh) * inv_ab;
+                        sx += wt * ex[b];
+                        sy += wt * ey[b];
+                    }
+                }
+            }
+        }
+        fx[i] = sx;
+        fy[i] = sy;
+    }
+}
+
 void or_scale_fixed(int nbins, const int64_t *fixed_q, double rho_t, int64_t *out) {
     for (int b = 0; b < nbins; ++b) out[b] = llrint(rho_t * (double)fixed_q[b]);
 }
@@ -506,7 +546,8 @@ static void evaluate(or_placer *o, int gamma_mode) {
         o->hpwl = hp;
     }
     if (gamma_mode == 2) o->gamma = gamma_of(o, o->tau);
-    or_field_solve(o->p.mx, o->p.my, o->bh / o->bw, o->d, NULL, o->ex, o->ey);
+    if (or_field_solve_fft(o->p.mx, o->p.my, o->bh / o->bw, o->d, NULL, o->ex, o->ey) != 0)
+        or_field_solve(o->p.mx, o->p.my, o->bh / o->bw, o->d, NULL, o->ex, o->ey);
 #pragma omp parallel for schedule(static)
     for (int i = 0; i < o->n_mov; ++i) {
         gather_ctx g = {o->ex, o->ey, 0.0, 0.0, 1.0 / o->ab};

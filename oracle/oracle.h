@@ -62,6 +62,14 @@ void or_grid_init(or_grid *g, float die_w, float die_h, int mx, int my);
 void or_density_q(const or_grid *g, int n_nodes, const float *x, const float *y, const float *w,
                   const float *h, const uint8_t *include, int64_t *rho_q);
 
+/* Placer::nudgeNode per-component force (AIEplace.cpp:1004-1046): F_i =
+ * sum over the bins node i overlaps of (overlap / bin area) * E_b, with the
+ * fixed-point overlaps of or_density_q and FP64 sums; fx/fy overwritten
+ * (0 for nodes with include[i] == 0 or no overlap). */
+void or_node_force(const or_grid *g, int n_nodes, const float *x, const float *y, const float *w,
+                   const float *h, const uint8_t *include, const double *ex, const double *ey, double *fx,
+                   double *fy);
+
 /* Overflow: tau = sum_b max(0, tot_b - rho_t*A_b) / movable area (ePlace),
  * and the reference absolute form sum_b max(0, overlap_b - A_b)
  * (Grid.cpp:144-151, Bin.h:123-126).  tot = mov + fixed_scaled. */
@@ -82,6 +90,14 @@ void or_density_float(const or_grid *g, const int64_t *mov_q, const int64_t *fix
  * mx*my; phi may be NULL.  bin_ratio = bh/bw (fft.cpp:172-175). */
 void or_field_solve(int mx, int my, double bin_ratio, const double *d, double *phi, double *ex,
                     double *ey);
+
+/* The same sums as or_field_solve in O(n^2 log n) (fft_solve.c: fast
+ * DCT-II / cosine / sine sums through radix-2 complex FFTs, Makhoul 1980).
+ * n = mx = my a power of two; returns 0, or -1 for other sizes.  The oracle
+ * loop and the timed CPU baseline use this one; the dense solve above is
+ * the checker it is pinned against. */
+int or_field_solve_fft(int mx, int my, double bin_ratio, const double *d, double *phi, double *ex,
+                       double *ey);
 
 /* DCT.cpp:24-82 DCT_naive / IDCT_naive / IDXST_naive in FP64 */
 void or_dct_1d(int n, const double *in, double *out);

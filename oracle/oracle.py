@@ -16,8 +16,11 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "liboracle.so")
+SYNTH_PATH = os.path.join(HERE, "libsynth.so")
 REF_PATH = os.path.join(HERE, "_ref", "libref.so")
-REF_SRC = os.environ.get("AP_REFERENCE_DIR", "/root/reference")
+# the reference checkout, where one exists: AP_REFERENCE_DIR, or the
+# `ref_dir` argument of build(); there is no default location
+REF_SRC = os.environ.get("AP_REFERENCE_DIR", "")
 
 _f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
 _f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
@@ -26,11 +29,15 @@ _i64p = np.ctypeslib.ndpointer(np.int64, flags="C_CONTIGUOUS")
 _u8p = np.ctypeslib.ndpointer(np.uint8, flags="C_CONTIGUOUS")
 
 
-def build(with_ref: bool | None = None) -> None:
-    """Compile liboracle.so, and _ref/libref.so when the reference checkout exists."""
-    subprocess.run(["make", "-s", "-C", HERE, "liboracle.so"], check=True)
+def build(with_ref: bool | None = None, ref_dir: str | None = None) -> None:
+    """Compile liboracle.so and libsynth.so, and _ref/libref.so when a
+    reference checkout is named (ref_dir, else AP_REFERENCE_DIR) and exists."""
+    global REF_SRC
+    if ref_dir:
+        REF_SRC = ref_dir
+    subprocess.run(["make", "-s", "-C", HERE, "liboracle.so", "libsynth.so"], check=True)
     if with_ref is None:
-        with_ref = os.path.isdir(REF_SRC)
+        with_ref = bool(REF_SRC) and os.path.isdir(REF_SRC)
     if with_ref:
         subprocess.run(["make", "-s", "-C", HERE, f"REF={REF_SRC}", "ref"], check=True)
 
@@ -75,9 +82,13 @@ def lib():
         L.or_density_q.argtypes = [C.POINTER(OrGrid), C.c_int, _f32p, _f32p, _f32p, _f32p, C.c_void_p, _i64p]
         L.or_overflow.argtypes = [C.POINTER(OrGrid), _i64p, C.c_void_p, C.c_void_p, C.c_double, C.c_double,
                                   C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        L.or_node_force.argtypes = [C.POINTER(OrGrid), C.c_int, _f32p, _f32p, _f32p, _f32p, C.c_void_p, _f64p,
+                                    _f64p, _f64p, _f64p]
         L.or_scale_fixed.argtypes = [C.c_int, _i64p, C.c_double, _i64p]
         L.or_density_float.argtypes = [C.POINTER(OrGrid), _i64p, C.c_void_p, _f32p]
         L.or_field_solve.argtypes = [C.c_int, C.c_int, C.c_double, _f64p, C.c_void_p, _f64p, _f64p]
+        L.or_field_solve_fft.restype = C.c_int
+        L.or_field_solve_fft.argtypes = [C.c_int, C.c_int, C.c_double, _f64p, C.c_void_p, _f64p, _f64p]
         for n in ("or_dct_1d", "or_idct_1d", "or_idxst_1d"):
             getattr(L, n).argtypes = [C.c_int, _f64p, _f64p]
         L.or_create.restype = C.c_void_p
@@ -163,6 +174,17 @@ def density_q(g: OrGrid, x, y, w, h, include=None):
     return rho
 
 
+def node_force(g: OrGrid, x, y, w, h, ex, ey, include=None):
+    """Per-node overlap-weighted field (FP64), nudgeNode's force."""
+    n = len(x)
+    fx, fy = np.zeros(n), np.zeros(n)
+    inc = None if include is None else np.ascontiguousarray(include, dtype=np.uint8)
+    lib().or_node_force(C.byref(g), n, _f32(x), _f32(y), _f32(w), _f32(h), None if inc is None else inc.ctypes.data,
+                        np.ascontiguousarray(ex, np.float64).reshape(-1),
+                        np.ascontiguousarray(ey, np.float64).reshape(-1), fx, fy)
+    return fx, fy
+
+
 def scale_fixed(fixed_q, rho_t):
     out = np.zeros_like(fixed_q)
     lib().or_scale_fixed(len(fixed_q), np.ascontiguousarray(fixed_q), rho_t, out)
@@ -189,6 +211,17 @@ def field_solve(d, m: int, bin_ratio: float = 1.0, want_phi: bool = False):
     ex, ey = np.zeros(m * m), np.zeros(m * m)
     phi = np.zeros(m * m) if want_phi else None
     lib().or_field_solve(m, m, bin_ratio, d, None if phi is None else phi.ctypes.data, ex, ey)
+    return (ex, ey, phi) if want_phi else (ex, ey)
+
+
+def field_solve_fft(d, m: int, bin_ratio: float = 1.0, want_phi: bool = False):
+    """The same sums as field_solve through fast transforms (fft_solve.c)."""
+    d = np.ascontiguousarray(d, dtype=np.float64).reshape(-1)
+    ex, ey = np.zeros(m * m), np.zeros(m * m)
+    phi = np.zeros(m * m) if want_phi else None
+    rc = lib().or_field_solve_fft(m, m, bin_ratio, d, None if phi is None else phi.ctypes.data, ex, ey)
+    if rc != 0:
+        raise ValueError(f"or_field_solve_fft: unsupported size {m}")
     return (ex, ey, phi) if want_phi else (ex, ey)
 
 
@@ -263,6 +296,68 @@ def _f32(a):
 
 def _i32(a):
     return np.ascontiguousarray(a, dtype=np.int32)
+
+
+# ---- seeded synthetic netlists (libsynth.so) ------------------------------------
+# The generator of the product library built on its own, so that CPU-only
+# processes (the reference arm of bench.py) draw the same netlists without
+# loading the product library.
+
+class SynthConfig(C.Structure):
+    _fields_ = [("num_cells", C.c_int32), ("num_nets", C.c_int32), ("num_macros", C.c_int32),
+                ("num_pads", C.c_int32), ("unit_cells", C.c_int32), ("degree_mix", C.c_int32),
+                ("locality", C.c_float), ("window", C.c_int32), ("macro_area_min", C.c_float),
+                ("macro_area_max", C.c_float), ("target_density", C.c_float), ("die_side", C.c_float),
+                ("seed", C.c_uint64)]
+
+
+_synth = None
+
+
+def synth_lib():
+    global _synth
+    if _synth is None:
+        if not os.path.exists(SYNTH_PATH):
+            build(with_ref=False)
+        L = C.CDLL(SYNTH_PATH)
+        vp = C.c_void_p
+        L.ap_synth_counts.argtypes = [C.POINTER(SynthConfig), C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                                      C.POINTER(C.c_int32)]
+        L.ap_synth_generate.argtypes = [C.POINTER(SynthConfig), vp, vp, vp, vp, vp, vp, vp, vp]
+        _synth = L
+    return _synth
+
+
+def synth_generate(spec: dict, seed: int = 1) -> dict:
+    """The netlist of a preset spec (aieplace_gb300/presets.py) as numpy
+    arrays, identical to aieplace_gb300.synth.generate(spec, seed)."""
+    spec = dict(spec)
+    bins = spec.pop("bins")
+    cfg = SynthConfig(spec["num_cells"], spec["num_nets"], spec["num_macros"], spec["num_pads"],
+                      spec["unit_cells"], spec["degree_mix"], spec["locality"], spec["window"],
+                      spec.get("macro_area_min", 20.0), spec.get("macro_area_max", 200.0),
+                      spec["target_density"], spec["die_side"], seed)
+    nn, ne, npins = C.c_int32(), C.c_int32(), C.c_int32()
+    L = synth_lib()
+    if L.ap_synth_counts(C.byref(cfg), C.byref(nn), C.byref(ne), C.byref(npins)) != 0:
+        raise ValueError("ap_synth_counts rejected the spec")
+    out = {
+        "net_ptr": np.zeros(ne.value + 1, np.int32),
+        "pin_node": np.zeros(max(npins.value, 1), np.int32)[: npins.value],
+        "node_w": np.zeros(nn.value, np.float32),
+        "node_h": np.zeros(nn.value, np.float32),
+        "node_x": np.zeros(nn.value, np.float32),
+        "node_y": np.zeros(nn.value, np.float32),
+        "node_fixed": np.zeros(nn.value, np.uint8),
+        "die": np.zeros(4, np.float32),
+    }
+    keys = ("net_ptr", "pin_node", "node_w", "node_h", "node_x", "node_y", "node_fixed", "die")
+    if L.ap_synth_generate(C.byref(cfg), *[C.c_void_p(out[k].ctypes.data) for k in keys]) != 0:
+        raise ValueError("ap_synth_generate failed")
+    out["bins"] = bins
+    out["target_density"] = spec["target_density"]
+    out["seed"] = seed
+    return out
 
 
 # ---- learned surrogate network (surrogate.c) -----------------------------------

@@ -17,7 +17,7 @@ def pytest_configure(config):
 def oracle_lib():
     import oracle
 
-    oracle.build(with_ref=os.path.isdir(oracle.REF_SRC))
+    oracle.build()  # _ref/libref.so too where a reference checkout is named
     return oracle
 
 

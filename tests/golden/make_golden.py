@@ -2,8 +2,10 @@
 
 Run here (not on the GPU machine, which has no reference checkout):
 
-    make -C oracle ref            # builds oracle/_ref/libref.so from the reference sources
-    python tests/golden/make_golden.py [/path/to/reference]
+    python tests/golden/make_golden.py <path of the reference checkout>
+
+(it builds oracle/_ref/libref.so from the reference sources first, through
+`make -C oracle ref REF=<path>`).
 
 Sources of each fixture:
   aie_partials.npz   vck5000/aie/golden_data/partials/*.dat (createGoldenPartials.py:28-132)
@@ -148,11 +150,12 @@ def ref_grid(R):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("AP_REFERENCE_DIR", "/root/reference")
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("AP_REFERENCE_DIR", "")
+    if not ref or not os.path.isdir(ref):
+        sys.exit("usage: make_golden.py <path of the searsm8/AIEplace checkout> (or set AP_REFERENCE_DIR)")
     import oracle  # noqa: E402
 
-    oracle.REF_SRC = ref
-    oracle.build(with_ref=True)
+    oracle.build(with_ref=True, ref_dir=ref)
     R = oracle.ref_lib()
     assert R is not None, "oracle/_ref/libref.so did not build"
     aie_partials(ref)

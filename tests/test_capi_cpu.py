@@ -116,3 +116,18 @@ def test_generator_deterministic_and_shaped(lib):
             j += 1
     c0 = synth.generate("c0", seed=1)
     assert len(c0["node_w"]) == 600 and c0["die"][2] == 24.0
+
+
+@pytest.mark.parametrize("preset", ["c0", "c1_small"])
+def test_standalone_generator_matches_library(lib, preset):
+    """oracle/libsynth.so (the generator built on its own, for CPU-only
+    processes) draws the same netlists as the product library."""
+    import oracle
+
+    import aieplace_gb300 as ap
+
+    oracle.build(with_ref=False)
+    a = ap.synth.generate(preset, seed=3)
+    b = oracle.synth_generate(ap.synth.PRESETS[preset], seed=3)
+    for k in ("net_ptr", "pin_node", "node_w", "node_h", "node_x", "node_y", "node_fixed", "die"):
+        assert np.array_equal(a[k], b[k]), k

@@ -108,6 +108,31 @@ def test_field_solve_matches_replace_fft(oracle_lib, case):
         assert np.abs(mine - ref).max() <= 2e-6 * np.abs(ref).max() + 1e-9
 
 
+@pytest.mark.parametrize("case", ["run_fft4", "rand16", "rand32", "rand64"])
+def test_fast_field_solve_matches_replace_fft(oracle_lib, case):
+    """The O(n^2 log n) solve that the oracle loop and the CPU baseline use,
+    pinned to the reference's own Ooura solver output like the dense one."""
+    g = golden("replace_field.npz")
+    d = g[f"{case}_density"].astype(np.float64)
+    m = d.shape[0]
+    ex, ey, phi = oracle_lib.field_solve_fft(d, m, want_phi=True)
+    for mine, ref in ((ex, g[f"{case}_ex"]), (ey, g[f"{case}_ey"]), (phi, g[f"{case}_phi"])):
+        ref = ref.reshape(-1).astype(np.float64)
+        assert np.abs(mine - ref).max() <= 2e-6 * np.abs(ref).max() + 1e-9
+
+
+@pytest.mark.parametrize("m,ratio", [(8, 1.0), (64, 1.0), (256, 1.5), (1024, 1.0)])
+def test_fast_field_solve_matches_dense(oracle_lib, m, ratio):
+    """Fast transforms against the dense FP64 sums (the checker): the same
+    sums in another order, so agreement is at FP64 rounding level."""
+    rng = np.random.default_rng(m)
+    d = rng.random(m * m) + np.where(rng.random(m * m) < 0.01, 5.0, 0.0)
+    ex, ey, phi = oracle_lib.field_solve(d, m, ratio, want_phi=True)
+    fx, fy, fphi = oracle_lib.field_solve_fft(d, m, ratio, want_phi=True)
+    for a, b in ((ex, fx), (ey, fy), (phi, fphi)):
+        assert np.abs(a - b).max() <= 1e-11 * np.abs(a).max()
+
+
 def test_density_matches_reference_grid(oracle_lib):
     g = golden("ref_grid.npz")
     W, M = float(g["die"][0]), int(g["m"])
