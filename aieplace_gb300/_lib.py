@@ -23,6 +23,8 @@ EXPORTS = [
     "ap_snapshot_size", "ap_snapshot",
     "ap_restore",
     "ap_synth_counts", "ap_synth_generate",
+    "ap_design_read", "ap_design_read_dir", "ap_design_get_info", "ap_design_netlist", "ap_design_name",
+    "ap_design_node_name", "ap_design_write_def", "ap_design_last_error", "ap_design_destroy",
     "ap_create_batch", "ap_batch_destroy", "ap_batch_init_seeded", "ap_batch_step", "ap_batch_run",
     "ap_batch_get_stats", "ap_batch_get_positions",
     "ap_surrogate_config_default", "ap_surrogate_create", "ap_surrogate_destroy", "ap_surrogate_num_params",
@@ -86,6 +88,12 @@ class SurrogateStats(C.Structure):
     _fields_ = [("used", C.c_int32), ("judged", C.c_int32), ("fallbacks", C.c_int32), ("last_error", C.c_double)]
 
 
+class DesignInfo(C.Structure):
+    _fields_ = [("num_nodes", C.c_int32), ("num_nets", C.c_int32), ("num_pins", C.c_int32),
+                ("num_components", C.c_int32), ("num_io_pins", C.c_int32), ("units_per_micron", C.c_int32),
+                ("die_xl", C.c_float), ("die_yl", C.c_float), ("die_xh", C.c_float), ("die_yh", C.c_float)]
+
+
 class SynthConfig(C.Structure):
     _fields_ = [("num_cells", C.c_int32), ("num_nets", C.c_int32), ("num_macros", C.c_int32),
                 ("num_pads", C.c_int32), ("unit_cells", C.c_int32), ("degree_mix", C.c_int32),
@@ -125,6 +133,18 @@ def lib():
         L.ap_wirelength_grad.argtypes = [vp, vp, vp, f32, vp, vp, C.POINTER(C.c_double), C.POINTER(C.c_double)]
         L.ap_node_force.argtypes = [vp, vp, vp, vp, vp, f32, f32, vp, vp, vp, vp]
         L.ap_debug_inject.argtypes = [vp, i32, C.c_int64]
+        L.ap_design_read.argtypes = [C.POINTER(C.c_char_p), i32, C.c_char_p, i32, C.POINTER(vp)]
+        L.ap_design_read_dir.argtypes = [C.c_char_p, i32, C.POINTER(vp)]
+        L.ap_design_get_info.argtypes = [vp, C.POINTER(DesignInfo)]
+        L.ap_design_netlist.argtypes = [vp, C.POINTER(Netlist)]
+        L.ap_design_name.restype = C.c_char_p
+        L.ap_design_name.argtypes = [vp]
+        L.ap_design_node_name.restype = C.c_char_p
+        L.ap_design_node_name.argtypes = [vp, i32]
+        L.ap_design_write_def.argtypes = [vp, vp, vp, C.c_char_p]
+        L.ap_design_last_error.restype = C.c_char_p
+        L.ap_design_last_error.argtypes = []
+        L.ap_design_destroy.argtypes = [vp]
         L.ap_density_map.argtypes = [vp, vp, vp, vp]
         L.ap_field_solve.argtypes = [vp, vp, vp, vp, i32]
         L.ap_field_solve_noalloc.argtypes = [vp, vp, vp, i32, f32, vp]

@@ -17,7 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libaieplace_gb300.so")
 SOURCES = ["capi.cu", "k_wirelength.cu", "k_density.cu", "k_field_simt.cu", "k_field_tc.cu", "k_surrogate.cu",
-           "synth.cpp"]
+           "synth.cpp", "lefdef.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -97,7 +97,11 @@ struct RhoArgs {
     const long long *fixs_q;    // fixed nodes scaled by rho_t
     long long cap_q, ab_q;
     double inv_ab;
-    float inv_ab_f;             // (float)(1 / ab_q): density = (float)tot * inv_ab_f
+    float inv_ab_f;             // (float)(1 / ab_q): density = (float)tot * inv_ab_f - d_shift
+    // A constant taken off the solver input: the field ignores the map's mean
+    // (the DC coefficient is dropped, phi_00 = 0), and without it the large
+    // mean's rounding in the transforms' DC sums swamps the small AC terms
+    float d_shift;
     float *d_f32;               // FP32 solver input, or null
     __nv_bfloat16 *d_hi, *d_lo; // BF16x3 solver input, or null
     DevScalars *sc;

@@ -45,6 +45,7 @@ struct ap_handle {
     Grid g{};
     long long cap_q = 0, ab_q = 0;
     double inv_ab = 0, mov_area_q = 0;
+    float d_shift = 0.f;  // mean density of the loop's solver input, taken off before the solve
     // device state
     int *d_net_ptr = nullptr, *d_pin_node = nullptr;
     float *d_w = nullptr, *d_h = nullptr;
@@ -142,6 +143,7 @@ RhoArgs rho_args(ap_handle *h, int mode, double *out) {
     a.ab_q = h->ab_q;
     a.inv_ab = h->inv_ab;
     a.inv_ab_f = (float)h->inv_ab;
+    a.d_shift = h->d_shift;
     if (h->p.field_solver == AP_FIELD_BF16X3) {
         a.d_hi = h->d_dens_hi;
         a.d_lo = h->d_dens_lo;
@@ -798,7 +800,14 @@ int ap_create(const ap_netlist *nl, const ap_params *params, ap_handle **out) {
         launch_scatter(s, 0);
         std::vector<long long> fq(nb), fs(nb);
         A(cudaMemcpy(fq.data(), h->d_mov_q, sizeof(long long) * nb, cudaMemcpyDeviceToHost));
-        for (size_t b = 0; b < nb; ++b) fs[b] = llrint((double)p.target_density * (double)fq[b]);
+        double fixed_scaled = 0.0;
+        for (size_t b = 0; b < nb; ++b) {
+            fs[b] = llrint((double)p.target_density * (double)fq[b]);
+            fixed_scaled += (double)fs[b];
+        }
+        // mean of movable + scaled fixed density over the bins (the movable
+        // nodes stay on the die, so their total is constant)
+        h->d_shift = (float)((mov_area_q + fixed_scaled) * h->inv_ab / (double)nb);
         A(cudaMemcpy(h->d_fix_q, fq.data(), sizeof(long long) * nb, cudaMemcpyHostToDevice));
         A(cudaMemcpy(h->d_fixs_q, fs.data(), sizeof(long long) * nb, cudaMemcpyHostToDevice));
         A(cudaMemset(h->d_mov_q, 0, sizeof(ull) * nb));
@@ -1220,7 +1229,14 @@ int ap_field_solve(ap_handle *h, const float *density, float *ex, float *ey, int
     if (sv != AP_FIELD_FP32 && sv != AP_FIELD_BF16X3) return AP_ERR_INVALID_ARG;
     const int nb = h->p.bins_x * h->p.bins_y;
     if (sv == AP_FIELD_BF16X3 && !h->fs.tc_ready) return AP_ERR_UNSUPPORTED;
-    CK(cudaMemcpyAsync(h->d_dens, density, sizeof(float) * nb, cudaMemcpyHostToDevice, h->stream));
+    // the field does not depend on the map's mean (phi_00 = 0); taking it off
+    // keeps the transforms' DC sums from swamping the AC terms in rounding
+    double mean = 0.0;
+    for (int b = 0; b < nb; ++b) mean += (double)density[b];
+    mean /= (double)nb;
+    std::vector<float> shifted((size_t)nb);
+    for (int b = 0; b < nb; ++b) shifted[(size_t)b] = density[b] - (float)mean;
+    CK(cudaMemcpyAsync(h->d_dens, shifted.data(), sizeof(float) * nb, cudaMemcpyHostToDevice, h->stream));
     if (sv == AP_FIELD_BF16X3) launch_split_bf16(nb, h->d_dens, h->d_dens_hi, h->d_dens_lo, h->stream);
     int r = run_field(h, sv, h->stream);
     if (r != AP_OK) return r;

@@ -480,7 +480,7 @@ __global__ void __launch_bounds__(kThreads) rho_kernel(RhoArgs a) {
                 over += t > 0 ? t : 0;
                 const long long ab = m[k] + f[k] - a.ab_q;
                 over_abs += ab > 0 ? ab : 0;
-                d[k] = ll2f_rn_bits(tot) * a.inv_ab_f;  // same float ops as or_density_float
+                d[k] = ll2f_rn_bits(tot) * a.inv_ab_f - a.d_shift;
             }
             if (a.d_f32) reinterpret_cast<float2 *>(a.d_f32)[p] = make_float2(d[0], d[1]);
             if (a.d_hi) {

@@ -353,6 +353,59 @@ int ap_surrogate_validate(ap_surrogate *s, int32_t first, int32_t count, double 
 int ap_attach_surrogate(ap_handle *h, ap_surrogate *s, const ap_surrogate_policy *policy);
 int ap_surrogate_get_stats(ap_handle *h, ap_surrogate_stats *stats);
 
+/* ---- LEF/DEF designs ---------------------------------------------------------
+ * Replaces the reference host's DataBase ingest (DataBase.cpp:42-96, readLEF
+ * / readDEF through Limbo, and the callbacks that keep data, :340-416) and
+ * DataBase::writeDEF (:538-655), for the subset those callbacks consume: LEF
+ * MACRO SIZE; DEF DESIGN, UNITS DISTANCE MICRONS, DIEAREA, COMPONENTS, PINS
+ * (first LAYER rectangle, placement, direction) and NETS (component and IO
+ * pin connections).  Other statements and sections are skipped.
+ * Netlist view (ap_design_netlist): nodes are the DEF components in file
+ * order, then the DEF IO pins; coordinates are DEF database units.
+ * Components placed FIXED or COVER are fixed; IO pins are fixed zero-area
+ * nodes carrying pins only (the reference leaves them out of the density
+ * map, AIEplace.cpp:937-958).
+ * Macro sizes: AP_LEF_SIZE_DBU scales the LEF SIZE (microns) by UNITS
+ * DISTANCE MICRONS and swaps width and height of components placed E, W, FE
+ * or FW, so sizes and positions share one unit; AP_LEF_SIZE_AS_READ takes the
+ * LEF numbers as they are and ignores orientation, as the reference host
+ * does (lef_macro_cbk keeps lefiMacro::sizeX/sizeY beside DEF coordinates in
+ * database units). */
+enum { AP_LEF_SIZE_DBU = 0, AP_LEF_SIZE_AS_READ = 1 };
+
+typedef struct ap_design ap_design;
+
+typedef struct ap_design_info {
+    int32_t num_nodes, num_nets, num_pins;  /* sizes of the netlist view */
+    int32_t num_components, num_io_pins;
+    int32_t units_per_micron;               /* DEF UNITS DISTANCE MICRONS */
+    float die_xl, die_yl, die_xh, die_yh;   /* DIEAREA (bounding box), database units */
+} ap_design_info;
+
+/* LEF files are read in order (a later MACRO of a name replaces an earlier
+ * one), then the DEF.  Syntax errors and references to undefined macros,
+ * components or pins return AP_ERR_BAD_NETLIST; ap_design_last_error() then
+ * names the file, line and cause. */
+int ap_design_read(const char *const *lef_paths, int32_t n_lef, const char *def_path, int32_t size_mode,
+                   ap_design **out);
+/* The reference's input convention (DataBase.cpp:42-96): every *.lef file of
+ * `dir` (in name order) and dir/floorplan.def. */
+int ap_design_read_dir(const char *dir, int32_t size_mode, ap_design **out);
+int ap_design_get_info(ap_design *d, ap_design_info *info);
+/* Fills *nl with pointers into the design (valid until ap_design_destroy);
+ * ready for ap_create. */
+int ap_design_netlist(ap_design *d, ap_netlist *nl);
+const char *ap_design_name(ap_design *d);
+const char *ap_design_node_name(ap_design *d, int32_t node);
+/* Writes the design as DEF 5.8 with the node positions x, y (netlist order,
+ * database units, lower-left corners, as ap_get_positions returns them)
+ * rounded to integers: movable components PLACED at their new position, fixed
+ * ones where they were.  The position export a downstream legaliser reads. */
+int ap_design_write_def(ap_design *d, const float *x, const float *y, const char *path);
+/* the message of the last failed read or write on this thread ("" if none) */
+const char *ap_design_last_error(void);
+int ap_design_destroy(ap_design *d);
+
 /* ---- seeded synthetic netlists ------------------------------------------ */
 /* Stands in for the ISPD suites the reference reads through LEF/DEF.  Nodes
  * are ordered: movable cells, fixed macros, IO pads. */
