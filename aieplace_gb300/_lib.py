@@ -19,12 +19,13 @@ EXPORTS = [
     "ap_set_stream", "ap_init_positions", "ap_init_seeded", "ap_step", "ap_step_async",
     "ap_profile_stages", "ap_solver_info", "ap_run", "ap_step_host",
     "ap_get_positions", "ap_get_stats", "ap_hpwl", "ap_overflow", "ap_wirelength_grad",
-    "ap_density_map", "ap_field_solve", "ap_node_force", "ap_debug_inject", "ap_field_solve_noalloc", "ap_selftest_numerics",
+    "ap_density_map", "ap_field_solve", "ap_node_force", "ap_debug_inject", "ap_set_log", "ap_get_fillers",
+    "ap_run_config_default", "ap_run_config_read", "ap_last_error", "ap_field_solve_noalloc", "ap_selftest_numerics",
     "ap_snapshot_size", "ap_snapshot",
     "ap_restore",
     "ap_synth_counts", "ap_synth_generate",
     "ap_design_read", "ap_design_read_dir", "ap_design_get_info", "ap_design_netlist", "ap_design_name",
-    "ap_design_node_name", "ap_design_write_def", "ap_design_last_error", "ap_design_destroy",
+    "ap_design_node_name", "ap_design_write_def", "ap_design_destroy",
     "ap_create_batch", "ap_batch_destroy", "ap_batch_init_seeded", "ap_batch_step", "ap_batch_run",
     "ap_batch_get_stats", "ap_batch_get_positions",
     "ap_surrogate_config_default", "ap_surrogate_create", "ap_surrogate_destroy", "ap_surrogate_num_params",
@@ -59,7 +60,8 @@ class Params(C.Structure):
                 ("lambda_mu_max", C.c_float), ("lambda_mu_min", C.c_float),
                 ("init_step_coef", C.c_float), ("target_overflow", C.c_float),
                 ("max_iterations", C.c_int32), ("check_interval", C.c_int32),
-                ("use_graph", C.c_int32), ("max_backtracks", C.c_int32), ("restart_mode", C.c_int32)]
+                ("use_graph", C.c_int32), ("max_backtracks", C.c_int32), ("restart_mode", C.c_int32),
+                ("filler_cells", C.c_int32)]
 
 
 class Stats(C.Structure):
@@ -86,6 +88,13 @@ class SurrogatePolicy(C.Structure):
 
 class SurrogateStats(C.Structure):
     _fields_ = [("used", C.c_int32), ("judged", C.c_int32), ("fallbacks", C.c_int32), ("last_error", C.c_double)]
+
+
+class RunConfig(C.Structure):
+    _fields_ = [("input_dir", C.c_char * 1024), ("output_dir", C.c_char * 1024), ("log_path", C.c_char * 1024),
+                ("size_mode", C.c_int32), ("wirelength_method", C.c_int32), ("init_sigma", C.c_float),
+                ("seed", C.c_uint64), ("filler_cells", C.c_int32), ("use_aie", C.c_int32),
+                ("ignored_learning_rate", C.c_float)]
 
 
 class DesignInfo(C.Structure):
@@ -133,6 +142,7 @@ def lib():
         L.ap_wirelength_grad.argtypes = [vp, vp, vp, f32, vp, vp, C.POINTER(C.c_double), C.POINTER(C.c_double)]
         L.ap_node_force.argtypes = [vp, vp, vp, vp, vp, f32, f32, vp, vp, vp, vp]
         L.ap_debug_inject.argtypes = [vp, i32, C.c_int64]
+        L.ap_set_log.argtypes = [vp, C.c_char_p, i32]
         L.ap_design_read.argtypes = [C.POINTER(C.c_char_p), i32, C.c_char_p, i32, C.POINTER(vp)]
         L.ap_design_read_dir.argtypes = [C.c_char_p, i32, C.POINTER(vp)]
         L.ap_design_get_info.argtypes = [vp, C.POINTER(DesignInfo)]
@@ -142,8 +152,11 @@ def lib():
         L.ap_design_node_name.restype = C.c_char_p
         L.ap_design_node_name.argtypes = [vp, i32]
         L.ap_design_write_def.argtypes = [vp, vp, vp, C.c_char_p]
-        L.ap_design_last_error.restype = C.c_char_p
-        L.ap_design_last_error.argtypes = []
+        L.ap_last_error.restype = C.c_char_p
+        L.ap_last_error.argtypes = []
+        L.ap_get_fillers.argtypes = [vp, C.POINTER(i32), C.POINTER(f32), C.POINTER(f32)]
+        L.ap_run_config_default.argtypes = [C.POINTER(Params), C.POINTER(RunConfig)]
+        L.ap_run_config_read.argtypes = [C.c_char_p, C.POINTER(Params), C.POINTER(RunConfig)]
         L.ap_design_destroy.argtypes = [vp]
         L.ap_density_map.argtypes = [vp, vp, vp, vp]
         L.ap_field_solve.argtypes = [vp, vp, vp, vp, i32]

@@ -16,8 +16,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libaieplace_gb300.so")
+CLI = os.path.join(HERE, "aieplace")  # the command-line placer (csrc/cli.cpp), linked to LIB
 SOURCES = ["capi.cu", "k_wirelength.cu", "k_density.cu", "k_field_simt.cu", "k_field_tc.cu", "k_surrogate.cu",
-           "synth.cpp", "lefdef.cpp"]
+           "synth.cpp", "lefdef.cpp", "config.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -53,9 +54,10 @@ def build(force: bool = False, verbose_ptxas: bool = False) -> str:
     srcs = [os.path.join(CSRC, s) for s in SOURCES]
     hdrs = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
     hdrs.append(os.path.join(os.path.dirname(HERE), "include", "aieplace.h"))
-    if not force and os.path.exists(LIB):
-        newest = max(os.path.getmtime(p) for p in srcs + hdrs)
-        if os.path.getmtime(LIB) >= newest:
+    cli_src = os.path.join(CSRC, "cli.cpp")
+    if not force and os.path.exists(LIB) and os.path.exists(CLI):
+        newest = max(os.path.getmtime(p) for p in srcs + hdrs + [cli_src])
+        if os.path.getmtime(LIB) >= newest and os.path.getmtime(CLI) >= newest:
             return LIB
     with ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         objs = list(ex.map(lambda s: _compile(s, verbose_ptxas), SOURCES))
@@ -65,6 +67,12 @@ def build(force: bool = False, verbose_ptxas: bool = False) -> str:
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, LIB)
+    cmd = ["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-I", os.path.join(os.path.dirname(HERE), "include"),
+           cli_src, "-L", HERE, "-laieplace_gb300", "-Wl,-rpath,$ORIGIN", "-o", CLI + ".tmp"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"build of the command-line placer failed:\n{r.stdout}\n{r.stderr}")
+    os.replace(CLI + ".tmp", CLI)
     return LIB
 
 

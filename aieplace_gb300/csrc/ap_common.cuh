@@ -24,6 +24,19 @@ constexpr int kGateSurr = (1 << kFieldSurr) | (1 << kFieldJudge);
 constexpr int kGateJudge = 1 << kFieldJudge;
 constexpr int kThreads = 256;
 
+// One trial of the loop, as the trajectory log keeps it: written by the
+// gather's last block into a ring in device memory, drained by the host
+// whenever it reads the scalars (no synchronisation per iteration).
+struct TrajRec {
+    int eval;        // trial number (gradient evaluations before it)
+    int iteration;   // accepted iterations after it
+    int accepted;    // 1 accepted, 0 retried with a shorter step, -1 diverged
+    int field_mode;  // kFieldExact / kFieldSurr / kFieldJudge
+    double hpwl, overflow, overflow_abs, lambda, alpha, gamma;
+    double surr_err;               // last judged surrogate field error
+    unsigned long long t_ns;       // device clock (%globaltimer) at the trial's end
+};
+
 // FP64 scalars of the optimiser; live in device memory so a whole iteration
 // runs without host round trips (and can be captured in a CUDA graph).
 // Each launch of the iteration sequence is one trial step from the accepted
@@ -71,6 +84,9 @@ struct DevScalars {
     // (a double -> float conversion in every thread costs FP64-pipe time);
     // refreshed by publish_f32 wherever the doubles change on the device
     float f_alpha, f_mom, f_lambda, f_gamma;
+    // trajectory log (null: off): record of trial e at traj[e % traj_cap]
+    TrajRec *traj;
+    int traj_cap;
 };
 
 __device__ __forceinline__ void publish_f32(DevScalars *sc) {

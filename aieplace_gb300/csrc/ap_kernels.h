@@ -51,7 +51,8 @@ constexpr int kWaMaxBlocks = 2432;
 struct ScatterArgs {
     Grid g;
     const float *w, *h;
-    // plain mode: scatter nodes [lo, hi) at (px, py)
+    // the bin adds take nodes [lo, hi): plain mode at (px, py), update mode
+    // from the records the position update wrote
     const float *px, *py;
     int lo, hi;
     // update mode: movable nodes [0, n_mov) step from the accepted state
@@ -93,6 +94,7 @@ enum { RHO_OUT_ONLY = 0, RHO_LOOP = 1, RHO_INIT = 2 };
 struct RhoArgs {
     int nbins;
     ull *mov_q;                 // read, then cleared for the next iteration
+    ull *fill_q;                // filler cells (null: none): in the solver input, not in the overflow; cleared
     const long long *fix_q;     // fixed nodes at weight 1
     const long long *fixs_q;    // fixed nodes scaled by rho_t
     long long cap_q, ab_q;

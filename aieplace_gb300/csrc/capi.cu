@@ -37,8 +37,14 @@ cudaError_t dalloc(T **p, size_t n) {
 
 struct ap_handle {
     // sizes
+    // internal node order: real movable cells [0, n_real), filler cells
+    // [n_real, n_mov), fixed nodes with area [n_mov, n_mov + n_fixa), then
+    // zero-area fixed nodes; n_nodes counts all of them, n_ext the netlist's
     int n_nodes = 0, n_mov = 0, n_fixa = 0, n_nets = 0, n_pins = 0, n_small = 0;
-    std::vector<int> ext2int, int2ext;
+    int n_ext = 0, n_real = 0, n_fill = 0;
+    float fill_w = 0.f, fill_h = 0.f;
+    std::vector<float> fill_x0, fill_y0;  // fillers' starting points (internal die coordinates)
+    std::vector<int> ext2int, int2ext;    // int2ext[i] = -1 for fillers
     bool identity = true;
     float die_xl = 0, die_yl = 0, die_w = 0, die_h = 0;
     ap_params p{};
@@ -58,6 +64,7 @@ struct ap_handle {
     ull *d_gq = nullptr;                     // packed WA gradient accumulators (pack_q)
     ull *d_gqx = nullptr, *d_gqy = nullptr;  // per axis, nodes of more than kPackMaxPins pins
     ull *d_mov_q = nullptr;
+    ull *d_fill_q = nullptr;  // filler cells' map: in the field, not in the overflow
     long long *d_fix_q = nullptr, *d_fixs_q = nullptr;
     float *d_dens = nullptr, *d_ex = nullptr, *d_ey = nullptr;
     __nv_bfloat16 *d_dens_hi = nullptr, *d_dens_lo = nullptr;
@@ -93,6 +100,14 @@ struct ap_handle {
     cudaEvent_t ev_start = nullptr, ev_in[4] = {nullptr, nullptr, nullptr, nullptr};
     float *d_ix = nullptr, *d_iy = nullptr;
     ap_surrogate_policy policy{0.3f, 8, 0.02f, 1};
+    // trajectory log: device ring of per-trial records, drained into `log`
+    // (JSON lines) whenever the scalars are read
+    TrajRec *d_traj = nullptr;
+    int traj_cap = 0;
+    FILE *log = nullptr;
+    long long log_next = 0;         // first trial not yet written
+    unsigned long long log_t0 = 0;  // device clock of the first record written
+    std::vector<TrajRec> log_buf;
 };
 
 namespace {
@@ -137,6 +152,7 @@ RhoArgs rho_args(ap_handle *h, int mode, double *out) {
     RhoArgs a{};
     a.nbins = h->p.bins_x * h->p.bins_y;
     a.mov_q = h->d_mov_q;
+    a.fill_q = h->d_fill_q;
     a.fix_q = h->d_fix_q;
     a.fixs_q = h->d_fixs_q;
     a.cap_q = h->cap_q;
@@ -218,7 +234,24 @@ ScatterArgs loop_scatter_args(ap_handle *h) {
     s.update = 1;
     s.rec_bin = h->d_rec_bin;
     s.rec_ov = h->d_rec_ov;
+    s.lo = 0;
+    s.hi = h->n_mov;
     return s;
+}
+
+// Bin adds of the movable nodes (either mode): real cells into the movable
+// map, filler cells into their own.
+void launch_movable_bins(ap_handle *h, ScatterArgs s, cudaStream_t st) {
+    s.lo = 0;
+    s.hi = h->n_real;
+    s.rho_q = h->d_mov_q;
+    launch_scatter_bins(s, st);
+    if (h->n_fill) {
+        s.lo = h->n_real;
+        s.hi = h->n_mov;
+        s.rho_q = h->d_fill_q;
+        launch_scatter_bins(s, st);
+    }
 }
 
 GatherArgs loop_gather_args(ap_handle *h) {
@@ -268,10 +301,9 @@ int join_wa(ap_handle *h, cudaStream_t st) {
 
 // The trial after its position update.
 int enqueue_after_update(ap_handle *h, cudaStream_t st) {
-    const ScatterArgs sa = loop_scatter_args(h);
     int r = fork_wa(h, st);
     if (r != AP_OK) return r;
-    launch_scatter_bins(sa, st);
+    launch_movable_bins(h, loop_scatter_args(h), st);
     launch_rho(rho_args(h, RHO_LOOP, nullptr), st);
     if (h->surr) {
         r = enqueue_field_surrogate(h, st, -1);
@@ -297,9 +329,7 @@ int enqueue_eval(ap_handle *h, int at, int rho_mode, int wa_mode, cudaStream_t s
     s.update = 0;
     s.px = h->d_px[at];
     s.py = h->d_py[at];
-    s.lo = 0;
-    s.hi = h->n_mov;
-    launch_scatter(s, st);
+    launch_movable_bins(h, s, st);
     launch_rho(rho_args(h, rho_mode, h->d_out), st);
     launch_wirelength(wa_args(h, h->d_px[at], h->d_py[at], 0.f, h->n_mov, wa_mode, h->d_out + 2), st);
     return run_field(h, h->p.field_solver, st);
@@ -338,7 +368,7 @@ int capture_trial_switched(ap_handle *h) {
     launch_update(sa, st);
     const int fr = fork_wa(h, st);
     if (fr != AP_OK) return fr;
-    launch_scatter_bins(sa, st);
+    launch_movable_bins(h, sa, st);
     RhoArgs ra = rho_args(h, RHO_LOOP, nullptr);
     ra.field_switch = sw_handle;
     launch_rho(ra, st);
@@ -392,6 +422,11 @@ int upload_positions(ap_handle *h, int at, const float *x, const float *y) {
     std::vector<float> ix((size_t)h->n_mov), iy((size_t)h->n_mov);
     for (int i = 0; i < h->n_mov; ++i) {
         const int e = h->int2ext[(size_t)i];
+        if (e < 0) {  // filler cells start where ap_create put them
+            ix[(size_t)i] = h->fill_x0[(size_t)(i - h->n_real)];
+            iy[(size_t)i] = h->fill_y0[(size_t)(i - h->n_real)];
+            continue;
+        }
         ix[(size_t)i] = x[e] - h->die_xl;
         iy[(size_t)i] = y[e] - h->die_yl;
         if (!std::isfinite(ix[(size_t)i]) || !std::isfinite(iy[(size_t)i])) return AP_ERR_NONFINITE;
@@ -401,9 +436,49 @@ int upload_positions(ap_handle *h, int at, const float *x, const float *y) {
     return sync(h);
 }
 
+// Writes the trajectory records of the trials run since the last drain (the
+// scalars in h_sc are fresh).  A ring that wrapped since then loses its
+// oldest records; the log says how many.
+int drain_log(ap_handle *h) {
+    const long long ev = h->h_sc->evals;
+    if (ev < h->log_next) h->log_next = 0;  // the optimiser was reset
+    if (ev == h->log_next) return AP_OK;
+    if (ev - h->log_next > h->traj_cap) {
+        fprintf(h->log, "{\"lost_trials\": %lld}\n", ev - h->traj_cap - h->log_next);
+        h->log_next = ev - h->traj_cap;
+    }
+    const long long n = ev - h->log_next;
+    h->log_buf.resize((size_t)n);
+    const long long first = h->log_next % h->traj_cap;
+    const long long run1 = std::min(n, h->traj_cap - first);
+    CK(cudaMemcpyAsync(h->log_buf.data(), h->d_traj + first, sizeof(TrajRec) * run1, cudaMemcpyDeviceToHost,
+                       h->stream));
+    if (run1 < n)
+        CK(cudaMemcpyAsync(h->log_buf.data() + run1, h->d_traj, sizeof(TrajRec) * (n - run1), cudaMemcpyDeviceToHost,
+                           h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    static const char *fields[] = {"exact", "surrogate", "judged"};
+    for (const TrajRec &r : h->log_buf) {
+        if (!h->log_t0) h->log_t0 = r.t_ns;
+        const char *fm = r.field_mode >= 0 && r.field_mode < 3 ? fields[r.field_mode] : "exact";
+        fprintf(h->log,
+                "{\"eval\": %d, \"iteration\": %d, \"accepted\": %s, \"hpwl\": %.17g, \"overflow\": %.17g, "
+                "\"overflow_abs\": %.17g, \"lambda\": %.17g, \"alpha\": %.17g, \"gamma\": %.17g, \"field\": \"%s\", "
+                "\"surrogate_error\": %.9g, \"t_ms\": %.6f}\n",
+                r.eval, r.iteration, r.accepted > 0 ? "true" : (r.accepted == 0 ? "false" : "\"diverged\""), r.hpwl,
+                r.overflow, r.overflow_abs, r.lambda, r.alpha, r.gamma, fm, r.surr_err,
+                (double)(r.t_ns - h->log_t0) * 1e-6);
+    }
+    fflush(h->log);
+    h->log_next = ev;
+    return AP_OK;
+}
+
 int read_scalars(ap_handle *h) {
     CK(cudaMemcpyAsync(h->h_sc, h->d_sc, sizeof(DevScalars), cudaMemcpyDeviceToHost, h->stream));
-    return sync(h);
+    const int r = sync(h);
+    if (r != AP_OK || !h->log) return r;
+    return drain_log(h);
 }
 
 // Positions of the accepted buffer (device scalar `cur`) <-> staging arrays,
@@ -483,11 +558,16 @@ int init_optimizer(ap_handle *h) {
     sc.surr_judge_every = h->policy.judge_every;
     sc.surr_tau_min = h->policy.overflow_min;
     sc.surr_err_bound = h->policy.max_error;
+    sc.traj = h->d_traj;
+    sc.traj_cap = h->traj_cap;
+    h->log_next = 0;
+    h->log_t0 = 0;
     CK(cudaMemcpyAsync(h->d_sc, &sc, sizeof(sc), cudaMemcpyHostToDevice, st));
     CK(cudaMemsetAsync(h->d_gq, 0, sizeof(ull) * h->n_nodes, st));
     CK(cudaMemsetAsync(h->d_gqx, 0, sizeof(ull) * h->n_nodes, st));
     CK(cudaMemsetAsync(h->d_gqy, 0, sizeof(ull) * h->n_nodes, st));
     CK(cudaMemsetAsync(h->d_mov_q, 0, sizeof(ull) * (size_t)h->p.bins_x * h->p.bins_y, st));
+    if (h->d_fill_q) CK(cudaMemsetAsync(h->d_fill_q, 0, sizeof(ull) * (size_t)h->p.bins_x * h->p.bins_y, st));
     CK(cudaMemsetAsync(h->d_counters, 0, sizeof(unsigned int) * 8, st));
     // u_0 = v_0
     CK(cudaMemcpyAsync(h->d_ux[0], h->d_px[0], sizeof(float) * h->n_mov, cudaMemcpyDeviceToDevice, st));
@@ -585,6 +665,7 @@ int ap_params_default(ap_params *p) {
     p->use_graph = 1;
     p->max_backtracks = 0;
     p->restart_mode = 4;
+    p->filler_cells = 0;
     return AP_OK;
 }
 
@@ -623,24 +704,88 @@ int ap_create(const ap_netlist *nl, const ap_params *params, ap_handle **out) {
     h->die_yl = nl->die_yl;
     h->die_w = die_w;
     h->die_h = die_h;
-    const int N = nl->num_nodes;
+    const int NE = nl->num_nodes;
+    h->n_ext = NE;
+    // filler cells (ePlace): unconnected movable cells that take the white
+    // space the target density leaves, so that the density force spreads
+    // the real cells evenly; the overflow counts real cells only
+    if (p.filler_cells) {
+        double a_mov = 0.0, a_fix = 0.0;
+        std::vector<double> areas;
+        for (int i = 0; i < NE; ++i) {
+            const bool fixed = nl->node_fixed && nl->node_fixed[i];
+            const double w = nl->node_w[i], hh = nl->node_h[i];
+            if (!fixed) {
+                a_mov += w * hh;
+                areas.push_back(w * hh);
+            } else {  // the part of the fixed node on the die
+                const double ox = std::min((double)nl->die_xh, (double)nl->node_x[i] + w) -
+                                  std::max((double)nl->die_xl, (double)nl->node_x[i]);
+                const double oy = std::min((double)nl->die_yh, (double)nl->node_y[i] + hh) -
+                                  std::max((double)nl->die_yl, (double)nl->node_y[i]);
+                if (ox > 0 && oy > 0) a_fix += ox * oy;
+            }
+        }
+        const double a_fill = (double)p.target_density * ((double)die_w * die_h - a_fix) - a_mov;
+        if (a_fill > 0 && !areas.empty()) {
+            // filler size: mean width and height of the cells between the 10th
+            // and the 90th area percentile (ePlace)
+            std::vector<int> idx;
+            for (int i = 0; i < NE; ++i)
+                if (!(nl->node_fixed && nl->node_fixed[i])) idx.push_back(i);
+            std::sort(idx.begin(), idx.end(), [&](int a, int b) {
+                return (double)nl->node_w[a] * nl->node_h[a] < (double)nl->node_w[b] * nl->node_h[b];
+            });
+            const size_t lo = idx.size() / 10, hi = idx.size() - idx.size() / 10;
+            double sw = 0, sh = 0;
+            for (size_t k = lo; k < hi; ++k) {
+                sw += nl->node_w[idx[k]];
+                sh += nl->node_h[idx[k]];
+            }
+            h->fill_w = (float)(sw / (double)(hi - lo));
+            h->fill_h = (float)(sh / (double)(hi - lo));
+            if (h->fill_w > 0.f && h->fill_h > 0.f)
+                h->n_fill = (int)std::min(a_fill / ((double)h->fill_w * h->fill_h), 2e9 - NE);
+        }
+    }
+    const int N = NE + h->n_fill;
     h->n_nodes = N;
-    // internal order: movable, fixed with area, zero-area fixed
-    h->ext2int.assign((size_t)N, -1);
-    for (int pass = 0; pass < 3; ++pass)
-        for (int i = 0; i < N; ++i) {
+    // internal order: movable, fillers, fixed with area, zero-area fixed
+    h->ext2int.assign((size_t)NE, -1);
+    for (int pass = 0; pass < 3; ++pass) {
+        for (int i = 0; i < NE; ++i) {
             const bool fixed = nl->node_fixed && nl->node_fixed[i];
             const bool area = nl->node_w[i] * nl->node_h[i] > 0.f;
             const int cls = !fixed ? 0 : (area ? 1 : 2);
             if (cls == pass) {
                 h->ext2int[(size_t)i] = (int)h->int2ext.size();
                 h->int2ext.push_back(i);
-                if (cls == 0) h->n_mov++;
+                if (cls == 0) h->n_real++;
                 if (cls == 1) h->n_fixa++;
             }
         }
-    for (int i = 0; i < N; ++i)
+        if (pass == 0) h->int2ext.insert(h->int2ext.end(), (size_t)h->n_fill, -1);
+    }
+    h->n_mov = h->n_real + h->n_fill;
+    h->identity = h->n_fill == 0;
+    for (int i = 0; i < NE; ++i)
         if (h->ext2int[(size_t)i] != i) h->identity = false;
+    if (h->n_fill) {  // seeded, uniform over the die
+        uint64_t z = 0x5EED0F111E4ull;
+        auto uni = [&]() {
+            z += 0x9E3779B97F4A7C15ull;
+            uint64_t t = z;
+            t = (t ^ (t >> 30)) * 0xBF58476D1CE4E5B9ull;
+            t = (t ^ (t >> 27)) * 0x94D049BB133111EBull;
+            return (double)((t ^ (t >> 31)) >> 11) * (1.0 / 9007199254740992.0);
+        };
+        h->fill_x0.resize((size_t)h->n_fill);
+        h->fill_y0.resize((size_t)h->n_fill);
+        for (int k = 0; k < h->n_fill; ++k) {
+            h->fill_x0[(size_t)k] = (float)(uni() * std::max(0.0, (double)die_w - h->fill_w));
+            h->fill_y0[(size_t)k] = (float)(uni() * std::max(0.0, (double)die_h - h->fill_h));
+        }
+    }
     // nets of degree >= 2 in degree buckets [2], [3,4], [5,8], [9,16], [17,32],
     // [33,64], [65,...); within a bucket by their lowest internal node index, so
     // neighbouring threads gather and accumulate neighbouring nodes
@@ -682,6 +827,14 @@ int ap_create(const ap_netlist *nl, const ap_params *params, ap_handle **out) {
     std::vector<float> w((size_t)N), hh((size_t)N), x((size_t)N), y((size_t)N), charge((size_t)N);
     for (int i = 0; i < N; ++i) {
         const int e = h->int2ext[(size_t)i];
+        if (e < 0) {
+            const size_t k = (size_t)(i - h->n_real);
+            w[(size_t)i] = h->fill_w;
+            hh[(size_t)i] = h->fill_h;
+            x[(size_t)i] = h->fill_x0[k];
+            y[(size_t)i] = h->fill_y0[k];
+            continue;
+        }
         w[(size_t)i] = nl->node_w[e];
         hh[(size_t)i] = nl->node_h[e];
         x[(size_t)i] = nl->node_x[e] - nl->die_xl;
@@ -700,9 +853,13 @@ int ap_create(const ap_netlist *nl, const ap_params *params, ap_handle **out) {
     h->cap_q = llrint((double)p.target_density * (double)h->ab_q);
     h->inv_ab = 1.0 / (double)h->ab_q;
     g.inv_ab = (float)h->inv_ab;
-    double mov_area_q = 0.0;
+    double mov_area_q = 0.0, fill_area_q = 0.0;  // the overflow's denominator counts real cells
     for (int i = 0; i < h->n_mov; ++i) {
-        mov_area_q += (double)(llrintf(w[(size_t)i] * 65536.0f) * llrintf(hh[(size_t)i] * 65536.0f));
+        const double a = (double)(llrintf(w[(size_t)i] * 65536.0f) * llrintf(hh[(size_t)i] * 65536.0f));
+        if (i < h->n_real)
+            mov_area_q += a;
+        else
+            fill_area_q += a;
         charge[(size_t)i] = (w[(size_t)i] * hh[(size_t)i]) / (g.bw * g.bh);
     }
     h->mov_area_q = mov_area_q;
@@ -732,6 +889,7 @@ int ap_create(const ap_netlist *nl, const ap_params *params, ap_handle **out) {
     A(dalloc(&h->d_gqx, N));
     A(dalloc(&h->d_gqy, N));
     A(dalloc(&h->d_mov_q, nb));
+    if (h->n_fill) A(dalloc(&h->d_fill_q, nb));
     A(dalloc(&h->d_fix_q, nb));
     A(dalloc(&h->d_fixs_q, nb));
     A(dalloc(&h->d_dens, nb));
@@ -781,6 +939,7 @@ int ap_create(const ap_netlist *nl, const ap_params *params, ap_handle **out) {
     A(cudaMemcpy(h->d_pins, pins.data(), sizeof(float) * N, cudaMemcpyHostToDevice));
     A(cudaMemcpy(h->d_charge, charge.data(), sizeof(float) * N, cudaMemcpyHostToDevice));
     A(cudaMemset(h->d_mov_q, 0, sizeof(ull) * nb));
+    if (h->d_fill_q) A(cudaMemset(h->d_fill_q, 0, sizeof(ull) * nb));
     A(cudaMemset(h->d_counters, 0, sizeof(unsigned int) * 8));
     A(cudaMemset(h->d_gq, 0, sizeof(ull) * N));
     A(cudaMemset(h->d_gqx, 0, sizeof(ull) * N));
@@ -807,7 +966,7 @@ int ap_create(const ap_netlist *nl, const ap_params *params, ap_handle **out) {
         }
         // mean of movable + scaled fixed density over the bins (the movable
         // nodes stay on the die, so their total is constant)
-        h->d_shift = (float)((mov_area_q + fixed_scaled) * h->inv_ab / (double)nb);
+        h->d_shift = (float)((mov_area_q + fill_area_q + fixed_scaled) * h->inv_ab / (double)nb);
         A(cudaMemcpy(h->d_fix_q, fq.data(), sizeof(long long) * nb, cudaMemcpyHostToDevice));
         A(cudaMemcpy(h->d_fixs_q, fs.data(), sizeof(long long) * nb, cudaMemcpyHostToDevice));
         A(cudaMemset(h->d_mov_q, 0, sizeof(ull) * nb));
@@ -835,6 +994,11 @@ int ap_create(const ap_netlist *nl, const ap_params *params, ap_handle **out) {
 int ap_destroy(ap_handle *h) {
     if (!h) return AP_ERR_INVALID_ARG;
     if (h->stream) cudaStreamSynchronize(h->stream);
+    if (h->log) {
+        if (h->initialized) read_scalars(h);  // the trials not yet written
+        fclose(h->log);
+    }
+    if (h->d_traj) cudaFree(h->d_traj);
     destroy_graphs(h);
     surr_state_free(h->surr_state);
     if (h->side) cudaStreamDestroy(h->side);
@@ -853,7 +1017,7 @@ int ap_destroy(ap_handle *h) {
                     h->d_py[0],   h->d_py[1],    h->d_gx[0],  h->d_gx[1],   h->d_gy[0], h->d_gy[1],
                     h->d_ux[0],   h->d_uy[0],    h->d_ux[1],  h->d_uy[1],
                     h->d_pins,    h->d_charge,   h->d_gqx,    h->d_gqy,
-                    h->d_mov_q,   h->d_fix_q,    h->d_fixs_q, h->d_dens,    h->d_ex,    h->d_ey,
+                    h->d_mov_q,   h->d_fill_q,   h->d_fix_q,  h->d_fixs_q,  h->d_dens,  h->d_ex,    h->d_ey,
                     h->d_dens_hi, h->d_dens_lo,  h->d_sx,     h->d_sy,      h->d_sc,    h->d_partials,
                     h->d_partials_ll, h->d_counters, h->d_out, h->d_rec_bin, h->d_rec_ov, h->d_gq,
                     h->d_ix,      h->d_iy};
@@ -863,6 +1027,14 @@ int ap_destroy(ap_handle *h) {
     if (h->h_out) cudaFreeHost(h->h_out);
     if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
     delete h;
+    return AP_OK;
+}
+
+int ap_get_fillers(ap_handle *h, int32_t *count, float *width, float *height) {
+    if (!h) return AP_ERR_INVALID_ARG;
+    if (count) *count = h->n_fill;
+    if (width) *width = h->fill_w;
+    if (height) *height = h->fill_h;
     return AP_OK;
 }
 
@@ -887,7 +1059,7 @@ int ap_init_positions(ap_handle *h, const float *x, const float *y) {
 int ap_init_seeded(ap_handle *h, uint64_t seed, float sigma) {
     if (!h) return AP_ERR_INVALID_ARG;
     // splitmix64 + Box-Muller, the generator's normal draw
-    std::vector<float> x((size_t)h->n_nodes, 0.f), y((size_t)h->n_nodes, 0.f);
+    std::vector<float> x((size_t)h->n_ext, 0.f), y((size_t)h->n_ext, 0.f);
     uint64_t z = seed;
     auto next = [&]() {
         z += 0x9E3779B97F4A7C15ull;
@@ -902,7 +1074,7 @@ int ap_init_seeded(ap_handle *h, uint64_t seed, float sigma) {
         return sqrt(-2.0 * log(u1)) * cos(6.283185307179586 * u2);
     };
     const double cx = h->die_xl + 0.5 * h->die_w, cy = h->die_yl + 0.5 * h->die_h;
-    for (int i = 0; i < h->n_mov; ++i) {
+    for (int i = 0; i < h->n_real; ++i) {
         const int e = h->int2ext[(size_t)i];
         x[(size_t)e] = (float)(cx + sigma * normal());
         y[(size_t)e] = (float)(cy + sigma * normal());
@@ -915,6 +1087,43 @@ int ap_step(ap_handle *h, int32_t n_iter) {
     if (!h->initialized) return AP_ERR_STATE;
     int r = step_n(h, n_iter);
     if (r != AP_OK) return r;
+    return sync(h);
+}
+
+int ap_set_log(ap_handle *h, const char *path, int32_t capacity) {
+    if (!h || (path && capacity < 1)) return AP_ERR_INVALID_ARG;
+    CK(cudaStreamSynchronize(h->stream));
+    if (h->log) {
+        if (h->initialized) {
+            const int r = read_scalars(h);  // what is left of the old log
+            if (r != AP_OK) return r;
+        }
+        fclose(h->log);
+        h->log = nullptr;
+    }
+    if (h->d_traj) {
+        CK(cudaFree(h->d_traj));
+        h->d_traj = nullptr;
+        h->traj_cap = 0;
+    }
+    if (path) {
+        h->log = fopen(path, "w");
+        if (!h->log) return AP_ERR_INVALID_ARG;
+        if (cudaMalloc((void **)&h->d_traj, sizeof(TrajRec) * (size_t)capacity) != cudaSuccess) {
+            fclose(h->log);
+            h->log = nullptr;
+            return AP_ERR_CUDA;
+        }
+        h->traj_cap = capacity;
+    }
+    if (!h->initialized) return AP_OK;  // init_optimizer installs the ring
+    CK(cudaMemcpyAsync(h->h_sc, h->d_sc, sizeof(DevScalars), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    h->h_sc->traj = h->d_traj;
+    h->h_sc->traj_cap = h->traj_cap;
+    h->log_next = h->h_sc->evals;
+    h->log_t0 = 0;
+    CK(cudaMemcpyAsync(h->d_sc, h->h_sc, sizeof(DevScalars), cudaMemcpyHostToDevice, h->stream));
     return sync(h);
 }
 
@@ -948,7 +1157,8 @@ int ap_profile_stages(ap_handle *h, int32_t n_trials, float *stage_ms, int32_t *
     int r = AP_OK;
     for (int t = 0; t < n_trials && r == AP_OK; ++t) {
         CK(cudaEventRecord(ev[0], st));
-        launch_scatter(loop_scatter_args(h), st);
+        launch_update(loop_scatter_args(h), st);
+        launch_movable_bins(h, loop_scatter_args(h), st);
         CK(cudaEventRecord(ev[1], st));
         launch_rho(rho_args(h, RHO_LOOP, nullptr), st);
         CK(cudaEventRecord(ev[2], st));
@@ -1007,6 +1217,7 @@ int ap_get_positions(ap_handle *h, float *x, float *y) {
     if (r != AP_OK) return r;
     for (int i = 0; i < h->n_nodes; ++i) {
         const int e = h->int2ext[(size_t)i];
+        if (e < 0) continue;  // filler cells are internal
         x[e] = ix[(size_t)i] + h->die_xl;
         y[e] = iy[(size_t)i] + h->die_yl;
     }
@@ -1159,6 +1370,11 @@ int stage_positions(ap_handle *h, const float *x, const float *y) {
     std::vector<float> ix((size_t)h->n_nodes), iy((size_t)h->n_nodes);
     for (int i = 0; i < h->n_nodes; ++i) {
         const int e = h->int2ext[(size_t)i];
+        if (e < 0) {  // filler cells: their starting points (no per-stage result depends on them)
+            ix[(size_t)i] = h->fill_x0[(size_t)(i - h->n_real)];
+            iy[(size_t)i] = h->fill_y0[(size_t)(i - h->n_real)];
+            continue;
+        }
         ix[(size_t)i] = x[e] - h->die_xl;
         iy[(size_t)i] = y[e] - h->die_yl;
         if (!std::isfinite(ix[(size_t)i]) || !std::isfinite(iy[(size_t)i])) return AP_ERR_NONFINITE;
@@ -1196,6 +1412,7 @@ int ap_wirelength_grad(ap_handle *h, const float *x, const float *y, float gamma
         const long long sx = lo + (long long)qx[i];
         const long long sy = (((long long)q[i] - lo) >> 32) + (long long)qy[i];
         const int e = h->int2ext[i];
+        if (e < 0) continue;
         gx[e] = (float)ldexp((double)sx, -20);  // kGradScale = 2^20
         gy[e] = (float)ldexp((double)sy, -20);
     }
@@ -1210,11 +1427,15 @@ int ap_density_map(ap_handle *h, const float *x, const float *y, int64_t *rho_q)
     if (r != AP_OK) return r;
     const size_t nb = (size_t)h->p.bins_x * h->p.bins_y;
     CK(cudaMemsetAsync(h->d_mov_q, 0, sizeof(ull) * nb, h->stream));
+    // the netlist's nodes: real movable cells and fixed nodes with area
     ScatterArgs s = scatter_args(h);
     s.update = 0;
     s.px = h->d_sx;
     s.py = h->d_sy;
     s.lo = 0;
+    s.hi = h->n_real;
+    launch_scatter(s, h->stream);
+    s.lo = h->n_mov;
     s.hi = h->n_mov + h->n_fixa;
     launch_scatter(s, h->stream);
     CK(cudaGetLastError());
@@ -1294,6 +1515,7 @@ int ap_node_force(ap_handle *h, const float *x, const float *y, const float *ex,
     if (r != AP_OK) return r;
     for (size_t i = 0; i < N; ++i) {
         const int e = h->int2ext[i];
+        if (e < 0) continue;
         const bool mov = i < M;
         fx[e] = mov ? hf[i] : 0.f;
         fy[e] = mov ? hf[M + i] : 0.f;
@@ -1395,6 +1617,9 @@ int ap_restore(ap_handle *h, const void *buf, size_t bytes) {
     sc.surr_tau_min = h->policy.overflow_min;
     sc.surr_err_bound = h->policy.max_error;
     sc.field_mode = kFieldExact;
+    sc.traj = h->d_traj;
+    sc.traj_cap = h->traj_cap;
+    h->log_next = sc.evals;  // the log goes on from the restored trial
     CK(cudaMemcpy(h->d_sc, &sc, sizeof(DevScalars), cudaMemcpyHostToDevice));
     const size_t N = (size_t)h->n_nodes, M = (size_t)h->n_mov;
     float *arrs_n[4] = {h->d_px[0], h->d_px[1], h->d_py[0], h->d_py[1]};
@@ -1411,6 +1636,7 @@ int ap_restore(ap_handle *h, const void *buf, size_t bytes) {
     CK(cudaMemset(h->d_gqx, 0, sizeof(ull) * N));
     CK(cudaMemset(h->d_gqy, 0, sizeof(ull) * N));
     CK(cudaMemset(h->d_mov_q, 0, sizeof(ull) * (size_t)h->p.bins_x * h->p.bins_y));
+    if (h->d_fill_q) CK(cudaMemset(h->d_fill_q, 0, sizeof(ull) * (size_t)h->p.bins_x * h->p.bins_y));
     CK(cudaMemset(h->d_counters, 0, sizeof(unsigned int) * 8));
     h->initialized = true;
     if (h->p.use_graph && !h->graph_ok) return build_graphs(h);
@@ -1492,7 +1718,8 @@ int ap_surrogate_collect(ap_handle *h, ap_surrogate *s, int32_t n_trials, int32_
     int got = 0;
     cudaStream_t st = h->stream;
     for (int t = 1; t <= n_trials && r == AP_OK; ++t) {
-        launch_scatter(loop_scatter_args(h), st);
+        launch_update(loop_scatter_args(h), st);
+        launch_movable_bins(h, loop_scatter_args(h), st);
         launch_rho(rho_args(h, RHO_LOOP, nullptr), st);
         launch_wirelength(wa_args(h, h->d_px[0], h->d_py[0], 0.f, h->n_mov, WA_LOOP, nullptr), st);
         r = run_field(h, h->p.field_solver, st);

@@ -39,19 +39,29 @@ __device__ __forceinline__ double block_max_f(float v, double *smem) {
 
 }  // namespace
 
-// Each block owns a contiguous chunk of kScatterChunk nodes.  Nodes with
-// nearby indices share nets and sit close together, so a chunk's bins usually
-// span a small rectangle: when that rectangle fits kScatterWindow bins the
-// block accumulates in shared memory and adds only its non-zero bins to the
-// global map (one global atomic per bin and block instead of one per node
-// and bin -- right after initial placement every node sits in a few bins).
-// Integer sums make both paths give the same map bit for bit.
-constexpr int kScatterThreads = 512;
-constexpr int kScatterPerThread = 4;
-constexpr int kScatterChunk = kScatterThreads * kScatterPerThread;
-constexpr int kScatterWarps = kScatterThreads / 32;
-constexpr int kScatterWindow = 4096;
-constexpr int kScatterWindowSide = 64;  // window columns when the bounding box does not fit
+// The density scatter.  A node adds ow(c) * oh(r) to every bin (c, r) it
+// overlaps, ow and oh its fixed-point overlaps with column c and row r, so
+// a set of nodes adds a sum of outer products.  Right after the initial
+// placement -- for hundreds of iterations of the 2M-cell workload -- most
+// nodes sit in a dense core a few bins across (up to ~450k nodes in one
+// bin), where atomic adds to the map collide; later they spread over the die,
+// where plain global reductions run at the L2's rate (measured on GB300:
+// 4.5M int64 reductions to spread addresses in ~23 us, 428 us when they
+// crowd into a few bins).  Each block therefore takes a contiguous range of
+// nodes and:
+//   1. finds the mean base bin of its range and puts a kTile x kTile bin tile
+//      there;
+//   2. accumulates every node whose bins all lie inside the tile into int64
+//      registers as the outer product ow x oh (kTile^2 multiply-adds, no
+//      atomics, no lane matching; a warp runs this only when one of its
+//      lanes has such a node);
+//   3. adds every other node's bins straight to the map (red.global.add);
+//   4. sums the tile over the block (shuffles, then shared memory) and adds
+//      its kTile^2 bins to the map once.
+// All sums are integers, so the map is the same bit for bit whatever the
+// path or the order (and equal to or_density_q).
+constexpr int kTile = 6;
+constexpr int kScatterThreads = 256;
 
 // A node's contribution as a record of 5 int32: the base bin (c0, r0), the
 // spans nc, nr <= 8 and a small-node flag packed in `bin` (non-negative), the
@@ -217,187 +227,136 @@ __global__ void __launch_bounds__(kThreads) update_kernel(ScatterArgs a) {
 }
 
 __global__ void __launch_bounds__(kScatterThreads, 2) scatter_kernel(ScatterArgs a) {
-    __shared__ int box[8];  // bin bounding box of the chunk: c0, c1, r0, r1; sums of c0, r0; count; inside
-    __shared__ ull win[kScatterWindow];
-    const int n = a.update ? a.n_mov : (a.hi - a.lo);
-    // update mode: the trial point and its records come from update_kernel
+    __shared__ long long red[kScatterThreads / 32][kTile * kTile];
+    __shared__ long long sums[3];
     const int nxt = a.update ? 1 - a.sc->cur : 0;
     const Grid g = a.g;
-    if (threadIdx.x == 0) {
-        box[0] = box[2] = 0x7fffffff;
-        box[1] = box[3] = -1;
-        box[4] = box[5] = box[6] = box[7] = 0;
-    }
-    __syncthreads();
-    NodeRec rec[kScatterPerThread];
-    int bc0 = 0x7fffffff, bc1 = -1, br0 = 0x7fffffff, br1 = -1;
-    const int base = blockIdx.x * kScatterChunk;
-#pragma unroll
-    for (int k = 0; k < kScatterPerThread; ++k) {
-        const int i = base + k * kScatterThreads + threadIdx.x;
-        rec[k].bin = kRecNone;
-        if (i >= n) continue;
-        int c0, c1, r0, r1;
+    const int n = a.hi - a.lo;
+    const int per = (n + (int)gridDim.x - 1) / (int)gridDim.x;
+    const int r_lo = min(n, (int)blockIdx.x * per), r_hi = min(n, r_lo + per);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    // 1. the mean base bin of the range (update mode: from the records;
+    //    plain mode: from the positions)
+    long long sc = 0, sr = 0, cnt = 0;
+    for (int i = r_lo + tid; i < r_hi; i += kScatterThreads) {
+        const int node = a.lo + i;
         if (a.update) {
-            const int bin = a.rec_bin[i];
-            const int4 o = a.rec_ov[i];
-            rec[k] = NodeRec{bin, o.x, o.y, o.z, o.w};
-            c1 = r1 = -1;
-            if (bin >= 0) {
-                c0 = rec_c0(bin);
-                r0 = rec_r0(bin);
-                c1 = (bin & kRecSmall) ? c0 : c0 + rec_nc(bin) - 1;
-                r1 = (bin & kRecSmall) ? r0 : r0 + rec_nr(bin) - 1;
-            } else if (bin == kRecFull) {
-                bool small;
-                if (!bin_range(g, a.vx[nxt][i], a.vy[nxt][i], __ldg(a.w + i), __ldg(a.h + i), c0, c1, r0, r1,
-                               small))
-                    c1 = r1 = -1;
+            const int b = __ldg(a.rec_bin + node);
+            if (b >= 0) {
+                sc += rec_c0(b);
+                sr += rec_r0(b);
+                ++cnt;
             }
         } else {
-            const int node = a.lo + i;
-            rec[k] = make_rec(g, __ldg(a.px + node), __ldg(a.py + node), __ldg(a.w + node), __ldg(a.h + node), c0,
-                              c1, r0, r1);
-        }
-        if (c1 >= 0) {
-            bc0 = min(bc0, c0);
-            bc1 = max(bc1, c1);
-            br0 = min(br0, r0);
-            br1 = max(br1, r1);
+            const float qx = __ldg(a.px + node) / g.bw, qy = __ldg(a.py + node) / g.bh;
+            if (qx > 0.f && qx < (float)g.mx && qy > 0.f && qy < (float)g.my) {
+                sc += f2i_rz_small(qx);
+                sr += f2i_rz_small(qy);
+                ++cnt;
+            }
         }
     }
-    // sums for the chunk's mean bin, from the records (re-evaluated nodes left out)
-    int sc0 = 0, sr0 = 0, cnt = 0;
-#pragma unroll
-    for (int k = 0; k < kScatterPerThread; ++k) {
-        if (rec[k].bin >= 0) {
-            sc0 += rec_c0(rec[k].bin);
-            sr0 += rec_r0(rec[k].bin);
-            ++cnt;
-        }
-    }
-    // the chunk's bin bounding box: warp reduction, then one shared atomic per warp
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        bc0 = min(bc0, __shfl_xor_sync(0xffffffffu, bc0, o));
-        bc1 = max(bc1, __shfl_xor_sync(0xffffffffu, bc1, o));
-        br0 = min(br0, __shfl_xor_sync(0xffffffffu, br0, o));
-        br1 = max(br1, __shfl_xor_sync(0xffffffffu, br1, o));
-        sc0 += __shfl_xor_sync(0xffffffffu, sc0, o);
-        sr0 += __shfl_xor_sync(0xffffffffu, sr0, o);
-        cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
-    }
-    if ((threadIdx.x & 31) == 0 && bc1 >= 0) {
-        atomicMin(box + 0, bc0);
-        atomicMax(box + 1, bc1);
-        atomicMin(box + 2, br0);
-        atomicMax(box + 3, br1);
-        atomicAdd(box + 4, sc0);
-        atomicAdd(box + 5, sr0);
-        atomicAdd(box + 6, cnt);
+    sc = warp_sum(sc);
+    sr = warp_sum(sr);
+    cnt = warp_sum(cnt);
+    if (tid < 3) sums[tid] = 0;
+    __syncthreads();
+    if (lane == 0) {
+        atomicAdd(reinterpret_cast<ull *>(sums + 0), (ull)sc);
+        atomicAdd(reinterpret_cast<ull *>(sums + 1), (ull)sr);
+        atomicAdd(reinterpret_cast<ull *>(sums + 2), (ull)cnt);
     }
     __syncthreads();
-    // The window: the chunk's bounding box if it fits kScatterWindow bins, else
-    // a kScatterWindow-bin rectangle about the chunk's mean bin (a dense core
-    // with outliers, as in the first iterations); adds outside it go straight
-    // to the global map.
-    int wc0 = box[0], wr0 = box[2];
-    int wc = box[1] - wc0 + 1, wr = box[3] - wr0 + 1;
-    bool use_win = box[1] >= 0;
-    if (use_win && wc * wr > kScatterWindow) {
-        const int nm = max(box[6], 1);
-        const int mc = box[4] / nm, mr = box[5] / nm;
-        const int tc = min(wc, kScatterWindowSide), tr = min(wr, kScatterWindow / tc);
-        wc0 = min(max(mc - tc / 2, wc0), wc0 + wc - tc);
-        wr0 = min(max(mr - tr / 2, wr0), wr0 + wr - tr);
-        wc = tc;
-        wr = tr;
-        // worth it only if at least half of the chunk's nodes start inside
-        int in = 0;
+    const long long tot = sums[2];
+    const int mc = tot ? (int)((2 * sums[0] + tot) / (2 * tot)) : 0;  // rounded means
+    const int mr = tot ? (int)((2 * sums[1] + tot) / (2 * tot)) : 0;
+    const int tc0 = min(max(mc - kTile / 2, 0), g.mx - kTile), tr0 = min(max(mr - kTile / 2, 0), g.my - kTile);
+    const int bw = (int)g.bw_q, bh = (int)g.bh_q;  // record arithmetic is int32 (checked at record time)
+
+    // 2.-3. the range's nodes
+    long long acc[kTile][kTile];
 #pragma unroll
-        for (int k = 0; k < kScatterPerThread; ++k)
-            in += rec[k].bin >= 0 && (unsigned)(rec_c0(rec[k].bin) - wc0) < (unsigned)wc &&
-                  (unsigned)(rec_r0(rec[k].bin) - wr0) < (unsigned)wr;
-        in = __reduce_add_sync(0xffffffffu, in);
-        if ((threadIdx.x & 31) == 0) atomicAdd(box + 7, in);
-        __syncthreads();
-        use_win = 2 * box[7] >= nm;
-    }
-    const int W = use_win ? wc * wr : 0;
-    // Clustered chunk (e.g. right after initial placement, every node in a few
-    // bins): one private window per warp.  In every window the lanes of a warp
-    // that add to the same slot are summed first (exact: three 21-bit chunks
-    // through redux), so no two adds of one instruction hit one address: in
-    // the first hundreds of iterations this took the scatter from 264 to
-    // 170 us (2M cells), at 6% extra cost mid-run.
-    const bool clustered = use_win && W <= kScatterWindow / kScatterWarps;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (use_win) {
-        const int nw = clustered ? kScatterWarps * W : W;
-        for (int t = threadIdx.x; t < nw; t += kScatterThreads) win[t] = 0ull;
-        __syncthreads();
-    }
-    // shared-space reduction (red.shared.add.u64) into the window
-    const unsigned win_s = (unsigned)__cvta_generic_to_shared(win) + (clustered ? 8u * (unsigned)(warp * W) : 0u);
-    auto add_win = [&](int c, int r, long long v) {
-        if ((unsigned)(c - wc0) >= (unsigned)wc || (unsigned)(r - wr0) >= (unsigned)wr) {
-            atomicAdd(a.rho_q + (long long)c * g.my + r, (ull)v);  // outside the window
-            return;
-        }
-        const int slot = (c - wc0) * wr + (r - wr0);
-        {
-            const unsigned peers = __match_any_sync(__activemask(), slot);
-            if (peers != (1u << lane)) {
-                const ull u = (ull)v;
-                const unsigned s0 = __reduce_add_sync(peers, (unsigned)(u & 0x1FFFFFull));
-                const unsigned s1 = __reduce_add_sync(peers, (unsigned)((u >> 21) & 0x1FFFFFull));
-                const int s2 = __reduce_add_sync(peers, (int)(v >> 42));
-                if (lane != __ffs(peers) - 1) return;
-                v = (long long)s0 + (long long)s1 * (1ll << 21) + (long long)s2 * (1ll << 42);
-            }
-        }
-        asm volatile("red.shared.add.u64 [%0], %1;" ::"r"(win_s + 8u * (unsigned)slot), "l"(v) : "memory");
-    };
+    for (int u = 0; u < kTile; ++u)
+#pragma unroll
+        for (int v = 0; v < kTile; ++v) acc[u][v] = 0;
     auto add_glb = [&](int c, int r, long long v) { atomicAdd(a.rho_q + (long long)c * g.my + r, (ull)v); };
-#pragma unroll
-    for (int k = 0; k < kScatterPerThread; ++k) {
-        if (rec[k].bin == kRecNone) continue;
-        if (rec[k].bin == kRecFull) {
-            // re-evaluated from the node's position (this thread wrote it above)
-            const int i = base + k * kScatterThreads + threadIdx.x;
-            const int node = a.update ? i : a.lo + i;
-            const float x = a.update ? a.vx[nxt][i] : __ldg(a.px + node);
-            const float y = a.update ? a.vy[nxt][i] : __ldg(a.py + node);
-            const float w = __ldg(a.w + node), h = __ldg(a.h + node);
-            if (use_win)
-                for_each_overlap(g, x, y, w, h, add_win);
-            else
-                for_each_overlap(g, x, y, w, h, add_glb);
-            continue;
-        }
-        const NodeRec &q = rec[k];
-        if (use_win)
-            emit_rec(g, q.bin, q.xr, q.wq, q.yr, q.hq, add_win);
-        else
-            emit_rec(g, q.bin, q.xr, q.wq, q.yr, q.hq, add_glb);
-    }
-    if (use_win) {
-        __syncthreads();
-        // (column, row) of window slot t, advanced without a division per slot
-        const int step_c = kScatterThreads / wr, step_r = kScatterThreads % wr;
-        int c = threadIdx.x / wr, r = threadIdx.x % wr;
-        for (int t = threadIdx.x; t < wc * wr; t += kScatterThreads) {
-            ull v = win[t];
-            if (clustered)
-                for (int w = 1; w < kScatterWarps; ++w) v += win[w * W + t];
-            if (v) atomicAdd(a.rho_q + (long long)(wc0 + c) * g.my + (wr0 + r), v);
-            c += step_c;
-            r += step_r;
-            if (r >= wr) {
-                r -= wr;
-                ++c;
+    int had = 0;  // this thread accumulated a node into the tile
+    for (int base = r_lo; base < r_hi; base += kScatterThreads) {  // the same trip count in every lane
+        const int i = base + tid;
+        const bool valid = i < r_hi;
+        const int node = a.lo + i;
+        NodeRec q{kRecNone, 0, 0, 0, 0};
+        if (valid) {
+            if (a.update) {
+                q.bin = __ldg(a.rec_bin + node);
+                const int4 o = __ldg(a.rec_ov + node);
+                q.xr = o.x;
+                q.wq = o.y;
+                q.yr = o.z;
+                q.hq = o.w;
+            } else {
+                int c0, c1, r0, r1;
+                q = make_rec(g, __ldg(a.px + node), __ldg(a.py + node), __ldg(a.w + node), __ldg(a.h + node), c0, c1,
+                             r0, r1);
             }
         }
+        bool fits = false;
+        int qc0 = 0, qr0 = 0, qnc = 1, qnr = 1;
+        if (q.bin >= 0) {
+            qc0 = rec_c0(q.bin) - tc0;
+            qr0 = rec_r0(q.bin) - tr0;
+            if (!(q.bin & kRecSmall)) {
+                qnc = rec_nc(q.bin);
+                qnr = rec_nr(q.bin);
+            }
+            fits = qc0 >= 0 && qr0 >= 0 && qc0 + qnc <= kTile && qr0 + qnr <= kTile;
+        }
+        if (__any_sync(0xffffffffu, fits)) {
+            // this node's column and row overlaps over the tile (zero outside
+            // its bins, and for lanes whose node does not fit)
+            int ow[kTile], oh[kTile];
+            const bool sm = (q.bin & kRecSmall) != 0;
+#pragma unroll
+            for (int u = 0; u < kTile; ++u) {
+                const int j = u - qc0;
+                ow[u] = fits && j >= 0 && j < qnc ? (sm ? q.wq : overlap_1d32(j * bw, bw, q.xr, q.wq)) : 0;
+            }
+#pragma unroll
+            for (int v = 0; v < kTile; ++v) {
+                const int k = v - qr0;
+                oh[v] = fits && k >= 0 && k < qnr ? (sm ? q.hq : overlap_1d32(k * bh, bh, q.yr, q.hq)) : 0;
+            }
+#pragma unroll
+            for (int u = 0; u < kTile; ++u)
+#pragma unroll
+                for (int v = 0; v < kTile; ++v) acc[u][v] += (long long)ow[u] * oh[v];
+            had |= fits;
+        }
+        if (fits || q.bin == kRecNone) continue;
+        if (q.bin == kRecFull) {
+            // outside the record's range: re-evaluated from the node's position
+            const float x = a.update ? a.vx[nxt][node] : __ldg(a.px + node);
+            const float y = a.update ? a.vy[nxt][node] : __ldg(a.py + node);
+            for_each_overlap(g, x, y, __ldg(a.w + node), __ldg(a.h + node), add_glb);
+        } else {
+            emit_rec(g, q.bin, q.xr, q.wq, q.yr, q.hq, add_glb);
+        }
+    }
+    // 4. the tile, summed over the block and added once
+    if (!__syncthreads_or(had)) return;  // uniform: no node of the range went into the tile
+#pragma unroll
+    for (int u = 0; u < kTile; ++u)
+#pragma unroll
+        for (int v = 0; v < kTile; ++v) {
+            const long long t = warp_sum(acc[u][v]);
+            if (lane == 0) red[warp][u * kTile + v] = t;
+        }
+    __syncthreads();
+    if (tid < kTile * kTile) {
+        long long t = 0;
+#pragma unroll
+        for (int w = 0; w < kScatterThreads / 32; ++w) t += red[w][tid];
+        if (t) add_glb(tc0 + tid / kTile, tr0 + tid % kTile, t);
     }
 }
 
@@ -423,9 +382,21 @@ int launch_update(const ScatterArgs &a, cudaStream_t st) {
 }
 
 void launch_scatter_bins(const ScatterArgs &a, cudaStream_t st) {
-    const int n = a.update ? a.n_mov : (a.hi - a.lo);
+    const int n = a.hi - a.lo;
     if (n <= 0) return;
-    const int blocks = (n + kScatterChunk - 1) / kScatterChunk;
+    // one wave of resident blocks, each a contiguous range of nodes (fewer
+    // blocks: fewer tile flushes onto the dense core's bins)
+    static int wave = 0;
+    if (wave <= 0) {
+        int dev = 0, sms = 0, per_sm = 0;
+        if (cudaGetDevice(&dev) == cudaSuccess &&
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess &&
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, scatter_kernel, kScatterThreads, 0) == cudaSuccess)
+            wave = sms * per_sm;
+        if (wave <= 0) wave = 304;
+    }
+    int blocks = (n + kScatterThreads - 1) / kScatterThreads;
+    if (blocks > wave) blocks = wave;
     scatter_kernel<<<blocks, kScatterThreads, 0, st>>>(a);
 }
 
@@ -454,16 +425,19 @@ __global__ void __launch_bounds__(kThreads) rho_kernel(RhoArgs a) {
     longlong2 *mov2 = reinterpret_cast<longlong2 *>(a.mov_q);
     const longlong2 *__restrict__ fs2 = reinterpret_cast<const longlong2 *>(a.fixs_q);
     const longlong2 *__restrict__ fx2 = reinterpret_cast<const longlong2 *>(a.fix_q);
+    longlong2 *fl2 = reinterpret_cast<longlong2 *>(a.fill_q);  // filler cells, or null
     const int stride = gridDim.x * blockDim.x;
     for (int p0 = blockIdx.x * blockDim.x + threadIdx.x; p0 < npairs; p0 += kRhoBatch * stride) {
-        longlong2 mv[kRhoBatch], fs[kRhoBatch], fx[kRhoBatch];
+        longlong2 mv[kRhoBatch], fs[kRhoBatch], fx[kRhoBatch], fl[kRhoBatch];
 #pragma unroll
         for (int j = 0; j < kRhoBatch; ++j) {
             const int p = p0 + j * stride;
+            fl[j] = make_longlong2(0, 0);
             if (p < npairs) {
                 mv[j] = __ldcg(mov2 + p);
                 fs[j] = __ldg(fs2 + p);
                 fx[j] = __ldg(fx2 + p);
+                if (fl2) fl[j] = __ldcg(fl2 + p);
             }
         }
 #pragma unroll
@@ -471,7 +445,9 @@ __global__ void __launch_bounds__(kThreads) rho_kernel(RhoArgs a) {
             const int p = p0 + j * stride;
             if (p >= npairs) break;
             mov2[p] = make_longlong2(0, 0);
+            if (fl2) fl2[p] = make_longlong2(0, 0);
             const long long m[2] = {mv[j].x, mv[j].y}, sq[2] = {fs[j].x, fs[j].y}, f[2] = {fx[j].x, fx[j].y};
+            const long long fil[2] = {fl[j].x, fl[j].y};
             float d[2];
 #pragma unroll
             for (int k = 0; k < 2; ++k) {
@@ -480,7 +456,7 @@ __global__ void __launch_bounds__(kThreads) rho_kernel(RhoArgs a) {
                 over += t > 0 ? t : 0;
                 const long long ab = m[k] + f[k] - a.ab_q;
                 over_abs += ab > 0 ? ab : 0;
-                d[k] = ll2f_rn_bits(tot) * a.inv_ab_f - a.d_shift;
+                d[k] = ll2f_rn_bits(tot + fil[k]) * a.inv_ab_f - a.d_shift;
             }
             if (a.d_f32) reinterpret_cast<float2 *>(a.d_f32)[p] = make_float2(d[0], d[1]);
             if (a.d_hi) {
@@ -564,6 +540,27 @@ void launch_rho(const RhoArgs &a, cudaStream_t st) {
     rho_kernel<<<blocks, kThreads, 0, st>>>(a);
 }
 
+// The trajectory record of the trial just decided (trial number sc->evals - 1).
+__device__ void log_trial(DevScalars *sc, int accepted) {
+    if (!sc->traj) return;
+    TrajRec r;
+    r.eval = sc->evals - 1;
+    r.iteration = sc->iteration;
+    r.accepted = accepted;
+    r.field_mode = sc->field_mode;
+    r.hpwl = sc->t_hpwl;
+    r.overflow = sc->t_tau;
+    r.overflow_abs = sc->t_tau_abs;
+    r.lambda = sc->lambda;
+    r.alpha = sc->alpha;
+    r.gamma = sc->gamma;
+    r.surr_err = sc->surr_err;
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    r.t_ns = t;
+    sc->traj[(unsigned)r.eval % (unsigned)sc->traj_cap] = r;
+}
+
 // Accept / retry decision of one trial (one thread).  Mirrors or_step in the
 // oracle: backtracking while the re-predicted step falls below 0.95 of the
 // step tried; on acceptance the momentum restart test, the density-penalty
@@ -578,11 +575,13 @@ __device__ void finish_trial(DevScalars *sc, double dv2, double dg2) {
     const double ahat = dg2 > 0.0 ? (double)(sqrtf((float)dv2) / sqrtf((float)dg2)) : 0.0;
     if (!isfinite(ahat) || !isfinite(dv2) || !isfinite(dg2)) {
         sc->status = 9;
+        log_trial(sc, -1);
         return;
     }
     if (ahat <= 0.95 * sc->alpha && sc->backtracks < sc->max_backtracks) {
         sc->alpha = ahat;
         sc->backtracks += 1;
+        log_trial(sc, 0);
         return;
     }
     bool restart = false;
@@ -613,6 +612,7 @@ __device__ void finish_trial(DevScalars *sc, double dv2, double dg2) {
     sc->backtracks = 0;
     sc->cur = 1 - sc->cur;
     sc->iteration += 1;
+    log_trial(sc, 1);
 }
 
 __global__ void __launch_bounds__(kThreads, 4) gather_kernel(GatherArgs a) {

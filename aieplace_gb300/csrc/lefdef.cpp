@@ -581,7 +581,11 @@ const char *status_name(int s) { return s == 2 ? "FIXED" : s == 3 ? "COVER" : "P
 
 extern "C" {
 
-const char *ap_design_last_error(void) { return g_last_error.c_str(); }
+const char *ap_last_error(void) { return g_last_error.c_str(); }
+
+__attribute__((visibility("hidden"))) void ap_internal_set_error(const char *msg) {
+    g_last_error = msg ? msg : "";
+}
 
 int ap_design_read(const char *const *lef_paths, int32_t n_lef, const char *def_path, int32_t size_mode,
                    ap_design **out) {

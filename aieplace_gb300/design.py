@@ -15,7 +15,7 @@ SIZE_AS_READ = 1   # LEF numbers as they are, orientation ignored (the reference
 
 def _check(fn: str, st: int):
     if st != 0:
-        msg = lib().ap_design_last_error().decode() or lib().ap_status_string(st).decode()
+        msg = lib().ap_last_error().decode() or lib().ap_status_string(st).decode()
         raise APError(fn, st, msg)
 
 

@@ -98,6 +98,10 @@ class Placer:
         check("ap_profile_stages", lib().ap_profile_stages(self._h, int(n_trials), ptr(out), C.byref(n)))
         return [float(v) for v in out[: n.value]]
 
+    def set_log(self, path: str | None, capacity: int = 65536):
+        """Per-trial JSON-lines trajectory log (None stops it)."""
+        check("ap_set_log", lib().ap_set_log(self._h, None if path is None else str(path).encode(), capacity))
+
     def solver_info(self) -> dict:
         tv, st = C.c_int32(), C.c_int32()
         tms, sms = np.zeros(3, np.float32), np.zeros(2, np.float32)

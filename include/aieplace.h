@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-#define AP_ABI_VERSION 1
+#define AP_ABI_VERSION 2
 
 /* ---- status codes ------------------------------------------------------ */
 enum {
@@ -87,6 +87,11 @@ typedef struct ap_params {
     int32_t use_graph;          /* capture the iteration in a CUDA graph (1) or launch eagerly (0) */
     int32_t max_backtracks;     /* step re-predictions per iteration (ePlace backtracking), 0 = off */
     int32_t restart_mode;       /* momentum restart: 0 none, 1 gradient, 2 every step, 3 speed, 4 overflow rise */
+    int32_t filler_cells;       /* 1: add ePlace filler cells (internal, unconnected, movable) that take the
+                                   white space target_density leaves: area rho_t (die - fixed) - movable, size
+                                   the mean width x height of the cells between the 10th and 90th area
+                                   percentile; they are in the density the field sees, not in the overflow,
+                                   and never appear in positions passed in or out */
 } ap_params;
 
 /* Per-iteration readout; the fields of printIterationResults (AIEplace.cpp:1048-1070)
@@ -119,6 +124,9 @@ int ap_params_default(ap_params *p);
 int ap_create(const ap_netlist *netlist, const ap_params *params, ap_handle **out);
 int ap_destroy(ap_handle *h);
 
+/* Filler cells the handle added (ap_params.filler_cells): count and size. */
+int ap_get_fillers(ap_handle *h, int32_t *count, float *width, float *height);
+
 /* Runs all following device work of this handle on `stream` (a cudaStream_t). */
 int ap_set_stream(ap_handle *h, void *cuda_stream);
 
@@ -149,6 +157,19 @@ int ap_step_async(ap_handle *h, int32_t n_trials);
  * [1] density -> solver input + overflow, [2] wirelength gradient,
  * [3] field solve, [4] field gather + step control.  *n_stages = 5. */
 int ap_profile_stages(ap_handle *h, int32_t n_trials, float *stage_ms, int32_t *n_stages);
+
+/* Per-trial trajectory log, one JSON object a line: eval, iteration,
+ * accepted, hpwl, overflow, overflow_abs, lambda, alpha, gamma, field (exact,
+ * surrogate or judged), surrogate_error (the last judged surrogate field
+ * error), t_ms (device clock since the first record).  The reference prints
+ * the same quantities per iteration (printIterationResults,
+ * AIEplace.cpp:1048-1070).  The loop writes each trial's record into a
+ * device ring of `capacity` records; the host drains it into `path` whenever
+ * a call reads the optimiser's state (ap_run every check_interval
+ * iterations, ap_step, ap_step_host, ap_get_stats ...), so logging adds no
+ * synchronisation to the loop.  Trials overwritten in the ring before a
+ * drain are counted in a {"lost_trials": n} line.  path NULL stops logging. */
+int ap_set_log(ap_handle *h, const char *path, int32_t capacity);
 
 /* Tile shapes the autotuner picked at ap_create for this bin count, and the
  * solve times it measured: tc_variant is the tensor-core candidate (0: 128 x 64
@@ -384,7 +405,7 @@ typedef struct ap_design_info {
 
 /* LEF files are read in order (a later MACRO of a name replaces an earlier
  * one), then the DEF.  Syntax errors and references to undefined macros,
- * components or pins return AP_ERR_BAD_NETLIST; ap_design_last_error() then
+ * components or pins return AP_ERR_BAD_NETLIST; ap_last_error() then
  * names the file, line and cause. */
 int ap_design_read(const char *const *lef_paths, int32_t n_lef, const char *def_path, int32_t size_mode,
                    ap_design **out);
@@ -402,9 +423,41 @@ const char *ap_design_node_name(ap_design *d, int32_t node);
  * rounded to integers: movable components PLACED at their new position, fixed
  * ones where they were.  The position export a downstream legaliser reads. */
 int ap_design_write_def(ap_design *d, const float *x, const float *y, const char *path);
-/* the message of the last failed read or write on this thread ("" if none) */
-const char *ap_design_last_error(void);
 int ap_design_destroy(ap_design *d);
+
+/* ---- run configuration -----------------------------------------------------
+ * The placer's configuration file, the counterpart of the reference host's
+ * host/config_aieplace.json (read at AIEplace.cpp:87-109).  Keys under
+ * "params" (or at the top level).  Reference keys: use_aie (accepted,
+ * unused), input_filepath (design directory: *.lef + floorplan.def),
+ * output_filepath (directory of the placed <design>.def), wirelength_method
+ * ("HPWL" | "WA", the wirelength reported), bins_per_row (bins_x = bins_y),
+ * gamma (gamma_base_bins: WA smoothing in bins, scaled with the overflow),
+ * max_iterations, init_learning_rate (accepted, unused: the Nesterov loop
+ * predicts its steps), init_global_lambda (init_density_weight if > 0).
+ * Keys of this placer: every ap_params field by name (field_solver "fp32" |
+ * "bf16x3"), log_path, lef_size_mode ("dbu" | "as_read"), seed, init_sigma
+ * (die units; 0 = one bin width), filler_cells.  Unknown keys and
+ * ill-typed values return AP_ERR_INVALID_ARG, ap_last_error() naming them. */
+typedef struct ap_run_config {
+    char input_dir[1024];
+    char output_dir[1024];
+    char log_path[1024];         /* per-trial trajectory (ap_set_log); "" = none */
+    int32_t size_mode;           /* AP_LEF_SIZE_* */
+    int32_t wirelength_method;   /* 0 HPWL, 1 WA */
+    float init_sigma;            /* seeded initial spread, die units; 0 = one bin width */
+    uint64_t seed;
+    int32_t filler_cells;        /* 1: ap_params.filler_cells */
+    int32_t use_aie;             /* as read; unused */
+    float ignored_learning_rate; /* init_learning_rate as read; unused */
+} ap_run_config;
+
+int ap_run_config_default(ap_params *params, ap_run_config *run);
+int ap_run_config_read(const char *path, ap_params *params, ap_run_config *run);
+
+/* the message of the last failed design read/write or config read on this
+ * thread ("" if none) */
+const char *ap_last_error(void);
 
 /* ---- seeded synthetic netlists ------------------------------------------ */
 /* Stands in for the ISPD suites the reference reads through LEF/DEF.  Nodes

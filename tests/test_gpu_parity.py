@@ -51,21 +51,25 @@ def test_density_map_bit_exact(ap, oracle_lib, preset, bins):
     assert np.array_equal(got, ref)
 
 
-@pytest.mark.parametrize("preset,bins,sigma,outliers", [("c1_small", 512, 1.0, 0.0), ("c1_small", 128, 0.3, 0.0),
-                                                         ("c0", 32, 0.5, 0.0), ("c1_small", 512, 4.0, 0.01)])
-def test_density_map_bit_exact_clustered(ap, oracle_lib, preset, bins, sigma, outliers):
-    """Nodes packed around the die centre (the initial placement): the
-    scatter's per-warp windows with same-slot lane aggregation; with a few
-    outliers anywhere on the die, the window about the chunk's mean bin plus
-    global adds for the rest."""
+@pytest.mark.parametrize("preset,bins,sigma,outliers,at", [("c1_small", 512, 1.0, 0.0, 0.5),
+                                                            ("c1_small", 128, 0.3, 0.0, 0.5),
+                                                            ("c0", 32, 0.5, 0.0, 0.5),
+                                                            ("c1_small", 512, 4.0, 0.01, 0.5),
+                                                            ("c1_small", 128, 2.0, 0.02, 0.0),
+                                                            ("c1_small", 512, 1.5, 0.0, 1.0)])
+def test_density_map_bit_exact_clustered(ap, oracle_lib, preset, bins, sigma, outliers, at):
+    """Nodes packed around one point (the die centre: the initial placement;
+    a die corner: the scatter's register tile clamped to the edge, nodes
+    partly off the die): the tile's outer products for nodes inside it,
+    global adds for the rest and for outliers anywhere on the die."""
     nl = ap.synth.generate(preset, seed=5)
     rng = np.random.default_rng(2)
     W, H = float(nl["die"][2]), float(nl["die"][3])
     x = nl["node_x"].copy()
     y = nl["node_y"].copy()
     mov = nl["node_fixed"] == 0
-    x[mov] = (W / 2 + sigma * rng.standard_normal(mov.sum())).astype(np.float32)
-    y[mov] = (H / 2 + sigma * rng.standard_normal(mov.sum())).astype(np.float32)
+    x[mov] = (W * at + sigma * rng.standard_normal(mov.sum())).astype(np.float32)
+    y[mov] = (H * at + sigma * rng.standard_normal(mov.sum())).astype(np.float32)
     far = np.flatnonzero(mov)[rng.random(mov.sum()) < outliers]
     x[far] = rng.uniform(0, W, far.size).astype(np.float32)
     y[far] = rng.uniform(0, H, far.size).astype(np.float32)

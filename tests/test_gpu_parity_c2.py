@@ -218,8 +218,14 @@ def test_node_force_and_gradient_vs_oracle(ap, oracle_lib, preset):
             # difference of the two terms, and of the preconditioner
             bound = ((pins * 2.0 ** -20 + lam * 1e-5 * scl + 1e-6 * (np.abs(wl) + lam * np.abs(f))) / hd
                      + 1e-5 * np.abs(ref))[mov]
-            print(f"\n{preset} precond grad (lambda {lam:.3g}): max(|dg|/bound) {(err / bound).max():.3f} "
+            ratio = err / np.maximum(bound, 1e-300)
+            print(f"\n{preset} precond grad (lambda {lam:.3g}): max(|dg|/bound) {ratio.max():.3f} "
                   f"rel {quantiles(err / np.maximum(np.abs(ref[mov]), 1e-30))}")
+            if not (err <= bound).all():
+                ids = np.flatnonzero(mov)[np.argsort(-ratio)[:5]]
+                for i in ids:
+                    print(f"  node {i}: got {got[i]!r} ref {ref[i]!r} wl {wl[i]!r} F {f[i]!r} scl {scl[i]!r} "
+                          f"pins {pins[i]} hd {hd[i]!r} x {x[i]!r} y {y[i]!r}")
             assert (err <= bound).all()
             assert (got[~mov] == 0).all()
 
@@ -251,3 +257,26 @@ def test_loop_c1_final_hpwl_and_overflow_match_oracle(ap, oracle_lib, solver):
     assert s["overflow"] < 0.10 and rs["overflow"] < 0.10
     assert abs(s["hpwl"] - rs["hpwl"]) <= 0.005 * rs["hpwl"], (s, rs)
     assert abs(s["overflow"] - rs["overflow"]) <= 0.005, (s, rs)
+
+
+@pytest.mark.parametrize("preset,iters,fillers", [("c1_small", 3, 0), ("c1_small", 40, 1), ("c2", 5, 0),
+                                                  ("c2", 60, 0)])
+def test_loop_density_matches_oracle_at_its_positions(ap, oracle_lib, preset, iters, fillers):
+    """The loop's own density pass (position update -> bin records -> scatter,
+    filler cells in their own map) through its overflow readout: after some
+    iterations from the clustered start, both overflow forms equal the
+    oracle's at the loop's accepted positions, bit for bit."""
+    nl = netlist(ap, preset) if preset == "c2" else ap.synth.generate(preset, seed=3)
+    with ap.Placer(nl, filler_cells=fillers) as pl:
+        pl.initialize_placement(seed=11, sigma=1.0)
+        pl.perform_iteration(iters)
+        s = pl.stats()
+        x, y = pl.positions()
+    g, mov_q, fix_q, fs_q, _ = oracle_density(oracle_lib, nl, x, y)
+    mov = nl["node_fixed"] == 0
+    wq = np.rint(nl["node_w"][mov] * np.float32(65536.0)).astype(np.int64)
+    hq = np.rint(nl["node_h"][mov] * np.float32(65536.0)).astype(np.int64)
+    area_q = np.cumsum((wq * hq).astype(np.float64))[-1]
+    tau, tau_abs = oracle_lib.overflow(g, mov_q, fix_q, fs_q, float(np.float32(nl["target_density"])), area_q)
+    print(f"\n{preset} after {iters}: overflow {s['overflow']!r} vs {tau!r}")
+    assert s["overflow"] == tau and s["overflow_abs"] == tau_abs
