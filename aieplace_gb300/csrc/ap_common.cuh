@@ -178,11 +178,14 @@ __device__ __forceinline__ long long to_q(float v) {
     return __float2ll_rn(s);
 }
 
-// float of an int64 fixed-point value (exact below 2^22, else through two
-// 32-bit conversions, within one ulp)
+// float of an int64 fixed-point value, rounded to nearest (= (float)q):
+// exact below 2^22 by the magic-number addition, else by integer arithmetic.
+// (Splitting q into 32-bit halves and converting each is not: for a small
+// negative q the low word is close to 2^32, and its rounding to 24 bits is
+// off by up to 256 units -- 2.4e-4 on a WA gradient below -4.)
 __device__ __forceinline__ float i64_to_float(long long q) {
     if (q > -4194304ll && q < 4194304ll) return i2f_small((int)q);
-    return fmaf(__int2float_rn((int)(q >> 32)), 4294967296.0f, __uint2float_rn((unsigned)q));
+    return ll2f_rn_bits(q);
 }
 
 // per-pin WA contribution in the int64 accumulators' fixed point: g 2^20

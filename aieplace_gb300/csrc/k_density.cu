@@ -55,12 +55,16 @@ __device__ __forceinline__ double block_max_f(float v, double *smem) {
 //      registers as the outer product ow x oh (kTile^2 multiply-adds, no
 //      atomics, no lane matching; a warp runs this only when one of its
 //      lanes has such a node);
-//   3. adds every other node's bins straight to the map (red.global.add);
+//   3. adds the bins of every other node inside a kWin x kWin bin window
+//      about the same mean bin to the window in shared memory
+//      (red.shared.add: the nodes just outside the dense core), and the rest
+//      straight to the map (red.global.add);
 //   4. sums the tile over the block (shuffles, then shared memory) and adds
-//      its kTile^2 bins to the map once.
+//      its kTile^2 bins to the map once, and the window's non-zero bins.
 // All sums are integers, so the map is the same bit for bit whatever the
 // path or the order (and equal to or_density_q).
 constexpr int kTile = 6;
+constexpr int kWin = 64;
 constexpr int kScatterThreads = 256;
 
 // A node's contribution as a record of 5 int32: the base bin (c0, r0), the
@@ -228,6 +232,7 @@ __global__ void __launch_bounds__(kThreads) update_kernel(ScatterArgs a) {
 
 __global__ void __launch_bounds__(kScatterThreads, 2) scatter_kernel(ScatterArgs a) {
     __shared__ long long red[kScatterThreads / 32][kTile * kTile];
+    __shared__ ull win[kWin * kWin];
     __shared__ long long sums[3];
     const int nxt = a.update ? 1 - a.sc->cur : 0;
     const Grid g = a.g;
@@ -272,6 +277,12 @@ __global__ void __launch_bounds__(kScatterThreads, 2) scatter_kernel(ScatterArgs
     const int mr = tot ? (int)((2 * sums[1] + tot) / (2 * tot)) : 0;
     const int tc0 = min(max(mc - kTile / 2, 0), g.mx - kTile), tr0 = min(max(mr - kTile / 2, 0), g.my - kTile);
     const int bw = (int)g.bw_q, bh = (int)g.bh_q;  // record arithmetic is int32 (checked at record time)
+    // the window: kWin x kWin bins (or the whole grid, if smaller) about the mean
+    const int wcn = min(kWin, g.mx), wrn = min(kWin, g.my);
+    const int wc0 = min(max(mc - wcn / 2, 0), g.mx - wcn), wr0 = min(max(mr - wrn / 2, 0), g.my - wrn);
+    for (int t = tid; t < wcn * wrn; t += kScatterThreads) win[t] = 0ull;
+    __syncthreads();
+    const unsigned win_s = (unsigned)__cvta_generic_to_shared(win);
 
     // 2.-3. the range's nodes
     long long acc[kTile][kTile];
@@ -280,24 +291,48 @@ __global__ void __launch_bounds__(kScatterThreads, 2) scatter_kernel(ScatterArgs
 #pragma unroll
         for (int v = 0; v < kTile; ++v) acc[u][v] = 0;
     auto add_glb = [&](int c, int r, long long v) { atomicAdd(a.rho_q + (long long)c * g.my + r, (ull)v); };
-    int had = 0;  // this thread accumulated a node into the tile
+    auto add_win = [&](int c, int r, long long v) {
+        asm volatile("red.shared.add.u64 [%0], %1;" ::"r"(win_s + 8u * (unsigned)((c - wc0) * wrn + (r - wr0))),
+                     "l"(v)
+                     : "memory");
+    };
+    int had = 0;      // this thread accumulated a node into the tile
+    int had_win = 0;  // ... or into the window
+    // a node's raw inputs (update mode: its record; plain mode: x, y, w, h as
+    // bits), loaded one iteration ahead: the loads of the next node are in
+    // flight while this one is added
+    auto load_raw = [&](int i, int &rb, int4 &ro) {
+        rb = kRecNone;
+        ro = make_int4(0, 0, 0, 0);
+        if (i >= r_hi) return;
+        const int node = a.lo + i;
+        if (a.update) {
+            rb = __ldg(a.rec_bin + node);
+            ro = __ldg(a.rec_ov + node);
+        } else {
+            rb = 0;
+            ro = make_int4(__float_as_int(__ldg(a.px + node)), __float_as_int(__ldg(a.py + node)),
+                           __float_as_int(__ldg(a.w + node)), __float_as_int(__ldg(a.h + node)));
+        }
+    };
+    int next_b;
+    int4 next_o;
+    load_raw(r_lo + tid, next_b, next_o);
     for (int base = r_lo; base < r_hi; base += kScatterThreads) {  // the same trip count in every lane
         const int i = base + tid;
         const bool valid = i < r_hi;
         const int node = a.lo + i;
+        const int rb = next_b;
+        const int4 ro = next_o;
+        load_raw(i + kScatterThreads, next_b, next_o);
         NodeRec q{kRecNone, 0, 0, 0, 0};
         if (valid) {
             if (a.update) {
-                q.bin = __ldg(a.rec_bin + node);
-                const int4 o = __ldg(a.rec_ov + node);
-                q.xr = o.x;
-                q.wq = o.y;
-                q.yr = o.z;
-                q.hq = o.w;
+                q = NodeRec{rb, ro.x, ro.y, ro.z, ro.w};
             } else {
                 int c0, c1, r0, r1;
-                q = make_rec(g, __ldg(a.px + node), __ldg(a.py + node), __ldg(a.w + node), __ldg(a.h + node), c0, c1,
-                             r0, r1);
+                q = make_rec(g, __int_as_float(ro.x), __int_as_float(ro.y), __int_as_float(ro.z),
+                             __int_as_float(ro.w), c0, c1, r0, r1);
             }
         }
         bool fits = false;
@@ -333,6 +368,14 @@ __global__ void __launch_bounds__(kScatterThreads, 2) scatter_kernel(ScatterArgs
             had |= fits;
         }
         if (fits || q.bin == kRecNone) continue;
+        if (q.bin >= 0) {
+            const int c0 = rec_c0(q.bin) - wc0, r0 = rec_r0(q.bin) - wr0;
+            if (c0 >= 0 && r0 >= 0 && c0 + qnc <= wcn && r0 + qnr <= wrn) {
+                emit_rec(g, q.bin, q.xr, q.wq, q.yr, q.hq, add_win);
+                had_win = 1;
+                continue;
+            }
+        }
         if (q.bin == kRecFull) {
             // outside the record's range: re-evaluated from the node's position
             const float x = a.update ? a.vx[nxt][node] : __ldg(a.px + node);
@@ -342,7 +385,13 @@ __global__ void __launch_bounds__(kScatterThreads, 2) scatter_kernel(ScatterArgs
             emit_rec(g, q.bin, q.xr, q.wq, q.yr, q.hq, add_glb);
         }
     }
-    // 4. the tile, summed over the block and added once
+    // 4. the window's non-zero bins, then the tile summed over the block
+    if (__syncthreads_or(had_win)) {  // uniform
+        for (int t = tid; t < wcn * wrn; t += kScatterThreads) {
+            const ull v = win[t];
+            if (v) add_glb(wc0 + t / wrn, wr0 + t % wrn, (long long)v);
+        }
+    }
     if (!__syncthreads_or(had)) return;  // uniform: no node of the range went into the tile
 #pragma unroll
     for (int u = 0; u < kTile; ++u)
@@ -891,7 +940,8 @@ __global__ void numerics_selftest_kernel(long long n, ull seed, int *mism) {
         if (__float_as_uint(ll2f_rn_bits(v)) != __float_as_uint(__ll2float_rn(v))) atomicAdd(mism + 2, 1);
         const float c = (__uint_as_float(0x3F800000u | (lo >> 9)) - 1.5f) * 7.98f;  // [-3.99, 3.99)
         if ((long long)grad_q(c) != (long long)__float2int_rn(c * kGradScale)) atomicAdd(mism + 3, 1);
-        const long long q = (long long)(lo % 8388607u) - 4194303ll;  // |q| < 2^22
+        // |q| < 2^22 (the magic-number path) or any int64 of either sign
+        const long long q = (hi & 0x1000u) ? v : (long long)(lo % 8388607u) - 4194303ll;
         if (__float_as_uint(i64_to_float(q)) != __float_as_uint(__ll2float_rn(q))) atomicAdd(mism + 4, 1);
         // (-1, 2^23): [1, 2^23) with every exponent, or (-1, 1)
         const float t = __uint_as_float((lo & 0x007FFFFFu) | ((127u + (hi >> 12) % 23u) << 23));
@@ -904,7 +954,8 @@ __global__ void numerics_selftest_kernel(long long n, ull seed, int *mism) {
 
 /* Self-check of the conversion helpers; no counterpart in the reference.
  * mismatches[0..5]: f2i_rn_bits, f2i_rz_bits, ll2f_rn_bits, grad_q,
- * i64_to_float, f2i_rz_small, each over `samples` hashed inputs. */
+ * i64_to_float (small and any int64), f2i_rz_small, each over `samples`
+ * hashed inputs. */
 extern "C" int ap_selftest_numerics(int32_t *mismatches, int64_t samples) {
     if (!mismatches || samples <= 0 || samples > (1ll << 32)) return 1;  // AP_ERR_INVALID_ARG
     int *d = nullptr;

@@ -262,7 +262,8 @@ int ap_field_solve_noalloc(const float *density, float *ex, float *ey, int32_t b
  * GPU's own conversion instructions.  No counterpart in the reference.
  * mismatches[6] receives the number of differing results of: round-to-nearest
  * float->int32, truncating float->int32, int64->float, the gradient
- * quantiser, small int64->float, truncating float->int32 on (-1, 2^23); each
+ * quantiser, fixed-point int64->float (|q| < 2^22 and any int64), truncating
+ * float->int32 on (-1, 2^23); each
  * over `samples` (<= 2^32) hashed inputs
  * including rounding ties.  Runs on the current device, synchronously. */
 int ap_selftest_numerics(int32_t *mismatches, int64_t samples);

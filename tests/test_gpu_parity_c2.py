@@ -194,6 +194,7 @@ def test_node_force_and_gradient_vs_oracle(ap, oracle_lib, preset):
                                max(np.abs(rfx).sum() + np.abs(rfy).sum(), 1e-30)))
         with ap.Placer(nl) as pl:
             fx, fy, gx, gy = pl.compute_node_forces(x, y, ex, ey, gamma, lam)
+            wgx, wgy, _, _ = pl.compute_all_partials(x, y, gamma)
         # sum_b w_ib |E_b| as the error scale; a weight can be a hair below
         # zero where a node edge sits between the float bin edge that picks
         # the bin index and the fixed-point one (both sides use the same
@@ -223,9 +224,12 @@ def test_node_force_and_gradient_vs_oracle(ap, oracle_lib, preset):
                   f"rel {quantiles(err / np.maximum(np.abs(ref[mov]), 1e-30))}")
             if not (err <= bound).all():
                 ids = np.flatnonzero(mov)[np.argsort(-ratio)[:5]]
+                gw = wgx if got is gx else wgy
+                gf = fx if got is gx else fy
                 for i in ids:
-                    print(f"  node {i}: got {got[i]!r} ref {ref[i]!r} wl {wl[i]!r} F {f[i]!r} scl {scl[i]!r} "
-                          f"pins {pins[i]} hd {hd[i]!r} x {x[i]!r} y {y[i]!r}")
+                    print(f"  node {i}: got {got[i]!r} ref {ref[i]!r} wl {wl[i]!r} gpu-wl {gw[i]!r} F {f[i]!r} "
+                          f"gpu-F {gf[i]!r} pins {pins[i]} hd {hd[i]!r} charge {charge[i]!r} "
+                          f"from-gpu-parts {(gw[i] - lam * gf[i]) / hd[i]!r} x {x[i]!r} y {y[i]!r}")
             assert (err <= bound).all()
             assert (got[~mov] == 0).all()
 
