@@ -179,12 +179,18 @@ __device__ __forceinline__ long long to_q(float v) {
 }
 
 // float of an int64 fixed-point value, rounded to nearest (= (float)q):
-// exact below 2^22 by the magic-number addition, else by integer arithmetic.
-// (Splitting q into 32-bit halves and converting each is not: for a small
+// exact below 2^22 by the magic-number addition, in the int32 range by one
+// FMA of two exact parts, else by integer arithmetic.  (Splitting q into 32-bit halves and converting each is not: for a small
 // negative q the low word is close to 2^32, and its rounding to 24 bits is
 // off by up to 256 units -- 2.4e-4 on a WA gradient below -4.)
 __device__ __forceinline__ float i64_to_float(long long q) {
     if (q > -4194304ll && q < 4194304ll) return i2f_small((int)q);
+    if (q >= -2147483647ll && q <= 2147483647ll) {
+        // q = hi 2^12 + lo with |hi| < 2^19 and 0 <= lo < 2^12: both parts
+        // are exact by the magic number, and the FMA rounds their exact sum once
+        const int v = (int)q, hi = v >> 12, lo = v & 0xFFF;
+        return fmaf(i2f_small(hi), 4096.0f, i2f_small(lo));
+    }
     return ll2f_rn_bits(q);
 }
 

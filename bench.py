@@ -389,6 +389,71 @@ def train_surrogate(ap, preset: str, solver: str):
     return s, info
 
 
+def surrogate_study(args):
+    """The learned surrogate at its own workload (200k cells, 512^2 bins,
+    256^2 coarse grid) trained to the full budget: 20k (density, field) pairs,
+    every trial of the first 2000 of 10 seeded exact runs on 10 seeded
+    netlists; held-out pairs from an 11th netlist, their errors split by the
+    overflow at which they were taken (the surrogate stands in while the
+    overflow is above 0.3); then the time to 10% overflow of the mixed form
+    with the trained net, with its coarse spectral layer alone and without a
+    surrogate (three seeded starts each)."""
+    import numpy as np
+    import torch
+
+    import aieplace_gb300 as ap
+    from aieplace_gb300 import build as b
+
+    b.build()
+    runs, per_run, held, every_held = 10, 2000, 400, 5
+    s = ap.Surrogate(factor=2, kernels=(3, 1, 1, 1))
+    s.reserve(runs * per_run + held, 256)
+    t0 = time.perf_counter()
+    for k in range(runs):
+        nl = ap.synth.generate("c1", seed=100 + k)
+        with ap.Placer(nl, field_solver="bf16x3") as pl:
+            pl.initialize_placement(seed=200 + k, sigma=1.0)
+            assert s.collect(pl, per_run, 1) == per_run
+    held_tau = []
+    nl = ap.synth.generate("c1", seed=150)
+    with ap.Placer(nl, field_solver="bf16x3") as pl:
+        pl.initialize_placement(seed=250, sigma=1.0)
+        for _ in range(held // 10):
+            tau0 = pl.stats()["overflow"]
+            s.collect(pl, 10 * every_held, every_held)
+            held_tau += [0.5 * (tau0 + pl.stats()["overflow"])] * 10
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    steps = args.steps if args.steps > 200 else 20000
+    losses = s.train(steps=steps, batch=8, crop=64, lr=2e-3, seed=1, first=0, count=runs * per_run)
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    en, ec = s.validate(runs * per_run, held)
+    tau = np.array(held_tau)
+    hi = tau > 0.3
+    nl = ap.synth.generate("c1", seed=1)
+    res = {"mixed": time_to_target(ap, nl, "bf16x3"), "plain": time_to_target(ap, nl, "fp32"),
+           "mixed_surrogate": time_to_target(ap, nl, "bf16x3", surrogate=s, use_net=True),
+           "mixed_surrogate_coarse_only": time_to_target(ap, nl, "bf16x3", surrogate=s, use_net=False)}
+    for k in ("mixed", "mixed_surrogate", "mixed_surrogate_coarse_only"):
+        res[k]["speedup_vs_plain"] = res["plain"]["seconds"] / res[k]["seconds"]
+    s.close()
+
+    def stat(v):
+        return {"mean": float(v.mean()), "p50": float(np.median(v))} if v.size else None
+
+    print(json.dumps({
+        "study": "learned surrogate, 200k cells / 512^2 bins / 256^2 coarse grid, net kernels 3-1-1-1, 32 channels",
+        "train_pairs": runs * per_run, "runs": runs, "heldout_pairs": held, "collect_s": t1 - t0,
+        "train_steps": steps, "train_s": t2 - t1, "loss_first100": float(losses[:100].mean()),
+        "loss_last500": float(losses[-500:].mean()),
+        "heldout_err_net": stat(en), "heldout_err_coarse": stat(ec),
+        "heldout_pairs_overflow_above_0.3": int(hi.sum()),
+        "heldout_err_net_overflow_above_0.3": stat(en[hi]),
+        "heldout_err_coarse_overflow_above_0.3": stat(ec[hi]),
+        "time_to_10pct_overflow": res}), flush=True)
+
+
 def main():
     ap_ = argparse.ArgumentParser()
     ap_.add_argument("--gpus", type=int, default=1)
@@ -401,6 +466,9 @@ def main():
     ap_.add_argument("--no-ttt", action="store_true", help="skip the time-to-10%% runs")
     ap_.add_argument("--no-c4", action="store_true",
                      help="skip the surrogate's own workload (200k cells, 512^2 bins, 256^2 coarse grid)")
+    ap_.add_argument("--surrogate-study", action="store_true",
+                     help="train the surrogate on 20k pairs from 10 runs of the 200k-cell workload and report "
+                          "held-out errors and time to 10%% overflow")
     ap_.add_argument("--batch", type=int, default=0,
                      help="batched form instead: this many instances (5k-150k cells) in one graph")
     ap_.add_argument("--profile-after", type=int, default=-1,
@@ -412,6 +480,8 @@ def main():
         return reference_arm(args)
     if args.profile_after >= 0:
         return profile_mode(args)
+    if args.surrogate_study:
+        return surrogate_study(args)
     if args.batch:
         return batch_mode(args)
 
