@@ -344,8 +344,9 @@ def time_to_target_once(ap, nl, solver, target, max_iter, surrogate, use_net, se
 
 def c4_block(ap):
     """The learned surrogate's own workload: 200k cells, 512^2 bins, the
-    surrogate on the 256^2-pooled density (factor 2), trained here as for
-    C2; time to 10% overflow of the plain, mixed and mixed + surrogate forms."""
+    surrogate on the 256^2-pooled density (factor 2), trained here to the
+    full budget (20k pairs from 10 seeded runs, SURROGATE_BUDGET); time to 10%
+    overflow of the plain, mixed and mixed + surrogate forms."""
     nl = ap.synth.generate("c1", seed=1)
     out = {"workload": "c1: 200000 movable cells, 4000 fixed macros, 210000 nets, 512x512 bins, target "
                        "density 0.7, seed 1; surrogate factor 2 (256x256 coarse grid)",
@@ -360,98 +361,80 @@ def c4_block(ap):
     return out
 
 
+# Training budgets of the learned surrogate: pairs from `runs` seeded exact
+# loops (every `every`-th of their first `runs_trials` trials), Adam steps, and
+# held-out pairs from another netlist.  The 200k-cell workload (coarse factor
+# 2, 3.7 MB a pair) takes the full 20k-pair budget; the 2M-cell workload
+# (factor 4, 13 MB a pair) 4000 pairs, which fit beside it in HBM.
+SURROGATE_BUDGET = {"c1": dict(runs=10, runs_trials=2000, every=1, steps=20000, held=400, held_every=5),
+                    "c2": dict(runs=8, runs_trials=1000, every=2, steps=10000, held=100, held_every=20)}
+
+
 def train_surrogate(ap, preset: str, solver: str):
     """The learned surrogate of the mixed+surrogate form, trained here on the GPU
-    by the library's own kernels: 140 (density, field) pairs from the exact
-    loop of another seeded netlist of the same shape (every 14th of 1960
-    trials), 1500 Adam steps on 8 random 64 x 64 crops, then 20 held-out pairs
-    from a third netlist.  The coarse grid is 256^2 (factor bins / 256)."""
+    by the library's own kernels on (density, field) pairs the exact solve
+    produces in seeded loops on other netlists of the same shape
+    (SURROGATE_BUDGET), Adam on 8 random 64 x 64 crops a step; then held-out
+    pairs from another netlist, their errors also split by the overflow at
+    which they were taken (the surrogate stands in above 0.3).  The coarse
+    grid is 256^2 (factor bins / 256)."""
+    import numpy as np
     import torch
 
+    bud = SURROGATE_BUDGET[preset]
     f = max(1, int(ap.synth.PRESETS[preset]["bins"]) // 256)
+    per_run = bud["runs_trials"] // bud["every"]
+    n_train = bud["runs"] * per_run
     t0 = time.perf_counter()
     s = ap.Surrogate(factor=f, kernels=(3, 1, 1, 1))
-    s.reserve(160, 256)
-    for seed, n, every in ((2, 140, 14), (3, 20, 98)):
-        nl = ap.synth.generate(preset, seed=seed)
+    s.reserve(n_train + bud["held"], 256)
+    for k in range(bud["runs"]):
+        nl = ap.synth.generate(preset, seed=100 + k)
         with ap.Placer(nl, field_solver=solver) as pl:
-            pl.initialize_placement(seed=10 * seed + 1, sigma=1.0)
-            s.collect(pl, n * every, every)
+            pl.initialize_placement(seed=200 + k, sigma=1.0)
+            s.collect(pl, bud["runs_trials"], bud["every"])
+    held_tau = []
+    nl = ap.synth.generate(preset, seed=150)
+    with ap.Placer(nl, field_solver=solver) as pl:
+        pl.initialize_placement(seed=250, sigma=1.0)
+        for _ in range(bud["held"] // 10):
+            tau0 = pl.stats()["overflow"]
+            s.collect(pl, 10 * bud["held_every"], bud["held_every"])
+            held_tau += [0.5 * (tau0 + pl.stats()["overflow"])] * 10
+    torch.cuda.synchronize()
     t1 = time.perf_counter()
-    losses = s.train(steps=1500, batch=8, crop=64, lr=2e-3, seed=1, first=0, count=140)
+    losses = s.train(steps=bud["steps"], batch=8, crop=64, lr=2e-3, seed=1, first=0, count=n_train)
     torch.cuda.synchronize()
     t2 = time.perf_counter()
-    en, ec = s.validate(140, 20)
-    info = {"factor": f, "kernels": [3, 1, 1, 1], "width": 32, "params": s.num_params, "train_pairs": 140,
-            "collect_s": t1 - t0, "train_s": t2 - t1, "loss_first20": float(losses[:20].mean()),
-            "loss_last50": float(losses[-50:].mean()),
-            "heldout_field_err_net_mean": float(en.mean()), "heldout_field_err_coarse_mean": float(ec.mean())}
+    en, ec = s.validate(n_train, bud["held"])
+    hi = np.array(held_tau) > 0.3
+
+    def stat(v):
+        return {"mean": float(v.mean()), "p50": float(np.median(v))} if v.size else None
+
+    info = {"factor": f, "kernels": [3, 1, 1, 1], "width": 32, "params": s.num_params, "train_pairs": n_train,
+            "runs": bud["runs"], "train_steps": bud["steps"], "heldout_pairs": bud["held"],
+            "collect_s": t1 - t0, "train_s": t2 - t1, "loss_first100": float(losses[:100].mean()),
+            "loss_last500": float(losses[-500:].mean()),
+            "heldout_field_err_net": stat(en), "heldout_field_err_coarse": stat(ec),
+            "heldout_pairs_overflow_above_0.3": int(hi.sum()),
+            "heldout_field_err_net_overflow_above_0.3": stat(en[hi]),
+            "heldout_field_err_coarse_overflow_above_0.3": stat(ec[hi])}
     return s, info
 
 
 def surrogate_study(args):
     """The learned surrogate at its own workload (200k cells, 512^2 bins,
-    256^2 coarse grid) trained to the full budget: 20k (density, field) pairs,
-    every trial of the first 2000 of 10 seeded exact runs on 10 seeded
-    netlists; held-out pairs from an 11th netlist, their errors split by the
-    overflow at which they were taken (the surrogate stands in while the
-    overflow is above 0.3); then the time to 10% overflow of the mixed form
-    with the trained net, with its coarse spectral layer alone and without a
+    256^2 coarse grid) trained to the full budget (20k pairs from 10 seeded
+    runs): held-out errors and the time to 10% overflow of the mixed form with
+    the trained net, with its coarse spectral layer alone and without a
     surrogate (three seeded starts each)."""
-    import numpy as np
-    import torch
-
     import aieplace_gb300 as ap
     from aieplace_gb300 import build as b
 
     b.build()
-    runs, per_run, held, every_held = 10, 2000, 400, 5
-    s = ap.Surrogate(factor=2, kernels=(3, 1, 1, 1))
-    s.reserve(runs * per_run + held, 256)
-    t0 = time.perf_counter()
-    for k in range(runs):
-        nl = ap.synth.generate("c1", seed=100 + k)
-        with ap.Placer(nl, field_solver="bf16x3") as pl:
-            pl.initialize_placement(seed=200 + k, sigma=1.0)
-            assert s.collect(pl, per_run, 1) == per_run
-    held_tau = []
-    nl = ap.synth.generate("c1", seed=150)
-    with ap.Placer(nl, field_solver="bf16x3") as pl:
-        pl.initialize_placement(seed=250, sigma=1.0)
-        for _ in range(held // 10):
-            tau0 = pl.stats()["overflow"]
-            s.collect(pl, 10 * every_held, every_held)
-            held_tau += [0.5 * (tau0 + pl.stats()["overflow"])] * 10
-    torch.cuda.synchronize()
-    t1 = time.perf_counter()
-    steps = args.steps if args.steps > 200 else 20000
-    losses = s.train(steps=steps, batch=8, crop=64, lr=2e-3, seed=1, first=0, count=runs * per_run)
-    torch.cuda.synchronize()
-    t2 = time.perf_counter()
-    en, ec = s.validate(runs * per_run, held)
-    tau = np.array(held_tau)
-    hi = tau > 0.3
-    nl = ap.synth.generate("c1", seed=1)
-    res = {"mixed": time_to_target(ap, nl, "bf16x3"), "plain": time_to_target(ap, nl, "fp32"),
-           "mixed_surrogate": time_to_target(ap, nl, "bf16x3", surrogate=s, use_net=True),
-           "mixed_surrogate_coarse_only": time_to_target(ap, nl, "bf16x3", surrogate=s, use_net=False)}
-    for k in ("mixed", "mixed_surrogate", "mixed_surrogate_coarse_only"):
-        res[k]["speedup_vs_plain"] = res["plain"]["seconds"] / res[k]["seconds"]
-    s.close()
-
-    def stat(v):
-        return {"mean": float(v.mean()), "p50": float(np.median(v))} if v.size else None
-
-    print(json.dumps({
-        "study": "learned surrogate, 200k cells / 512^2 bins / 256^2 coarse grid, net kernels 3-1-1-1, 32 channels",
-        "train_pairs": runs * per_run, "runs": runs, "heldout_pairs": held, "collect_s": t1 - t0,
-        "train_steps": steps, "train_s": t2 - t1, "loss_first100": float(losses[:100].mean()),
-        "loss_last500": float(losses[-500:].mean()),
-        "heldout_err_net": stat(en), "heldout_err_coarse": stat(ec),
-        "heldout_pairs_overflow_above_0.3": int(hi.sum()),
-        "heldout_err_net_overflow_above_0.3": stat(en[hi]),
-        "heldout_err_coarse_overflow_above_0.3": stat(ec[hi]),
-        "time_to_10pct_overflow": res}), flush=True)
+    print(json.dumps({"study": "learned surrogate, 200k cells / 512^2 bins / 256^2 coarse grid",
+                      **c4_block(ap)}), flush=True)
 
 
 def main():
