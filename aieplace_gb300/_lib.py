@@ -27,7 +27,8 @@ EXPORTS = [
     "ap_design_read", "ap_design_read_dir", "ap_design_get_info", "ap_design_netlist", "ap_design_name",
     "ap_design_node_name", "ap_design_write_def", "ap_design_destroy",
     "ap_create_batch", "ap_batch_destroy", "ap_batch_init_seeded", "ap_batch_step", "ap_batch_run",
-    "ap_batch_get_stats", "ap_batch_get_positions",
+    "ap_batch_get_stats", "ap_batch_get_positions", "ap_batch_set_form", "ap_batch_get_info",
+    "ap_batch_debug_inject",
     "ap_surrogate_config_default", "ap_surrogate_create", "ap_surrogate_destroy", "ap_surrogate_num_params",
     "ap_surrogate_get_params", "ap_surrogate_set_params", "ap_surrogate_forward", "ap_surrogate_gradient",
     "ap_surrogate_reserve", "ap_surrogate_num_samples", "ap_surrogate_collect", "ap_surrogate_train",
@@ -62,6 +63,16 @@ class Params(C.Structure):
                 ("max_iterations", C.c_int32), ("check_interval", C.c_int32),
                 ("use_graph", C.c_int32), ("max_backtracks", C.c_int32), ("restart_mode", C.c_int32),
                 ("filler_cells", C.c_int32)]
+
+
+class BatchInfo(C.Structure):
+    _fields_ = [("form", C.c_int32), ("instances", C.c_int32), ("active", C.c_int32), ("field_tile", C.c_int32),
+                ("field_tune_ms", C.c_float * 2), ("records", C.c_int32 * 6)]
+
+    def as_dict(self) -> dict:
+        return {"form": ("graph", "persistent")[self.form], "instances": self.instances, "active": self.active,
+                "field_tile": self.field_tile, "field_tune_ms": list(self.field_tune_ms),
+                "records": dict(zip(("update", "scatter", "rho", "wa", "field", "gather"), self.records))}
 
 
 class Stats(C.Structure):
@@ -172,6 +183,9 @@ def lib():
         L.ap_batch_run.argtypes = [vp, vp]
         L.ap_batch_get_stats.argtypes = [vp, i32, C.POINTER(Stats)]
         L.ap_batch_get_positions.argtypes = [vp, i32, vp, vp]
+        L.ap_batch_set_form.argtypes = [vp, i32]
+        L.ap_batch_get_info.argtypes = [vp, C.POINTER(BatchInfo)]
+        L.ap_batch_debug_inject.argtypes = [vp, i32, C.c_int64]
         L.ap_surrogate_config_default.argtypes = [C.POINTER(SurrogateConfig)]
         L.ap_surrogate_create.argtypes = [C.POINTER(SurrogateConfig), C.POINTER(vp)]
         L.ap_surrogate_destroy.argtypes = [vp]

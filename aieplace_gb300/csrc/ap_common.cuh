@@ -351,16 +351,26 @@ __device__ __forceinline__ float kahan_strided(const float *partials, int i0, in
     return s;
 }
 
+// One block of a launch: its index and the launch's block count.  A kernel
+// body written against VBlock instead of blockIdx.x / gridDim.x runs both as
+// a launch of its own (grid_block()) and as a work item of a persistent
+// launch that executes the blocks of many such launches (the batched form).
+struct VBlock {
+    int id, n;
+};
+__device__ __forceinline__ VBlock grid_block() { return VBlock{(int)blockIdx.x, (int)gridDim.x}; }
+
 // Last-block detection for grid-wide reductions without waiting: every block
-// publishes its partials, the block that arrives last reduces them in block
-// order (so the result does not depend on scheduling) and resets the counter.
-__device__ __forceinline__ bool arrive_last(unsigned int *counter) {
+// publishes its partials, the block that arrives last of `blocks` reduces
+// them in block order (so the result does not depend on scheduling) and
+// resets the counter.
+__device__ __forceinline__ bool arrive_last(unsigned int *counter, int blocks) {
     __shared__ bool last;
     __syncthreads();
     if (threadIdx.x == 0) {
         __threadfence();
         const unsigned int t = atomicAdd(counter, 1u);
-        last = (t == gridDim.x - 1);
+        last = (t == (unsigned int)blocks - 1u);
     }
     __syncthreads();
     if (last) __threadfence();

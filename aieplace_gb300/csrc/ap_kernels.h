@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include "ap_common.cuh"
+#include "ap_persist.cuh"
 
 namespace ap {
 
@@ -23,8 +24,13 @@ struct WaArgs {
     int n_small, n_nets;
     int bucket_lo[kWaBuckets + 1];
     int bucket_blocks[kWaBuckets];  // grid of each bucket's launch (filled by the launcher)
-    const float *px, *py;  // positions of all nodes (modes other than WA_LOOP)
-    const float *pxs[2], *pys[2];  // WA_LOOP: the trial point is buffer [1 - sc->cur]
+    // positions of all nodes, interleaved (one 8-byte load per pin), read by
+    // the kernels: in WA_LOOP mode written by the position update (movable
+    // nodes) and once at creation (the fixed ones); in the other modes
+    // filled by launch_wirelength from (px, py)
+    float2 *xy;
+    int n_nodes;
+    const float *px, *py;  // modes other than WA_LOOP: positions of all nodes
     float gamma;           // > 0 overrides sc->gamma
     DevScalars *sc;
     ull *gq;               // int64 fixed-point gradient accumulators, both axes packed (pack_q)
@@ -36,8 +42,11 @@ struct WaArgs {
     double *out;           // [2]: HPWL, WA
     int mode;
 };
-// launches the four bucket kernels; the last one (warp per net) folds the sums
+// launches the four bucket kernels (after filling a.xy from a.px, a.py in
+// the modes other than WA_LOOP); the last one (warp per net) folds the sums
 void launch_wirelength(const WaArgs &a, cudaStream_t st);
+// xy[i] = (px[i], py[i]), i < n
+void launch_interleave(int n, const float *px, const float *py, float2 *xy, cudaStream_t st);
 // Block partials buffer (doubles; the per-block partials are FP32, two per
 // double): holds 2 FP32 per block of the four WA launches at kWaMaxBlocks
 // each, 4 per gather block at kGatherMaxBlocks, 2 per update block (at most
@@ -74,6 +83,9 @@ struct ScatterArgs {
     // update mode, optional: the trial point also written here (movable
     // nodes), for a copy to the host that overlaps the rest of the trial
     float *trial_x, *trial_y;
+    // update mode, optional: the trial point interleaved (movable nodes),
+    // for the loop's WA kernels
+    float2 *xy_out;
     // update mode, optional: the accepted point read from here instead of
     // buffers [cur] (a host step's input)
     const float *in_x, *in_y;
@@ -206,5 +218,41 @@ int field_solver_status(FieldSolver &f, unsigned int *out);
 int field_solver_clear_status(FieldSolver &f);
 // float -> bf16 hi/lo split (for per-stage API calls)
 void launch_split_bf16(int n, const float *src, __nv_bfloat16 *hi, __nv_bfloat16 *lo, cudaStream_t st);
+
+// ---- batched form: persistent launches (ap_persist.cuh) ----------------------
+enum { PS_UPDATE = 0, PS_SCATTER = 1, PS_RHO = 2, PS_WA = 3, PS_FIELD = 4, PS_GATHER = 5 };
+
+// resident blocks of `kernel` on the whole GPU, or `fallback`
+int wave_of(const void *kernel, int threads, int fallback);
+// the grids the launchers give an instance's own launches (a persistent
+// record of the same instance runs the same blocks)
+int update_grid(const ScatterArgs &a);
+int scatter_grid(int n);
+int rho_grid(int nbins);
+int gather_grid(int n_mov);
+// fills bucket_blocks and small_blocks as launch_wirelength does; returns
+// the blocks of all four bucket launches
+int wa_plan(WaArgs &a);
+
+// One contraction stage of an FP32 field solve (S1..S4 of k_field_simt.cu):
+// D[z] = A[z] B[z]^T on an m x m grid in bm x bm tiles, `batch` values of z,
+// the spectral epilogue (phi -> px, py) when `spectral`.
+struct FieldRec {
+    const float *A[2];
+    const float *B[2];
+    float *C[2];
+    float *px, *py;
+    const float *wx, *wy;
+    float scale;
+    int m, bm, spectral, batch;
+};
+// the four stages of field_solve_fp32(f, d, ex, ey) with the solver's tuned tile
+void field_records(const FieldSolver &f, const float *d, float *ex, float *ey, FieldRec rec[4]);
+inline int field_rec_blocks(const FieldRec &r) { return (r.m / r.bm) * (r.m / r.bm) * r.batch; }
+
+// one persistent launch of a stage over the records `recs` (device memory)
+void launch_persist_density(int stage, const PersistQueue &q, const void *recs, cudaStream_t st);
+void launch_persist_wa(const PersistQueue &q, const WaArgs *recs, cudaStream_t st);
+void launch_persist_field(const PersistQueue &q, const FieldRec *recs, cudaStream_t st);
 
 }  // namespace ap

@@ -56,6 +56,10 @@ struct ap_handle {
     int *d_net_ptr = nullptr, *d_pin_node = nullptr;
     float *d_w = nullptr, *d_h = nullptr;
     float *d_px[2] = {nullptr, nullptr}, *d_py[2] = {nullptr, nullptr};
+    // all nodes' positions interleaved for the WA kernels: the loop's trial
+    // point (movable nodes written by each position update, fixed nodes at
+    // creation), and a scratch copy for WA evaluations at other points
+    float2 *d_xy_loop = nullptr, *d_xy_tmp = nullptr;
     float *d_ux[2] = {nullptr, nullptr}, *d_uy[2] = {nullptr, nullptr};
     float *d_gx[2] = {nullptr, nullptr}, *d_gy[2] = {nullptr, nullptr};
     float *d_pins = nullptr, *d_charge = nullptr;
@@ -184,10 +188,8 @@ WaArgs wa_args(ap_handle *h, const float *px, const float *py, float gamma, int 
     a.n_nets = h->n_nets;
     a.px = px;
     a.py = py;
-    for (int b = 0; b < 2; ++b) {
-        a.pxs[b] = h->d_px[b];
-        a.pys[b] = h->d_py[b];
-    }
+    a.xy = mode == WA_LOOP ? h->d_xy_loop : h->d_xy_tmp;
+    a.n_nodes = h->n_nodes;
     a.gamma = gamma;
     a.sc = h->d_sc;
     a.gq = h->d_gq;
@@ -234,6 +236,7 @@ ScatterArgs loop_scatter_args(ap_handle *h) {
     s.update = 1;
     s.rec_bin = h->d_rec_bin;
     s.rec_ov = h->d_rec_ov;
+    s.xy_out = h->d_xy_loop;
     s.lo = 0;
     s.hi = h->n_mov;
     return s;
@@ -874,6 +877,7 @@ int ap_create(const ap_netlist *nl, const ap_params *params, ap_handle **out) {
     for (int b = 0; b < 2; ++b) {
         A(dalloc(&h->d_px[b], N));
         A(dalloc(&h->d_py[b], N));
+        A(dalloc(b ? &h->d_xy_tmp : &h->d_xy_loop, N));
         A(dalloc(&h->d_gx[b], std::max(1, h->n_mov)));
         A(dalloc(&h->d_gy[b], std::max(1, h->n_mov)));
     }
@@ -936,6 +940,8 @@ int ap_create(const ap_netlist *nl, const ap_params *params, ap_handle **out) {
         A(cudaMemcpy(h->d_px[b], x.data(), sizeof(float) * N, cudaMemcpyHostToDevice));
         A(cudaMemcpy(h->d_py[b], y.data(), sizeof(float) * N, cudaMemcpyHostToDevice));
     }
+    launch_interleave(N, h->d_px[0], h->d_py[0], h->d_xy_loop, 0);
+    A(cudaGetLastError());
     A(cudaMemcpy(h->d_pins, pins.data(), sizeof(float) * N, cudaMemcpyHostToDevice));
     A(cudaMemcpy(h->d_charge, charge.data(), sizeof(float) * N, cudaMemcpyHostToDevice));
     A(cudaMemset(h->d_mov_q, 0, sizeof(ull) * nb));
@@ -1020,7 +1026,7 @@ int ap_destroy(ap_handle *h) {
                     h->d_mov_q,   h->d_fill_q,   h->d_fix_q,  h->d_fixs_q,  h->d_dens,  h->d_ex,    h->d_ey,
                     h->d_dens_hi, h->d_dens_lo,  h->d_sx,     h->d_sy,      h->d_sc,    h->d_partials,
                     h->d_partials_ll, h->d_counters, h->d_out, h->d_rec_bin, h->d_rec_ov, h->d_gq,
-                    h->d_ix,      h->d_iy};
+                    h->d_ix,      h->d_iy,       h->d_xy_loop, h->d_xy_tmp};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     if (h->h_sc) cudaFreeHost(h->h_sc);
@@ -1750,6 +1756,23 @@ int ap_surrogate_collect(ap_handle *h, ap_surrogate *s, int32_t n_trials, int32_
 
 // ---- batched form ---------------------------------------------------------------
 
+// The persistent form's device tables, rebuilt whenever the set of active
+// instances changes.  Stage records in item order; the field stage holds
+// four records per instance (its contractions S1..S4), all instances' S1
+// first, record k + 1 of an instance depending on its record k.
+struct PersistPlan {
+    int n_rec[6] = {0, 0, 0, 0, 0, 0};
+    void *d_recs[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    int *d_start[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    int *d_dep = nullptr;
+    // queue heads and the field stage's done counters, laid out so that each
+    // launch zeroes the counters of the launch before it on the stream as
+    // one range: [0] gather, [1] update, [2] scatter, [3] rho, [4] WA,
+    // [5] field, [6 ..) field done counters
+    unsigned int *d_cnt = nullptr;
+    int field_bm = 0;  // 0: each instance's own tuned tile; else 32 or 64 for all
+};
+
 struct ap_batch {
     std::vector<ap_handle *> inst;
     std::vector<char> active;
@@ -1757,6 +1780,16 @@ struct ap_batch {
     cudaEvent_t fork = nullptr;
     std::vector<cudaEvent_t> join;
     cudaGraphExec_t graph = nullptr;
+    int form = AP_BATCH_GRAPH;
+    // persistent form
+    PersistPlan plan;
+    cudaStream_t wa_stream = nullptr;
+    cudaEvent_t wa_fork = nullptr, wa_join = nullptr;
+    unsigned int *d_status = nullptr;  // a dependency wait of a persistent launch gave up
+    unsigned long long wait_ns = 1000000000ull;
+    int never_arrive = 0;
+    int tuned_bm = 0;                  // the field tile the batch autotuner chose (0: not tuned)
+    float tune_ms[2] = {0.f, 0.f};     // persistent field launch with 32 / 64 tiles
 };
 
 namespace {
@@ -1766,30 +1799,232 @@ void batch_free_graph(ap_batch *b) {
     b->graph = nullptr;
 }
 
-// One graph: fork from the main stream to every active instance's stream,
-// one trial step per instance, join back.
-int batch_build_graph(ap_batch *b) {
-    batch_free_graph(b);
-    cudaGraph_t gr = nullptr;
-    CK(cudaStreamBeginCapture(b->main, cudaStreamCaptureModeThreadLocal));
-    cudaError_t e = cudaEventRecord(b->fork, b->main);
-    int r = e == cudaSuccess ? AP_OK : AP_ERR_CUDA;
-    for (size_t i = 0; i < b->inst.size() && r == AP_OK; ++i) {
+void plan_free(PersistPlan &pp) {
+    for (int k = 0; k < 6; ++k) {
+        if (pp.d_recs[k]) cudaFree(pp.d_recs[k]);
+        if (pp.d_start[k]) cudaFree(pp.d_start[k]);
+    }
+    if (pp.d_dep) cudaFree(pp.d_dep);
+    if (pp.d_cnt) cudaFree(pp.d_cnt);
+    const int bm = pp.field_bm;
+    pp = PersistPlan();
+    pp.field_bm = bm;
+}
+
+// Whether the persistent form serves every instance: the FP32 field solve,
+// no surrogate.
+bool persist_supported(const ap_batch *b) {
+    for (const ap_handle *h : b->inst)
+        if (h->p.field_solver == AP_FIELD_BF16X3 || h->surr) return false;
+    return true;
+}
+
+template <typename T>
+int upload_stage(PersistPlan &pp, int k, const std::vector<T> &recs, const std::vector<int> &blocks) {
+    std::vector<int> start(blocks.size() + 1, 0);
+    for (size_t r = 0; r < blocks.size(); ++r) start[r + 1] = start[r] + blocks[r];
+    pp.n_rec[k] = (int)recs.size();
+    CK(dalloc(reinterpret_cast<T **>(&pp.d_recs[k]), recs.size()));
+    CK(dalloc(&pp.d_start[k], start.size()));
+    if (!recs.empty()) CK(cudaMemcpy(pp.d_recs[k], recs.data(), sizeof(T) * recs.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(pp.d_start[k], start.data(), sizeof(int) * start.size(), cudaMemcpyHostToDevice));
+    return AP_OK;
+}
+
+// Records of every active instance, each stage as the instance's own
+// launches would run it (enqueue_iteration).
+int plan_build(ap_batch *b, PersistPlan &pp) {
+    plan_free(pp);
+    std::vector<ScatterArgs> upd, sct;
+    std::vector<RhoArgs> rho;
+    std::vector<WaArgs> wa;
+    std::vector<GatherArgs> gat;
+    std::vector<int> bu, bs, br, bw, bg;
+    std::vector<FieldRec> fld[4];
+    for (size_t i = 0; i < b->inst.size(); ++i) {
         if (!b->active[i]) continue;
         ap_handle *h = b->inst[i];
-        if (cudaStreamWaitEvent(h->stream, b->fork, 0) != cudaSuccess) r = AP_ERR_CUDA;
-        if (r == AP_OK) r = enqueue_iteration(h, h->stream);
-        if (r == AP_OK && cudaEventRecord(b->join[i], h->stream) != cudaSuccess) r = AP_ERR_CUDA;
-        if (r == AP_OK && cudaStreamWaitEvent(b->main, b->join[i], 0) != cudaSuccess) r = AP_ERR_CUDA;
+        if (h->n_mov <= 0) return AP_ERR_UNSUPPORTED;
+        const ScatterArgs sa = loop_scatter_args(h);
+        upd.push_back(sa);
+        bu.push_back(update_grid(sa));
+        ScatterArgs s = sa;  // launch_movable_bins: real cells, then fillers
+        s.lo = 0;
+        s.hi = h->n_real;
+        s.rho_q = h->d_mov_q;
+        if (s.hi > s.lo) {
+            sct.push_back(s);
+            bs.push_back(scatter_grid(s.hi - s.lo));
+        }
+        if (h->n_fill) {
+            s.lo = h->n_real;
+            s.hi = h->n_mov;
+            s.rho_q = h->d_fill_q;
+            sct.push_back(s);
+            bs.push_back(scatter_grid(s.hi - s.lo));
+        }
+        const RhoArgs ra = rho_args(h, RHO_LOOP, nullptr);
+        rho.push_back(ra);
+        br.push_back(rho_grid(ra.nbins));
+        WaArgs wr = wa_args(h, h->d_px[0], h->d_py[0], 0.f, h->n_mov, WA_LOOP, nullptr);
+        bw.push_back(wa_plan(wr));
+        wa.push_back(wr);
+        FieldRec fr[4];
+        field_records(h->fs, h->d_dens, h->d_ex, h->d_ey, fr);
+        for (int k = 0; k < 4; ++k) {
+            if (pp.field_bm == 64 && fr[k].m % 64 == 0) fr[k].bm = 64;
+            if (pp.field_bm == 32) fr[k].bm = 32;
+            fld[k].push_back(fr[k]);
+        }
+        gat.push_back(loop_gather_args(h));
+        bg.push_back(gather_grid(h->n_mov));
     }
-    e = cudaStreamEndCapture(b->main, &gr);
+    const int ni = (int)upd.size();
+    if (4 * ni > kPersistMaxRecords || (int)sct.size() > kPersistMaxRecords) return AP_ERR_UNSUPPORTED;
+    std::vector<FieldRec> fall;
+    std::vector<int> bf, dep;
+    for (int k = 0; k < 4; ++k)
+        for (int i = 0; i < ni; ++i) {
+            fall.push_back(fld[k][i]);
+            bf.push_back(field_rec_blocks(fld[k][i]));
+            dep.push_back(k == 0 ? -1 : (k - 1) * ni + i);
+        }
+    int r = upload_stage(pp, PS_UPDATE, upd, bu);
+    if (r == AP_OK) r = upload_stage(pp, PS_SCATTER, sct, bs);
+    if (r == AP_OK) r = upload_stage(pp, PS_RHO, rho, br);
+    if (r == AP_OK) r = upload_stage(pp, PS_WA, wa, bw);
+    if (r == AP_OK) r = upload_stage(pp, PS_FIELD, fall, bf);
+    if (r == AP_OK) r = upload_stage(pp, PS_GATHER, gat, bg);
+    if (r != AP_OK) return r;
+    CK(dalloc(&pp.d_dep, dep.size()));
+    CK(cudaMemcpy(pp.d_dep, dep.data(), sizeof(int) * dep.size(), cudaMemcpyHostToDevice));
+    CK(dalloc(&pp.d_cnt, 6 + dep.size()));
+    CK(cudaMemset(pp.d_cnt, 0, sizeof(unsigned int) * (6 + dep.size())));
+    return AP_OK;
+}
+
+PersistQueue plan_queue(const ap_batch *b, int k, int reset_lo, int reset_n) {
+    const PersistPlan &pp = b->plan;
+    PersistQueue q{};
+    q.start = pp.d_start[k];
+    q.n_rec = pp.n_rec[k];
+    static const int head_slot[6] = {1, 2, 3, 4, 5, 0};  // PS_* -> counter slot
+    q.head = pp.d_cnt + head_slot[k];
+    q.status = b->d_status;
+    q.wait_ns = b->wait_ns;
+    q.reset = pp.d_cnt + reset_lo;
+    q.n_reset = reset_n;
+    if (k == PS_FIELD) {
+        q.dep = pp.d_dep;
+        q.done = pp.d_cnt + 6;
+        q.never_arrive = b->never_arrive;
+    }
+    return q;
+}
+
+// One trial step of every active instance as six persistent launches: the
+// position update; the WA gradient on a second stream beside scatter ->
+// density/overflow -> field; the gather with each instance's accept / retry.
+int enqueue_persist(ap_batch *b, cudaStream_t st) {
+    const PersistPlan &pp = b->plan;
+    const int nf = pp.n_rec[PS_FIELD];
+    launch_persist_density(PS_UPDATE, plan_queue(b, PS_UPDATE, 0, 1), pp.d_recs[PS_UPDATE], st);
+    CK(cudaEventRecord(b->wa_fork, st));
+    CK(cudaStreamWaitEvent(b->wa_stream, b->wa_fork, 0));
+    launch_persist_wa(plan_queue(b, PS_WA, 0, 0), static_cast<const WaArgs *>(pp.d_recs[PS_WA]), b->wa_stream);
+    CK(cudaEventRecord(b->wa_join, b->wa_stream));
+    launch_persist_density(PS_SCATTER, plan_queue(b, PS_SCATTER, 1, 1), pp.d_recs[PS_SCATTER], st);
+    launch_persist_density(PS_RHO, plan_queue(b, PS_RHO, 2, 1), pp.d_recs[PS_RHO], st);
+    launch_persist_field(plan_queue(b, PS_FIELD, 3, 1), static_cast<const FieldRec *>(pp.d_recs[PS_FIELD]), st);
+    CK(cudaStreamWaitEvent(st, b->wa_join, 0));
+    launch_persist_density(PS_GATHER, plan_queue(b, PS_GATHER, 4, 2 + nf), pp.d_recs[PS_GATHER], st);
+    return cudaGetLastError() == cudaSuccess ? AP_OK : AP_ERR_CUDA;
+}
+
+// One graph: fork from the main stream to every active instance's stream,
+// one trial step per instance, join back (graph form); or the six
+// persistent launches over all active instances (persistent form).
+int batch_build_graph(ap_batch *b) {
+    batch_free_graph(b);
+    if (b->form == AP_BATCH_PERSISTENT) {
+        const int pr = plan_build(b, b->plan);
+        if (pr != AP_OK) return pr;
+    }
+    cudaGraph_t gr = nullptr;
+    CK(cudaStreamBeginCapture(b->main, cudaStreamCaptureModeThreadLocal));
+    int r = AP_OK;
+    if (b->form == AP_BATCH_PERSISTENT) {
+        r = enqueue_persist(b, b->main);
+    } else {
+        cudaError_t e = cudaEventRecord(b->fork, b->main);
+        r = e == cudaSuccess ? AP_OK : AP_ERR_CUDA;
+        for (size_t i = 0; i < b->inst.size() && r == AP_OK; ++i) {
+            if (!b->active[i]) continue;
+            ap_handle *h = b->inst[i];
+            if (cudaStreamWaitEvent(h->stream, b->fork, 0) != cudaSuccess) r = AP_ERR_CUDA;
+            if (r == AP_OK) r = enqueue_iteration(h, h->stream);
+            if (r == AP_OK && cudaEventRecord(b->join[i], h->stream) != cudaSuccess) r = AP_ERR_CUDA;
+            if (r == AP_OK && cudaStreamWaitEvent(b->main, b->join[i], 0) != cudaSuccess) r = AP_ERR_CUDA;
+        }
+    }
+    const cudaError_t e = cudaStreamEndCapture(b->main, &gr);
     if (r != AP_OK || e != cudaSuccess) {
         if (gr) cudaGraphDestroy(gr);
         return r != AP_OK ? r : AP_ERR_CUDA;
     }
-    e = cudaGraphInstantiate(&b->graph, gr, cudaGraphInstantiateFlagUseNodePriority);
+    const cudaError_t ei = cudaGraphInstantiate(&b->graph, gr, cudaGraphInstantiateFlagUseNodePriority);
     cudaGraphDestroy(gr);
-    return e == cudaSuccess ? AP_OK : AP_ERR_CUDA;
+    return ei == cudaSuccess ? AP_OK : AP_ERR_CUDA;
+}
+
+// Synchronises the batch stream; AP_ERR_TIMEOUT once a persistent wait gave up.
+int batch_sync(ap_batch *b) {
+    CK(cudaStreamSynchronize(b->main));
+    if (b->d_status) {
+        unsigned int st = 0;
+        CK(cudaMemcpy(&st, b->d_status, sizeof(st), cudaMemcpyDeviceToHost));
+        if (st) return AP_ERR_TIMEOUT;
+    }
+    return AP_OK;
+}
+
+// Tile autotuner of the persistent field launch: every active instance's
+// four contractions with 32 x 32 and with 64 x 64 tiles (instances whose
+// grid is not a multiple of 64 keep 32), 2 warm and 5 timed launches each on
+// the instances' own scratch; the faster is kept.  The tile does not change
+// the results (each output sums its products in the same order).
+int batch_tune_field(ap_batch *b) {
+    if (b->form != AP_BATCH_PERSISTENT) return AP_OK;
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    int r = AP_OK;
+    const int cand[2] = {32, 64};
+    for (int v = 0; v < 2 && r == AP_OK; ++v) {
+        b->plan.field_bm = cand[v];
+        r = plan_build(b, b->plan);
+        if (r != AP_OK) break;
+        const int nf = b->plan.n_rec[PS_FIELD];
+        for (int t = 0; t < 7 && r == AP_OK; ++t) {
+            if (t == 2 && cudaEventRecord(e0, b->main) != cudaSuccess) r = AP_ERR_CUDA;
+            // zero the field counters the way the launch before it would
+            if (cudaMemsetAsync(b->plan.d_cnt + 5, 0, sizeof(unsigned int) * (1 + nf), b->main) != cudaSuccess)
+                r = AP_ERR_CUDA;
+            launch_persist_field(plan_queue(b, PS_FIELD, 3, 0),
+                                 static_cast<const FieldRec *>(b->plan.d_recs[PS_FIELD]), b->main);
+        }
+        if (r == AP_OK && (cudaEventRecord(e1, b->main) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess))
+            r = AP_ERR_CUDA;
+        float ms = 0.f;
+        if (r == AP_OK) cudaEventElapsedTime(&ms, e0, e1);
+        b->tune_ms[v] = ms / 5.f;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (r == AP_OK) r = batch_sync(b);
+    b->tuned_bm = b->tune_ms[0] <= b->tune_ms[1] ? 32 : 64;
+    b->plan.field_bm = b->tuned_bm;
+    return r;
 }
 
 }  // namespace
@@ -1809,18 +2044,29 @@ int ap_create_batch(int32_t n, const ap_netlist *netlists, const ap_params *para
         if (r == AP_OK) b->inst.push_back(h);
     }
     if (r == AP_OK && (cudaStreamCreateWithFlags(&b->main, cudaStreamNonBlocking) != cudaSuccess ||
-                       cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) != cudaSuccess))
+                       cudaStreamCreateWithFlags(&b->wa_stream, cudaStreamNonBlocking) != cudaSuccess ||
+                       cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) != cudaSuccess ||
+                       cudaEventCreateWithFlags(&b->wa_fork, cudaEventDisableTiming) != cudaSuccess ||
+                       cudaEventCreateWithFlags(&b->wa_join, cudaEventDisableTiming) != cudaSuccess ||
+                       dalloc(&b->d_status, 1) != cudaSuccess ||
+                       cudaMemset(b->d_status, 0, sizeof(unsigned int)) != cudaSuccess))
         r = AP_ERR_CUDA;
     for (int i = 0; i < n && r == AP_OK; ++i) {
         cudaEvent_t ev;
         if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) r = AP_ERR_CUDA;
         else b->join.push_back(ev);
     }
+    b->active.assign((size_t)n, 1);
+    // the persistent form where it serves every instance, its field tile
+    // chosen by the batch autotuner
+    if (r == AP_OK && persist_supported(b)) {
+        b->form = AP_BATCH_PERSISTENT;
+        r = batch_tune_field(b);
+    }
     if (r != AP_OK) {
         ap_batch_destroy(b);
         return r;
     }
-    b->active.assign((size_t)n, 1);
     *out = b;
     return AP_OK;
 }
@@ -1828,21 +2074,70 @@ int ap_create_batch(int32_t n, const ap_netlist *netlists, const ap_params *para
 int ap_batch_destroy(ap_batch *b) {
     if (!b) return AP_ERR_INVALID_ARG;
     if (b->main) cudaStreamSynchronize(b->main);
+    if (b->wa_stream) cudaStreamSynchronize(b->wa_stream);
     batch_free_graph(b);
+    plan_free(b->plan);
     for (ap_handle *h : b->inst) ap_destroy(h);
     for (cudaEvent_t e : b->join) cudaEventDestroy(e);
     if (b->fork) cudaEventDestroy(b->fork);
+    if (b->wa_fork) cudaEventDestroy(b->wa_fork);
+    if (b->wa_join) cudaEventDestroy(b->wa_join);
+    if (b->d_status) cudaFree(b->d_status);
+    if (b->wa_stream) cudaStreamDestroy(b->wa_stream);
     if (b->main) cudaStreamDestroy(b->main);
     delete b;
     return AP_OK;
 }
 
+int ap_batch_set_form(ap_batch *b, int32_t form) {
+    if (!b || (form != AP_BATCH_GRAPH && form != AP_BATCH_PERSISTENT)) return AP_ERR_INVALID_ARG;
+    if (form == AP_BATCH_PERSISTENT && !persist_supported(b)) return AP_ERR_UNSUPPORTED;
+    CK(cudaStreamSynchronize(b->main));
+    const bool rebuild = b->graph != nullptr;
+    b->form = form;
+    if (form == AP_BATCH_PERSISTENT && !b->tuned_bm) {
+        const int r = batch_tune_field(b);
+        if (r != AP_OK) return r;
+    }
+    return rebuild ? batch_build_graph(b) : AP_OK;
+}
+
+int ap_batch_get_info(ap_batch *b, ap_batch_info *info) {
+    if (!b || !info) return AP_ERR_INVALID_ARG;
+    memset(info, 0, sizeof(*info));
+    info->form = b->form;
+    info->instances = (int32_t)b->inst.size();
+    int act = 0;
+    for (char a : b->active) act += a ? 1 : 0;
+    info->active = act;
+    info->field_tile = b->tuned_bm;
+    info->field_tune_ms[0] = b->tune_ms[0];
+    info->field_tune_ms[1] = b->tune_ms[1];
+    for (int k = 0; k < 6; ++k) info->records[k] = b->plan.n_rec[k];
+    return AP_OK;
+}
+
+int ap_batch_debug_inject(ap_batch *b, int32_t kind, int64_t wait_ns) {
+    if (!b) return AP_ERR_INVALID_ARG;
+    if (kind != AP_FAULT_NONE && kind != AP_FAULT_NEVER_ARRIVE) return AP_ERR_INVALID_ARG;
+    if (kind == AP_FAULT_NEVER_ARRIVE && (wait_ns < 1000000 || wait_ns > 2000000000)) return AP_ERR_INVALID_ARG;
+    if (kind == AP_FAULT_NEVER_ARRIVE && b->form != AP_BATCH_PERSISTENT) return AP_ERR_UNSUPPORTED;
+    CK(cudaStreamSynchronize(b->main));
+    b->never_arrive = kind == AP_FAULT_NEVER_ARRIVE;
+    b->wait_ns = kind == AP_FAULT_NEVER_ARRIVE ? (unsigned long long)wait_ns : 1000000000ull;
+    if (kind == AP_FAULT_NONE) CK(cudaMemset(b->d_status, 0, sizeof(unsigned int)));
+    return b->graph ? batch_build_graph(b) : AP_OK;
+}
+
 int ap_batch_init_seeded(ap_batch *b, uint64_t seed, float sigma) {
     if (!b) return AP_ERR_INVALID_ARG;
+    CK(cudaStreamSynchronize(b->main));
     for (size_t i = 0; i < b->inst.size(); ++i) {
         int r = ap_init_seeded(b->inst[i], seed + i, sigma);
         if (r != AP_OK) return r;
     }
+    CK(cudaDeviceSynchronize());  // the instances' streams before the batch stream's first launch
+    CK(cudaMemset(b->d_status, 0, sizeof(unsigned int)));
     b->active.assign(b->inst.size(), 1);
     return batch_build_graph(b);
 }
@@ -1851,8 +2146,7 @@ int ap_batch_step(ap_batch *b, int32_t n_trials) {
     if (!b || n_trials < 0) return AP_ERR_INVALID_ARG;
     if (!b->graph) return AP_ERR_STATE;
     for (int t = 0; t < n_trials; ++t) CK(cudaGraphLaunch(b->graph, b->main));
-    CK(cudaStreamSynchronize(b->main));
-    return AP_OK;
+    return batch_sync(b);
 }
 
 int ap_batch_run(ap_batch *b, int32_t *iterations) {
@@ -1863,7 +2157,8 @@ int ap_batch_run(ap_batch *b, int32_t *iterations) {
         for (size_t i = 0; i < b->inst.size(); ++i)
             if (b->active[i]) interval = std::max(interval, b->inst[i]->p.check_interval);
         for (int t = 0; t < interval; ++t) CK(cudaGraphLaunch(b->graph, b->main));
-        CK(cudaStreamSynchronize(b->main));
+        const int sr = batch_sync(b);
+        if (sr != AP_OK) return sr;
         bool changed = false, any = false;
         for (size_t i = 0; i < b->inst.size(); ++i) {
             if (!b->active[i]) continue;

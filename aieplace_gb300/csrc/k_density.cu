@@ -16,6 +16,7 @@
 
 #include "ap_common.cuh"
 #include "ap_kernels.h"
+#include "ap_persist.cuh"
 
 namespace ap {
 
@@ -53,18 +54,25 @@ __device__ __forceinline__ double block_max_f(float v, double *smem) {
 //      there;
 //   2. accumulates every node whose bins all lie inside the tile into int64
 //      registers as the outer product ow x oh (kTile^2 multiply-adds, no
-//      atomics, no lane matching; a warp runs this only when one of its
-//      lanes has such a node);
+//      atomics, no lane matching); a warp runs this only when at least
+//      kTileMinLanes of its lanes have such a node, since the multiply-adds
+//      cost the same for 1 lane as for 32;
 //   3. adds the bins of every other node inside a kWin x kWin bin window
 //      about the same mean bin to the window in shared memory
-//      (red.shared.add: the nodes just outside the dense core), and the rest
-//      straight to the map (red.global.add);
+//      (red.shared.add: the nodes just outside the dense core, and the tile's
+//      nodes of a warp that skipped step 2), and the rest straight to the
+//      map (red.global.add).  The window is held in kWinCopies copies, lane
+//      l adding to copy l % kWinCopies, so that lanes whose nodes share a bin
+//      collide on one shared address less often;
 //   4. sums the tile over the block (shuffles, then shared memory) and adds
-//      its kTile^2 bins to the map once, and the window's non-zero bins.
+//      its kTile^2 bins to the map once, and the window's non-zero bins
+//      (the copies summed).
 // All sums are integers, so the map is the same bit for bit whatever the
 // path or the order (and equal to or_density_q).
 constexpr int kTile = 6;
-constexpr int kWin = 64;
+constexpr int kTileMinLanes = 16;
+constexpr int kWin = 32;
+constexpr int kWinCopies = 4;
 constexpr int kScatterThreads = 256;
 
 // A node's contribution as a record of 5 int32: the base bin (c0, r0), the
@@ -166,7 +174,7 @@ __device__ __forceinline__ void for_each_overlap(const Grid &g, float x, float y
 // streaming pass; block sums of |u' - u|^2 folded by the last block.  Split
 // from the bin adds, which need few threads per SM's worth of registers and
 // shared memory, so that this part runs at full occupancy.
-__global__ void __launch_bounds__(kThreads) update_kernel(ScatterArgs a) {
+__device__ __forceinline__ void update_body(const ScatterArgs &a, VBlock vb) {
     __shared__ double red[32];  // 64 floats: two block sums
     const float alpha = a.sc->f_alpha, mom = a.sc->f_mom;
     const int cur = a.sc->cur, nxt = 1 - cur;
@@ -184,7 +192,7 @@ __global__ void __launch_bounds__(kThreads) update_kernel(ScatterArgs a) {
     int *__restrict__ rbin = a.rec_bin;
     int4 *__restrict__ rov = a.rec_ov;
     const int lo = a.upd_hi > 0 ? a.upd_lo : 0, hi = a.upd_hi > 0 ? a.upd_hi : a.n_mov;
-    for (int i = lo + blockIdx.x * blockDim.x + threadIdx.x; i < hi; i += gridDim.x * blockDim.x) {
+    for (int i = lo + vb.id * blockDim.x + threadIdx.x; i < hi; i += vb.n * blockDim.x) {
         const float w = __ldg(a.w + i), h = __ldg(a.h + i);
         const float xhi = fmaxf(a.die_w - w, 0.f), yhi = fmaxf(a.die_h - h, 0.f);
         const float ux = uxc[i], uy = uyc[i];
@@ -201,6 +209,7 @@ __global__ void __launch_bounds__(kThreads) update_kernel(ScatterArgs a) {
             a.trial_x[i] = x;
             a.trial_y[i] = y;
         }
+        if (a.xy_out) a.xy_out[i] = make_float2(x, y);
         du += (nux - ux) * (nux - ux) + (nuy - uy) * (nuy - uy);
         dv += (x - vx) * (x - vx) + (y - vy) * (y - vy);
         int c0, c1, r0, r1;
@@ -212,33 +221,41 @@ __global__ void __launch_bounds__(kThreads) update_kernel(ScatterArgs a) {
     float bs[2] = {du, dv};
     block_sums_ff<2>(bs, reinterpret_cast<float *>(red));
     if (threadIdx.x == 0) {
-        pf[2 * (a.part_base + blockIdx.x)] = bs[0];
-        pf[2 * (a.part_base + blockIdx.x) + 1] = bs[1];
-    }
-    if (a.no_fold) return;  // uniform: an earlier chunk of a chunked update
-    if (arrive_last(a.counter)) {
-        // the partials of this launch and of the chunks before it (launched
-        // earlier on the same stream, so complete)
-        const int nb = a.part_base + (int)gridDim.x;
-        const double t = block_sum_f(kahan_strided(pf, threadIdx.x, nb, blockDim.x, 2), red);
-        const double t2 = block_sum_f(kahan_strided(pf + 1, threadIdx.x, nb, blockDim.x, 2), red);
-        if (threadIdx.x == 0) {
-            a.sc->t_du = t;
-            a.sc->t_dv2 = t2;
-            *a.counter = 0u;
-        }
+        pf[2 * (a.part_base + vb.id)] = bs[0];
+        pf[2 * (a.part_base + vb.id) + 1] = bs[1];
     }
 }
 
-__global__ void __launch_bounds__(kScatterThreads, 2) scatter_kernel(ScatterArgs a) {
+// The step sums of partials [0, nb) into the device scalars (one block).
+__device__ __forceinline__ void update_fold(const ScatterArgs &a, int nb) {
+    __shared__ double red[32];
+    const float *pf = reinterpret_cast<const float *>(a.partials);
+    const double t = block_sum_f(kahan_strided(pf, threadIdx.x, nb, blockDim.x, 2), red);
+    const double t2 = block_sum_f(kahan_strided(pf + 1, threadIdx.x, nb, blockDim.x, 2), red);
+    if (threadIdx.x == 0) {
+        a.sc->t_du = t;
+        a.sc->t_dv2 = t2;
+        *a.counter = 0u;
+    }
+}
+
+__global__ void __launch_bounds__(kThreads) update_kernel(ScatterArgs a) {
+    update_body(a, grid_block());
+    if (a.no_fold) return;  // uniform: an earlier chunk of a chunked update
+    // the partials of this launch and of the chunks before it (launched
+    // earlier on the same stream, so complete)
+    if (arrive_last(a.counter, gridDim.x)) update_fold(a, a.part_base + (int)gridDim.x);
+}
+
+__device__ __forceinline__ void scatter_body(const ScatterArgs &a, VBlock vb) {
     __shared__ long long red[kScatterThreads / 32][kTile * kTile];
-    __shared__ ull win[kWin * kWin];
+    __shared__ ull win[kWinCopies * kWin * kWin];
     __shared__ long long sums[3];
     const int nxt = a.update ? 1 - a.sc->cur : 0;
     const Grid g = a.g;
     const int n = a.hi - a.lo;
-    const int per = (n + (int)gridDim.x - 1) / (int)gridDim.x;
-    const int r_lo = min(n, (int)blockIdx.x * per), r_hi = min(n, r_lo + per);
+    const int per = (n + vb.n - 1) / vb.n;
+    const int r_lo = min(n, vb.id * per), r_hi = min(n, r_lo + per);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     // 1. the mean base bin of the range (update mode: from the records;
     //    plain mode: from the positions)
@@ -280,9 +297,10 @@ __global__ void __launch_bounds__(kScatterThreads, 2) scatter_kernel(ScatterArgs
     // the window: kWin x kWin bins (or the whole grid, if smaller) about the mean
     const int wcn = min(kWin, g.mx), wrn = min(kWin, g.my);
     const int wc0 = min(max(mc - wcn / 2, 0), g.mx - wcn), wr0 = min(max(mr - wrn / 2, 0), g.my - wrn);
-    for (int t = tid; t < wcn * wrn; t += kScatterThreads) win[t] = 0ull;
+    const int wsz = wcn * wrn;
+    for (int t = tid; t < kWinCopies * wsz; t += kScatterThreads) win[t] = 0ull;
     __syncthreads();
-    const unsigned win_s = (unsigned)__cvta_generic_to_shared(win);
+    const unsigned win_s = (unsigned)__cvta_generic_to_shared(win) + 8u * (unsigned)((lane % kWinCopies) * wsz);
 
     // 2.-3. the range's nodes
     long long acc[kTile][kTile];
@@ -346,6 +364,7 @@ __global__ void __launch_bounds__(kScatterThreads, 2) scatter_kernel(ScatterArgs
             }
             fits = qc0 >= 0 && qr0 >= 0 && qc0 + qnc <= kTile && qr0 + qnr <= kTile;
         }
+        if (__popc(__ballot_sync(0xffffffffu, fits)) < kTileMinLanes) fits = false;  // warp-uniform test
         if (__any_sync(0xffffffffu, fits)) {
             // this node's column and row overlaps over the tile (zero outside
             // its bins, and for lanes whose node does not fit)
@@ -387,8 +406,10 @@ __global__ void __launch_bounds__(kScatterThreads, 2) scatter_kernel(ScatterArgs
     }
     // 4. the window's non-zero bins, then the tile summed over the block
     if (__syncthreads_or(had_win)) {  // uniform
-        for (int t = tid; t < wcn * wrn; t += kScatterThreads) {
-            const ull v = win[t];
+        for (int t = tid; t < wsz; t += kScatterThreads) {
+            ull v = 0;
+#pragma unroll
+            for (int k = 0; k < kWinCopies; ++k) v += win[k * wsz + t];
             if (v) add_glb(wc0 + t / wrn, wr0 + t % wrn, (long long)v);
         }
     }
@@ -409,44 +430,55 @@ __global__ void __launch_bounds__(kScatterThreads, 2) scatter_kernel(ScatterArgs
     }
 }
 
-int launch_update(const ScatterArgs &a, cudaStream_t st) {
-    if (!a.update || a.n_mov <= 0) return 0;
+__global__ void __launch_bounds__(kScatterThreads, 2) scatter_kernel(ScatterArgs a) { scatter_body(a, grid_block()); }
+
+// Resident blocks of `kernel` on the whole GPU (one wave), or `fallback`.
+int wave_of(const void *kernel, int threads, int fallback) {
+    int dev = 0, sms = 0, per_sm = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess &&
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess &&
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, 0) == cudaSuccess &&
+        sms * per_sm > 0)
+        return sms * per_sm;
+    return fallback;
+}
+
+int update_grid(const ScatterArgs &a) {
     // one wave of resident blocks (at most 8192, the partials buffer),
     // grid-stride beyond: fewer block sums and last-block folds
     static int wave = 0;
     if (wave <= 0) {
-        int dev = 0, sms = 0, per_sm = 0;
-        if (cudaGetDevice(&dev) == cudaSuccess &&
-            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess &&
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, update_kernel, kThreads, 0) == cudaSuccess)
-            wave = sms * per_sm;
-        if (wave <= 0 || wave > 8192) wave = 1216;
+        wave = wave_of((const void *)update_kernel, kThreads, 1216);
+        if (wave > 8192) wave = 1216;
     }
     const int n = a.upd_hi > 0 ? a.upd_hi - a.upd_lo : a.n_mov;
     int ub = (n + kThreads - 1) / kThreads;
     if (ub > wave) ub = wave;
     if (ub < 1) ub = 1;  // an empty chunk still writes its partials (zero) and may fold
+    return ub;
+}
+
+int launch_update(const ScatterArgs &a, cudaStream_t st) {
+    if (!a.update || a.n_mov <= 0) return 0;
+    const int ub = update_grid(a);
     update_kernel<<<ub, kThreads, 0, st>>>(a);
     return ub;
+}
+
+int scatter_grid(int n) {
+    // one wave of resident blocks, each a contiguous range of nodes (fewer
+    // blocks: fewer tile flushes onto the dense core's bins)
+    static int wave = 0;
+    if (wave <= 0) wave = wave_of((const void *)scatter_kernel, kScatterThreads, 304);
+    int blocks = (n + kScatterThreads - 1) / kScatterThreads;
+    if (blocks > wave) blocks = wave;
+    return blocks < 1 ? 1 : blocks;
 }
 
 void launch_scatter_bins(const ScatterArgs &a, cudaStream_t st) {
     const int n = a.hi - a.lo;
     if (n <= 0) return;
-    // one wave of resident blocks, each a contiguous range of nodes (fewer
-    // blocks: fewer tile flushes onto the dense core's bins)
-    static int wave = 0;
-    if (wave <= 0) {
-        int dev = 0, sms = 0, per_sm = 0;
-        if (cudaGetDevice(&dev) == cudaSuccess &&
-            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess &&
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, scatter_kernel, kScatterThreads, 0) == cudaSuccess)
-            wave = sms * per_sm;
-        if (wave <= 0) wave = 304;
-    }
-    int blocks = (n + kScatterThreads - 1) / kScatterThreads;
-    if (blocks > wave) blocks = wave;
-    scatter_kernel<<<blocks, kScatterThreads, 0, st>>>(a);
+    scatter_kernel<<<scatter_grid(n), kScatterThreads, 0, st>>>(a);
 }
 
 void launch_scatter(const ScatterArgs &a, cudaStream_t st) {
@@ -464,7 +496,7 @@ __device__ __forceinline__ double gamma_of(const DevScalars *sc, double tau) {
 
 constexpr int kRhoBatch = 4;
 
-__global__ void __launch_bounds__(kThreads) rho_kernel(RhoArgs a) {
+__device__ __forceinline__ void rho_body(const RhoArgs &a, VBlock vb) {
     __shared__ long long red[32];
     long long over = 0, over_abs = 0;
     // two bins per 16-byte load of the int64 maps; kRhoBatch such pairs per
@@ -475,8 +507,8 @@ __global__ void __launch_bounds__(kThreads) rho_kernel(RhoArgs a) {
     const longlong2 *__restrict__ fs2 = reinterpret_cast<const longlong2 *>(a.fixs_q);
     const longlong2 *__restrict__ fx2 = reinterpret_cast<const longlong2 *>(a.fix_q);
     longlong2 *fl2 = reinterpret_cast<longlong2 *>(a.fill_q);  // filler cells, or null
-    const int stride = gridDim.x * blockDim.x;
-    for (int p0 = blockIdx.x * blockDim.x + threadIdx.x; p0 < npairs; p0 += kRhoBatch * stride) {
+    const int stride = vb.n * blockDim.x;
+    for (int p0 = vb.id * blockDim.x + threadIdx.x; p0 < npairs; p0 += kRhoBatch * stride) {
         longlong2 mv[kRhoBatch], fs[kRhoBatch], fx[kRhoBatch], fl[kRhoBatch];
 #pragma unroll
         for (int j = 0; j < kRhoBatch; ++j) {
@@ -519,75 +551,78 @@ __global__ void __launch_bounds__(kThreads) rho_kernel(RhoArgs a) {
     over = block_sum(over, red);
     over_abs = block_sum(over_abs, red);
     if (threadIdx.x == 0) {
-        a.partials[2 * blockIdx.x] = over;
-        a.partials[2 * blockIdx.x + 1] = over_abs;
-    }
-    if (arrive_last(a.counter)) {
-        long long o = 0, oa = 0;
-        for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) {
-            o += __ldcg(a.partials + 2 * i);
-            oa += __ldcg(a.partials + 2 * i + 1);
-        }
-        o = block_sum(o, red);
-        oa = block_sum(oa, red);
-        if (threadIdx.x == 0) {
-            DevScalars *sc = a.sc;
-            const double tau = sc->mov_area_q > 0 ? (double)o / sc->mov_area_q : 0.0;
-            const double tau_abs = (double)oa * 0x1p-32;  // exact power-of-two scaling
-            if (a.out) {
-                a.out[0] = tau;
-                a.out[1] = tau_abs;
-            }
-            if (a.mode == RHO_INIT) {
-                sc->tau = tau;
-                sc->tau_abs = tau_abs;
-            }
-            if (a.mode != RHO_OUT_ONLY) {
-                sc->t_tau = tau;
-                sc->t_tau_abs = tau_abs;
-                sc->gamma_next = gamma_of(sc, tau);
-            }
-            if (a.mode == RHO_INIT) {
-                // the first evaluation's WA uses its own overflow
-                sc->gamma = sc->gamma_next;
-                sc->f_gamma = (float)sc->gamma;
-            }
-            // field source of this trial: the surrogate while the overflow is
-            // above its threshold and its last judgement passed, the exact
-            // solve judging it every surr_judge_every trials
-            int fm = kFieldExact;
-            if (a.mode == RHO_LOOP && sc->surr_attached && tau > (double)sc->surr_tau_min) {
-                if (sc->evals % sc->surr_judge_every == 0)
-                    fm = kFieldJudge;
-                else if (sc->surr_ok)
-                    fm = kFieldSurr;
-            }
-            sc->field_mode = fm;
-            if (a.field_switch) cudaGraphSetConditional(a.field_switch, (unsigned int)fm);
-            if (fm == kFieldSurr) sc->surr_used += 1;
-            *a.counter = 0u;
-        }
+        a.partials[2 * vb.id] = over;
+        a.partials[2 * vb.id + 1] = over_abs;
     }
 }
 
-void launch_rho(const RhoArgs &a, cudaStream_t st) {
+// The overflow sums of partials [0, nb) into the device scalars, gamma of the
+// next evaluation and the trial's field source (one block).
+__device__ __forceinline__ void rho_fold(const RhoArgs &a, int nb) {
+    __shared__ long long red[32];
+    long long o = 0, oa = 0;
+    for (int i = threadIdx.x; i < nb; i += blockDim.x) {
+        o += __ldcg(a.partials + 2 * i);
+        oa += __ldcg(a.partials + 2 * i + 1);
+    }
+    o = block_sum(o, red);
+    oa = block_sum(oa, red);
+    if (threadIdx.x == 0) {
+        DevScalars *sc = a.sc;
+        const double tau = sc->mov_area_q > 0 ? (double)o / sc->mov_area_q : 0.0;
+        const double tau_abs = (double)oa * 0x1p-32;  // exact power-of-two scaling
+        if (a.out) {
+            a.out[0] = tau;
+            a.out[1] = tau_abs;
+        }
+        if (a.mode == RHO_INIT) {
+            sc->tau = tau;
+            sc->tau_abs = tau_abs;
+        }
+        if (a.mode != RHO_OUT_ONLY) {
+            sc->t_tau = tau;
+            sc->t_tau_abs = tau_abs;
+            sc->gamma_next = gamma_of(sc, tau);
+        }
+        if (a.mode == RHO_INIT) {
+            // the first evaluation's WA uses its own overflow
+            sc->gamma = sc->gamma_next;
+            sc->f_gamma = (float)sc->gamma;
+        }
+        // field source of this trial: the surrogate while the overflow is
+        // above its threshold and its last judgement passed, the exact
+        // solve judging it every surr_judge_every trials
+        int fm = kFieldExact;
+        if (a.mode == RHO_LOOP && sc->surr_attached && tau > (double)sc->surr_tau_min) {
+            if (sc->evals % sc->surr_judge_every == 0)
+                fm = kFieldJudge;
+            else if (sc->surr_ok)
+                fm = kFieldSurr;
+        }
+        sc->field_mode = fm;
+        if (a.field_switch) cudaGraphSetConditional(a.field_switch, (unsigned int)fm);
+        if (fm == kFieldSurr) sc->surr_used += 1;
+        *a.counter = 0u;
+    }
+}
+
+__global__ void __launch_bounds__(kThreads) rho_kernel(RhoArgs a) {
+    rho_body(a, grid_block());
+    if (arrive_last(a.counter, gridDim.x)) rho_fold(a, gridDim.x);
+}
+
+int rho_grid(int nbins) {
     // about one round of kRhoBatch pairs per thread, but no more blocks than
     // fit the GPU at once: a partial second wave nearly doubled the time
     // (512 blocks against 456 resident at 1024^2 bins: 19.0 -> 16.9 us)
     static int wave = 0;
-    if (wave <= 0) {
-        int dev = 0, sms = 0, per_sm = 0;
-        if (cudaGetDevice(&dev) == cudaSuccess &&
-            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess &&
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, rho_kernel, kThreads, 0) == cudaSuccess)
-            wave = sms * per_sm;
-        if (wave <= 0) wave = 1216;
-    }
-    int blocks = (a.nbins / 2 + kRhoBatch * kThreads - 1) / (kRhoBatch * kThreads);
+    if (wave <= 0) wave = wave_of((const void *)rho_kernel, kThreads, 1216);
+    int blocks = (nbins / 2 + kRhoBatch * kThreads - 1) / (kRhoBatch * kThreads);
     if (blocks > wave) blocks = wave;
-    if (blocks < 1) blocks = 1;
-    rho_kernel<<<blocks, kThreads, 0, st>>>(a);
+    return blocks < 1 ? 1 : blocks;
 }
+
+void launch_rho(const RhoArgs &a, cudaStream_t st) { rho_kernel<<<rho_grid(a.nbins), kThreads, 0, st>>>(a); }
 
 // The trajectory record of the trial just decided (trial number sc->evals - 1).
 __device__ void log_trial(DevScalars *sc, int accepted) {
@@ -664,7 +699,7 @@ __device__ void finish_trial(DevScalars *sc, double dv2, double dg2) {
     log_trial(sc, 1);
 }
 
-__global__ void __launch_bounds__(kThreads, 4) gather_kernel(GatherArgs a) {
+__device__ __forceinline__ void gather_body(const GatherArgs &a, VBlock vb) {
     __shared__ double red[64];  // 128 floats: four block sums
     const Grid g = a.g;
     const float lam = a.mode == GATHER_NODE_OUT ? a.lambda : a.sc->f_lambda;
@@ -676,7 +711,7 @@ __global__ void __launch_bounds__(kThreads, 4) gather_kernel(GatherArgs a) {
     // the block sums on -- the FP64 pipe of this part is narrow
     float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
     const bool use_rec = (a.mode == GATHER_STEP || a.mode == GATHER_NODE_OUT) && a.rec_bin != nullptr;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n_mov; i += gridDim.x * blockDim.x) {
+    for (int i = vb.id * blockDim.x + threadIdx.x; i < a.n_mov; i += vb.n * blockDim.x) {
         float fx = 0.f, fy = 0.f;
         int c0, c1, r0, r1;
         bool small;
@@ -803,72 +838,82 @@ __global__ void __launch_bounds__(kThreads, 4) gather_kernel(GatherArgs a) {
         block_sums_ff<4>(bs, reinterpret_cast<float *>(red));
     float *pf = reinterpret_cast<float *>(a.partials);
     if (threadIdx.x == 0) {
-        float *p = pf + 4 * blockIdx.x;
+        float *p = pf + 4 * vb.id;
         p[0] = bs[0];
         p[1] = bs[1];
         p[2] = bs[2];
         p[3] = bs[3];
     }
-    if (arrive_last(a.counter)) {
-        const int nb = (int)gridDim.x;
-        const double t0 = a.mode == GATHER_STEP
-                              ? 0.0
-                              : block_sum_f(kahan_strided(pf + 0, threadIdx.x, nb, blockDim.x, 4), red);
-        const double t1 = block_sum_f(kahan_strided(pf + 1, threadIdx.x, nb, blockDim.x, 4), red);
-        double t2;
-        if (is_max) {
-            float m = 0.f;
-            for (int k = threadIdx.x; k < nb; k += blockDim.x) m = fmaxf(m, __ldcg(pf + 4 * k + 2));
-            t2 = block_max_f(m, red);
+}
+
+// The sums of partials [0, nb) into the device scalars; in a loop trial the
+// accept / retry decision (one block).
+__device__ __forceinline__ void gather_fold(const GatherArgs &a, int nb) {
+    __shared__ double red[64];
+    const bool is_max = a.mode == GATHER_INIT_GRAD;
+    const float *pf = reinterpret_cast<const float *>(a.partials);
+    const double t0 = a.mode == GATHER_STEP
+                          ? 0.0
+                          : block_sum_f(kahan_strided(pf + 0, threadIdx.x, nb, blockDim.x, 4), red);
+    const double t1 = block_sum_f(kahan_strided(pf + 1, threadIdx.x, nb, blockDim.x, 4), red);
+    double t2;
+    if (is_max) {
+        float m = 0.f;
+        for (int k = threadIdx.x; k < nb; k += blockDim.x) m = fmaxf(m, __ldcg(pf + 4 * k + 2));
+        t2 = block_max_f(m, red);
+    } else {
+        t2 = block_sum_f(kahan_strided(pf + 2, threadIdx.x, nb, blockDim.x, 4), red);
+    }
+    const double t3 = block_sum_f(kahan_strided(pf + 3, threadIdx.x, nb, blockDim.x, 4), red);
+    if (threadIdx.x == 0) {
+        DevScalars *sc = a.sc;
+        if (a.mode == GATHER_INIT_NORMS) {
+            sc->sum_gwl = t2;
+            sc->sum_f = t3;
+            sc->lambda = t3 > 0.0 ? sc->init_density_weight * t2 / t3 : sc->init_density_weight;
+        } else if (a.mode == GATHER_INIT_GRAD) {
+            sc->gmax = t2;
+        } else if (a.mode == GATHER_INIT_PREV) {
+            // first predicted step from v_0 and the probe point v_{-1}
+            sc->sum_dv2 = t0;
+            sc->sum_dg2 = t1;
+            sc->alpha = t1 > 0.0 ? sqrt(t0) / sqrt(t1) : 0.0;
+            sc->a_k = 1.0;
+            sc->a_next = (1.0 + sqrt(5.0)) / 2.0;
+            sc->mom = 0.0;
+            if (!isfinite(sc->alpha)) sc->status = 9;
         } else {
-            t2 = block_sum_f(kahan_strided(pf + 2, threadIdx.x, nb, blockDim.x, 4), red);
+            // the next evaluation's WA smoothing: this trial's gamma(tau),
+            // whether the trial is accepted or not
+            sc->gamma = sc->gamma_next;
+            finish_trial(sc, sc->t_dv2, t1);
         }
-        const double t3 = block_sum_f(kahan_strided(pf + 3, threadIdx.x, nb, blockDim.x, 4), red);
-        if (threadIdx.x == 0) {
-            DevScalars *sc = a.sc;
-            if (a.mode == GATHER_INIT_NORMS) {
-                sc->sum_gwl = t2;
-                sc->sum_f = t3;
-                sc->lambda = t3 > 0.0 ? sc->init_density_weight * t2 / t3 : sc->init_density_weight;
-            } else if (a.mode == GATHER_INIT_GRAD) {
-                sc->gmax = t2;
-            } else if (a.mode == GATHER_INIT_PREV) {
-                // first predicted step from v_0 and the probe point v_{-1}
-                sc->sum_dv2 = t0;
-                sc->sum_dg2 = t1;
-                sc->alpha = t1 > 0.0 ? sqrt(t0) / sqrt(t1) : 0.0;
-                sc->a_k = 1.0;
-                sc->a_next = (1.0 + sqrt(5.0)) / 2.0;
-                sc->mom = 0.0;
-                if (!isfinite(sc->alpha)) sc->status = 9;
-            } else {
-                // the next evaluation's WA smoothing: this trial's gamma(tau),
-                // whether the trial is accepted or not
-                sc->gamma = sc->gamma_next;
-                finish_trial(sc, sc->t_dv2, t1);
-            }
-            publish_f32(sc);
-            *a.counter = 0u;
-        }
+        publish_f32(sc);
+        *a.counter = 0u;
     }
 }
 
-void launch_gather(const GatherArgs &a, cudaStream_t st) {
+__global__ void __launch_bounds__(kThreads, 4) gather_kernel(GatherArgs a) {
+    gather_body(a, grid_block());
+    if (a.mode == GATHER_FORCE_ONLY || a.mode == GATHER_NODE_OUT) return;
+    if (arrive_last(a.counter, gridDim.x)) gather_fold(a, gridDim.x);
+}
+
+int gather_grid(int n_mov) {
     // one wave of resident blocks, grid-stride beyond: 61 -> 50 us at 2M
     // nodes against 4096 blocks (a partial last wave, 912 blocks, 59 us)
     static int wave = 0;
     if (wave <= 0) {
-        int dev = 0, sms = 0, per_sm = 0;
-        if (cudaGetDevice(&dev) == cudaSuccess &&
-            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess &&
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gather_kernel, kThreads, 0) == cudaSuccess)
-            wave = sms * per_sm;
-        if (wave <= 0 || wave > kGatherMaxBlocks) wave = 608;
+        wave = wave_of((const void *)gather_kernel, kThreads, 608);
+        if (wave > kGatherMaxBlocks) wave = 608;
     }
-    int blocks = (a.n_mov + kThreads - 1) / kThreads;
+    int blocks = (n_mov + kThreads - 1) / kThreads;
     if (blocks > wave) blocks = wave;
-    if (blocks < 1) blocks = 1;
-    gather_kernel<<<blocks, kThreads, 0, st>>>(a);
+    return blocks < 1 ? 1 : blocks;
+}
+
+void launch_gather(const GatherArgs &a, cudaStream_t st) {
+    gather_kernel<<<gather_grid(a.n_mov), kThreads, 0, st>>>(a);
 }
 
 // Bin records of movable nodes at given positions, as update_kernel writes
@@ -947,6 +992,60 @@ __global__ void numerics_selftest_kernel(long long n, ull seed, int *mism) {
         const float t = __uint_as_float((lo & 0x007FFFFFu) | ((127u + (hi >> 12) % 23u) << 23));
         const float u = (hi & 0x800u) ? t : __fmul_rn(t, 1.0f / 4194304.0f) - 1.0f;
         if (u > -1.0f && f2i_rz_small(u) != __float2int_rz(u)) atomicAdd(mism + 5, 1);
+    }
+}
+
+// ---- persistent launches of the batched form ------------------------------
+// Each record is one instance's launch of the stage (its arguments and its
+// grid as the launchers above would size it); the per-instance sums fold in
+// the record's last block, as in the instance's own launch.
+
+__global__ void __launch_bounds__(kThreads) persist_update_kernel(PersistQueue q, const ScatterArgs *recs) {
+    persist_loop(q, recs, [](const ScatterArgs &a, VBlock vb, int) {
+        update_body(a, vb);
+        if (arrive_last(a.counter, vb.n)) update_fold(a, vb.n);
+    });
+}
+
+__global__ void __launch_bounds__(kScatterThreads, 2) persist_scatter_kernel(PersistQueue q, const ScatterArgs *recs) {
+    persist_loop(q, recs, [](const ScatterArgs &a, VBlock vb, int) { scatter_body(a, vb); });
+}
+
+__global__ void __launch_bounds__(kThreads) persist_rho_kernel(PersistQueue q, const RhoArgs *recs) {
+    persist_loop(q, recs, [](const RhoArgs &a, VBlock vb, int) {
+        rho_body(a, vb);
+        if (arrive_last(a.counter, vb.n)) rho_fold(a, vb.n);
+    });
+}
+
+__global__ void __launch_bounds__(kThreads, 4) persist_gather_kernel(PersistQueue q, const GatherArgs *recs) {
+    persist_loop(q, recs, [](const GatherArgs &a, VBlock vb, int) {
+        gather_body(a, vb);
+        if (arrive_last(a.counter, vb.n)) gather_fold(a, vb.n);
+    });
+}
+
+void launch_persist_density(int stage, const PersistQueue &q, const void *recs, cudaStream_t st) {
+    static int waves[4] = {0, 0, 0, 0};
+    switch (stage) {
+    case PS_UPDATE:
+        if (!waves[0]) waves[0] = wave_of((const void *)persist_update_kernel, kThreads, 1216);
+        persist_update_kernel<<<waves[0], kThreads, 0, st>>>(q, static_cast<const ScatterArgs *>(recs));
+        break;
+    case PS_SCATTER:
+        if (!waves[1]) waves[1] = wave_of((const void *)persist_scatter_kernel, kScatterThreads, 304);
+        persist_scatter_kernel<<<waves[1], kScatterThreads, 0, st>>>(q, static_cast<const ScatterArgs *>(recs));
+        break;
+    case PS_RHO:
+        if (!waves[2]) waves[2] = wave_of((const void *)persist_rho_kernel, kThreads, 1216);
+        persist_rho_kernel<<<waves[2], kThreads, 0, st>>>(q, static_cast<const RhoArgs *>(recs));
+        break;
+    case PS_GATHER:
+        if (!waves[3]) waves[3] = wave_of((const void *)persist_gather_kernel, kThreads, 608);
+        persist_gather_kernel<<<waves[3], kThreads, 0, st>>>(q, static_cast<const GatherArgs *>(recs));
+        break;
+    default:
+        break;
     }
 }
 

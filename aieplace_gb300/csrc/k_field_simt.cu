@@ -54,17 +54,17 @@ __device__ __forceinline__ void spectral_store(const SpectralEpi &e, int m, int 
     e.py[(size_t)u * m + v] = py;
 }
 
-// D = A B^T on an m x m problem; BM x BM output tile per block, 256 threads.
-template <int BM, bool SPECTRAL>
-__global__ void __launch_bounds__(256) gemm_tn_simt(int m, GemmSet s, SpectralEpi e) {
-    if (s.gate && !((1 << *s.gate) & s.gate_mask)) return;
+// One BM x BM output tile (rows i0.., columns j0..) of D = A B^T on an m x m
+// problem, 256 threads.  FRESH_B: B was written by other blocks of the same
+// launch (a persistent launch's earlier stage), so it is read through L2
+// (ld.global.cg) rather than the non-coherent read-only path.
+template <int BM, bool SPECTRAL, bool FRESH_B>
+__device__ __forceinline__ void gemm_tile(int m, const GemmSet &s, int z, const SpectralEpi &e, int i0, int j0) {
     constexpr int TM = BM / 16;
-    __shared__ __align__(16) float As[BK][BM + 4];
-    __shared__ __align__(16) float Bs[BK][BM + 4];
-    const int z = blockIdx.z;
     const float *__restrict__ A = s.A[z];
     const float *__restrict__ B = s.B[z];
-    const int i0 = blockIdx.y * BM, j0 = blockIdx.x * BM;
+    __shared__ __align__(16) float As[BK][BM + 4];
+    __shared__ __align__(16) float Bs[BK][BM + 4];
     const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
     float acc[TM][TM];
 #pragma unroll
@@ -75,7 +75,8 @@ __global__ void __launch_bounds__(256) gemm_tn_simt(int m, GemmSet s, SpectralEp
         for (int q = tid; q < BM * BK / 4; q += 256) {
             const int row = q >> 2, kq = (q & 3) * 4;
             const float4 va = *reinterpret_cast<const float4 *>(A + (size_t)(i0 + row) * m + k0 + kq);
-            const float4 vb = *reinterpret_cast<const float4 *>(B + (size_t)(j0 + row) * m + k0 + kq);
+            const float4 *pb = reinterpret_cast<const float4 *>(B + (size_t)(j0 + row) * m + k0 + kq);
+            const float4 vb = FRESH_B ? __ldcg(pb) : *pb;
             As[kq + 0][row] = va.x;
             As[kq + 1][row] = va.y;
             As[kq + 2][row] = va.z;
@@ -112,6 +113,14 @@ __global__ void __launch_bounds__(256) gemm_tn_simt(int m, GemmSet s, SpectralEp
                 s.C[z][(size_t)gi * m + gj] = acc[i][j];
         }
     }
+}
+
+// D = A B^T on an m x m problem; one BM x BM output tile per block.
+template <int BM, bool SPECTRAL>
+__global__ void __launch_bounds__(256) gemm_tn_simt(int m, GemmSet s, SpectralEpi e) {
+    if (s.gate && !((1 << *s.gate) & s.gate_mask)) return;
+    const int z = blockIdx.z;
+    gemm_tile<BM, SPECTRAL, false>(m, s, z, e, blockIdx.y * BM, blockIdx.x * BM);
 }
 
 // bm: output tile side chosen by the autotuner in field_solver_init (0 = size rule)
@@ -221,6 +230,71 @@ void field_solve_fp32(FieldSolver &f, const float *d, float *ex, float *ey, cuda
     gemm<false>(m, s3, 2, none, st, f.simt_bm);
     GemmSet s4{{f.St, f.Ct}, {f.ux, f.uy}, {ex, ey}, gate, gate_mask};
     gemm<false>(m, s4, 2, none, st, f.simt_bm);
+}
+
+void field_records(const FieldSolver &f, const float *d, float *ex, float *ey, FieldRec rec[4]) {
+    const int m = f.m;
+    const int bm = (f.simt_bm == 64 && m % 64 == 0) ? 64 : (f.simt_bm == 0 && m >= 512 && m % 64 == 0 ? 64 : 32);
+    const float scale = 4.0f / ((float)m * (float)m);
+    for (int k = 0; k < 4; ++k) {
+        rec[k] = FieldRec{};
+        rec[k].m = m;
+        rec[k].bm = bm;
+        rec[k].batch = k < 2 ? 1 : 2;
+    }
+    rec[0].A[0] = f.C;
+    rec[0].B[0] = d;
+    rec[0].C[0] = f.t0;
+    rec[1].A[0] = f.C;
+    rec[1].B[0] = f.t0;
+    rec[1].spectral = 1;
+    rec[1].px = f.px;
+    rec[1].py = f.py;
+    rec[1].wx = f.wx;
+    rec[1].wy = f.wy;
+    rec[1].scale = scale;
+    rec[2].A[0] = f.Ct;
+    rec[2].A[1] = f.St;
+    rec[2].B[0] = f.px;
+    rec[2].B[1] = f.py;
+    rec[2].C[0] = f.ux;
+    rec[2].C[1] = f.uy;
+    rec[3].A[0] = f.St;
+    rec[3].A[1] = f.Ct;
+    rec[3].B[0] = f.ux;
+    rec[3].B[1] = f.uy;
+    rec[3].C[0] = ex;
+    rec[3].C[1] = ey;
+}
+
+// The batched form: the four contractions of every instance in one launch,
+// record k + 1 of an instance waiting for its record k (the queue's
+// dependencies); tiles as gemm_tn_simt, B read through L2.
+__global__ void __launch_bounds__(256) persist_field_kernel(PersistQueue q, const FieldRec *recs) {
+    persist_loop(q, recs, [](const FieldRec &r, VBlock vb, int) {
+        const int nt = r.m / r.bm, tiles = nt * nt;
+        const int z = vb.id / tiles, t = vb.id - z * tiles;
+        const int i0 = (t / nt) * r.bm, j0 = (t % nt) * r.bm;
+        const GemmSet s{{r.A[0], r.A[1]}, {r.B[0], r.B[1]}, {r.C[0], r.C[1]}, nullptr, 0};
+        const SpectralEpi e{r.px, r.py, r.wx, r.wy, r.scale};
+        if (r.bm == 64) {
+            if (r.spectral)
+                gemm_tile<64, true, true>(r.m, s, z, e, i0, j0);
+            else
+                gemm_tile<64, false, true>(r.m, s, z, e, i0, j0);
+        } else {
+            if (r.spectral)
+                gemm_tile<32, true, true>(r.m, s, z, e, i0, j0);
+            else
+                gemm_tile<32, false, true>(r.m, s, z, e, i0, j0);
+        }
+    });
+}
+
+void launch_persist_field(const PersistQueue &q, const FieldRec *recs, cudaStream_t st) {
+    static int wave = 0;
+    if (!wave) wave = wave_of((const void *)persist_field_kernel, 256, 608);
+    persist_field_kernel<<<wave, 256, 0, st>>>(q, recs);
 }
 
 // Tile autotuner of the FP32 path: times a full solve with 32 and with 64

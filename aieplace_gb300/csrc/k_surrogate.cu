@@ -103,7 +103,7 @@ __global__ void scale_kernel(int R, int f, const float *cex, const float *cey, f
         acc += cex[q] * cex[q] + cey[q] * cey[q];
     const float b = block_sum_ff(acc, reinterpret_cast<float *>(red));
     if (threadIdx.x == 0) partials[blockIdx.x] = b;
-    if (arrive_last(counter)) {
+    if (arrive_last(counter, gridDim.x)) {
         const double t = block_sum_f(kahan_strided(partials, threadIdx.x, gridDim.x, blockDim.x, 1), red);
         if (threadIdx.x == 0) {
             const double ms = t * (double)f * (double)f / ((double)R * (double)R);
@@ -188,7 +188,7 @@ __global__ void sumsq_kernel(size_t n, const float *ex, const float *ey, float *
         acc += ex[k] * ex[k] + ey[k] * ey[k];
     const float bsum = block_sum_ff(acc, reinterpret_cast<float *>(red));
     if (threadIdx.x == 0) partials[blockIdx.x] = bsum;
-    if (arrive_last(counter)) {
+    if (arrive_last(counter, gridDim.x)) {
         const double t = block_sum_f(kahan_strided(partials, threadIdx.x, gridDim.x, blockDim.x, 1), red);
         if (threadIdx.x == 0) {
             *out = (float)t;
@@ -213,7 +213,7 @@ __global__ void diff_norms_kernel(size_t n, const float *y, const float *t, floa
         partials[2 * blockIdx.x] = ba;
         partials[2 * blockIdx.x + 1] = bb;
     }
-    if (arrive_last(counter)) {
+    if (arrive_last(counter, gridDim.x)) {
         const double ta = block_sum_f(kahan_strided(partials, threadIdx.x, gridDim.x, blockDim.x, 2), red);
         const double tb = block_sum_f(kahan_strided(partials + 1, threadIdx.x, gridDim.x, blockDim.x, 2), red);
         if (threadIdx.x == 0) {
@@ -528,7 +528,7 @@ __global__ void mse_kernel(int B, int C, int R, int margin, const float *y, cons
     }
     const float bsum = block_sum_ff(acc, reinterpret_cast<float *>(red));
     if (threadIdx.x == 0) partials[blockIdx.x] = bsum;
-    if (arrive_last(counter)) {
+    if (arrive_last(counter, gridDim.x)) {
         const double tot = block_sum_f(kahan_strided(partials, threadIdx.x, gridDim.x, blockDim.x, 1), red);
         if (threadIdx.x == 0) {
             *loss = (float)(tot * (double)inv_n);
@@ -607,7 +607,7 @@ __global__ void field_err_kernel(size_t n, const float *sx, const float *sy, con
         partials[2 * blockIdx.x] = ba;
         partials[2 * blockIdx.x + 1] = bb;
     }
-    if (arrive_last(counter)) {
+    if (arrive_last(counter, gridDim.x)) {
         const double ta = block_sum_f(kahan_strided(partials, threadIdx.x, gridDim.x, blockDim.x, 2), red);
         const double tb = block_sum_f(kahan_strided(partials + 1, threadIdx.x, gridDim.x, blockDim.x, 2), red);
         if (threadIdx.x == 0) {

@@ -91,7 +91,7 @@ __device__ __forceinline__ void group_max4(float v[4], int l, unsigned mask, int
 // in registers (pin j on lane j mod G): one load pass, each exponential once.
 template <int G, int P>
 __device__ __forceinline__ void net_group(const WaArgs &a, int s, int d, int l, unsigned mask, int base,
-                                          const float *px, const float *py, float inv_g, float &hpf, float &waf) {
+                                          const float2 *xy, float inv_g, float &hpf, float &waf) {
     bool v[P];
     int nd[P];
     float c[P][2];
@@ -100,8 +100,9 @@ __device__ __forceinline__ void net_group(const WaArgs &a, int s, int d, int l, 
         const int j = l + p * G;
         v[p] = j < d;
         nd[p] = v[p] ? __ldg(a.pin_node + s + j) : 0;  // raw entry (heavy flag)
-        c[p][0] = v[p] ? __ldg(px + (nd[p] & kPinNode)) : 0.f;
-        c[p][1] = v[p] ? __ldg(py + (nd[p] & kPinNode)) : 0.f;
+        const float2 q = v[p] ? __ldg(xy + (nd[p] & kPinNode)) : make_float2(0.f, 0.f);
+        c[p][0] = q.x;
+        c[p][1] = q.y;
     }
     float m4[4] = {-3.0e38f, -3.0e38f, -3.0e38f, -3.0e38f};  // max x, max y, -min x, -min y
 #pragma unroll
@@ -152,25 +153,25 @@ __device__ __forceinline__ void net_group(const WaArgs &a, int s, int d, int l, 
 }
 
 // Nets of sub-bucket [lo, hi) by groups of G lanes; the launch's blocks
-// [b0, b0 + nb) serve this sub-bucket.
+// [b0, b0 + nb) serve this sub-bucket, this one is block `bid`.
 template <int G, int P>
-__device__ __forceinline__ void net_groups(const WaArgs &a, int lo, int hi, int b0, int nb, const float *px,
-                                           const float *py, float inv_g, float &hpf, float &waf) {
+__device__ __forceinline__ void net_groups(const WaArgs &a, int bid, int lo, int hi, int b0, int nb,
+                                           const float2 *xy, float inv_g, float &hpf, float &waf) {
     constexpr int per_block = kThreads / G;
     const int lane = threadIdx.x & 31, l = lane & (G - 1), base = lane - l;
     const unsigned mask = G == 32 ? 0xffffffffu : (((1u << G) - 1u) << base);
-    const int group = ((int)blockIdx.x - b0) * per_block + (int)threadIdx.x / G, n_groups = nb * per_block;
+    const int group = (bid - b0) * per_block + (int)threadIdx.x / G, n_groups = nb * per_block;
     for (int e = lo + group; e < hi; e += n_groups) {
         const int s = __ldg(a.net_ptr + e), d = __ldg(a.net_ptr + e + 1) - s;
-        net_group<G, P>(a, s, d, l, mask, base, px, py, inv_g, hpf, waf);
+        net_group<G, P>(a, s, d, l, mask, base, xy, inv_g, hpf, waf);
     }
 }
 
 // One net with d <= D pins held in registers by one thread.
 template <int D>
-__device__ __forceinline__ void net_thread(const int *__restrict__ pins, int d, const float *__restrict__ px,
-                                           const float *__restrict__ py, float inv_g, ull *gq, ull *gqx,
-                                           ull *gqy, int n_grad, float &hp_acc, float &wa_acc) {
+__device__ __forceinline__ void net_thread(const int *__restrict__ pins, int d, const float2 *__restrict__ xy,
+                                           float inv_g, ull *gq, ull *gqx, ull *gqy, int n_grad, float &hp_acc,
+                                           float &wa_acc) {
     int node[D];
     float xs[D], ys[D];
     float xmx = -3.0e38f, xmn = 3.0e38f, ymx = -3.0e38f, ymn = 3.0e38f;
@@ -178,8 +179,9 @@ __device__ __forceinline__ void net_thread(const int *__restrict__ pins, int d, 
     for (int j = 0; j < D; ++j) {
         if (j < d) {
             node[j] = __ldg(pins + j);  // raw entry (heavy flag)
-            xs[j] = __ldg(px + (node[j] & kPinNode));
-            ys[j] = __ldg(py + (node[j] & kPinNode));
+            const float2 q = __ldg(xy + (node[j] & kPinNode));
+            xs[j] = q.x;
+            ys[j] = q.y;
             xmx = fmaxf(xmx, xs[j]);
             xmn = fminf(xmn, xs[j]);
             ymx = fmaxf(ymx, ys[j]);
@@ -232,16 +234,11 @@ __device__ __forceinline__ void net_thread(const int *__restrict__ pins, int d, 
 
 // Bucket B (degree <= D) of the thread-per-net nets: registers sized for D.
 template <int D, int B>
-__global__ void __launch_bounds__(kThreads) wa_small_kernel(WaArgs a) {
+__device__ __forceinline__ void wa_small_body(const WaArgs &a, VBlock vb) {
     __shared__ double red[32];
     const float gamma = a.gamma > 0.f ? a.gamma : a.sc->f_gamma;
     const float inv_g = 1.f / gamma;
-    const float *px = a.px, *py = a.py;
-    if (a.mode == WA_LOOP) {
-        const int t = 1 - a.sc->cur;
-        px = a.pxs[t];
-        py = a.pys[t];
-    }
+    const float2 *xy = a.xy;  // every node's position, interleaved
     // per-thread partials in FP32 (a thread owns a few nets), FP64 from the
     // block sum on: the FP64 pipe of this part is narrow
     float hpf = 0.f, waf = 0.f;
@@ -249,10 +246,10 @@ __global__ void __launch_bounds__(kThreads) wa_small_kernel(WaArgs a) {
     // every net of the 2-pin bucket has degree 2: its pins sit at a computed
     // offset, one dependent load fewer per net
     const int s0 = D == 2 && lo < hi ? __ldg(a.net_ptr + lo) : 0;
-    for (int e = lo + blockIdx.x * blockDim.x + threadIdx.x; e < hi; e += gridDim.x * blockDim.x) {
+    for (int e = lo + vb.id * blockDim.x + threadIdx.x; e < hi; e += vb.n * blockDim.x) {
         const int s = D == 2 ? s0 + 2 * (e - lo) : __ldg(a.net_ptr + e);
         const int d = D == 2 ? 2 : __ldg(a.net_ptr + e + 1) - s;
-        net_thread<D>(a.pin_node + s, d, px, py, inv_g, a.gq, a.gqx, a.gqy, a.n_grad, hpf, waf);
+        net_thread<D>(a.pin_node + s, d, xy, inv_g, a.gq, a.gqx, a.gqy, a.n_grad, hpf, waf);
     }
     // per-block partials in FP32 (folded with compensation by the last block
     // of the warp-per-net launch)
@@ -263,20 +260,24 @@ __global__ void __launch_bounds__(kThreads) wa_small_kernel(WaArgs a) {
     for (int b = 0; b < B; ++b) off += a.bucket_blocks[b];
     if (threadIdx.x == 0) {
         float *pf = reinterpret_cast<float *>(a.partials);
-        pf[2 * (off + blockIdx.x)] = hp;
-        pf[2 * (off + blockIdx.x) + 1] = wa;
+        pf[2 * (off + vb.id)] = hp;
+        pf[2 * (off + vb.id) + 1] = wa;
     }
 }
 
+template <int D, int B>
+__global__ void __launch_bounds__(kThreads) wa_small_kernel(WaArgs a) { wa_small_body<D, B>(a, grid_block()); }
+
 // General path of one net of any degree by a warp: three passes over the pins
 // (extrema; sums; gradients), pins lane, lane + 32, ...
-__device__ __forceinline__ void net_warp_loop(const WaArgs &a, int s, int d, const float *px, const float *py,
-                                              float inv_g, float &hpf, float &waf) {
+__device__ __forceinline__ void net_warp_loop(const WaArgs &a, int s, int d, const float2 *xy, float inv_g,
+                                              float &hpf, float &waf) {
     const int lane = threadIdx.x & 31;
     float m4[4] = {-3.0e38f, -3.0e38f, -3.0e38f, -3.0e38f};  // max x, max y, -min x, -min y
     for (int j = lane; j < d; j += 32) {
         const int n = __ldg(a.pin_node + s + j) & kPinNode;
-        const float x = __ldg(px + n), y = __ldg(py + n);
+        const float2 q = __ldg(xy + n);
+        const float x = q.x, y = q.y;
         m4[0] = fmaxf(m4[0], x);
         m4[1] = fmaxf(m4[1], y);
         m4[2] = fmaxf(m4[2], -x);
@@ -287,7 +288,8 @@ __device__ __forceinline__ void net_warp_loop(const WaArgs &a, int s, int d, con
     float s8[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};  // bp bm cp cm for x then y
     for (int j = lane; j < d; j += 32) {
         const int n = __ldg(a.pin_node + s + j) & kPinNode;
-        const float c2[2] = {__ldg(px + n), __ldg(py + n)};
+        const float2 q = __ldg(xy + n);
+        const float c2[2] = {q.x, q.y};
 #pragma unroll
         for (int ax = 0; ax < 2; ++ax) {
             const float dp = c2[ax] - (ax ? ymx : xmx), dm = c2[ax] - (ax ? ymn : xmn);
@@ -310,7 +312,8 @@ __device__ __forceinline__ void net_warp_loop(const WaArgs &a, int s, int d, con
     for (int j = lane; j < d; j += 32) {
         const int raw = __ldg(a.pin_node + s + j), n = raw & kPinNode;
         if (n >= a.n_grad) continue;
-        const float c2[2] = {__ldg(px + n), __ldg(py + n)};
+        const float2 q = __ldg(xy + n);
+        const float c2[2] = {q.x, q.y};
         float g[2];
 #pragma unroll
         for (int ax = 0; ax < 2; ++ax) {
@@ -332,68 +335,71 @@ __device__ __forceinline__ void net_warp_loop(const WaArgs &a, int s, int d, con
 // 16 lanes (four pins per lane: two nets per warp share each shuffle
 // reduction), and above 64 with a warp looping over the pins --
 // the lane group fits the net, so few lanes idle.
-__global__ void __launch_bounds__(kThreads) wa_large_kernel(WaArgs a) {
+__device__ __forceinline__ void wa_large_body(const WaArgs &a, VBlock vb) {
     __shared__ double red[32];
     const float gamma = a.gamma > 0.f ? a.gamma : a.sc->f_gamma;
     const float inv_g = 1.f / gamma;
-    const float *px = a.px, *py = a.py;
-    if (a.mode == WA_LOOP) {
-        const int t = 1 - a.sc->cur;
-        px = a.pxs[t];
-        py = a.pys[t];
-    }
+    const float2 *xy = a.xy;  // every node's position, interleaved
     // per-thread partials in FP32 (a thread owns a few nets), FP64 from the
     // block sum on: the FP64 pipe of this part is narrow
     float hpf = 0.f, waf = 0.f;
     int b0 = 0;
-    const int bid = blockIdx.x;
+    const int bid = vb.id;
     if (bid < b0 + a.bucket_blocks[3]) {
-        net_groups<16, 1>(a, a.bucket_lo[3], a.bucket_lo[4], b0, a.bucket_blocks[3], px, py, inv_g, hpf, waf);
+        net_groups<16, 1>(a, bid, a.bucket_lo[3], a.bucket_lo[4], b0, a.bucket_blocks[3], xy, inv_g, hpf, waf);
     } else if (bid < (b0 += a.bucket_blocks[3]) + a.bucket_blocks[4]) {
-        net_groups<32, 1>(a, a.bucket_lo[4], a.bucket_lo[5], b0, a.bucket_blocks[4], px, py, inv_g, hpf, waf);
+        net_groups<32, 1>(a, bid, a.bucket_lo[4], a.bucket_lo[5], b0, a.bucket_blocks[4], xy, inv_g, hpf, waf);
     } else if (bid < (b0 += a.bucket_blocks[4]) + a.bucket_blocks[5]) {
-        net_groups<16, 4>(a, a.bucket_lo[5], a.bucket_lo[6], b0, a.bucket_blocks[5], px, py, inv_g, hpf, waf);
+        net_groups<16, 4>(a, bid, a.bucket_lo[5], a.bucket_lo[6], b0, a.bucket_blocks[5], xy, inv_g, hpf, waf);
     } else {
         b0 += a.bucket_blocks[5];
         const int warp = ((bid - b0) * kThreads + (int)threadIdx.x) >> 5, nwarps = (a.bucket_blocks[6] * kThreads) >> 5;
         for (int e = a.bucket_lo[6] + warp; e < a.bucket_lo[7]; e += nwarps) {
             const int s = __ldg(a.net_ptr + e), d = __ldg(a.net_ptr + e + 1) - s;
-            net_warp_loop(a, s, d, px, py, inv_g, hpf, waf);
+            net_warp_loop(a, s, d, xy, inv_g, hpf, waf);
         }
     }
     const float hp = block_sum_ff(hpf, reinterpret_cast<float *>(red));
     const float wa = block_sum_ff(waf, reinterpret_cast<float *>(red));
     float *pf = reinterpret_cast<float *>(a.partials);
     if (threadIdx.x == 0) {
-        pf[2 * (a.small_blocks + blockIdx.x)] = hp;
-        pf[2 * (a.small_blocks + blockIdx.x) + 1] = wa;
-    }
-    // the last block of this launch folds both launches' partials
-    if (arrive_last(a.counter)) {
-        const int nb = a.small_blocks + gridDim.x;
-        const double h = block_sum_f(kahan_strided(pf, threadIdx.x, nb, blockDim.x, 2), red);
-        const double w = block_sum_f(kahan_strided(pf + 1, threadIdx.x, nb, blockDim.x, 2), red);
-        if (threadIdx.x == 0) {
-            if (a.out) {
-                a.out[0] = h;
-                a.out[1] = w;
-            }
-            DevScalars *sc = a.sc;
-            if (a.mode == WA_INIT) {
-                sc->hpwl = h;
-                sc->hpwl_prev = h;
-                sc->wa = w;
-            } else if (a.mode == WA_LOOP) {
-                sc->t_hpwl = h;  // becomes the reported HPWL if the trial is accepted
-                sc->t_wa = w;
-            }
-            *a.counter = 0u;
-        }
+        pf[2 * (a.small_blocks + vb.id)] = hp;
+        pf[2 * (a.small_blocks + vb.id) + 1] = wa;
     }
 }
 
-void launch_wirelength(const WaArgs &a0, cudaStream_t st) {
-    WaArgs a = a0;
+// HPWL and WA of partials [0, nb) of all four bucket launches (one block).
+__device__ __forceinline__ void wa_fold(const WaArgs &a, int nb) {
+    __shared__ double red[32];
+    const float *pf = reinterpret_cast<const float *>(a.partials);
+    const double h = block_sum_f(kahan_strided(pf, threadIdx.x, nb, blockDim.x, 2), red);
+    const double w = block_sum_f(kahan_strided(pf + 1, threadIdx.x, nb, blockDim.x, 2), red);
+    if (threadIdx.x == 0) {
+        if (a.out) {
+            a.out[0] = h;
+            a.out[1] = w;
+        }
+        DevScalars *sc = a.sc;
+        if (a.mode == WA_INIT) {
+            sc->hpwl = h;
+            sc->hpwl_prev = h;
+            sc->wa = w;
+        } else if (a.mode == WA_LOOP) {
+            sc->t_hpwl = h;  // becomes the reported HPWL if the trial is accepted
+            sc->t_wa = w;
+        }
+        *a.counter = 0u;
+    }
+}
+
+// The last of the four launches: it folds the partials of all of them (the
+// three before it ran earlier on the same stream).
+__global__ void __launch_bounds__(kThreads, 4) wa_large_kernel(WaArgs a) {
+    wa_large_body(a, grid_block());
+    if (arrive_last(a.counter, gridDim.x)) wa_fold(a, a.small_blocks + (int)gridDim.x);
+}
+
+int wa_plan(WaArgs &a) {
     auto grid = [](int items) {
         int b = (items + kThreads - 1) / kThreads;
         return b < 1 ? 1 : (b > kWaMaxBlocks ? kWaMaxBlocks : b);
@@ -407,10 +413,54 @@ void launch_wirelength(const WaArgs &a0, cudaStream_t st) {
         large += a.bucket_blocks[b];
     }
     a.small_blocks = a.bucket_blocks[0] + a.bucket_blocks[1] + a.bucket_blocks[2];
+    return a.small_blocks + large;
+}
+
+// Positions (px, py) of all nodes -> the interleaved copy the WA kernels read.
+__global__ void interleave_kernel(int n, const float *__restrict__ px, const float *__restrict__ py,
+                                  float2 *__restrict__ xy) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        xy[i] = make_float2(px[i], py[i]);
+}
+
+void launch_interleave(int n, const float *px, const float *py, float2 *xy, cudaStream_t st) {
+    if (n <= 0) return;
+    int blocks = (n + kThreads - 1) / kThreads;
+    if (blocks > 2048) blocks = 2048;
+    interleave_kernel<<<blocks, kThreads, 0, st>>>(n, px, py, xy);
+}
+
+void launch_wirelength(const WaArgs &a0, cudaStream_t st) {
+    WaArgs a = a0;
+    if (a.mode != WA_LOOP) launch_interleave(a.n_nodes, a.px, a.py, a.xy, st);
+    const int large = wa_plan(a) - a.small_blocks;
     wa_small_kernel<2, 0><<<a.bucket_blocks[0], kThreads, 0, st>>>(a);
     wa_small_kernel<4, 1><<<a.bucket_blocks[1], kThreads, 0, st>>>(a);
     wa_small_kernel<8, 2><<<a.bucket_blocks[2], kThreads, 0, st>>>(a);
     wa_large_kernel<<<large, kThreads, 0, st>>>(a);
+}
+
+// The batched form: one record per instance holding the blocks of its four
+// bucket launches in launch order; the record's last block folds the sums.
+__global__ void __launch_bounds__(kThreads, 3) persist_wa_kernel(PersistQueue q, const WaArgs *recs) {
+    persist_loop(q, recs, [](const WaArgs &a, VBlock vb, int) {
+        const int b0 = a.bucket_blocks[0], b1 = a.bucket_blocks[1], b2 = a.bucket_blocks[2];
+        if (vb.id < b0)
+            wa_small_body<2, 0>(a, VBlock{vb.id, b0});
+        else if (vb.id < b0 + b1)
+            wa_small_body<4, 1>(a, VBlock{vb.id - b0, b1});
+        else if (vb.id < a.small_blocks)
+            wa_small_body<8, 2>(a, VBlock{vb.id - b0 - b1, b2});
+        else
+            wa_large_body(a, VBlock{vb.id - a.small_blocks, vb.n - a.small_blocks});
+        if (arrive_last(a.counter, vb.n)) wa_fold(a, vb.n);
+    });
+}
+
+void launch_persist_wa(const PersistQueue &q, const WaArgs *recs, cudaStream_t st) {
+    static int wave = 0;
+    if (!wave) wave = wave_of((const void *)persist_wa_kernel, kThreads, 1216);
+    persist_wa_kernel<<<wave, kThreads, 0, st>>>(q, recs);
 }
 
 }  // namespace ap

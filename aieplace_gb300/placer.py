@@ -20,7 +20,7 @@ import ctypes as C
 
 import numpy as np
 
-from ._lib import (AP_FIELD_BF16X3, AP_FIELD_FP32, Netlist, Params, Stats, SurrogatePolicy, SurrogateStats, check,
+from ._lib import (AP_FIELD_BF16X3, AP_FIELD_FP32, BatchInfo, Netlist, Params, Stats, SurrogatePolicy, SurrogateStats, check,
                    lib, ptr)
 
 SOLVERS = {"fp32": AP_FIELD_FP32, "bf16x3": AP_FIELD_BF16X3}
@@ -219,7 +219,10 @@ class Placer:
 
 class BatchPlacer:
     """Independent placements stepped together (ap_create_batch): one CUDA
-    graph launch advances one trial step of every active instance."""
+    graph launch advances one trial step of every active instance, as six
+    persistent launches over all instances ("persistent", the default where
+    it serves every instance) or as every instance's own launches in
+    parallel branches ("graph")."""
 
     def __init__(self, netlists: list[dict], field_solver: str = "fp32", **overrides):
         n = len(netlists)
@@ -285,3 +288,11 @@ class BatchPlacer:
         y = np.zeros(self.sizes[i], np.float32)
         check("ap_batch_get_positions", lib().ap_batch_get_positions(self._h, int(i), ptr(x), ptr(y)))
         return x, y
+
+    def set_form(self, form: str):
+        check("ap_batch_set_form", lib().ap_batch_set_form(self._h, {"graph": 0, "persistent": 1}[form]))
+
+    def info(self) -> dict:
+        b = BatchInfo()
+        check("ap_batch_get_info", lib().ap_batch_get_info(self._h, C.byref(b)))
+        return b.as_dict()

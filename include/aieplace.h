@@ -277,7 +277,7 @@ int ap_selftest_numerics(int32_t *mismatches, int64_t samples);
  * of the handle returns AP_ERR_TIMEOUT; the GPU context stays usable.
  * AP_FAULT_NONE removes the injection and clears the handle's timeout status.
  * Needs the tensor-core solver (AP_ERR_UNSUPPORTED otherwise). */
-enum { AP_FAULT_NONE = 0, AP_FAULT_TC_STALL = 1 };
+enum { AP_FAULT_NONE = 0, AP_FAULT_TC_STALL = 1, AP_FAULT_NEVER_ARRIVE = 2 };
 int ap_debug_inject(ap_handle *h, int32_t kind, int64_t wait_ns);
 
 /* ---- checkpoint / resume ----------------------------------------------- */
@@ -288,11 +288,31 @@ int ap_restore(ap_handle *h, const void *buf, size_t bytes);
 /* ---- batched form ---------------------------------------------------------
  * Many independent placements stepped together.  The reference places one
  * design per run (Placer::run, AIEplace.cpp:44-76); small designs cannot fill
- * a GB300 alone, so a batch captures one trial step of every instance as
- * parallel branches of one CUDA graph and advances all of them with one graph
- * launch.  Instances keep their own parameters (bin counts may differ) and
- * produce exactly the results they produce when stepped alone. */
+ * a GB300 alone, so a batch advances every active instance by one trial step
+ * per launch of one CUDA graph, in one of two forms:
+ *   AP_BATCH_PERSISTENT  six persistent kernels per trial step, one per stage
+ *                        (position update, WA gradient, bin scatter,
+ *                        density/overflow, field solve, gather), each over all
+ *                        instances: its resident blocks pull (instance, block)
+ *                        work items off a device queue, so instances of uneven
+ *                        size share the GPU; the field solve's four
+ *                        contractions of an instance wait on one another
+ *                        inside the launch (bounded waits, below), with the
+ *                        tile chosen by the batch's autotuner.  Needs the FP32
+ *                        field solve and no surrogate; the default where it
+ *                        serves every instance.
+ *   AP_BATCH_GRAPH       every instance's own launches as parallel branches.
+ * Instances keep their own parameters (bin counts may differ) and produce,
+ * in either form, exactly the results they produce when stepped alone. */
 typedef struct ap_batch ap_batch;
+enum { AP_BATCH_GRAPH = 0, AP_BATCH_PERSISTENT = 1 };
+typedef struct {
+    int32_t form;                /* AP_BATCH_* */
+    int32_t instances, active;
+    int32_t field_tile;          /* persistent form: field tile of the autotuner (32 or 64; 0 = not tuned) */
+    float field_tune_ms[2];      /* its measured field launch with 32 and with 64 tiles */
+    int32_t records[6];          /* work records per persistent launch: update, scatter, rho, WA, field, gather */
+} ap_batch_info;
 
 int ap_create_batch(int32_t n, const ap_netlist *netlists, const ap_params *params, ap_batch **out);
 int ap_batch_destroy(ap_batch *b);
@@ -308,6 +328,19 @@ int ap_batch_step(ap_batch *b, int32_t n_trials);
 int ap_batch_run(ap_batch *b, int32_t *iterations);
 int ap_batch_get_stats(ap_batch *b, int32_t i, ap_stats *stats);
 int ap_batch_get_positions(ap_batch *b, int32_t i, float *x, float *y);
+/* switches the form (AP_ERR_UNSUPPORTED: the persistent form cannot serve
+ * every instance); takes effect at the next step */
+int ap_batch_set_form(ap_batch *b, int32_t form);
+int ap_batch_get_info(ap_batch *b, ap_batch_info *info);
+/* Failure injection (persistent form): AP_FAULT_NEVER_ARRIVE makes every
+ * dependency wait of the field launch wait for one block more than the
+ * awaited contraction has, bounded by wait_ns (1 ms .. 2 s): the first wait
+ * runs out, the launch's remaining items skip their work, the launch ends,
+ * and ap_batch_step / ap_batch_run return AP_ERR_TIMEOUT.  The instances'
+ * state is then undefined until ap_batch_init_seeded; AP_FAULT_NONE removes
+ * the injection and clears the status.  Without injection each wait is
+ * bounded by 1 s. */
+int ap_batch_debug_inject(ap_batch *b, int32_t kind, int64_t wait_ns);
 
 /* ---- learned density-to-field surrogate ------------------------------------
  * No counterpart in the reference (its field solves are exact).  A surrogate
