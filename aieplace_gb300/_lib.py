@@ -28,7 +28,7 @@ EXPORTS = [
     "ap_design_node_name", "ap_design_write_def", "ap_design_destroy",
     "ap_create_batch", "ap_batch_destroy", "ap_batch_init_seeded", "ap_batch_step", "ap_batch_run",
     "ap_batch_get_stats", "ap_batch_get_positions", "ap_batch_set_form", "ap_batch_get_info",
-    "ap_batch_debug_inject",
+    "ap_batch_debug_inject", "ap_batch_set_item_blocks", "ap_batch_profile",
     "ap_surrogate_config_default", "ap_surrogate_create", "ap_surrogate_destroy", "ap_surrogate_num_params",
     "ap_surrogate_get_params", "ap_surrogate_set_params", "ap_surrogate_forward", "ap_surrogate_gradient",
     "ap_surrogate_reserve", "ap_surrogate_num_samples", "ap_surrogate_collect", "ap_surrogate_train",
@@ -62,17 +62,22 @@ class Params(C.Structure):
                 ("init_step_coef", C.c_float), ("target_overflow", C.c_float),
                 ("max_iterations", C.c_int32), ("check_interval", C.c_int32),
                 ("use_graph", C.c_int32), ("max_backtracks", C.c_int32), ("restart_mode", C.c_int32),
-                ("filler_cells", C.c_int32)]
+                ("filler_cells", C.c_int32), ("block_nodes", C.c_int32)]
+
+
+STAGES6 = ("update", "scatter", "rho", "wa", "field", "gather")
 
 
 class BatchInfo(C.Structure):
     _fields_ = [("form", C.c_int32), ("instances", C.c_int32), ("active", C.c_int32), ("field_tile", C.c_int32),
-                ("field_tune_ms", C.c_float * 2), ("records", C.c_int32 * 6)]
+                ("field_tune_ms", C.c_float * 2), ("records", C.c_int32 * 6), ("item_blocks", C.c_int32 * 6),
+                ("items", C.c_int32 * 6)]
 
     def as_dict(self) -> dict:
         return {"form": ("graph", "persistent")[self.form], "instances": self.instances, "active": self.active,
                 "field_tile": self.field_tile, "field_tune_ms": list(self.field_tune_ms),
-                "records": dict(zip(("update", "scatter", "rho", "wa", "field", "gather"), self.records))}
+                "records": dict(zip(STAGES6, self.records)), "item_blocks": dict(zip(STAGES6, self.item_blocks)),
+                "items": dict(zip(STAGES6, self.items))}
 
 
 class Stats(C.Structure):
@@ -186,6 +191,8 @@ def lib():
         L.ap_batch_set_form.argtypes = [vp, i32]
         L.ap_batch_get_info.argtypes = [vp, C.POINTER(BatchInfo)]
         L.ap_batch_debug_inject.argtypes = [vp, i32, C.c_int64]
+        L.ap_batch_set_item_blocks.argtypes = [vp, i32]
+        L.ap_batch_profile.argtypes = [vp, i32, vp]
         L.ap_surrogate_config_default.argtypes = [C.POINTER(SurrogateConfig)]
         L.ap_surrogate_create.argtypes = [C.POINTER(SurrogateConfig), C.POINTER(vp)]
         L.ap_surrogate_destroy.argtypes = [vp]

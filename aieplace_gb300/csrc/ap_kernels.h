@@ -39,6 +39,7 @@ struct WaArgs {
     double *partials;      // 2 per block over all bucket launches
     unsigned int *counter;
     int small_blocks;      // blocks of the three thread-per-net launches together
+    int block_nets;        // nets (lanes of the larger nets) per block, at least (<= 256: one per thread)
     double *out;           // [2]: HPWL, WA
     int mode;
 };
@@ -93,6 +94,10 @@ struct ScatterArgs {
     // host step's input); block partials from slot part_base on; no_fold: a
     // later launch folds the sums
     int upd_lo, upd_hi, part_base, no_fold;
+    // nodes per block of the position update and the bin adds, at least
+    // (<= the block size: one per thread); results depend on it only
+    // through the order of the update's FP32 block sums
+    int block_nodes;
 };
 void launch_scatter(const ScatterArgs &a, cudaStream_t st);
 // the two launches of launch_scatter: the position update and records (update
@@ -159,6 +164,7 @@ struct GatherArgs {
     // GATHER_STEP / NODE_OUT, optional: the bin records of this point
     const int *rec_bin;
     const int4 *rec_ov;
+    int block_nodes;        // nodes per block, at least (<= the block size: one per thread)
 };
 void launch_gather(const GatherArgs &a, cudaStream_t st);
 // bin records (as the position update writes them) of movable nodes at (x, y)
@@ -220,16 +226,20 @@ int field_solver_clear_status(FieldSolver &f);
 void launch_split_bf16(int n, const float *src, __nv_bfloat16 *hi, __nv_bfloat16 *lo, cudaStream_t st);
 
 // ---- batched form: persistent launches (ap_persist.cuh) ----------------------
-enum { PS_UPDATE = 0, PS_SCATTER = 1, PS_RHO = 2, PS_WA = 3, PS_FIELD = 4, PS_GATHER = 5 };
+// the persistent launches of one trial step; PS_WA is the WA launch of the
+// nets of more than 8 pins (it folds the sums), PS_WA2/4/8 those of the
+// thread-per-net buckets (2, 3-4 and 5-8 pins)
+enum { PS_UPDATE = 0, PS_SCATTER = 1, PS_RHO = 2, PS_WA = 3, PS_FIELD = 4, PS_GATHER = 5,
+       PS_WA2 = 6, PS_WA4 = 7, PS_WA8 = 8, PS_COUNT = 9 };
 
 // resident blocks of `kernel` on the whole GPU, or `fallback`
 int wave_of(const void *kernel, int threads, int fallback);
 // the grids the launchers give an instance's own launches (a persistent
 // record of the same instance runs the same blocks)
 int update_grid(const ScatterArgs &a);
-int scatter_grid(int n);
+int scatter_grid(int n, int block_nodes);
 int rho_grid(int nbins);
-int gather_grid(int n_mov);
+int gather_grid(int n_mov, int block_nodes);
 // fills bucket_blocks and small_blocks as launch_wirelength does; returns
 // the blocks of all four bucket launches
 int wa_plan(WaArgs &a);
@@ -251,8 +261,12 @@ void field_records(const FieldSolver &f, const float *d, float *ex, float *ey, F
 inline int field_rec_blocks(const FieldRec &r) { return (r.m / r.bm) * (r.m / r.bm) * r.batch; }
 
 // one persistent launch of a stage over the records `recs` (device memory)
+// with the grid persist_*_wave() (one wave of resident blocks)
+int persist_density_wave(int stage);
+int persist_wa_wave(int bucket);  // 0, 1, 2: the thread-per-net buckets; 3: the larger nets
+int persist_field_wave();
 void launch_persist_density(int stage, const PersistQueue &q, const void *recs, cudaStream_t st);
-void launch_persist_wa(const PersistQueue &q, const WaArgs *recs, cudaStream_t st);
+void launch_persist_wa(int bucket, const PersistQueue &q, const WaArgs *recs, cudaStream_t st);
 void launch_persist_field(const PersistQueue &q, const FieldRec *recs, cudaStream_t st);
 
 }  // namespace ap

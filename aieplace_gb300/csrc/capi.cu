@@ -149,6 +149,7 @@ ScatterArgs scatter_args(ap_handle *h) {
     }
     a.partials = h->d_partials;
     a.counter = h->d_counters + 3;
+    a.block_nodes = h->p.block_nodes;
     return a;
 }
 
@@ -200,6 +201,7 @@ WaArgs wa_args(ap_handle *h, const float *px, const float *py, float gamma, int 
     a.counter = h->d_counters + 0;
     a.out = out;
     a.mode = mode;
+    a.block_nets = h->p.block_nodes;
     return a;
 }
 
@@ -227,6 +229,7 @@ GatherArgs gather_args(ap_handle *h, int at, int mode) {
     a.partials = h->d_partials;
     a.counter = h->d_counters + 2;
     a.mode = mode;
+    a.block_nodes = h->p.block_nodes;
     return a;
 }
 
@@ -669,6 +672,7 @@ int ap_params_default(ap_params *p) {
     p->max_backtracks = 0;
     p->restart_mode = 4;
     p->filler_cells = 0;
+    p->block_nodes = 0;
     return AP_OK;
 }
 
@@ -1761,17 +1765,27 @@ int ap_surrogate_collect(ap_handle *h, ap_surrogate *s, int32_t n_trials, int32_
 // four records per instance (its contractions S1..S4), all instances' S1
 // first, record k + 1 of an instance depending on its record k.
 struct PersistPlan {
-    int n_rec[6] = {0, 0, 0, 0, 0, 0};
-    void *d_recs[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
-    int *d_start[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    int n_rec[PS_COUNT] = {};
+    int chunk[PS_COUNT] = {};  // blocks per work item
+    int items[PS_COUNT] = {};
+    void *d_recs[PS_COUNT] = {};
+    int *d_start[PS_COUNT] = {};
+    int *d_nblk[PS_COUNT] = {};
     int *d_dep = nullptr;
     // queue heads and the field stage's done counters, laid out so that each
-    // launch zeroes the counters of the launch before it on the stream as
-    // one range: [0] gather, [1] update, [2] scatter, [3] rho, [4] WA,
-    // [5] field, [6 ..) field done counters
+    // launch zeroes the counters of the launch before it on its stream as
+    // one range: [0] gather, [1] update, [2] scatter, [3] rho, [4..7] the
+    // four WA launches, [8] field, [9 ..) field done counters (the gather
+    // follows the field and the WA launches)
     unsigned int *d_cnt = nullptr;
     int field_bm = 0;  // 0: each instance's own tuned tile; else 32 or 64 for all
+    int item_blocks = 0;  // blocks per work item of the non-field stages; 0: the size rule
 };
+
+// Nodes per block of a batch instance's node- and net-parallel launches
+// unless its parameters set them: instances of a few thousand cells would
+// otherwise spend more on each block's sums and folds than on its nodes.
+constexpr int kBatchBlockNodes = 2048;
 
 struct ap_batch {
     std::vector<ap_handle *> inst;
@@ -1789,6 +1803,7 @@ struct ap_batch {
     unsigned long long wait_ns = 1000000000ull;
     int never_arrive = 0;
     int tuned_bm = 0;                  // the field tile the batch autotuner chose (0: not tuned)
+    int item_blocks = 0;               // blocks per work item (0: the size rule)
     float tune_ms[2] = {0.f, 0.f};     // persistent field launch with 32 / 64 tiles
 };
 
@@ -1800,15 +1815,17 @@ void batch_free_graph(ap_batch *b) {
 }
 
 void plan_free(PersistPlan &pp) {
-    for (int k = 0; k < 6; ++k) {
+    for (int k = 0; k < PS_COUNT; ++k) {
         if (pp.d_recs[k]) cudaFree(pp.d_recs[k]);
         if (pp.d_start[k]) cudaFree(pp.d_start[k]);
+        if (pp.d_nblk[k]) cudaFree(pp.d_nblk[k]);
     }
     if (pp.d_dep) cudaFree(pp.d_dep);
     if (pp.d_cnt) cudaFree(pp.d_cnt);
-    const int bm = pp.field_bm;
+    const int bm = pp.field_bm, ib = pp.item_blocks;
     pp = PersistPlan();
     pp.field_bm = bm;
+    pp.item_blocks = ib;
 }
 
 // Whether the persistent form serves every instance: the FP32 field solve,
@@ -1819,14 +1836,55 @@ bool persist_supported(const ap_batch *b) {
     return true;
 }
 
+constexpr int kFieldDone = 9;  // first field done counter in PersistPlan::d_cnt
+
+int stage_wave(int k) {
+    switch (k) {
+    case PS_WA2:
+        return persist_wa_wave(0);
+    case PS_WA4:
+        return persist_wa_wave(1);
+    case PS_WA8:
+        return persist_wa_wave(2);
+    case PS_WA:
+        return persist_wa_wave(3);
+    case PS_FIELD:
+        return persist_field_wave();
+    default:
+        return persist_density_wave(k);
+    }
+}
+
+// Blocks per work item of a stage: every stage but the field (whose items
+// are contraction tiles waited on one by one) takes about kItemsPerBlock
+// items per resident block, so that the per-item costs (queue fetch,
+// argument copy, barriers) stay small against the work.
+constexpr int kItemsPerBlock = 4;
+
+int stage_chunk(const PersistPlan &pp, int k, long long blocks) {
+    if (k == PS_FIELD) return 1;
+    if (pp.item_blocks > 0) return pp.item_blocks;
+    const long long per = (long long)kItemsPerBlock * std::max(1, stage_wave(k));
+    return (int)std::max(1ll, blocks / per);
+}
+
 template <typename T>
 int upload_stage(PersistPlan &pp, int k, const std::vector<T> &recs, const std::vector<int> &blocks) {
+    long long total = 0;
+    for (int b : blocks) total += b;
+    const int chunk = stage_chunk(pp, k, total);
     std::vector<int> start(blocks.size() + 1, 0);
-    for (size_t r = 0; r < blocks.size(); ++r) start[r + 1] = start[r] + blocks[r];
+    for (size_t r = 0; r < blocks.size(); ++r) start[r + 1] = start[r] + (blocks[r] + chunk - 1) / chunk;
     pp.n_rec[k] = (int)recs.size();
+    pp.chunk[k] = chunk;
+    pp.items[k] = start.back();
     CK(dalloc(reinterpret_cast<T **>(&pp.d_recs[k]), recs.size()));
     CK(dalloc(&pp.d_start[k], start.size()));
-    if (!recs.empty()) CK(cudaMemcpy(pp.d_recs[k], recs.data(), sizeof(T) * recs.size(), cudaMemcpyHostToDevice));
+    CK(dalloc(&pp.d_nblk[k], blocks.size()));
+    if (!recs.empty()) {
+        CK(cudaMemcpy(pp.d_recs[k], recs.data(), sizeof(T) * recs.size(), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(pp.d_nblk[k], blocks.data(), sizeof(int) * blocks.size(), cudaMemcpyHostToDevice));
+    }
     CK(cudaMemcpy(pp.d_start[k], start.data(), sizeof(int) * start.size(), cudaMemcpyHostToDevice));
     return AP_OK;
 }
@@ -1839,7 +1897,7 @@ int plan_build(ap_batch *b, PersistPlan &pp) {
     std::vector<RhoArgs> rho;
     std::vector<WaArgs> wa;
     std::vector<GatherArgs> gat;
-    std::vector<int> bu, bs, br, bw, bg;
+    std::vector<int> bu, bs, br, bg, bw[4];
     std::vector<FieldRec> fld[4];
     for (size_t i = 0; i < b->inst.size(); ++i) {
         if (!b->active[i]) continue;
@@ -1854,20 +1912,22 @@ int plan_build(ap_batch *b, PersistPlan &pp) {
         s.rho_q = h->d_mov_q;
         if (s.hi > s.lo) {
             sct.push_back(s);
-            bs.push_back(scatter_grid(s.hi - s.lo));
+            bs.push_back(scatter_grid(s.hi - s.lo, s.block_nodes));
         }
         if (h->n_fill) {
             s.lo = h->n_real;
             s.hi = h->n_mov;
             s.rho_q = h->d_fill_q;
             sct.push_back(s);
-            bs.push_back(scatter_grid(s.hi - s.lo));
+            bs.push_back(scatter_grid(s.hi - s.lo, s.block_nodes));
         }
         const RhoArgs ra = rho_args(h, RHO_LOOP, nullptr);
         rho.push_back(ra);
         br.push_back(rho_grid(ra.nbins));
         WaArgs wr = wa_args(h, h->d_px[0], h->d_py[0], 0.f, h->n_mov, WA_LOOP, nullptr);
-        bw.push_back(wa_plan(wr));
+        const int all = wa_plan(wr);
+        for (int k = 0; k < 3; ++k) bw[k].push_back(wr.bucket_blocks[k]);
+        bw[3].push_back(all - wr.small_blocks);
         wa.push_back(wr);
         FieldRec fr[4];
         field_records(h->fs, h->d_dens, h->d_ex, h->d_ey, fr);
@@ -1877,7 +1937,7 @@ int plan_build(ap_batch *b, PersistPlan &pp) {
             fld[k].push_back(fr[k]);
         }
         gat.push_back(loop_gather_args(h));
-        bg.push_back(gather_grid(h->n_mov));
+        bg.push_back(gather_grid(h->n_mov, h->p.block_nodes));
     }
     const int ni = (int)upd.size();
     if (4 * ni > kPersistMaxRecords || (int)sct.size() > kPersistMaxRecords) return AP_ERR_UNSUPPORTED;
@@ -1892,14 +1952,17 @@ int plan_build(ap_batch *b, PersistPlan &pp) {
     int r = upload_stage(pp, PS_UPDATE, upd, bu);
     if (r == AP_OK) r = upload_stage(pp, PS_SCATTER, sct, bs);
     if (r == AP_OK) r = upload_stage(pp, PS_RHO, rho, br);
-    if (r == AP_OK) r = upload_stage(pp, PS_WA, wa, bw);
+    if (r == AP_OK) r = upload_stage(pp, PS_WA2, wa, bw[0]);
+    if (r == AP_OK) r = upload_stage(pp, PS_WA4, wa, bw[1]);
+    if (r == AP_OK) r = upload_stage(pp, PS_WA8, wa, bw[2]);
+    if (r == AP_OK) r = upload_stage(pp, PS_WA, wa, bw[3]);
     if (r == AP_OK) r = upload_stage(pp, PS_FIELD, fall, bf);
     if (r == AP_OK) r = upload_stage(pp, PS_GATHER, gat, bg);
     if (r != AP_OK) return r;
     CK(dalloc(&pp.d_dep, dep.size()));
     CK(cudaMemcpy(pp.d_dep, dep.data(), sizeof(int) * dep.size(), cudaMemcpyHostToDevice));
-    CK(dalloc(&pp.d_cnt, 6 + dep.size()));
-    CK(cudaMemset(pp.d_cnt, 0, sizeof(unsigned int) * (6 + dep.size())));
+    CK(dalloc(&pp.d_cnt, kFieldDone + dep.size()));
+    CK(cudaMemset(pp.d_cnt, 0, sizeof(unsigned int) * (kFieldDone + dep.size())));
     return AP_OK;
 }
 
@@ -1907,8 +1970,11 @@ PersistQueue plan_queue(const ap_batch *b, int k, int reset_lo, int reset_n) {
     const PersistPlan &pp = b->plan;
     PersistQueue q{};
     q.start = pp.d_start[k];
+    q.nblk = pp.d_nblk[k];
     q.n_rec = pp.n_rec[k];
-    static const int head_slot[6] = {1, 2, 3, 4, 5, 0};  // PS_* -> counter slot
+    q.chunk = pp.chunk[k];
+    // PS_* -> counter slot (PersistPlan::d_cnt)
+    static const int head_slot[PS_COUNT] = {1, 2, 3, 7, 8, 0, 4, 5, 6};
     q.head = pp.d_cnt + head_slot[k];
     q.status = b->d_status;
     q.wait_ns = b->wait_ns;
@@ -1916,29 +1982,91 @@ PersistQueue plan_queue(const ap_batch *b, int k, int reset_lo, int reset_n) {
     q.n_reset = reset_n;
     if (k == PS_FIELD) {
         q.dep = pp.d_dep;
-        q.done = pp.d_cnt + 6;
+        q.done = pp.d_cnt + kFieldDone;
         q.never_arrive = b->never_arrive;
     }
     return q;
 }
 
-// One trial step of every active instance as six persistent launches: the
-// position update; the WA gradient on a second stream beside scatter ->
+// Synchronises the batch stream; AP_ERR_TIMEOUT once a persistent wait gave up.
+int batch_sync(ap_batch *b) {
+    CK(cudaStreamSynchronize(b->main));
+    if (b->d_status) {
+        unsigned int st = 0;
+        CK(cudaMemcpy(&st, b->d_status, sizeof(st), cudaMemcpyDeviceToHost));
+        if (st) return AP_ERR_TIMEOUT;
+    }
+    return AP_OK;
+}
+
+// The four WA launches of a trial (stream `st`): the thread-per-net buckets,
+// then the larger nets, whose records fold the sums.
+void enqueue_persist_wa(ap_batch *b, cudaStream_t st) {
+    const PersistPlan &pp = b->plan;
+    const int stage[4] = {PS_WA2, PS_WA4, PS_WA8, PS_WA};
+    for (int k = 0; k < 4; ++k)
+        launch_persist_wa(k, plan_queue(b, stage[k], 0, 0), static_cast<const WaArgs *>(pp.d_recs[stage[k]]), st);
+}
+
+// The gather zeroes the counters of the field and the WA launches.
+int gather_reset_n(const PersistPlan &pp) { return kFieldDone - 4 + pp.n_rec[PS_FIELD]; }
+
+// One trial step of every active instance as nine persistent launches: the
+// position update; the four WA launches on a second stream beside scatter ->
 // density/overflow -> field; the gather with each instance's accept / retry.
 int enqueue_persist(ap_batch *b, cudaStream_t st) {
     const PersistPlan &pp = b->plan;
-    const int nf = pp.n_rec[PS_FIELD];
     launch_persist_density(PS_UPDATE, plan_queue(b, PS_UPDATE, 0, 1), pp.d_recs[PS_UPDATE], st);
     CK(cudaEventRecord(b->wa_fork, st));
     CK(cudaStreamWaitEvent(b->wa_stream, b->wa_fork, 0));
-    launch_persist_wa(plan_queue(b, PS_WA, 0, 0), static_cast<const WaArgs *>(pp.d_recs[PS_WA]), b->wa_stream);
+    enqueue_persist_wa(b, b->wa_stream);
     CK(cudaEventRecord(b->wa_join, b->wa_stream));
     launch_persist_density(PS_SCATTER, plan_queue(b, PS_SCATTER, 1, 1), pp.d_recs[PS_SCATTER], st);
     launch_persist_density(PS_RHO, plan_queue(b, PS_RHO, 2, 1), pp.d_recs[PS_RHO], st);
     launch_persist_field(plan_queue(b, PS_FIELD, 3, 1), static_cast<const FieldRec *>(pp.d_recs[PS_FIELD]), st);
     CK(cudaStreamWaitEvent(st, b->wa_join, 0));
-    launch_persist_density(PS_GATHER, plan_queue(b, PS_GATHER, 4, 2 + nf), pp.d_recs[PS_GATHER], st);
+    launch_persist_density(PS_GATHER, plan_queue(b, PS_GATHER, 4, gather_reset_n(pp)), pp.d_recs[PS_GATHER], st);
     return cudaGetLastError() == cudaSuccess ? AP_OK : AP_ERR_CUDA;
+}
+
+// n_trials trial steps of the persistent form as eager launches, the WA
+// launches between the update and the scatter on the same stream, with
+// events around each stage: the mean milliseconds of each (update, scatter,
+// rho, WA -- its four launches --, field, gather) in ms[6].
+int persist_profile(ap_batch *b, int n_trials, float *ms) {
+    const PersistPlan &pp = b->plan;
+    cudaEvent_t ev[7];
+    for (cudaEvent_t &e : ev) CK(cudaEventCreate(&e));
+    double acc[6] = {0, 0, 0, 0, 0, 0};
+    int r = AP_OK;
+    cudaStream_t st = b->main;
+    for (int t = 0; t < n_trials && r == AP_OK; ++t) {
+        CK(cudaEventRecord(ev[0], st));
+        launch_persist_density(PS_UPDATE, plan_queue(b, PS_UPDATE, 0, 1), pp.d_recs[PS_UPDATE], st);
+        CK(cudaEventRecord(ev[1], st));
+        enqueue_persist_wa(b, st);
+        CK(cudaEventRecord(ev[2], st));
+        launch_persist_density(PS_SCATTER, plan_queue(b, PS_SCATTER, 1, 1), pp.d_recs[PS_SCATTER], st);
+        CK(cudaEventRecord(ev[3], st));
+        launch_persist_density(PS_RHO, plan_queue(b, PS_RHO, 2, 1), pp.d_recs[PS_RHO], st);
+        CK(cudaEventRecord(ev[4], st));
+        launch_persist_field(plan_queue(b, PS_FIELD, 3, 1), static_cast<const FieldRec *>(pp.d_recs[PS_FIELD]), st);
+        CK(cudaEventRecord(ev[5], st));
+        launch_persist_density(PS_GATHER, plan_queue(b, PS_GATHER, 4, gather_reset_n(pp)), pp.d_recs[PS_GATHER],
+                               st);
+        CK(cudaEventRecord(ev[6], st));
+        r = batch_sync(b);
+        // the events around each stage, in the order update, scatter, rho, WA, field, gather
+        const int from[6] = {0, 2, 3, 1, 4, 5};
+        for (int k = 0; k < 6 && r == AP_OK; ++k) {
+            float v = 0.f;
+            cudaEventElapsedTime(&v, ev[from[k]], ev[from[k] + 1]);
+            acc[k] += v;
+        }
+    }
+    for (cudaEvent_t &e : ev) cudaEventDestroy(e);
+    for (int k = 0; k < 6; ++k) ms[k] = n_trials > 0 ? (float)(acc[k] / n_trials) : 0.f;
+    return r;
 }
 
 // One graph: fork from the main stream to every active instance's stream,
@@ -1977,17 +2105,6 @@ int batch_build_graph(ap_batch *b) {
     return ei == cudaSuccess ? AP_OK : AP_ERR_CUDA;
 }
 
-// Synchronises the batch stream; AP_ERR_TIMEOUT once a persistent wait gave up.
-int batch_sync(ap_batch *b) {
-    CK(cudaStreamSynchronize(b->main));
-    if (b->d_status) {
-        unsigned int st = 0;
-        CK(cudaMemcpy(&st, b->d_status, sizeof(st), cudaMemcpyDeviceToHost));
-        if (st) return AP_ERR_TIMEOUT;
-    }
-    return AP_OK;
-}
-
 // Tile autotuner of the persistent field launch: every active instance's
 // four contractions with 32 x 32 and with 64 x 64 tiles (instances whose
 // grid is not a multiple of 64 keep 32), 2 warm and 5 timed launches each on
@@ -2008,7 +2125,8 @@ int batch_tune_field(ap_batch *b) {
         for (int t = 0; t < 7 && r == AP_OK; ++t) {
             if (t == 2 && cudaEventRecord(e0, b->main) != cudaSuccess) r = AP_ERR_CUDA;
             // zero the field counters the way the launch before it would
-            if (cudaMemsetAsync(b->plan.d_cnt + 5, 0, sizeof(unsigned int) * (1 + nf), b->main) != cudaSuccess)
+            if (cudaMemsetAsync(b->plan.d_cnt + kFieldDone - 1, 0, sizeof(unsigned int) * (1 + nf), b->main) !=
+                cudaSuccess)
                 r = AP_ERR_CUDA;
             launch_persist_field(plan_queue(b, PS_FIELD, 3, 0),
                                  static_cast<const FieldRec *>(b->plan.d_recs[PS_FIELD]), b->main);
@@ -2039,6 +2157,7 @@ int ap_create_batch(int32_t n, const ap_netlist *netlists, const ap_params *para
     for (int i = 0; i < n && r == AP_OK; ++i) {
         ap_params p = params[i];
         p.use_graph = 0;  // the batch graph replaces the per-instance graphs
+        if (p.block_nodes <= 0) p.block_nodes = kBatchBlockNodes;
         ap_handle *h = nullptr;
         r = ap_create(&netlists[i], &p, &h);
         if (r == AP_OK) b->inst.push_back(h);
@@ -2113,8 +2232,30 @@ int ap_batch_get_info(ap_batch *b, ap_batch_info *info) {
     info->field_tile = b->tuned_bm;
     info->field_tune_ms[0] = b->tune_ms[0];
     info->field_tune_ms[1] = b->tune_ms[1];
-    for (int k = 0; k < 6; ++k) info->records[k] = b->plan.n_rec[k];
+    for (int k = 0; k < 6; ++k) {  // the WA entry: the launch of the larger nets; its items: all four launches'
+        info->records[k] = b->plan.n_rec[k];
+        info->item_blocks[k] = b->plan.chunk[k];
+        info->items[k] = b->plan.items[k] + (k == PS_WA ? b->plan.items[PS_WA2] + b->plan.items[PS_WA4] +
+                                                              b->plan.items[PS_WA8]
+                                                        : 0);
+    }
     return AP_OK;
+}
+
+int ap_batch_set_item_blocks(ap_batch *b, int32_t blocks) {
+    if (!b || blocks < 0 || blocks > 4096) return AP_ERR_INVALID_ARG;
+    CK(cudaStreamSynchronize(b->main));
+    b->item_blocks = blocks;
+    b->plan.item_blocks = blocks;
+    return b->graph ? batch_build_graph(b) : AP_OK;
+}
+
+int ap_batch_profile(ap_batch *b, int32_t n_trials, float *stage_ms) {
+    if (!b || n_trials <= 0 || !stage_ms) return AP_ERR_INVALID_ARG;
+    if (b->form != AP_BATCH_PERSISTENT) return AP_ERR_UNSUPPORTED;
+    if (!b->graph) return AP_ERR_STATE;
+    CK(cudaStreamSynchronize(b->main));
+    return persist_profile(b, n_trials, stage_ms);
 }
 
 int ap_batch_debug_inject(ap_batch *b, int32_t kind, int64_t wait_ns) {

@@ -63,7 +63,8 @@ __device__ __forceinline__ double block_max_f(float v, double *smem) {
 //      nodes of a warp that skipped step 2), and the rest straight to the
 //      map (red.global.add).  The window is held in kWinCopies copies, lane
 //      l adding to copy l % kWinCopies, so that lanes whose nodes share a bin
-//      collide on one shared address less often;
+//      collide on one shared address less often; blocks of fewer than
+//      kWinMinNodes nodes (small instances) add the rest straight to the map;
 //   4. sums the tile over the block (shuffles, then shared memory) and adds
 //      its kTile^2 bins to the map once, and the window's non-zero bins
 //      (the copies summed).
@@ -73,6 +74,7 @@ constexpr int kTile = 6;
 constexpr int kTileMinLanes = 16;
 constexpr int kWin = 32;
 constexpr int kWinCopies = 4;
+constexpr int kWinMinNodes = 2048;
 constexpr int kScatterThreads = 256;
 
 // A node's contribution as a record of 5 int32: the base bin (c0, r0), the
@@ -294,9 +296,13 @@ __device__ __forceinline__ void scatter_body(const ScatterArgs &a, VBlock vb) {
     const int mr = tot ? (int)((2 * sums[1] + tot) / (2 * tot)) : 0;
     const int tc0 = min(max(mc - kTile / 2, 0), g.mx - kTile), tr0 = min(max(mr - kTile / 2, 0), g.my - kTile);
     const int bw = (int)g.bw_q, bh = (int)g.bh_q;  // record arithmetic is int32 (checked at record time)
-    // the window: kWin x kWin bins (or the whole grid, if smaller) about the mean
-    const int wcn = min(kWin, g.mx), wrn = min(kWin, g.my);
-    const int wc0 = min(max(mc - wcn / 2, 0), g.mx - wcn), wr0 = min(max(mr - wrn / 2, 0), g.my - wrn);
+    // the window: kWin x kWin bins (or the whole grid, if smaller) about the
+    // mean, for ranges of at least kWinMinNodes nodes (uniform; below that
+    // its clearing and flush cost more than the reductions it saves)
+    const bool use_win = r_hi - r_lo >= kWinMinNodes;
+    const int wcn = use_win ? min(kWin, g.mx) : 0, wrn = use_win ? min(kWin, g.my) : 0;
+    const int wc0 = use_win ? min(max(mc - wcn / 2, 0), g.mx - wcn) : 0;
+    const int wr0 = use_win ? min(max(mr - wrn / 2, 0), g.my - wrn) : 0;
     const int wsz = wcn * wrn;
     for (int t = tid; t < kWinCopies * wsz; t += kScatterThreads) win[t] = 0ull;
     __syncthreads();
@@ -452,7 +458,8 @@ int update_grid(const ScatterArgs &a) {
         if (wave > 8192) wave = 1216;
     }
     const int n = a.upd_hi > 0 ? a.upd_hi - a.upd_lo : a.n_mov;
-    int ub = (n + kThreads - 1) / kThreads;
+    const int per = a.block_nodes > kThreads ? a.block_nodes : kThreads;
+    int ub = (n + per - 1) / per;
     if (ub > wave) ub = wave;
     if (ub < 1) ub = 1;  // an empty chunk still writes its partials (zero) and may fold
     return ub;
@@ -465,12 +472,13 @@ int launch_update(const ScatterArgs &a, cudaStream_t st) {
     return ub;
 }
 
-int scatter_grid(int n) {
+int scatter_grid(int n, int block_nodes) {
     // one wave of resident blocks, each a contiguous range of nodes (fewer
     // blocks: fewer tile flushes onto the dense core's bins)
     static int wave = 0;
     if (wave <= 0) wave = wave_of((const void *)scatter_kernel, kScatterThreads, 304);
-    int blocks = (n + kScatterThreads - 1) / kScatterThreads;
+    const int per = block_nodes > kScatterThreads ? block_nodes : kScatterThreads;
+    int blocks = (n + per - 1) / per;
     if (blocks > wave) blocks = wave;
     return blocks < 1 ? 1 : blocks;
 }
@@ -478,7 +486,7 @@ int scatter_grid(int n) {
 void launch_scatter_bins(const ScatterArgs &a, cudaStream_t st) {
     const int n = a.hi - a.lo;
     if (n <= 0) return;
-    scatter_kernel<<<scatter_grid(n), kScatterThreads, 0, st>>>(a);
+    scatter_kernel<<<scatter_grid(n, a.block_nodes), kScatterThreads, 0, st>>>(a);
 }
 
 void launch_scatter(const ScatterArgs &a, cudaStream_t st) {
@@ -899,7 +907,7 @@ __global__ void __launch_bounds__(kThreads, 4) gather_kernel(GatherArgs a) {
     if (arrive_last(a.counter, gridDim.x)) gather_fold(a, gridDim.x);
 }
 
-int gather_grid(int n_mov) {
+int gather_grid(int n_mov, int block_nodes) {
     // one wave of resident blocks, grid-stride beyond: 61 -> 50 us at 2M
     // nodes against 4096 blocks (a partial last wave, 912 blocks, 59 us)
     static int wave = 0;
@@ -907,13 +915,14 @@ int gather_grid(int n_mov) {
         wave = wave_of((const void *)gather_kernel, kThreads, 608);
         if (wave > kGatherMaxBlocks) wave = 608;
     }
-    int blocks = (n_mov + kThreads - 1) / kThreads;
+    const int per = block_nodes > kThreads ? block_nodes : kThreads;
+    int blocks = (n_mov + per - 1) / per;
     if (blocks > wave) blocks = wave;
     return blocks < 1 ? 1 : blocks;
 }
 
 void launch_gather(const GatherArgs &a, cudaStream_t st) {
-    gather_kernel<<<gather_grid(a.n_mov), kThreads, 0, st>>>(a);
+    gather_kernel<<<gather_grid(a.n_mov, a.block_nodes), kThreads, 0, st>>>(a);
 }
 
 // Bin records of movable nodes at given positions, as update_kernel writes
@@ -1025,24 +1034,40 @@ __global__ void __launch_bounds__(kThreads, 4) persist_gather_kernel(PersistQueu
     });
 }
 
-void launch_persist_density(int stage, const PersistQueue &q, const void *recs, cudaStream_t st) {
+int persist_density_wave(int stage) {
     static int waves[4] = {0, 0, 0, 0};
     switch (stage) {
     case PS_UPDATE:
         if (!waves[0]) waves[0] = wave_of((const void *)persist_update_kernel, kThreads, 1216);
-        persist_update_kernel<<<waves[0], kThreads, 0, st>>>(q, static_cast<const ScatterArgs *>(recs));
-        break;
+        return waves[0];
     case PS_SCATTER:
         if (!waves[1]) waves[1] = wave_of((const void *)persist_scatter_kernel, kScatterThreads, 304);
-        persist_scatter_kernel<<<waves[1], kScatterThreads, 0, st>>>(q, static_cast<const ScatterArgs *>(recs));
-        break;
+        return waves[1];
     case PS_RHO:
         if (!waves[2]) waves[2] = wave_of((const void *)persist_rho_kernel, kThreads, 1216);
-        persist_rho_kernel<<<waves[2], kThreads, 0, st>>>(q, static_cast<const RhoArgs *>(recs));
-        break;
+        return waves[2];
     case PS_GATHER:
         if (!waves[3]) waves[3] = wave_of((const void *)persist_gather_kernel, kThreads, 608);
-        persist_gather_kernel<<<waves[3], kThreads, 0, st>>>(q, static_cast<const GatherArgs *>(recs));
+        return waves[3];
+    default:
+        return 0;
+    }
+}
+
+void launch_persist_density(int stage, const PersistQueue &q, const void *recs, cudaStream_t st) {
+    const int w = persist_density_wave(stage);
+    switch (stage) {
+    case PS_UPDATE:
+        persist_update_kernel<<<w, kThreads, 0, st>>>(q, static_cast<const ScatterArgs *>(recs));
+        break;
+    case PS_SCATTER:
+        persist_scatter_kernel<<<w, kScatterThreads, 0, st>>>(q, static_cast<const ScatterArgs *>(recs));
+        break;
+    case PS_RHO:
+        persist_rho_kernel<<<w, kThreads, 0, st>>>(q, static_cast<const RhoArgs *>(recs));
+        break;
+    case PS_GATHER:
+        persist_gather_kernel<<<w, kThreads, 0, st>>>(q, static_cast<const GatherArgs *>(recs));
         break;
     default:
         break;

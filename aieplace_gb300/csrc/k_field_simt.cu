@@ -291,10 +291,14 @@ __global__ void __launch_bounds__(256) persist_field_kernel(PersistQueue q, cons
     });
 }
 
-void launch_persist_field(const PersistQueue &q, const FieldRec *recs, cudaStream_t st) {
+int persist_field_wave() {
     static int wave = 0;
     if (!wave) wave = wave_of((const void *)persist_field_kernel, 256, 608);
-    persist_field_kernel<<<wave, 256, 0, st>>>(q, recs);
+    return wave;
+}
+
+void launch_persist_field(const PersistQueue &q, const FieldRec *recs, cudaStream_t st) {
+    persist_field_kernel<<<persist_field_wave(), 256, 0, st>>>(q, recs);
 }
 
 // Tile autotuner of the FP32 path: times a full solve with 32 and with 64

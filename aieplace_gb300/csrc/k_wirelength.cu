@@ -400,8 +400,9 @@ __global__ void __launch_bounds__(kThreads, 4) wa_large_kernel(WaArgs a) {
 }
 
 int wa_plan(WaArgs &a) {
-    auto grid = [](int items) {
-        int b = (items + kThreads - 1) / kThreads;
+    const int per = a.block_nets > kThreads ? a.block_nets : kThreads;
+    auto grid = [per](int items) {
+        int b = (items + per - 1) / per;
         return b < 1 ? 1 : (b > kWaMaxBlocks ? kWaMaxBlocks : b);
     };
     for (int b = 0; b < 3; ++b) a.bucket_blocks[b] = grid(a.bucket_lo[b + 1] - a.bucket_lo[b]);
@@ -440,27 +441,49 @@ void launch_wirelength(const WaArgs &a0, cudaStream_t st) {
     wa_large_kernel<<<large, kThreads, 0, st>>>(a);
 }
 
-// The batched form: one record per instance holding the blocks of its four
-// bucket launches in launch order; the record's last block folds the sums.
-__global__ void __launch_bounds__(kThreads, 3) persist_wa_kernel(PersistQueue q, const WaArgs *recs) {
+// The batched form: the four bucket launches of every instance as four
+// persistent launches (one record per instance each; registers sized per
+// bucket as in the instance's own launches); the last one folds each
+// instance's sums in the record's last block, after the other three ended.
+template <int D, int B>
+__global__ void __launch_bounds__(kThreads, D == 8 ? 3 : 4) persist_wa_small_kernel(PersistQueue q, const WaArgs *recs) {
+    persist_loop(q, recs, [](const WaArgs &a, VBlock vb, int) { wa_small_body<D, B>(a, vb); });
+}
+
+__global__ void __launch_bounds__(kThreads, 4) persist_wa_large_kernel(PersistQueue q, const WaArgs *recs) {
     persist_loop(q, recs, [](const WaArgs &a, VBlock vb, int) {
-        const int b0 = a.bucket_blocks[0], b1 = a.bucket_blocks[1], b2 = a.bucket_blocks[2];
-        if (vb.id < b0)
-            wa_small_body<2, 0>(a, VBlock{vb.id, b0});
-        else if (vb.id < b0 + b1)
-            wa_small_body<4, 1>(a, VBlock{vb.id - b0, b1});
-        else if (vb.id < a.small_blocks)
-            wa_small_body<8, 2>(a, VBlock{vb.id - b0 - b1, b2});
-        else
-            wa_large_body(a, VBlock{vb.id - a.small_blocks, vb.n - a.small_blocks});
-        if (arrive_last(a.counter, vb.n)) wa_fold(a, vb.n);
+        wa_large_body(a, vb);
+        if (arrive_last(a.counter, vb.n)) wa_fold(a, a.small_blocks + vb.n);
     });
 }
 
-void launch_persist_wa(const PersistQueue &q, const WaArgs *recs, cudaStream_t st) {
-    static int wave = 0;
-    if (!wave) wave = wave_of((const void *)persist_wa_kernel, kThreads, 1216);
-    persist_wa_kernel<<<wave, kThreads, 0, st>>>(q, recs);
+int persist_wa_wave(int bucket) {
+    static int waves[4] = {0, 0, 0, 0};
+    if (bucket < 0 || bucket > 3) return 0;
+    if (!waves[bucket]) {
+        const void *k[4] = {(const void *)persist_wa_small_kernel<2, 0>, (const void *)persist_wa_small_kernel<4, 1>,
+                            (const void *)persist_wa_small_kernel<8, 2>, (const void *)persist_wa_large_kernel};
+        waves[bucket] = wave_of(k[bucket], kThreads, 1216);
+    }
+    return waves[bucket];
+}
+
+void launch_persist_wa(int bucket, const PersistQueue &q, const WaArgs *recs, cudaStream_t st) {
+    const int w = persist_wa_wave(bucket);
+    switch (bucket) {
+    case 0:
+        persist_wa_small_kernel<2, 0><<<w, kThreads, 0, st>>>(q, recs);
+        break;
+    case 1:
+        persist_wa_small_kernel<4, 1><<<w, kThreads, 0, st>>>(q, recs);
+        break;
+    case 2:
+        persist_wa_small_kernel<8, 2><<<w, kThreads, 0, st>>>(q, recs);
+        break;
+    default:
+        persist_wa_large_kernel<<<w, kThreads, 0, st>>>(q, recs);
+        break;
+    }
 }
 
 }  // namespace ap

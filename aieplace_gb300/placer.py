@@ -219,7 +219,7 @@ class Placer:
 
 class BatchPlacer:
     """Independent placements stepped together (ap_create_batch): one CUDA
-    graph launch advances one trial step of every active instance, as six
+    graph launch advances one trial step of every active instance, as nine
     persistent launches over all instances ("persistent", the default where
     it serves every instance) or as every instance's own launches in
     parallel branches ("graph")."""
@@ -291,6 +291,16 @@ class BatchPlacer:
 
     def set_form(self, form: str):
         check("ap_batch_set_form", lib().ap_batch_set_form(self._h, {"graph": 0, "persistent": 1}[form]))
+
+    def set_item_blocks(self, blocks: int):
+        check("ap_batch_set_item_blocks", lib().ap_batch_set_item_blocks(self._h, int(blocks)))
+
+    def profile(self, n_trials: int = 10) -> dict:
+        """Mean ms per persistent launch over n_trials eager trial steps
+        (they advance the instances)."""
+        ms = np.zeros(6, np.float32)
+        check("ap_batch_profile", lib().ap_batch_profile(self._h, int(n_trials), ptr(ms)))
+        return dict(zip(("update", "scatter", "rho", "wa", "field", "gather"), [float(v) for v in ms]))
 
     def info(self) -> dict:
         b = BatchInfo()

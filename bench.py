@@ -257,7 +257,7 @@ def profile_mode(args):
 def batch_mode(args):
     """Batched form: n instances (cell counts LogUniform[5k, 150k], bins 128..512,
     FP32) stepped together.  Reports instance-iterations per second over K
-    graph launches for the persistent form (six persistent launches per trial
+    graph launches for the persistent form (nine persistent launches per trial
     step over all instances, the default) and for the graph of per-instance
     branches, the wall time until every instance is below 10% overflow, and
     the instances stepped one after another on their own graphs."""
@@ -283,6 +283,17 @@ def batch_mode(args):
             el = time.perf_counter() - t0
             it1 = sum(bp.stats(i)["iteration"] for i in range(bp.n))
             info = bp.info()
+            stage_ms = bp.profile(10) if form == "persistent" else None
+            one_block = None
+            if form == "persistent":
+                # the same launches with one block per work item
+                bp.set_item_blocks(1)
+                bp.step(args.warmup)
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                bp.step(args.steps)
+                one_block = {"graph_launch_ms": 1000 * (time.perf_counter() - t0) / args.steps,
+                             "stage_ms": bp.profile(10), "info": bp.info()}
         with ap.BatchPlacer(nls, max_iterations=4000, check_interval=32) as bp:
             bp.set_form(form)
             bp.initialize_placement(seed=5, sigma=1.0)
@@ -298,6 +309,9 @@ def batch_mode(args):
         forms[form] = {"instance_iters_per_s": (it1 - it0) / el, "graph_launch_ms": 1000 * el / args.steps,
                        "time_to_10pct_all_s": ttt, "iterations": its, "reached": sum(o < 0.10 for o in over),
                        "not_reached": missed, "info": info}
+        if stage_ms:
+            forms[form]["stage_ms"] = stage_ms
+            forms[form]["one_block_per_item"] = one_block
     # the same instances one after another, each on its own graph
     t0 = time.perf_counter()
     seq_its = 0

@@ -92,6 +92,10 @@ typedef struct ap_params {
                                    the mean width x height of the cells between the 10th and 90th area
                                    percentile; they are in the density the field sees, not in the overflow,
                                    and never appear in positions passed in or out */
+    int32_t block_nodes;        /* nodes (nets) per block of the node- and net-parallel launches, at least;
+                                   0 = one per thread, the GPU filled by one instance (the batched form
+                                   uses 2048 when 0).  Results depend on it only through the order of
+                                   FP32 block sums */
 } ap_params;
 
 /* Per-iteration readout; the fields of printIterationResults (AIEplace.cpp:1048-1070)
@@ -290,10 +294,11 @@ int ap_restore(ap_handle *h, const void *buf, size_t bytes);
  * design per run (Placer::run, AIEplace.cpp:44-76); small designs cannot fill
  * a GB300 alone, so a batch advances every active instance by one trial step
  * per launch of one CUDA graph, in one of two forms:
- *   AP_BATCH_PERSISTENT  six persistent kernels per trial step, one per stage
- *                        (position update, WA gradient, bin scatter,
- *                        density/overflow, field solve, gather), each over all
- *                        instances: its resident blocks pull (instance, block)
+ *   AP_BATCH_PERSISTENT  nine persistent kernels per trial step, one per stage
+ *                        (position update, four WA launches by net degree, bin
+ *                        scatter, density/overflow, field solve, gather), each
+ *                        over all instances: its resident blocks pull
+ *                        (instance, block)
  *                        work items off a device queue, so instances of uneven
  *                        size share the GPU; the field solve's four
  *                        contractions of an instance wait on one another
@@ -312,6 +317,8 @@ typedef struct {
     int32_t field_tile;          /* persistent form: field tile of the autotuner (32 or 64; 0 = not tuned) */
     float field_tune_ms[2];      /* its measured field launch with 32 and with 64 tiles */
     int32_t records[6];          /* work records per persistent launch: update, scatter, rho, WA, field, gather */
+    int32_t item_blocks[6];      /* blocks of a record's own launch per work item */
+    int32_t items[6];            /* work items per persistent launch */
 } ap_batch_info;
 
 int ap_create_batch(int32_t n, const ap_netlist *netlists, const ap_params *params, ap_batch **out);
@@ -332,8 +339,18 @@ int ap_batch_get_positions(ap_batch *b, int32_t i, float *x, float *y);
  * every instance); takes effect at the next step */
 int ap_batch_set_form(ap_batch *b, int32_t form);
 int ap_batch_get_info(ap_batch *b, ap_batch_info *info);
+/* persistent form: blocks of a record's own launch per work item of the
+ * non-field stages (1 .. 4096); 0 (the default) sizes them so that each
+ * launch has about four items per resident block.  Results do not depend on
+ * it. */
+int ap_batch_set_item_blocks(ap_batch *b, int32_t blocks);
+/* persistent form: n_trials trial steps (they advance the instances) as
+ * eager launches with events around each; stage_ms[6] receives the mean
+ * milliseconds of the update, scatter, rho, WA, field and gather launches
+ * (the WA launch then runs alone, not beside the density chain) */
+int ap_batch_profile(ap_batch *b, int32_t n_trials, float *stage_ms);
 /* Failure injection (persistent form): AP_FAULT_NEVER_ARRIVE makes every
- * dependency wait of the field launch wait for one block more than the
+ * dependency wait of the field launch wait for one work item more than the
  * awaited contraction has, bounded by wait_ns (1 ms .. 2 s): the first wait
  * runs out, the launch's remaining items skip their work, the launch ends,
  * and ap_batch_step / ap_batch_run return AP_ERR_TIMEOUT.  The instances'

@@ -1,8 +1,8 @@
 """The batched form (ap_create_batch).
 
-Both forms -- six persistent launches over all instances, and every
+Both forms -- nine persistent launches over all instances, and every
 instance's own launches as parallel graph branches -- give, bit for bit,
-what each instance gives when stepped alone (the single-instance loop is
+what each instance gives when stepped alone with the same parameters (the single-instance loop is
 itself checked against the FP64 oracle in test_gpu_parity*.py), with
 instances of uneven size and grid, and with filler cells (two scatter records
 per instance).  The persistent field launch's dependency waits are bounded:
@@ -42,9 +42,10 @@ def small_batch(ap, n=3, lo=3000, hi=12000, seed=4):
 
 
 def singles(ap, nls, trials, seed, **kw):
+    """Each instance alone, with the batch's grid policy (2048 nodes per block)."""
     out = []
     for i, nl in enumerate(nls):
-        with ap.Placer(nl, **kw) as pl:
+        with ap.Placer(nl, block_nodes=2048, **kw) as pl:
             pl.initialize_placement(seed=seed + i, sigma=1.0)
             pl.step_async(trials)
             out.append((pl.positions(), pl.stats()))
@@ -86,6 +87,26 @@ def test_persistent_uneven_instances_with_fillers(ap):
         np.testing.assert_array_equal(bx, x)
         np.testing.assert_array_equal(by, y)
         assert bs["hpwl"] == s["hpwl"] and bs["overflow"] == s["overflow"]
+
+
+@pytest.mark.parametrize("item_blocks", [3, 64])
+def test_persistent_items_of_several_blocks(ap, item_blocks):
+    """Work items of several of a record's blocks (3; 64 -- more than most
+    records have) give the same results; the stage profile times all six."""
+    nls = small_batch(ap, n=4, lo=2000, hi=150000, seed=10)
+    with ap.BatchPlacer(nls) as b:
+        b.set_item_blocks(item_blocks)
+        b.initialize_placement(seed=70, sigma=1.0)
+        b.step(12)
+        prof = b.profile(3)  # 3 more trial steps
+        batch = [(b.positions(i), b.stats(i)) for i in range(len(nls))]
+        info = b.info()
+    assert all(v > 0 for v in prof.values()), prof
+    assert info["item_blocks"]["update"] == item_blocks and info["item_blocks"]["field"] == 1
+    for ((bx, by), bs), ((x, y), s) in zip(batch, singles(ap, nls, 15, 70)):
+        np.testing.assert_array_equal(bx, x)
+        np.testing.assert_array_equal(by, y)
+        assert bs["hpwl"] == s["hpwl"]
 
 
 def test_batch_run_reaches_targets(ap):
