@@ -232,8 +232,9 @@ void launch_split_bf16(int n, const float *src, __nv_bfloat16 *hi, __nv_bfloat16
 enum { PS_UPDATE = 0, PS_SCATTER = 1, PS_RHO = 2, PS_WA = 3, PS_FIELD = 4, PS_GATHER = 5,
        PS_WA2 = 6, PS_WA4 = 7, PS_WA8 = 8, PS_COUNT = 9 };
 
-// resident blocks of `kernel` on the whole GPU, or `fallback`
-int wave_of(const void *kernel, int threads, int fallback);
+// resident blocks of `kernel` on the whole GPU (dyn_smem bytes of dynamic
+// shared memory per block), or `fallback`
+int wave_of(const void *kernel, int threads, int fallback, int dyn_smem = 0);
 // the grids the launchers give an instance's own launches (a persistent
 // record of the same instance runs the same blocks)
 int update_grid(const ScatterArgs &a);

@@ -14,6 +14,8 @@
 //                  reference moves by a fixed learning rate instead.
 #include <math.h>
 
+#include <algorithm>
+
 #include "ap_common.cuh"
 #include "ap_kernels.h"
 #include "ap_persist.cuh"
@@ -41,40 +43,36 @@ __device__ __forceinline__ double block_max_f(float v, double *smem) {
 }  // namespace
 
 // The density scatter.  A node adds ow(c) * oh(r) to every bin (c, r) it
-// overlaps, ow and oh its fixed-point overlaps with column c and row r, so
-// a set of nodes adds a sum of outer products.  Right after the initial
-// placement -- for hundreds of iterations of the 2M-cell workload -- most
-// nodes sit in a dense core a few bins across (up to ~450k nodes in one
-// bin), where atomic adds to the map collide; later they spread over the die,
-// where plain global reductions run at the L2's rate (measured on GB300:
-// 4.5M int64 reductions to spread addresses in ~23 us, 428 us when they
-// crowd into a few bins).  Each block therefore takes a contiguous range of
-// nodes and:
-//   1. finds the mean base bin of its range and puts a kTile x kTile bin tile
-//      there;
-//   2. accumulates every node whose bins all lie inside the tile into int64
-//      registers as the outer product ow x oh (kTile^2 multiply-adds, no
-//      atomics, no lane matching); a warp runs this only when at least
-//      kTileMinLanes of its lanes have such a node, since the multiply-adds
-//      cost the same for 1 lane as for 32;
-//   3. adds the bins of every other node inside a kWin x kWin bin window
-//      about the same mean bin to the window in shared memory
-//      (red.shared.add: the nodes just outside the dense core, and the tile's
-//      nodes of a warp that skipped step 2), and the rest straight to the
-//      map (red.global.add).  The window is held in kWinCopies copies, lane
-//      l adding to copy l % kWinCopies, so that lanes whose nodes share a bin
-//      collide on one shared address less often; blocks of fewer than
-//      kWinMinNodes nodes (small instances) add the rest straight to the map;
-//   4. sums the tile over the block (shuffles, then shared memory) and adds
-//      its kTile^2 bins to the map once, and the window's non-zero bins
-//      (the copies summed).
-// All sums are integers, so the map is the same bit for bit whatever the
-// path or the order (and equal to or_density_q).
-constexpr int kTile = 6;
-constexpr int kTileMinLanes = 16;
-constexpr int kWin = 32;
-constexpr int kWinCopies = 4;
+// overlaps, ow and oh its fixed-point overlaps with column c and row r.
+// Right after the initial placement -- for hundreds of iterations of the
+// 2M-cell workload -- most nodes sit in a dense core a few bins across (up
+// to ~450k nodes in one bin), where atomic adds to the map collide; later
+// they spread over the die, where plain global reductions run at the L2's
+// rate (measured on GB300: 4.5M int64 reductions to spread addresses in
+// ~23 us, 428 us when they crowd into a few bins).  Each block therefore
+// takes a contiguous range of nodes, finds the mean base bin of a sample of
+// the range (its first node per thread) and counts the sample's nodes inside
+// a kCoreT x kCoreT tile and a kWinT x kWinT window about it; then,
+// uniformly over the block:
+//   * 85% or more in the core: the core tile in shared memory, kCoreC copies
+//     (lane l adds to copy l % kCoreC, so a warp's lanes hitting the same
+//     bin do not collide);
+//   * else half or more in the window (ranges of kWinMinNodes or more): the window
+//     in shared memory, kWinC copies;
+//   * else no tile.
+// Nodes inside the tile add to it (red.shared.add.u64), the rest straight to
+// the map (red.global.add); at the end each tile bin's copies are summed and
+// the non-zero bins added to the map once.  Copy k of bin e sits at
+// [k t^2 + e].  All sums are integers, so the map is the same bit for bit
+// whatever the path or the order (and equal to or_density_q).
+constexpr int kCoreT = 8;
+constexpr int kCoreC = 32;
+constexpr int kWinT = 32;
+constexpr int kWinC = 8;
 constexpr int kWinMinNodes = 2048;
+// dynamic shared memory of the scatter: the larger of the two tiles
+constexpr int kScatterSmem = 8 * (kCoreT * kCoreT * kCoreC > kWinT * kWinT * kWinC ? kCoreT * kCoreT * kCoreC
+                                                                                  : kWinT * kWinT * kWinC);
 constexpr int kScatterThreads = 256;
 
 // A node's contribution as a record of 5 int32: the base bin (c0, r0), the
@@ -249,82 +247,107 @@ __global__ void __launch_bounds__(kThreads) update_kernel(ScatterArgs a) {
     if (arrive_last(a.counter, gridDim.x)) update_fold(a, a.part_base + (int)gridDim.x);
 }
 
+// Per block: the shared tile's shape and place, from where the block's
+// nodes lie (uniform over the block).
+struct TileShape {
+    int t, c;       // t x t bins, c copies; t == 0: no tile (every add to the map)
+    int c0, r0;     // the tile's first column and row
+    int n, m;       // its bins inside the grid (t, or fewer at a small grid)
+};
+
+// The non-zero bins of the shared tile (copy k of bin e at [k t^2 + e])
+// into the map, a thread per bin.
+__device__ __forceinline__ void flush_tile(const ull *acc, const TileShape &s, const Grid &g, ull *map) {
+    const int tt = s.t * s.t;
+    for (int e = threadIdx.x; e < tt; e += kScatterThreads) {
+        ull v = 0ull;
+        for (int k = 0; k < s.c; ++k) v += acc[k * tt + e];
+        const int u = e / s.t, w = e - u * s.t;
+        if (v && u < s.n && w < s.m) atomicAdd(map + (long long)(s.c0 + u) * g.my + s.r0 + w, v);
+    }
+}
+
+// The bin adds of nodes [lo, hi) split into vb.n contiguous ranges; this
+// block takes range vb.id.  Dynamic shared memory: kScatterSmem bytes.
 __device__ __forceinline__ void scatter_body(const ScatterArgs &a, VBlock vb) {
-    __shared__ long long red[kScatterThreads / 32][kTile * kTile];
-    __shared__ ull win[kWinCopies * kWin * kWin];
-    __shared__ long long sums[3];
+    extern __shared__ __align__(16) ull scatter_acc[];
+    __shared__ long long sums[2];
     const int nxt = a.update ? 1 - a.sc->cur : 0;
     const Grid g = a.g;
     const int n = a.hi - a.lo;
     const int per = (n + vb.n - 1) / vb.n;
     const int r_lo = min(n, vb.id * per), r_hi = min(n, r_lo + per);
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    // 1. the mean base bin of the range (update mode: from the records;
-    //    plain mode: from the positions)
-    long long sc = 0, sr = 0, cnt = 0;
-    for (int i = r_lo + tid; i < r_hi; i += kScatterThreads) {
-        const int node = a.lo + i;
+    const int tid = threadIdx.x, lane = tid & 31;
+    // 1. a sample of the range, its first kScatterThreads nodes (one per
+    //    thread, kept in registers): their mean base bin places the tiles
+    int sb = kRecNone;
+    if (r_lo + tid < r_hi) {
+        const int node = a.lo + r_lo + tid;
         if (a.update) {
-            const int b = __ldg(a.rec_bin + node);
-            if (b >= 0) {
-                sc += rec_c0(b);
-                sr += rec_r0(b);
-                ++cnt;
-            }
+            sb = __ldg(a.rec_bin + node);
         } else {
-            const float qx = __ldg(a.px + node) / g.bw, qy = __ldg(a.py + node) / g.bh;
-            if (qx > 0.f && qx < (float)g.mx && qy > 0.f && qy < (float)g.my) {
-                sc += f2i_rz_small(qx);
-                sr += f2i_rz_small(qy);
-                ++cnt;
-            }
+            int c0, c1, r0, r1;
+            sb = make_rec(g, __ldg(a.px + node), __ldg(a.py + node), __ldg(a.w + node), __ldg(a.h + node), c0, c1,
+                          r0, r1)
+                     .bin;
         }
     }
-    sc = warp_sum(sc);
-    sr = warp_sum(sr);
-    cnt = warp_sum(cnt);
-    if (tid < 3) sums[tid] = 0;
+    const bool valid = sb >= 0;
+    const int scol = valid ? rec_c0(sb) : 0, srow = valid ? rec_r0(sb) : 0;
+    const int snc = valid && !(sb & kRecSmall) ? rec_nc(sb) : 1, snr = valid && !(sb & kRecSmall) ? rec_nr(sb) : 1;
+    const int wsc = __reduce_add_sync(0xffffffffu, scol), wsr = __reduce_add_sync(0xffffffffu, srow);
+    if (tid < 2) sums[tid] = 0;
     __syncthreads();
     if (lane == 0) {
-        atomicAdd(reinterpret_cast<ull *>(sums + 0), (ull)sc);
-        atomicAdd(reinterpret_cast<ull *>(sums + 1), (ull)sr);
-        atomicAdd(reinterpret_cast<ull *>(sums + 2), (ull)cnt);
+        atomicAdd(reinterpret_cast<ull *>(sums + 0), (ull)(long long)wsc);
+        atomicAdd(reinterpret_cast<ull *>(sums + 1), (ull)(long long)wsr);
     }
-    __syncthreads();
-    const long long tot = sums[2];
+    const int n_valid = __syncthreads_count(valid);  // also orders the adds above before the reads below
+    const long long tot = n_valid;
     const int mc = tot ? (int)((2 * sums[0] + tot) / (2 * tot)) : 0;  // rounded means
     const int mr = tot ? (int)((2 * sums[1] + tot) / (2 * tot)) : 0;
-    const int tc0 = min(max(mc - kTile / 2, 0), g.mx - kTile), tr0 = min(max(mr - kTile / 2, 0), g.my - kTile);
-    const int bw = (int)g.bw_q, bh = (int)g.bh_q;  // record arithmetic is int32 (checked at record time)
-    // the window: kWin x kWin bins (or the whole grid, if smaller) about the
-    // mean, for ranges of at least kWinMinNodes nodes (uniform; below that
-    // its clearing and flush cost more than the reductions it saves)
-    const bool use_win = r_hi - r_lo >= kWinMinNodes;
-    const int wcn = use_win ? min(kWin, g.mx) : 0, wrn = use_win ? min(kWin, g.my) : 0;
-    const int wc0 = use_win ? min(max(mc - wcn / 2, 0), g.mx - wcn) : 0;
-    const int wr0 = use_win ? min(max(mr - wrn / 2, 0), g.my - wrn) : 0;
-    const int wsz = wcn * wrn;
-    for (int t = tid; t < kWinCopies * wsz; t += kScatterThreads) win[t] = 0ull;
+    // the core tile and the window about the mean (clamped to the grid)
+    auto place = [&](int t, int c) {
+        TileShape s;
+        s.t = t;
+        s.c = c;
+        s.n = min(t, g.mx);
+        s.m = min(t, g.my);
+        s.c0 = min(max(mc - s.n / 2, 0), g.mx - s.n);
+        s.r0 = min(max(mr - s.m / 2, 0), g.my - s.m);
+        return s;
+    };
+    const TileShape core = place(kCoreT, kCoreC), win = place(kWinT, kWinC);
+    auto inside = [](const TileShape &s, int c0, int r0, int nc, int nr) {
+        return c0 >= s.c0 && r0 >= s.r0 && c0 + nc <= s.c0 + s.n && r0 + nr <= s.r0 + s.m;
+    };
+    // 2. the tile shape, from the sample: the core tile when it holds at
+    //    least 85% of the sample (with fewer, the dense ring around it goes
+    //    to the map's atomics and the window is faster: measured 37 against
+    //    74 us at 60%); else, for ranges of kWinMinNodes or more, the window
+    //    when it holds half; else none
+    const int in_core = __syncthreads_count(valid && inside(core, scol, srow, snc, snr));
+    const int in_win = __syncthreads_count(valid && inside(win, scol, srow, snc, snr));
+    TileShape ts = place(0, 0);
+    if (n_valid > 0 && 20 * in_core >= 17 * n_valid) ts = core;
+    else if (n_valid > 0 && r_hi - r_lo >= kWinMinNodes && 2 * in_win >= n_valid) ts = win;
+    // 3. clear the tile (kScatterSmem bytes hold either shape)
+    const int nz = ts.t * ts.t * ts.c;
+    for (int t = tid; t < nz / 2; t += kScatterThreads)
+        reinterpret_cast<ulonglong2 *>(scatter_acc)[t] = make_ulonglong2(0ull, 0ull);
     __syncthreads();
-    const unsigned win_s = (unsigned)__cvta_generic_to_shared(win) + 8u * (unsigned)((lane % kWinCopies) * wsz);
-
-    // 2.-3. the range's nodes
-    long long acc[kTile][kTile];
-#pragma unroll
-    for (int u = 0; u < kTile; ++u)
-#pragma unroll
-        for (int v = 0; v < kTile; ++v) acc[u][v] = 0;
+    const unsigned tile_s = (unsigned)__cvta_generic_to_shared(scatter_acc) +
+                            8u * (unsigned)(ts.c ? (lane % ts.c) * ts.t * ts.t : 0);
     auto add_glb = [&](int c, int r, long long v) { atomicAdd(a.rho_q + (long long)c * g.my + r, (ull)v); };
-    auto add_win = [&](int c, int r, long long v) {
-        asm volatile("red.shared.add.u64 [%0], %1;" ::"r"(win_s + 8u * (unsigned)((c - wc0) * wrn + (r - wr0))),
+    auto add_tile = [&](int c, int r, long long v) {
+        asm volatile("red.shared.add.u64 [%0], %1;" ::"r"(tile_s + 8u * (unsigned)((c - ts.c0) * ts.t + (r - ts.r0))),
                      "l"(v)
                      : "memory");
     };
-    int had = 0;      // this thread accumulated a node into the tile
-    int had_win = 0;  // ... or into the window
+    int had = 0;  // this thread added to the tile
     // a node's raw inputs (update mode: its record; plain mode: x, y, w, h as
-    // bits), loaded one iteration ahead: the loads of the next node are in
-    // flight while this one is added
+    // bits), loaded two iterations ahead: the loads of the next two nodes are
+    // in flight while this one is added
     auto load_raw = [&](int i, int &rb, int4 &ro) {
         rb = kRecNone;
         ro = make_int4(0, 0, 0, 0);
@@ -339,111 +362,55 @@ __device__ __forceinline__ void scatter_body(const ScatterArgs &a, VBlock vb) {
                            __float_as_int(__ldg(a.w + node)), __float_as_int(__ldg(a.h + node)));
         }
     };
-    int next_b;
-    int4 next_o;
-    load_raw(r_lo + tid, next_b, next_o);
-    for (int base = r_lo; base < r_hi; base += kScatterThreads) {  // the same trip count in every lane
+    int next_b[2];  // two nodes ahead
+    int4 next_o[2];
+    load_raw(r_lo + tid, next_b[0], next_o[0]);
+    load_raw(r_lo + tid + kScatterThreads, next_b[1], next_o[1]);
+    for (int base = r_lo; base < r_hi; base += kScatterThreads) {
         const int i = base + tid;
-        const bool valid = i < r_hi;
         const int node = a.lo + i;
-        const int rb = next_b;
-        const int4 ro = next_o;
-        load_raw(i + kScatterThreads, next_b, next_o);
-        NodeRec q{kRecNone, 0, 0, 0, 0};
-        if (valid) {
-            if (a.update) {
-                q = NodeRec{rb, ro.x, ro.y, ro.z, ro.w};
+        const int rb = next_b[0];
+        const int4 ro = next_o[0];
+        next_b[0] = next_b[1];
+        next_o[0] = next_o[1];
+        load_raw(i + 2 * kScatterThreads, next_b[1], next_o[1]);
+        if (i >= r_hi) continue;
+        NodeRec q;
+        if (a.update) {
+            q = NodeRec{rb, ro.x, ro.y, ro.z, ro.w};
+        } else {
+            int c0, c1, r0, r1;
+            q = make_rec(g, __int_as_float(ro.x), __int_as_float(ro.y), __int_as_float(ro.z),
+                         __int_as_float(ro.w), c0, c1, r0, r1);
+        }
+        if (q.bin == kRecNone) continue;
+        if (q.bin >= 0) {
+            const int nc = (q.bin & kRecSmall) ? 1 : rec_nc(q.bin), nr = (q.bin & kRecSmall) ? 1 : rec_nr(q.bin);
+            if (inside(ts, rec_c0(q.bin), rec_r0(q.bin), nc, nr)) {
+                emit_rec(g, q.bin, q.xr, q.wq, q.yr, q.hq, add_tile);
+                had = 1;
             } else {
-                int c0, c1, r0, r1;
-                q = make_rec(g, __int_as_float(ro.x), __int_as_float(ro.y), __int_as_float(ro.z),
-                             __int_as_float(ro.w), c0, c1, r0, r1);
+                emit_rec(g, q.bin, q.xr, q.wq, q.yr, q.hq, add_glb);
             }
-        }
-        bool fits = false;
-        int qc0 = 0, qr0 = 0, qnc = 1, qnr = 1;
-        if (q.bin >= 0) {
-            qc0 = rec_c0(q.bin) - tc0;
-            qr0 = rec_r0(q.bin) - tr0;
-            if (!(q.bin & kRecSmall)) {
-                qnc = rec_nc(q.bin);
-                qnr = rec_nr(q.bin);
-            }
-            fits = qc0 >= 0 && qr0 >= 0 && qc0 + qnc <= kTile && qr0 + qnr <= kTile;
-        }
-        if (__popc(__ballot_sync(0xffffffffu, fits)) < kTileMinLanes) fits = false;  // warp-uniform test
-        if (__any_sync(0xffffffffu, fits)) {
-            // this node's column and row overlaps over the tile (zero outside
-            // its bins, and for lanes whose node does not fit)
-            int ow[kTile], oh[kTile];
-            const bool sm = (q.bin & kRecSmall) != 0;
-#pragma unroll
-            for (int u = 0; u < kTile; ++u) {
-                const int j = u - qc0;
-                ow[u] = fits && j >= 0 && j < qnc ? (sm ? q.wq : overlap_1d32(j * bw, bw, q.xr, q.wq)) : 0;
-            }
-#pragma unroll
-            for (int v = 0; v < kTile; ++v) {
-                const int k = v - qr0;
-                oh[v] = fits && k >= 0 && k < qnr ? (sm ? q.hq : overlap_1d32(k * bh, bh, q.yr, q.hq)) : 0;
-            }
-#pragma unroll
-            for (int u = 0; u < kTile; ++u)
-#pragma unroll
-                for (int v = 0; v < kTile; ++v) acc[u][v] += (long long)ow[u] * oh[v];
-            had |= fits;
-        }
-        if (fits || q.bin == kRecNone) continue;
-        if (q.bin >= 0) {
-            const int c0 = rec_c0(q.bin) - wc0, r0 = rec_r0(q.bin) - wr0;
-            if (c0 >= 0 && r0 >= 0 && c0 + qnc <= wcn && r0 + qnr <= wrn) {
-                emit_rec(g, q.bin, q.xr, q.wq, q.yr, q.hq, add_win);
-                had_win = 1;
-                continue;
-            }
-        }
-        if (q.bin == kRecFull) {
+        } else {
             // outside the record's range: re-evaluated from the node's position
             const float x = a.update ? a.vx[nxt][node] : __ldg(a.px + node);
             const float y = a.update ? a.vy[nxt][node] : __ldg(a.py + node);
             for_each_overlap(g, x, y, __ldg(a.w + node), __ldg(a.h + node), add_glb);
-        } else {
-            emit_rec(g, q.bin, q.xr, q.wq, q.yr, q.hq, add_glb);
         }
     }
-    // 4. the window's non-zero bins, then the tile summed over the block
-    if (__syncthreads_or(had_win)) {  // uniform
-        for (int t = tid; t < wsz; t += kScatterThreads) {
-            ull v = 0;
-#pragma unroll
-            for (int k = 0; k < kWinCopies; ++k) v += win[k * wsz + t];
-            if (v) add_glb(wc0 + t / wrn, wr0 + t % wrn, (long long)v);
-        }
-    }
-    if (!__syncthreads_or(had)) return;  // uniform: no node of the range went into the tile
-#pragma unroll
-    for (int u = 0; u < kTile; ++u)
-#pragma unroll
-        for (int v = 0; v < kTile; ++v) {
-            const long long t = warp_sum(acc[u][v]);
-            if (lane == 0) red[warp][u * kTile + v] = t;
-        }
-    __syncthreads();
-    if (tid < kTile * kTile) {
-        long long t = 0;
-#pragma unroll
-        for (int w = 0; w < kScatterThreads / 32; ++w) t += red[w][tid];
-        if (t) add_glb(tc0 + tid / kTile, tr0 + tid % kTile, t);
-    }
+    // 4. the tile's non-zero bins (the test is a barrier after the last shared add)
+    if (__syncthreads_or(had)) flush_tile(scatter_acc, ts, g, a.rho_q);
 }
 
-__global__ void __launch_bounds__(kScatterThreads, 2) scatter_kernel(ScatterArgs a) { scatter_body(a, grid_block()); }
+__global__ void __launch_bounds__(kScatterThreads, 3) scatter_kernel(ScatterArgs a) { scatter_body(a, grid_block()); }
 
 // Resident blocks of `kernel` on the whole GPU (one wave), or `fallback`.
-int wave_of(const void *kernel, int threads, int fallback) {
+int wave_of(const void *kernel, int threads, int fallback, int dyn_smem) {
     int dev = 0, sms = 0, per_sm = 0;
     if (cudaGetDevice(&dev) == cudaSuccess &&
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess &&
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, 0) == cudaSuccess &&
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, (size_t)dyn_smem) == cudaSuccess &&
         sms * per_sm > 0)
         return sms * per_sm;
     return fallback;
@@ -476,7 +443,10 @@ int scatter_grid(int n, int block_nodes) {
     // one wave of resident blocks, each a contiguous range of nodes (fewer
     // blocks: fewer tile flushes onto the dense core's bins)
     static int wave = 0;
-    if (wave <= 0) wave = wave_of((const void *)scatter_kernel, kScatterThreads, 304);
+    if (wave <= 0) {
+        cudaFuncSetAttribute(scatter_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kScatterSmem);
+        wave = wave_of((const void *)scatter_kernel, kScatterThreads, 304, kScatterSmem);
+    }
     const int per = block_nodes > kScatterThreads ? block_nodes : kScatterThreads;
     int blocks = (n + per - 1) / per;
     if (blocks > wave) blocks = wave;
@@ -486,7 +456,7 @@ int scatter_grid(int n, int block_nodes) {
 void launch_scatter_bins(const ScatterArgs &a, cudaStream_t st) {
     const int n = a.hi - a.lo;
     if (n <= 0) return;
-    scatter_kernel<<<scatter_grid(n, a.block_nodes), kScatterThreads, 0, st>>>(a);
+    scatter_kernel<<<scatter_grid(n, a.block_nodes), kScatterThreads, kScatterSmem, st>>>(a);
 }
 
 void launch_scatter(const ScatterArgs &a, cudaStream_t st) {
@@ -1016,7 +986,7 @@ __global__ void __launch_bounds__(kThreads) persist_update_kernel(PersistQueue q
     });
 }
 
-__global__ void __launch_bounds__(kScatterThreads, 2) persist_scatter_kernel(PersistQueue q, const ScatterArgs *recs) {
+__global__ void __launch_bounds__(kScatterThreads, 3) persist_scatter_kernel(PersistQueue q, const ScatterArgs *recs) {
     persist_loop(q, recs, [](const ScatterArgs &a, VBlock vb, int) { scatter_body(a, vb); });
 }
 
@@ -1041,7 +1011,18 @@ int persist_density_wave(int stage) {
         if (!waves[0]) waves[0] = wave_of((const void *)persist_update_kernel, kThreads, 1216);
         return waves[0];
     case PS_SCATTER:
-        if (!waves[1]) waves[1] = wave_of((const void *)persist_scatter_kernel, kScatterThreads, 304);
+        // two blocks per SM, not the three that fit: the WA launches run
+        // beside the scatter and need shared memory and warp slots too
+        if (!waves[1]) {
+            cudaFuncSetAttribute(persist_scatter_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kScatterSmem);
+            int dev = 0, sms = 0;
+            const int full = wave_of((const void *)persist_scatter_kernel, kScatterThreads, 304, kScatterSmem);
+            if (cudaGetDevice(&dev) == cudaSuccess &&
+                cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && sms > 0)
+                waves[1] = std::min(full, 2 * sms);
+            else
+                waves[1] = full;
+        }
         return waves[1];
     case PS_RHO:
         if (!waves[2]) waves[2] = wave_of((const void *)persist_rho_kernel, kThreads, 1216);
@@ -1061,7 +1042,7 @@ void launch_persist_density(int stage, const PersistQueue &q, const void *recs, 
         persist_update_kernel<<<w, kThreads, 0, st>>>(q, static_cast<const ScatterArgs *>(recs));
         break;
     case PS_SCATTER:
-        persist_scatter_kernel<<<w, kScatterThreads, 0, st>>>(q, static_cast<const ScatterArgs *>(recs));
+        persist_scatter_kernel<<<w, kScatterThreads, kScatterSmem, st>>>(q, static_cast<const ScatterArgs *>(recs));
         break;
     case PS_RHO:
         persist_rho_kernel<<<w, kThreads, 0, st>>>(q, static_cast<const RhoArgs *>(recs));

@@ -255,12 +255,13 @@ def profile_mode(args):
 
 
 def batch_mode(args):
-    """Batched form: n instances (cell counts LogUniform[5k, 150k], bins 128..512,
-    FP32) stepped together.  Reports instance-iterations per second over K
-    graph launches for the persistent form (nine persistent launches per trial
-    step over all instances, the default) and for the graph of per-instance
-    branches, the wall time until every instance is below 10% overflow, and
-    the instances stepped one after another on their own graphs."""
+    """Batched form: n instances (cell counts LogUniform[5k, 150k], bins 128..512)
+    stepped together.  Reports instance-iterations per second over K graph
+    launches for the persistent form (nine persistent launches per trial step
+    over all instances, FP32 field, the default), for the graph of
+    per-instance branches with the FP32 field and with the BF16x3 tensor-core
+    field, the wall time until every instance is below 10% overflow, and the
+    instances stepped one after another on their own graphs."""
     import torch
 
     import aieplace_gb300 as ap
@@ -271,9 +272,10 @@ def batch_mode(args):
     nls = [ap.synth.generate(s, seed=100 + i) for i, s in enumerate(specs)]
     cells = sum(int((nl["node_fixed"] == 0).sum()) for nl in nls)
     forms = {}
-    for form in ("persistent", "graph"):
-        with ap.BatchPlacer(nls, max_iterations=4000, check_interval=32) as bp:
-            bp.set_form(form)
+    for form in ("persistent", "graph", "graph_bf16x3"):
+        solver = "bf16x3" if form == "graph_bf16x3" else "fp32"
+        with ap.BatchPlacer(nls, field_solver=solver, max_iterations=4000, check_interval=32) as bp:
+            bp.set_form("graph" if form == "graph_bf16x3" else form)
             bp.initialize_placement(seed=5, sigma=1.0)
             bp.step(args.warmup)
             it0 = sum(bp.stats(i)["iteration"] for i in range(bp.n))
@@ -294,8 +296,8 @@ def batch_mode(args):
                 bp.step(args.steps)
                 one_block = {"graph_launch_ms": 1000 * (time.perf_counter() - t0) / args.steps,
                              "stage_ms": bp.profile(10), "info": bp.info()}
-        with ap.BatchPlacer(nls, max_iterations=4000, check_interval=32) as bp:
-            bp.set_form(form)
+        with ap.BatchPlacer(nls, field_solver=solver, max_iterations=4000, check_interval=32) as bp:
+            bp.set_form("graph" if form == "graph_bf16x3" else form)
             bp.initialize_placement(seed=5, sigma=1.0)
             torch.cuda.synchronize()
             t0 = time.perf_counter()
@@ -323,7 +325,8 @@ def batch_mode(args):
             seq_its += pl.stats()["iteration"]
     seq_el = time.perf_counter() - t0
     print(json.dumps({
-        "metric": "batched instance-iterations/s", "value": forms["persistent"]["instance_iters_per_s"],
+        "metric": "batched instance-iterations/s", "value": max(f["instance_iters_per_s"] for f in forms.values()),
+        "best_form": max(forms, key=lambda k: forms[k]["instance_iters_per_s"]),
         "unit": "instance-iters/s", "instances": len(nls), "cells_total": cells, "steps": args.steps,
         "warmup": args.warmup, "forms": forms,
         "sequential_instance_iters_per_s_first8": seq_its / seq_el,
