@@ -30,6 +30,11 @@ struct AxisTerms {
     float inv_bp, inv_bm, wp, wm;  // 1/b+, 1/b-, shifted WA+ - x_max, WA- - x_min
 };
 
+// 1/b for the sums b+- (1 <= b <= net degree: the extreme pin adds exp(0)):
+// the 2-ulp reciprocal, well inside its range; IEEE division spent a dozen
+// instructions and a branch per call here
+__device__ __forceinline__ float rcp(float b) { return __fdividef(1.f, b); }
+
 // one pin's gradient into its node's accumulators; `raw` is the pin_node entry
 __device__ __forceinline__ void add_grad(ull *gq, ull *gqx, ull *gqy, int raw, float gx, float gy) {
     const int n = raw & kPinNode;
@@ -134,7 +139,7 @@ __device__ __forceinline__ void net_group(const WaArgs &a, int s, int d, int l, 
     float g[P][2], wa_net = 0.f;
 #pragma unroll
     for (int ax = 0; ax < 2; ++ax) {
-        const float ibp = 1.f / s8[4 * ax + 0], ibm = 1.f / s8[4 * ax + 1];
+        const float ibp = rcp(s8[4 * ax + 0]), ibm = rcp(s8[4 * ax + 1]);
         const float wp = s8[4 * ax + 2] * ibp, wm = s8[4 * ax + 3] * ibm;
 #pragma unroll
         for (int p = 0; p < P; ++p) {
@@ -210,7 +215,7 @@ __device__ __forceinline__ void net_thread(const int *__restrict__ pins, int d, 
                 cm += em[j] * dm;
             }
         }
-        const float ibp = 1.f / bp, ibm = 1.f / bm, wp = cp * ibp, wm = cm * ibm;
+        const float ibp = rcp(bp), ibm = rcp(bm), wp = cp * ibp, wm = cm * ibm;
         wa_net += (cmx - cmn) + wp - wm;
 #pragma unroll
         for (int j = 0; j < D; ++j) {
@@ -230,6 +235,31 @@ __device__ __forceinline__ void net_thread(const int *__restrict__ pins, int d, 
     wa_acc += wa_net;
 }
 
+// One 2-pin net (pins a, b) in closed form.  With d = |x_a - x_b|, e =
+// exp(-d/g) and r = 1/(1 + e), the terms above reduce to b+ = b- = 1 + e and
+//   dWA/dx_max = (1 - e) r + 2 d e r^2 / g = -dWA/dx_min,
+//   WA = d (1 - e) r,  HPWL = d
+// (the same quantities; one exponential per axis instead of four).
+__device__ __forceinline__ void net_pair(const WaArgs &a, int s, const float2 *__restrict__ xy, float inv_g,
+                                         float &hp_acc, float &wa_acc) {
+    const int na = __ldg(a.pin_node + s), nb = __ldg(a.pin_node + s + 1);  // raw entries (heavy flag)
+    const float2 pa = __ldg(xy + (na & kPinNode)), pb = __ldg(xy + (nb & kPinNode));
+    const float dd[2] = {pa.x - pb.x, pa.y - pb.y};
+    float g[2];
+#pragma unroll
+    for (int ax = 0; ax < 2; ++ax) {
+        const float d = fabsf(dd[ax]);
+        const float e = __expf(-d * inv_g);
+        const float r = rcp(1.f + e);
+        const float gmax = r * (1.f - e) + 2.f * d * e * r * r * inv_g;
+        g[ax] = dd[ax] >= 0.f ? gmax : -gmax;  // pin a is the larger coordinate, or they coincide (g = 0)
+        hp_acc += d;
+        wa_acc += d * (1.f - e) * r;
+    }
+    if ((na & kPinNode) < a.n_grad) add_grad(a.gq, a.gqx, a.gqy, na, g[0], g[1]);
+    if ((nb & kPinNode) < a.n_grad) add_grad(a.gq, a.gqx, a.gqy, nb, -g[0], -g[1]);
+}
+
 }  // namespace
 
 // Bucket B (degree <= D) of the thread-per-net nets: registers sized for D.
@@ -247,9 +277,13 @@ __device__ __forceinline__ void wa_small_body(const WaArgs &a, VBlock vb) {
     // offset, one dependent load fewer per net
     const int s0 = D == 2 && lo < hi ? __ldg(a.net_ptr + lo) : 0;
     for (int e = lo + vb.id * blockDim.x + threadIdx.x; e < hi; e += vb.n * blockDim.x) {
-        const int s = D == 2 ? s0 + 2 * (e - lo) : __ldg(a.net_ptr + e);
-        const int d = D == 2 ? 2 : __ldg(a.net_ptr + e + 1) - s;
-        net_thread<D>(a.pin_node + s, d, xy, inv_g, a.gq, a.gqx, a.gqy, a.n_grad, hpf, waf);
+        if (D == 2) {
+            net_pair(a, s0 + 2 * (e - lo), xy, inv_g, hpf, waf);
+        } else {
+            const int s = __ldg(a.net_ptr + e);
+            net_thread<D>(a.pin_node + s, __ldg(a.net_ptr + e + 1) - s, xy, inv_g, a.gq, a.gqx, a.gqy, a.n_grad,
+                          hpf, waf);
+        }
     }
     // per-block partials in FP32 (folded with compensation by the last block
     // of the warp-per-net launch)
@@ -304,8 +338,8 @@ __device__ __forceinline__ void net_warp_loop(const WaArgs &a, int s, int d, con
     AxisTerms t[2];
 #pragma unroll
     for (int ax = 0; ax < 2; ++ax) {
-        t[ax].inv_bp = 1.f / s8[4 * ax + 0];
-        t[ax].inv_bm = 1.f / s8[4 * ax + 1];
+        t[ax].inv_bp = rcp(s8[4 * ax + 0]);
+        t[ax].inv_bm = rcp(s8[4 * ax + 1]);
         t[ax].wp = s8[4 * ax + 2] * t[ax].inv_bp;
         t[ax].wm = s8[4 * ax + 3] * t[ax].inv_bm;
     }
@@ -331,10 +365,11 @@ __device__ __forceinline__ void net_warp_loop(const WaArgs &a, int s, int d, con
 }
 
 // Nets of degree > 8 (buckets 3..6): blocks [0, b3) take degrees 9..16 with
-// 16 lanes per net, then 17..32 with a warp (one pin per lane), 33..64 with
-// 16 lanes (four pins per lane: two nets per warp share each shuffle
-// reduction), and above 64 with a warp looping over the pins --
-// the lane group fits the net, so few lanes idle.
+// 8 lanes per net (two pins per lane, four nets per warp), then 17..32 with 16
+// lanes (two pins per lane), 33..64 with 16 lanes (four pins per lane), and
+// above 64 with a warp looping over the pins -- the lane group fits the net,
+// so few lanes idle, and each group reduction serves two or four pins per lane
+// (one pin per lane on 16 and 32 lanes took 9% longer for the stage).
 __device__ __forceinline__ void wa_large_body(const WaArgs &a, VBlock vb) {
     __shared__ double red[32];
     const float gamma = a.gamma > 0.f ? a.gamma : a.sc->f_gamma;
@@ -346,9 +381,9 @@ __device__ __forceinline__ void wa_large_body(const WaArgs &a, VBlock vb) {
     int b0 = 0;
     const int bid = vb.id;
     if (bid < b0 + a.bucket_blocks[3]) {
-        net_groups<16, 1>(a, bid, a.bucket_lo[3], a.bucket_lo[4], b0, a.bucket_blocks[3], xy, inv_g, hpf, waf);
+        net_groups<8, 2>(a, bid, a.bucket_lo[3], a.bucket_lo[4], b0, a.bucket_blocks[3], xy, inv_g, hpf, waf);
     } else if (bid < (b0 += a.bucket_blocks[3]) + a.bucket_blocks[4]) {
-        net_groups<32, 1>(a, bid, a.bucket_lo[4], a.bucket_lo[5], b0, a.bucket_blocks[4], xy, inv_g, hpf, waf);
+        net_groups<16, 2>(a, bid, a.bucket_lo[4], a.bucket_lo[5], b0, a.bucket_blocks[4], xy, inv_g, hpf, waf);
     } else if (bid < (b0 += a.bucket_blocks[4]) + a.bucket_blocks[5]) {
         net_groups<16, 4>(a, bid, a.bucket_lo[5], a.bucket_lo[6], b0, a.bucket_blocks[5], xy, inv_g, hpf, waf);
     } else {
@@ -407,7 +442,7 @@ int wa_plan(WaArgs &a) {
     };
     for (int b = 0; b < 3; ++b) a.bucket_blocks[b] = grid(a.bucket_lo[b + 1] - a.bucket_lo[b]);
     // large-net sub-buckets: lanes per net 16, 32, 16, 32; <= kWaMaxBlocks in all
-    const int lanes[4] = {16, 32, 16, 32};
+    const int lanes[4] = {8, 16, 16, 32};
     int large = 0;
     for (int b = 3; b < kWaBuckets; ++b) {
         a.bucket_blocks[b] = std::min(grid((a.bucket_lo[b + 1] - a.bucket_lo[b]) * lanes[b - 3]), kWaMaxBlocks / 4);
