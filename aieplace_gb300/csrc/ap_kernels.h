@@ -179,6 +179,8 @@ void launch_perturb(int n_mov, const float *vx, const float *vy, const float *gx
 
 // ---- field solve ------------------------------------------------------------
 // Spectral solver state for an m x m grid (square, m a multiple of 32).
+constexpr int kTcCandidates = 5;  // tensor-core solve variants the autotuner times
+
 struct FieldSolver {
     int m;
     float bin_ratio;
@@ -195,9 +197,13 @@ struct FieldSolver {
     void *tc_maps;           // tensor maps of the tcgen05 path (host table)
     int tc_ready;
     unsigned int *tc_status; // device error flag of the tcgen05 kernels
+    unsigned int *tc_sync;   // row-block counters of the persistent tcgen05 solve
+    float *tc_part;          // its split-K partials
     // tile autotuner results
-    int tc_variant;          // 0: 128 x 64 tiles, 1: 128 x 128, 2: 128 x 64 with 2 stages (2 CTAs per SM)
-    float tc_tune_ms[3];     // measured solve time of each variant
+    int tc_variant;          // 0: 128 x 64 tiles, 1: 128 x 128, 2: 128 x 64 with 2 stages (2 CTAs per SM),
+                             // 3, 4: one persistent launch of 128 x 128 tiles, K of stages 1-2
+                             // split in two (3) or not (4)
+    float tc_tune_ms[kTcCandidates];  // measured solve time of each variant (-1: not run)
     int simt_bm;             // FP32 path tile (32 or 64); 0 = size rule
     float simt_tune_ms[2];   // measured solve time with 32 / 64 tiles
     // failure injection (ap_debug_inject): the tcgen05 kernels issue no loads

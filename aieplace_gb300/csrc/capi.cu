@@ -1141,7 +1141,7 @@ int ap_solver_info(ap_handle *h, int32_t *tc_variant, float *tc_ms, int32_t *sim
     if (!h) return AP_ERR_INVALID_ARG;
     if (tc_variant) *tc_variant = h->fs.tc_ready ? h->fs.tc_variant : -1;
     if (tc_ms)
-        for (int v = 0; v < 3; ++v) tc_ms[v] = h->fs.tc_tune_ms[v];
+        for (int v = 0; v < kTcCandidates; ++v) tc_ms[v] = h->fs.tc_tune_ms[v];
     if (simt_tile) *simt_tile = h->fs.simt_bm;
     if (simt_ms) {
         simt_ms[0] = h->fs.simt_tune_ms[0];

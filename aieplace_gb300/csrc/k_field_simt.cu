@@ -210,7 +210,7 @@ void field_solver_free(FieldSolver &f) {
     void *ptrs[] = {f.C,       f.Ct,      f.St,      f.C_hi,    f.C_lo,    f.Ct_hi,   f.Ct_lo,
                     f.St_hi,   f.St_lo,   f.wx,      f.wy,      f.t0,      f.px,      f.py,
                     f.ux,      f.uy,      f.b_t_hi,  f.b_t_lo,  f.b_px_hi, f.b_px_lo, f.b_py_hi,
-                    f.b_py_lo, f.b_ux_hi, f.b_ux_lo, f.b_uy_hi, f.b_uy_lo, f.tc_status};
+                    f.b_py_lo, f.b_ux_hi, f.b_ux_lo, f.b_uy_hi, f.b_uy_lo, f.tc_status, f.tc_sync, f.tc_part};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     free(f.tc_maps);  // host-side tensor-map table

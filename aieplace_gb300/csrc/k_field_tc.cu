@@ -25,6 +25,8 @@
 // Every mbarrier wait is bounded; a wait that gives up sets the solver's
 // status word and the CTA drains and exits without further issue.
 #include <cuda.h>
+
+#include <algorithm>
 #include <cudaTypedefs.h>
 #include <stdint.h>
 #include <stdio.h>
@@ -53,7 +55,10 @@ struct TileCfg {
 using Tile64 = TileCfg<64, 4>;    // 48 KB stages
 using Tile128 = TileCfg<128, 3>;  // 64 KB stages
 using Tile64x2 = TileCfg<64, 2>;  // 2 stages, ~97 KB: two CTAs per SM
-constexpr int kTcVariants = 3;
+// variants 0-2: the four-launch solve with these tiles; 3, 4: the persistent
+// solve (one launch) with Tile128 pipelines, stages 1-2 with K split in two (3)
+// or not (4)
+constexpr int kTcVariants = kTcCandidates;
 
 enum { EPI_SPLIT = 0, EPI_SPECTRAL = 1, EPI_F32 = 2 };
 
@@ -169,6 +174,26 @@ __device__ __forceinline__ float2 ld_shared_f2(uint32_t addr) {
     return v;
 }
 
+__device__ __forceinline__ void st_shared_f1(uint32_t addr, float v) {
+    asm volatile("st.shared.f32 [%0], %1;" ::"r"(addr), "f"(v) : "memory");
+}
+
+__device__ __forceinline__ float ld_shared_f1(uint32_t addr) {
+    float v;
+    asm volatile("ld.shared.f32 %0, [%1];" : "=f"(v) : "r"(addr));
+    return v;
+}
+
+// explicit global stores: a generic store could alias shared memory, and the
+// staging loads that follow it would wait for it
+__device__ __forceinline__ void st_global_f2(float *p, float a, float b) {
+    asm volatile("st.global.v2.f32 [%0], {%1, %2};" ::"l"(p), "f"(a), "f"(b) : "memory");
+}
+
+__device__ __forceinline__ void st_global_u32(void *p, uint32_t v) {
+    asm volatile("st.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
 __device__ __forceinline__ float4 ld_shared_f4(uint32_t addr) {
     float4 v;
     asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];" : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "r"(addr));
@@ -245,6 +270,14 @@ __device__ __forceinline__ void store_split_vec(const float (&v)[VEC], __nv_bflo
         *reinterpret_cast<uint32_t *>(hi) = h[0];
         *reinterpret_cast<uint32_t *>(lo) = l[0];
     }
+}
+
+// Two adjacent FP32 outputs -> their BF16 hi and lo pairs (4-byte stores)
+__device__ __forceinline__ void st_split2(__nv_bfloat16 *hi, __nv_bfloat16 *lo, float a, float b) {
+    const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+    const float2 hf = __bfloat1622float2(h);
+    st_global_u32(hi, *reinterpret_cast<const uint32_t *>(&h));
+    st_global_u32(lo, pack_bf16(a - hf.x, b - hf.y));
 }
 
 // Output pointers of one CTA's stage epilogue, resolved before the row loop:
@@ -517,6 +550,541 @@ __global__ void __launch_bounds__(THREADS, 1) gemm_bf16x3_kernel(const __grid_co
     }
 }
 
+// ---- persistent dataflow solve ------------------------------------------------
+//
+// All four stages in one launch of at most one CTA per SM, 128 x 128 output
+// tiles.  The work items are the stages' output tiles in a fixed order
+// (stage; row block; the product z of stages 3-4; column block; for stages
+// 1-2 with K split, the half of K), claimed one at a time from a device
+// queue.  The data operand of a tile (mb, nb) of stage s > 1 is rows
+// [nb BN, nb BN + BN) of stage s-1's output: row block R = nb BN / 128 of
+// that stage, complete once the four epilogue warps of each of its m / BN
+// tiles have stored their rows and each bumped the row block's counter.  An
+// item waits only on items of lower index, and those were claimed earlier by
+// CTAs that are running, so the lowest unfinished item always proceeds,
+// however many of the CTAs are resident (other kernels, or another
+// instance's solve in a batch, may hold SMs).
+//
+// Stages 1-2 have only (m/128)^2 tiles -- 64 at 1024^2 bins, against 152 SMs
+// -- so with ks = 2 each of their tiles is two items, one per half of K.  Both
+// halves store their FP32 partial (a per-stage scratch); the epilogue warp
+// that arrives second on the tile's counter (one counter per warp, its 32
+// rows) adds partial 0 and partial 1 in that order -- the same bits whichever
+// half ends first -- and finishes the rows.
+//
+// Warps 0-3 epilogue (TMEM lanes 32w..32w+31 = rows), warp 4 lane 0 TMA
+// producer (it claims the items and hands them to the other roles through a
+// ring of kItemRing slots), warp 5 lane 0 MMA issuer.  Two accumulators in
+// TMEM: the epilogue of one tile runs while the MMAs of the CTA's next tile
+// fill the other, and the producer's ring of pipeline stages runs on across
+// tiles.  Every wait is bounded; one that gives up sets the solver's status
+// word, and the other CTAs' dependency waits then give up at once.
+
+constexpr int P_THREADS = 192;
+constexpr int P_STG_FLOATS = 4 * 32 * 33;  // per epilogue warp: 32 rows x 32 columns, row stride 33
+constexpr int kItemRing = 4;
+
+template <class T>
+struct PCfg {
+    static constexpr int SMEM_BYTES = T::STAGES * T::STAGE_BYTES + P_STG_FLOATS * 4 + 1024 + 512;
+};
+
+// outputs of the persistent solve, 32 x 32 boxes (stores): [0, 1] T hi/lo,
+// [2, 3] Px hi/lo, [4, 5] Py hi/lo, [6, 7] Ux hi/lo, [8, 9] Uy hi/lo, [10, 11] Ex, Ey
+enum { OUT_T = 0, OUT_PX = 2, OUT_PY = 4, OUT_UX = 6, OUT_UY = 8, OUT_EX = 10, kOutMaps = 12 };
+constexpr int kBox = 32;
+
+struct PMaps {
+    Maps st[4];
+    CUtensorMap out[kOutMaps];
+};
+
+struct PEpi {
+    int m;
+    int ks;  // K split of stages 1-2 (1 or 2)
+    __nv_bfloat16 *t_hi, *t_lo, *px_hi, *px_lo, *py_hi, *py_lo, *ux_hi, *ux_lo, *uy_hi, *uy_lo;
+    float *ex, *ey;
+    const float *wx, *wy;
+    float scale;
+    unsigned int *status;
+    // [0] the item queue's head; [1] CTAs finished; [2 + (2 s + z) nM + R]
+    // epilogue warps (four a tile) done with stage s, product z, row block R;
+    // then, with ks = 2, [2 + 8 nM + 4 (s tiles + tile) + warp] halves of
+    // stage s < 2's tile whose partial rows of that warp are stored.  The
+    // last CTA to finish zeroes them all.
+    unsigned int *sync;
+    float *part;  // ks = 2: FP32 partials [stage][half][tile][128 x BN]
+    const int *gate;
+    int gate_mask;
+    int skip_loads;
+    unsigned long long wait_ns;
+};
+
+struct PItem {
+    int s, z, mb, nb, kh;
+};
+
+__device__ __forceinline__ PItem p_item(int t, int nM, int nN, int ks) {
+    const int one = nM * nN;  // tiles of a product; stages 3 and 4 have two products
+    PItem it;
+    it.kh = 0;
+    it.z = 0;
+    if (t < 2 * ks * one) {
+        it.s = t / (ks * one);
+        const int r = t - it.s * ks * one;
+        const int tile = r / ks;
+        it.kh = r - tile * ks;
+        it.mb = tile / nN;
+        it.nb = tile - it.mb * nN;
+    } else {
+        int r = t - 2 * ks * one;
+        it.s = r < 2 * one ? 2 : 3;
+        if (it.s == 3) r -= 2 * one;
+        it.mb = r / (2 * nN);
+        const int q = r - it.mb * 2 * nN;
+        it.z = q / nN;
+        it.nb = q - it.z * nN;
+    }
+    return it;
+}
+
+__device__ __forceinline__ unsigned int ld_acquire_u32(const unsigned int *p) {
+    unsigned int v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Bounded wait that also gives up once the CTA is aborting.
+__device__ __forceinline__ bool mbar_wait_ab(uint64_t *bar, uint32_t parity, unsigned int *status,
+                                             unsigned long long wait_ns, volatile int *abort_flag) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const unsigned long long t0 = global_ns();
+    for (;;) {
+        for (int i = 0; i < 64; ++i)
+            if (mbar_try_wait(bar, parity)) return true;
+        if (*abort_flag) return false;
+        if (global_ns() - t0 > wait_ns) {
+            atomicOr(status, 1u);
+            *abort_flag = 1;
+            return false;
+        }
+    }
+}
+
+// Until the row block's counter reaches `need`; false once the wait ran out,
+// this CTA is aborting or another CTA reported a failure.
+__device__ __forceinline__ bool dep_wait(const unsigned int *c, unsigned int need, unsigned int *status,
+                                         unsigned long long wait_ns, volatile int *abort_flag) {
+    if (ld_acquire_u32(c) >= need) return true;
+    const unsigned long long t0 = global_ns();
+    for (;;) {
+        for (int i = 0; i < 16; ++i) {
+            if (ld_acquire_u32(c) >= need) return true;
+            __nanosleep(100);
+        }
+        if (*abort_flag || *(volatile unsigned int *)status != 0u) return false;
+        if (global_ns() - t0 > wait_ns) {
+            atomicOr(status, 1u);
+            return false;
+        }
+    }
+}
+
+// tile stores by the tensor memory accelerator: shared -> global, one
+// bulk group per issuing thread
+__device__ __forceinline__ void tma_store_2d(const CUtensorMap *map, uint32_t src, int x, int y) {
+    asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%2, %3}], [%1];" ::"l"((uint64_t)map),
+                 "r"(src), "r"(x), "r"(y)
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+// the issued stores have read their shared-memory source
+__device__ __forceinline__ void bulk_wait_read() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+// the issued stores are complete in global memory
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void st_shared_u32(uint32_t addr, uint32_t v) {
+    asm volatile("st.shared.b32 [%0], %1;" ::"r"(addr), "r"(v) : "memory");
+}
+__device__ __forceinline__ void st_shared_f2(uint32_t addr, float a, float b) {
+    asm volatile("st.shared.v2.f32 [%0], {%1, %2};" ::"r"(addr), "f"(a), "f"(b) : "memory");
+}
+
+__device__ __forceinline__ void st_global_f4(float *p, float4 v) {
+    asm volatile("st.global.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(p), "f"(v.x), "f"(v.y), "f"(v.z), "f"(v.w)
+                 : "memory");
+}
+
+template <class T>
+__global__ void __launch_bounds__(P_THREADS, 1) persist_solve_kernel(const __grid_constant__ PMaps maps, PEpi e) {
+    // uniform for the whole grid, before any barrier or TMEM allocation
+    if (e.gate && !((1 << *e.gate) & e.gate_mask)) return;
+    constexpr int BN = T::BN, STAGES = T::STAGES, STAGE_BYTES = T::STAGE_BYTES, B_TILE = T::B_TILE;
+    constexpr uint32_t TMEM_COLS = 2 * BN;  // two accumulators
+    extern __shared__ __align__(1024) uint8_t smem_raw[];
+    uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    float *stg = (float *)(smem + STAGES * STAGE_BYTES);
+    uint64_t *full = (uint64_t *)(stg + P_STG_FLOATS);
+    uint64_t *empty = full + STAGES;
+    uint64_t *acc_full = empty + STAGES;  // [2]
+    uint64_t *acc_empty = acc_full + 2;   // [2]
+    uint64_t *drain = acc_empty + 2;
+    uint64_t *item_full = drain + 1;               // [kItemRing], the producer's arrival
+    uint64_t *item_empty = item_full + kItemRing;  // [kItemRing], MMA issuer + 4 epilogue warps
+    uint32_t *tmem_slot = (uint32_t *)(item_empty + kItemRing);
+    volatile int *abort_flag = (volatile int *)(tmem_slot + 1);
+    volatile int *issued_kb = abort_flag + 1;    // producer: k-blocks whose loads were issued
+    volatile int *consumed_kb = abort_flag + 2;  // MMA issuer: k-blocks whose data it waited for
+    volatile int *item_ring = abort_flag + 3;    // [kItemRing] claimed items (>= total: no more)
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int m = e.m, nM = m / BM, nN = m / BN, nk = m / BK, ks = e.ks;
+    const int one = nM * nN, total = 2 * ks * one + 4 * one, G = (int)gridDim.x;
+    unsigned int *queue = e.sync, *finished = e.sync + 1, *rows_done = e.sync + 2;
+    unsigned int *halves = rows_done + 8 * nM;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < STAGES; ++s) {
+            mbar_init(full + s, 1);
+            mbar_init(empty + s, 1);
+        }
+        mbar_init(acc_full + 0, 1);
+        mbar_init(acc_full + 1, 1);
+        mbar_init(acc_empty + 0, 128);
+        mbar_init(acc_empty + 1, 128);
+        mbar_init(drain, 1);
+        for (int q = 0; q < kItemRing; ++q) {
+            mbar_init(item_full + q, 1);
+            mbar_init(item_empty + q, 5);
+        }
+        *abort_flag = 0;
+        *issued_kb = 0;
+        *consumed_kb = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+
+    if (warp == 4 && lane == 0) {
+        // ---- TMA producer
+        int g = 0;
+        for (int j = 0; !*abort_flag; ++j) {
+            const int q = j % kItemRing;
+            if (j >= kItemRing && !mbar_wait_ab(item_empty + q, ((j / kItemRing) - 1) & 1, e.status, e.wait_ns,
+                                                abort_flag))
+                break;
+            // failure injection: no item is taken, so the other roles' waits run out
+            int t = e.skip_loads ? -1 : (int)atomicAdd(queue, 1u);
+            if (t > total) t = total;
+            if (t < 0) break;
+            item_ring[q] = t;
+            asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(item_full + q)) : "memory");
+            if (t >= total) break;
+            {
+                const PItem it = p_item(t, nM, nN, ks);
+                if (it.s > 0) {
+                    // stage 2 and both products of stage 3 read stage 1 / stage 2's
+                    // single product; product z of stage 4 reads product z of stage 3
+                    const int zd = it.s == 3 ? it.z : 0;
+                    const unsigned int *c = rows_done + (2 * (it.s - 1) + zd) * nM + (it.nb * BN) / BM;
+                    if (!dep_wait(c, 4u * (unsigned int)nN, e.status, e.wait_ns, abort_flag)) {
+                        *abort_flag = 1;
+                        break;
+                    }
+                    // the previous stage's generic-proxy stores, acquired above,
+                    // before this thread's tensor (async-proxy) loads of them
+                    asm volatile("fence.proxy.async.global;" ::: "memory");
+                }
+                const Maps &mp = maps.st[it.s];
+                const int z = it.z, ay = it.mb * BM, by = it.nb * BN;
+                const int nki = it.s < 2 ? nk / ks : nk, kb0 = it.kh * nki;
+                bool ok = true;
+                for (int kb = 0; kb < nki; ++kb, ++g) {
+                    const int s = g % STAGES, round = g / STAGES;
+                    if (round > 0 && !mbar_wait_ab(empty + s, (round - 1) & 1, e.status, e.wait_ns, abort_flag)) {
+                        ok = false;
+                        break;
+                    }
+                    uint8_t *st = smem + s * STAGE_BYTES;
+                    mbar_expect_tx(full + s, STAGE_BYTES);
+                    const int kx = (kb0 + kb) * BK;
+                    tma_load_2d(&mp.a_hi[z], full + s, st, kx, ay);
+                    tma_load_2d(&mp.a_lo[z], full + s, st + A_TILE, kx, ay);
+                    tma_load_2d(&mp.b_hi[z], full + s, st + 2 * A_TILE, kx, by);
+                    tma_load_2d(&mp.b_lo[z], full + s, st + 2 * A_TILE + B_TILE, kx, by);
+                    *issued_kb = g + 1;
+                }
+                if (!ok) break;
+            }
+        }
+    } else if (warp == 5 && lane == 0) {
+        // ---- MMA issuer
+        constexpr uint32_t idesc = idesc_bf16(BM, BN);
+        int g = 0;
+        for (int j = 0; !*abort_flag; ++j) {
+            const int q = j % kItemRing;
+            if (!mbar_wait_ab(item_full + q, (j / kItemRing) & 1, e.status, e.wait_ns, abort_flag)) break;
+            const int t = item_ring[q];
+            asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(item_empty + q)) : "memory");
+            if (t >= total) break;
+            const int nki = t < 2 * ks * one ? nk / ks : nk;
+            const int b = j & 1, u = j >> 1;
+            if (u > 0 && !mbar_wait_ab(acc_empty + b, (u - 1) & 1, e.status, e.wait_ns, abort_flag)) break;
+            tc_fence_after();
+            const uint32_t d = tmem + (uint32_t)(b * BN);
+            bool ok = true;
+            for (int kb = 0; kb < nki; ++kb, ++g) {
+                const int s = g % STAGES, round = g / STAGES;
+                if (!mbar_wait_ab(full + s, round & 1, e.status, e.wait_ns, abort_flag)) {
+                    ok = false;
+                    break;
+                }
+                *consumed_kb = g + 1;
+                tc_fence_after();
+                const uint32_t base = smem_u32(smem + s * STAGE_BYTES);
+                const uint64_t ahi = smem_desc(base), alo = smem_desc(base + A_TILE);
+                const uint64_t bhi = smem_desc(base + 2 * A_TILE), blo = smem_desc(base + 2 * A_TILE + B_TILE);
+#pragma unroll
+                for (int k = 0; k < BK / 16; ++k) {
+                    const uint64_t adv = (uint64_t)((k * 32) >> 4);  // 16 bf16 = 32 bytes along K
+                    mma_bf16(d, ahi + adv, bhi + adv, idesc, (kb | k) != 0);
+                    mma_bf16(d, ahi + adv, blo + adv, idesc, 1u);
+                    mma_bf16(d, alo + adv, bhi + adv, idesc, 1u);
+                }
+                mma_commit(empty + s);  // stage s reusable once these MMAs have read it
+            }
+            if (!ok) break;
+            mma_commit(acc_full + b);  // accumulator b complete
+        }
+        mma_commit(drain);  // every MMA this thread issued has retired
+    } else if (warp < 4) {
+        // ---- epilogue: a warp's 32 rows through its own staging rows (lane =
+        // row -> lane = column), then two rows per store instruction, coalesced
+        float *wst = stg + warp * 32 * 33;
+        const uint32_t wst_s = smem_u32(wst);
+        const int rl = warp * 32 + lane;  // this lane's row in the tile
+        for (int j = 0;; ++j) {
+            // one decision for the warp on every wait (its lanes poll on their
+            // own, and the TMEM loads and warp syncs below need all of them)
+            const int q = j % kItemRing;
+            if (!__all_sync(0xffffffffu, mbar_wait_ab(item_full + q, (j / kItemRing) & 1, e.status, e.wait_ns,
+                                                      abort_flag)))
+                break;
+            const int t = item_ring[q];
+            __syncwarp();
+            if (lane == 0)
+                asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(item_empty + q)) : "memory");
+            if (t >= total) break;
+            const int b = j & 1, u = j >> 1;
+            if (!__all_sync(0xffffffffu, mbar_wait_ab(acc_full + b, u & 1, e.status, e.wait_ns, abort_flag))) break;
+            tc_fence_after();
+            const PItem it = p_item(t, nM, nN, ks);
+            const int row0 = it.mb * BM + warp * 32;
+            const bool split = it.s < 2 && ks > 1;
+            const int tile = it.mb * nN + it.nb;
+            // spectral stage: this lane's row frequency (rows row0 + lane)
+            const float wx_lane = it.s == 1 ? __ldg(e.wx + row0 + lane) : 0.f;
+            const float rscale = e.scale;
+            const size_t tile_elems = (size_t)BM * BN;
+            float *part_mine = split ? e.part + ((size_t)(it.s * 2 + it.kh) * one + tile) * tile_elems : nullptr;
+
+            // the staged 32 x 32 block of columns c0.. of this warp's rows ->
+            // the stage's outputs: every staging load first, then the same
+            // region holds the output boxes (32 x 32, row-major: two rows per
+            // store instruction, two adjacent columns per lane, packed BF16
+            // conversions), which lane 0 hands to the TMA as tile stores
+            const int box_x0 = it.nb * BN, box_y = row0;
+            auto store_chunk = [&](int c0) {
+                const int half = lane >> 4, cp = 2 * (lane & 15);
+                const int col = box_x0 + c0 + cp;
+                float v[32];
+#pragma unroll
+                for (int k = 0; k < 16; ++k) {
+                    const uint32_t sa = wst_s + (uint32_t)(((2 * k + half) * 33 + cp) * 4);
+                    v[2 * k] = ld_shared_f1(sa);
+                    v[2 * k + 1] = ld_shared_f1(sa + 4);
+                }
+                __syncwarp();  // the region is free for the boxes
+                auto put_split = [&](int map) {
+                    // hi box at +0, lo box at +2048 (64-byte rows)
+#pragma unroll
+                    for (int k = 0; k < 16; ++k) {
+                        const float a = v[2 * k], b = v[2 * k + 1];
+                        const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+                        const float2 hf = __bfloat1622float2(h);
+                        const uint32_t o = (uint32_t)((2 * k + half) * 64 + cp * 2);
+                        st_shared_u32(wst_s + o, *reinterpret_cast<const uint32_t *>(&h));
+                        st_shared_u32(wst_s + 2048 + o, pack_bf16(a - hf.x, b - hf.y));
+                    }
+                    fence_async_smem();
+                    __syncwarp();
+                    if (lane == 0) {
+                        tma_store_2d(&maps.out[map], wst_s, box_x0 + c0, box_y);
+                        tma_store_2d(&maps.out[map + 1], wst_s + 2048, box_x0 + c0, box_y);
+                        bulk_commit();
+                        bulk_wait_read();
+                    }
+                    __syncwarp();
+                };
+                if (it.s == 3) {
+#pragma unroll
+                    for (int k = 0; k < 16; ++k)
+                        st_shared_f2(wst_s + (uint32_t)((2 * k + half) * 128 + cp * 4), v[2 * k], v[2 * k + 1]);
+                    fence_async_smem();
+                    __syncwarp();
+                    if (lane == 0) {
+                        tma_store_2d(&maps.out[OUT_EX + it.z], wst_s, box_x0 + c0, box_y);
+                        bulk_commit();
+                        bulk_wait_read();
+                    }
+                    __syncwarp();
+                } else if (it.s == 1) {
+                    // spectral scaling of fft.cpp:217-273, as epi_store; Px then Py
+                    const float wy0 = __ldg(e.wy + col), wy1 = __ldg(e.wy + col + 1);
+                    float phi[32], wxr[16];
+#pragma unroll
+                    for (int k = 0; k < 16; ++k) {
+                        const int lr = 2 * k + half, row = row0 + lr;
+                        const float wx = __shfl_sync(0xffffffffu, wx_lane, lr);
+                        const float rs = row == 0 ? 0.5f * rscale : rscale;
+                        float v0 = v[2 * k] * rs, v1 = v[2 * k + 1] * rs;
+                        if (col == 0) v0 *= 0.5f;
+                        const float d0 = wx * wx + wy0 * wy0, d1 = wx * wx + wy1 * wy1;
+                        phi[2 * k] = d0 > 0.f ? __fdividef(v0, d0) : 0.f;
+                        phi[2 * k + 1] = d1 > 0.f ? __fdividef(v1, d1) : 0.f;
+                        wxr[k] = wx;
+                    }
+#pragma unroll
+                    for (int k = 0; k < 16; ++k) {
+                        v[2 * k] = phi[2 * k] * wxr[k];
+                        v[2 * k + 1] = phi[2 * k + 1] * wxr[k];
+                    }
+                    put_split(OUT_PX);
+#pragma unroll
+                    for (int k = 0; k < 16; ++k) {
+                        v[2 * k] = phi[2 * k] * wy0;
+                        v[2 * k + 1] = phi[2 * k + 1] * wy1;
+                    }
+                    put_split(OUT_PY);
+                } else {
+                    put_split(it.s == 0 ? OUT_T : (it.z ? OUT_UY : OUT_UX));
+                }
+            };
+
+            bool finish = true;
+#pragma unroll 1
+            for (int c0 = 0; c0 < BN; c0 += 32) {
+                uint32_t r[32];
+                tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(b * BN + c0), r);
+                if (c0 + 32 == BN) {
+                    // accumulator b read out: the MMAs of a later tile may overwrite it
+                    tc_fence_before();
+                    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(acc_empty + b))
+                                 : "memory");
+                }
+                if (split) {
+                    // this half's partial of the lane's row, 128 contiguous bytes
+                    float *pr = part_mine + (size_t)rl * BN + c0;
+#pragma unroll
+                    for (int i = 0; i < 8; ++i)
+                        st_global_f4(pr + 4 * i, make_float4(__uint_as_float(r[4 * i]), __uint_as_float(r[4 * i + 1]),
+                                                             __uint_as_float(r[4 * i + 2]),
+                                                             __uint_as_float(r[4 * i + 3])));
+                } else {
+#pragma unroll
+                    for (int i = 0; i < 32; ++i)
+                        st_shared_f1(wst_s + (uint32_t)((lane * 33 + i) * 4), __uint_as_float(r[i]));
+                    __syncwarp();
+                    store_chunk(c0);
+                    __syncwarp();
+                }
+            }
+            if (split) {
+                // the second of the two halves (per warp: its 32 rows) adds the
+                // partials in a fixed order and finishes the rows
+                __threadfence();
+                __syncwarp();
+                unsigned int prior = 0;
+                if (lane == 0) prior = atomicAdd(halves + 4 * (it.s * one + tile) + warp, 1u);
+                prior = __shfl_sync(0xffffffffu, prior, 0);
+                finish = prior == 1u;
+                if (finish) {
+                    __threadfence();
+                    const float *p0 = e.part + ((size_t)(it.s * 2 + 0) * one + tile) * tile_elems + (size_t)rl * BN;
+                    const float *p1 = e.part + ((size_t)(it.s * 2 + 1) * one + tile) * tile_elems + (size_t)rl * BN;
+#pragma unroll 1
+                    for (int c0 = 0; c0 < BN; c0 += 32) {
+                        float4 a[8], c[8];
+#pragma unroll
+                        for (int i = 0; i < 8; ++i) {
+                            a[i] = __ldcg(reinterpret_cast<const float4 *>(p0 + c0) + i);
+                            c[i] = __ldcg(reinterpret_cast<const float4 *>(p1 + c0) + i);
+                        }
+#pragma unroll
+                        for (int i = 0; i < 8; ++i) {
+                            const uint32_t sa = wst_s + (uint32_t)((lane * 33 + 4 * i) * 4);
+                            st_shared_f1(sa, a[i].x + c[i].x);
+                            st_shared_f1(sa + 4, a[i].y + c[i].y);
+                            st_shared_f1(sa + 8, a[i].z + c[i].z);
+                            st_shared_f1(sa + 12, a[i].w + c[i].w);
+                        }
+                        __syncwarp();
+                        store_chunk(c0);
+                        __syncwarp();
+                    }
+                }
+            }
+            if (finish && lane == 0) {
+                // this warp's tile stores complete in global memory before its
+                // count moves (their readers load them with the TMA too); each
+                // epilogue warp counts for itself (no barrier across warps that
+                // an abort could leave one of them waiting at)
+                bulk_wait_all();
+                asm volatile("fence.proxy.async.global;" ::: "memory");
+                __threadfence();
+                atomicAdd(rows_done + (2 * it.s + it.z) * nM + it.mb, 1u);
+            }
+            __syncwarp();
+        }
+        if (lane == 0) bulk_wait_all();  // no tile store in flight when the CTA leaves
+    }
+    __syncwarp();
+
+    // ---- teardown: no MMA in flight, no load in flight, then TMEM back
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        mbar_wait(drain, 0, e.status, 2 * e.wait_ns);
+        // loads issued but never waited for (after an abort): let them land
+        for (int kb = *consumed_kb; kb < *issued_kb; ++kb)
+            mbar_wait(full + (kb % STAGES), (kb / STAGES) & 1, e.status, e.wait_ns);
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
+    }
+    // the last CTA out leaves the queue and the counters at zero for the next solve
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(finished, 1u) == (unsigned int)G - 1u) {
+            *queue = 0u;
+            const int n = 8 * nM + (ks > 1 ? 8 * one : 0);
+            for (int i = 0; i < n; ++i) rows_done[i] = 0u;
+            __threadfence();
+            *finished = 0u;
+        }
+    }
+}
+
 // ---- host side ---------------------------------------------------------------
 
 PFN_cuTensorMapEncodeTiled_v12000 encoder() {
@@ -547,7 +1115,22 @@ bool make_map(CUtensorMap *map, const __nv_bfloat16 *base, int m, int box_rows) 
 
 struct StageMaps {
     Maps s1, s2, s3, s4;
+    CUtensorMap out[kOutMaps];  // the persistent solve's outputs ([10, 11]: set per call)
 };
+
+// m x m outputs of 2- or 4-byte elements, 32 x 32 boxes (tile stores)
+bool make_out_map(CUtensorMap *map, void *base, bool f32, int m) {
+    PFN_cuTensorMapEncodeTiled_v12000 enc = encoder();
+    if (!enc || ((uintptr_t)base & 15)) return false;
+    const int elem = f32 ? 4 : 2;
+    cuuint64_t dims[2] = {(cuuint64_t)m, (cuuint64_t)m};
+    cuuint64_t strides[1] = {(cuuint64_t)m * elem};
+    cuuint32_t box[2] = {(cuuint32_t)kBox, (cuuint32_t)kBox};
+    cuuint32_t estr[2] = {1, 1};
+    return enc(map, f32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, base, dims, strides,
+               box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
 
 // Tensor maps of the four stages for B tiles of `bn` rows.
 bool build_stage_maps(StageMaps &h, const FieldSolver &f, const __nv_bfloat16 *d_hi, const __nv_bfloat16 *d_lo,
@@ -568,6 +1151,9 @@ bool build_stage_maps(StageMaps &h, const FieldSolver &f, const __nv_bfloat16 *d
     ok &= make_map(&h.s4.b_hi[0], f.b_ux_hi, m, bn) && make_map(&h.s4.b_lo[0], f.b_ux_lo, m, bn);
     ok &= make_map(&h.s4.a_hi[1], f.Ct_hi, m, BM) && make_map(&h.s4.a_lo[1], f.Ct_lo, m, BM);
     ok &= make_map(&h.s4.b_hi[1], f.b_uy_hi, m, bn) && make_map(&h.s4.b_lo[1], f.b_uy_lo, m, bn);
+    __nv_bfloat16 *outs[10] = {f.b_t_hi, f.b_t_lo, f.b_px_hi, f.b_px_lo, f.b_py_hi,
+                               f.b_py_lo, f.b_ux_hi, f.b_ux_lo, f.b_uy_hi, f.b_uy_lo};
+    for (int i = 0; i < 10; ++i) ok &= make_out_map(&h.out[i], outs[i], false, m);
     // the batch-1 slots of S1/S2 repeat batch 0 (never read: those launches have gridDim.z == 1)
     h.s1.a_hi[1] = h.s1.a_hi[0]; h.s1.a_lo[1] = h.s1.a_lo[0]; h.s1.b_hi[1] = h.s1.b_hi[0]; h.s1.b_lo[1] = h.s1.b_lo[0];
     h.s2.a_hi[1] = h.s2.a_hi[0]; h.s2.a_lo[1] = h.s2.a_lo[0]; h.s2.b_hi[1] = h.s2.b_hi[0]; h.s2.b_lo[1] = h.s2.b_lo[0];
@@ -660,10 +1246,72 @@ void run_stages(const StageMaps &h, FieldSolver &f, float *ex, float *ey, cudaSt
     launch_stage<T>(h.s4, e, m, 2, per_sm, st);
 }
 
+// Resident CTAs of the persistent solve on the whole GPU (0: cannot run).
+template <class T>
+int persist_capacity() {
+    static int cap = -1;
+    if (cap < 0) {
+        int dev = 0, sms = 0, per_sm = 0;
+        cap = 0;
+        if (cudaGetDevice(&dev) == cudaSuccess &&
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess &&
+            cudaFuncSetAttribute(persist_solve_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 PCfg<T>::SMEM_BYTES) == cudaSuccess &&
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, persist_solve_kernel<T>, P_THREADS,
+                                                          PCfg<T>::SMEM_BYTES) == cudaSuccess)
+            cap = sms * per_sm;
+    }
+    return cap;
+}
+
+// false (nothing launched) if the field outputs cannot take tile stores
+template <class T>
+bool run_persistent(const StageMaps &h, FieldSolver &f, int ks, float *ex, float *ey, cudaStream_t st,
+                    const int *gate, int gate_mask) {
+    const int m = f.m, one = (m / BM) * (m / T::BN), total = 2 * ks * one + 4 * one;
+    const int grid = std::min(total, persist_capacity<T>());
+    PMaps pm;
+    pm.st[0] = h.s1;
+    pm.st[1] = h.s2;
+    pm.st[2] = h.s3;
+    pm.st[3] = h.s4;
+    for (int i = 0; i < OUT_EX; ++i) pm.out[i] = h.out[i];
+    // the field outputs are the caller's buffers: their maps are made per call
+    if (!make_out_map(&pm.out[OUT_EX], ex, true, m) || !make_out_map(&pm.out[OUT_EX + 1], ey, true, m)) return false;
+    PEpi e{};
+    e.m = m;
+    e.ks = ks;
+    e.part = f.tc_part;
+    e.t_hi = f.b_t_hi;
+    e.t_lo = f.b_t_lo;
+    e.px_hi = f.b_px_hi;
+    e.px_lo = f.b_px_lo;
+    e.py_hi = f.b_py_hi;
+    e.py_lo = f.b_py_lo;
+    e.ux_hi = f.b_ux_hi;
+    e.ux_lo = f.b_ux_lo;
+    e.uy_hi = f.b_uy_hi;
+    e.uy_lo = f.b_uy_lo;
+    e.ex = ex;
+    e.ey = ey;
+    e.wx = f.wx;
+    e.wy = f.wy;
+    e.scale = 4.0f / ((float)m * (float)m);
+    e.status = f.tc_status;
+    e.sync = f.tc_sync;
+    e.gate = gate;
+    e.gate_mask = gate_mask;
+    e.skip_loads = f.fault_stall;
+    e.wait_ns = f.fault_stall ? f.fault_wait_ns : WAIT_NS;
+    persist_solve_kernel<T><<<grid, P_THREADS, PCfg<T>::SMEM_BYTES, st>>>(pm, e);
+    return true;
+}
+
 void run_variant(int v, FieldSolver &f, float *ex, float *ey, cudaStream_t st, const int *gate = nullptr,
                  int gate_mask = 0) {
     const TcState &s = *reinterpret_cast<const TcState *>(f.tc_maps);
-    if (v == 1)
+    if (v >= 3 && run_persistent<Tile128>(s.maps[1], f, v == 3 ? 2 : 1, ex, ey, st, gate, gate_mask)) return;
+    if (v == 1 || v >= 3)
         run_stages<Tile128>(s.maps[1], f, ex, ey, st, gate, gate_mask);
     else if (v == 2)
         run_stages<Tile64x2>(s.maps[0], f, ex, ey, st, gate, gate_mask);
@@ -689,6 +1337,14 @@ int field_solver_bind_bf16(FieldSolver &f, const __nv_bfloat16 *d_hi, const __nv
     *reinterpret_cast<TcState *>(f.tc_maps) = s;
     if (!f.tc_status && cudaMalloc(&f.tc_status, sizeof(unsigned int)) != cudaSuccess) return AP_ERR_CUDA;
     if (cudaMemset(f.tc_status, 0, sizeof(unsigned int)) != cudaSuccess) return AP_ERR_CUDA;
+    // the persistent solve's counters (queue head, CTAs finished, 4 stages x 2
+    // products x row blocks, 2 stages x tiles x 4 warps of halves) and its
+    // split-K partials (2 stages x 2 halves x tiles of 128 x 128 FP32)
+    const size_t nm = (size_t)(f.m / BM), tiles = nm * nm;
+    const size_t sync_bytes = sizeof(unsigned int) * (2 + 8 * nm + 8 * tiles);
+    if (!f.tc_sync && cudaMalloc(&f.tc_sync, sync_bytes) != cudaSuccess) return AP_ERR_CUDA;
+    if (cudaMemset(f.tc_sync, 0, sync_bytes) != cudaSuccess) return AP_ERR_CUDA;
+    if (!f.tc_part && cudaMalloc(&f.tc_part, sizeof(float) * 4 * tiles * BM * BM) != cudaSuccess) return AP_ERR_CUDA;
     if (cudaFuncSetAttribute(gemm_bf16x3_kernel<Tile64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              Tile64::SMEM_BYTES) != cudaSuccess ||
         cudaFuncSetAttribute(gemm_bf16x3_kernel<Tile128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -702,28 +1358,38 @@ int field_solver_bind_bf16(FieldSolver &f, const __nv_bfloat16 *d_hi, const __nv
         return AP_ERR_CUDA;
     cudaEvent_t e0, e1;
     if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) return AP_ERR_CUDA;
-    float best = 1e30f;
-    f.tc_variant = 0;
-    for (int v = 0; v < kTcVariants; ++v) {
-        for (int w = 0; w < 3; ++w) run_variant(v, f, f.ux, f.uy, 0);
-        cudaEventRecord(e0, 0);
-        for (int t = 0; t < 5; ++t) run_variant(v, f, f.ux, f.uy, 0);
-        cudaEventRecord(e1, 0);
-        if (cudaEventSynchronize(e1) != cudaSuccess) {
-            cudaEventDestroy(e0);
-            cudaEventDestroy(e1);
-            return AP_ERR_CUDA;
-        }
-        float ms = 0.f;
-        cudaEventElapsedTime(&ms, e0, e1);
-        f.tc_tune_ms[v] = ms / 5;
-        if (ms < best) {
-            best = ms;
-            f.tc_variant = v;
+    // two passes over the candidates, each keeping its faster pass: the
+    // first candidate timed on a cold GPU (clocks, caches) would otherwise
+    // look slower than it is
+    for (int v = 0; v < kTcVariants; ++v) f.tc_tune_ms[v] = -1.f;  // not run
+    for (int pass = 0; pass < 2; ++pass) {
+        for (int v = 0; v < kTcVariants; ++v) {
+            if (v >= 3 && persist_capacity<Tile128>() <= 0) continue;
+            for (int w = 0; w < 3; ++w) run_variant(v, f, f.ux, f.uy, 0);
+            cudaEventRecord(e0, 0);
+            for (int t = 0; t < 5; ++t) run_variant(v, f, f.ux, f.uy, 0);
+            cudaEventRecord(e1, 0);
+            if (cudaEventSynchronize(e1) != cudaSuccess) {
+                cudaEventDestroy(e0);
+                cudaEventDestroy(e1);
+                return AP_ERR_CUDA;
+            }
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            ms /= 5;
+            if (f.tc_tune_ms[v] < 0.f || ms < f.tc_tune_ms[v]) f.tc_tune_ms[v] = ms;
         }
     }
+    f.tc_variant = 0;
+    for (int v = 1; v < kTcVariants; ++v)
+        if (f.tc_tune_ms[v] >= 0.f && f.tc_tune_ms[v] < f.tc_tune_ms[f.tc_variant]) f.tc_variant = v;
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
+    // AP_TC_VARIANT=0..4 pins a candidate that ran (tests of each variant)
+    if (const char *pin = getenv("AP_TC_VARIANT")) {
+        const int v = atoi(pin);
+        if (v >= 0 && v < kTcVariants && f.tc_tune_ms[v] >= 0.f) f.tc_variant = v;
+    }
     unsigned int st = 0;
     if (cudaMemcpy(&st, f.tc_status, sizeof(st), cudaMemcpyDeviceToHost) != cudaSuccess) return AP_ERR_CUDA;
     if (st) return AP_ERR_TIMEOUT;

@@ -104,7 +104,7 @@ class Placer:
 
     def solver_info(self) -> dict:
         tv, st = C.c_int32(), C.c_int32()
-        tms, sms = np.zeros(3, np.float32), np.zeros(2, np.float32)
+        tms, sms = np.zeros(5, np.float32), np.zeros(2, np.float32)
         check("ap_solver_info", lib().ap_solver_info(self._h, C.byref(tv), ptr(tms), C.byref(st), ptr(sms)))
         return {"tc_variant": tv.value, "tc_ms": [float(v) for v in tms], "simt_tile": st.value,
                 "simt_ms": [float(v) for v in sms]}

@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-#define AP_ABI_VERSION 2
+#define AP_ABI_VERSION 3
 
 /* ---- status codes ------------------------------------------------------ */
 enum {
@@ -176,10 +176,15 @@ int ap_profile_stages(ap_handle *h, int32_t n_trials, float *stage_ms, int32_t *
 int ap_set_log(ap_handle *h, const char *path, int32_t capacity);
 
 /* Tile shapes the autotuner picked at ap_create for this bin count, and the
- * solve times it measured: tc_variant is the tensor-core candidate (0: 128 x 64
- * tiles, 4 pipeline stages; 1: 128 x 128, 3 stages; 2: 128 x 64, 2 stages, two
- * CTAs per SM; -1 if the tensor-core path is unavailable), simt_tile the FP32
- * tile side (32 or 64); tc_ms[3] and simt_ms[2] the candidates' times. */
+ * solve times it measured: tc_variant is the tensor-core candidate (0: four
+ * launches of 128 x 64 tiles, 4 pipeline stages; 1: 128 x 128, 3 stages; 2:
+ * 128 x 64, 2 stages, two CTAs per SM; 3: one persistent launch over the four
+ * stages' 128 x 128 tiles, K of the first two stages split in two; 4: the
+ * same without the split; -1 if the
+ * tensor-core path is unavailable), simt_tile the FP32 tile side (32 or 64);
+ * tc_ms[5] and simt_ms[2] the candidates' times (-1: not run).  The
+ * environment variable AP_TC_VARIANT=0..4, read at ap_create, pins a
+ * candidate that ran instead of the fastest (for testing each one). */
 int ap_solver_info(ap_handle *h, int32_t *tc_variant, float *tc_ms, int32_t *simt_tile, float *simt_ms);
 
 /* Iterates until overflow < params.target_overflow or max_iterations;
