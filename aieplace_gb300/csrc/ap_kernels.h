@@ -98,6 +98,10 @@ struct ScatterArgs {
     // (<= the block size: one per thread); results depend on it only
     // through the order of the update's FP32 block sums
     int block_nodes;
+    // bin adds: the shared tile accumulates each value's bits [0, 16) and
+    // [16, 48) in two 32-bit words (set by the launcher where no word can
+    // overflow); 0: one 64-bit word
+    int tile32;
 };
 void launch_scatter(const ScatterArgs &a, cudaStream_t st);
 // the two launches of launch_scatter: the position update and records (update

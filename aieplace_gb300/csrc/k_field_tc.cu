@@ -24,6 +24,11 @@
 //                   epilogue and stores a warp per row, coalesced
 // Every mbarrier wait is bounded; a wait that gives up sets the solver's
 // status word and the CTA drains and exits without further issue.
+//
+// A second form, persist_solve_kernel, runs the four stages as one launch
+// (tiles claimed from a device queue, row-block dependency counters between
+// the stages, TMA tile stores); the tile autotuner times it beside the
+// four-launch shapes and keeps whichever is fastest.
 #include <cuda.h>
 
 #include <algorithm>

@@ -38,7 +38,7 @@ __device__ __forceinline__ float rcp(float b) { return __fdividef(1.f, b); }
 // one pin's gradient into its node's accumulators; `raw` is the pin_node entry
 __device__ __forceinline__ void add_grad(ull *gq, ull *gqx, ull *gqy, int raw, float gx, float gy) {
     const int n = raw & kPinNode;
-    if (raw >= 0) {
+    if (__builtin_expect(raw >= 0, 1)) {  // nodes of more than kPackMaxPins pins are rare
         atomicAdd(gq + n, pack_q(grad_q32(gx), grad_q32(gy)));
     } else {
         atomicAdd(gqx + n, grad_q(gx));
@@ -104,20 +104,21 @@ __device__ __forceinline__ void net_group(const WaArgs &a, int s, int d, int l, 
     for (int p = 0; p < P; ++p) {
         const int j = l + p * G;
         v[p] = j < d;
-        nd[p] = v[p] ? __ldg(a.pin_node + s + j) : 0;  // raw entry (heavy flag)
-        const float2 q = v[p] ? __ldg(xy + (nd[p] & kPinNode)) : make_float2(0.f, 0.f);
+        // a slot past the net's end repeats its last pin: the extrema are
+        // unchanged and no load waits on a branch (its terms are zeroed below)
+        nd[p] = __ldg(a.pin_node + s + min(j, d - 1));  // raw entry (heavy flag)
+        const float2 q = __ldg(xy + (nd[p] & kPinNode));
         c[p][0] = q.x;
         c[p][1] = q.y;
     }
     float m4[4] = {-3.0e38f, -3.0e38f, -3.0e38f, -3.0e38f};  // max x, max y, -min x, -min y
 #pragma unroll
-    for (int p = 0; p < P; ++p)
-        if (v[p]) {
-            m4[0] = fmaxf(m4[0], c[p][0]);
-            m4[1] = fmaxf(m4[1], c[p][1]);
-            m4[2] = fmaxf(m4[2], -c[p][0]);
-            m4[3] = fmaxf(m4[3], -c[p][1]);
-        }
+    for (int p = 0; p < P; ++p) {
+        m4[0] = fmaxf(m4[0], c[p][0]);
+        m4[1] = fmaxf(m4[1], c[p][1]);
+        m4[2] = fmaxf(m4[2], -c[p][0]);
+        m4[3] = fmaxf(m4[3], -c[p][1]);
+    }
     group_max4<G>(m4, l, mask, base);
     const float mx[2] = {m4[0], m4[1]}, mn[2] = {-m4[2], -m4[3]};
     float ep[P][2], em[P][2], s8[8];

@@ -611,10 +611,22 @@ def main():
             achieved = amount / (stage_ms[dom] / 1000.0) / 1e12
             peak = float(peaks.get("bf16_tflops", 1900.0))
             unit = "TFLOP/s"
+        # every stage against its own roof (HBM copy or dense BF16 burst)
+        per_stage = []
+        for i, name in enumerate(STAGES):
+            b_i, amt_i = model[name]
+            sec = stage_ms[i] / 1000.0
+            if b_i == "hbm":
+                ach_i, pk_i, u_i = amt_i / sec / 1e9, float(peaks.get("hbm_gbs", 6800.0)), "GB/s"
+            else:
+                ach_i, pk_i, u_i = amt_i / sec / 1e12, float(peaks.get("bf16_tflops", 1900.0)), "TFLOP/s"
+            per_stage.append({"stage": name, "bound": b_i, "algorithmic": amt_i, "us": stage_ms[i] * 1000.0,
+                              "achieved": ach_i, "unit": u_i, "frac": ach_i / pk_i,
+                              "traffic": read_traffic(name, args.preset)})
         roof = {"kernel": STAGES[dom], "bound": bound, "achieved": achieved, "peak": peak, "unit": unit,
                 "frac": achieved / peak, "traffic": read_traffic(STAGES[dom], args.preset),
                 "peak_source": "measured" if peaks else "fallback",
-                "stage_ms": dict(zip(STAGES, stage_ms))}
+                "stage_ms": dict(zip(STAGES, stage_ms)), "stages": per_stage}
         if not args.no_ttt:
             ttt = {"mixed": time_to_target(ap, nl, "bf16x3") if solver == "bf16x3" else None,
                    "plain": time_to_target(ap, nl, "fp32")}
