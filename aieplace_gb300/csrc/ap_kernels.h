@@ -249,6 +249,8 @@ int wave_of(const void *kernel, int threads, int fallback, int dyn_smem = 0);
 // record of the same instance runs the same blocks)
 int update_grid(const ScatterArgs &a);
 int scatter_grid(int n, int block_nodes);
+// whether the bin adds of n nodes over `blocks` blocks may use 32-bit tile slots
+bool tile32_exact(const Grid &g, int n, int blocks);
 int rho_grid(int nbins);
 int gather_grid(int n_mov, int block_nodes);
 // fills bucket_blocks and small_blocks as launch_wirelength does; returns

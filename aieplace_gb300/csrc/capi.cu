@@ -1911,15 +1911,17 @@ int plan_build(ap_batch *b, PersistPlan &pp) {
         s.hi = h->n_real;
         s.rho_q = h->d_mov_q;
         if (s.hi > s.lo) {
-            sct.push_back(s);
             bs.push_back(scatter_grid(s.hi - s.lo, s.block_nodes));
+            s.tile32 = tile32_exact(s.g, s.hi - s.lo, bs.back()) ? 1 : 0;
+            sct.push_back(s);
         }
         if (h->n_fill) {
             s.lo = h->n_real;
             s.hi = h->n_mov;
             s.rho_q = h->d_fill_q;
-            sct.push_back(s);
             bs.push_back(scatter_grid(s.hi - s.lo, s.block_nodes));
+            s.tile32 = tile32_exact(s.g, s.hi - s.lo, bs.back()) ? 1 : 0;
+            sct.push_back(s);
         }
         const RhoArgs ra = rho_args(h, RHO_LOOP, nullptr);
         rho.push_back(ra);
