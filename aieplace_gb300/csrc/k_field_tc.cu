@@ -607,8 +607,7 @@ struct PMaps {
 struct PEpi {
     int m;
     int ks;  // K split of stages 1-2 (1 or 2)
-    __nv_bfloat16 *t_hi, *t_lo, *px_hi, *px_lo, *py_hi, *py_lo, *ux_hi, *ux_lo, *uy_hi, *uy_lo;
-    float *ex, *ey;
+    // the outputs are written through the tile-store maps of PMaps::out
     const float *wx, *wy;
     float scale;
     unsigned int *status;
@@ -1287,18 +1286,6 @@ bool run_persistent(const StageMaps &h, FieldSolver &f, int ks, float *ex, float
     e.m = m;
     e.ks = ks;
     e.part = f.tc_part;
-    e.t_hi = f.b_t_hi;
-    e.t_lo = f.b_t_lo;
-    e.px_hi = f.b_px_hi;
-    e.px_lo = f.b_px_lo;
-    e.py_hi = f.b_py_hi;
-    e.py_lo = f.b_py_lo;
-    e.ux_hi = f.b_ux_hi;
-    e.ux_lo = f.b_ux_lo;
-    e.uy_hi = f.b_uy_hi;
-    e.uy_lo = f.b_uy_lo;
-    e.ex = ex;
-    e.ey = ey;
     e.wx = f.wx;
     e.wy = f.wy;
     e.scale = 4.0f / ((float)m * (float)m);

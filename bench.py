@@ -41,7 +41,16 @@ sys.path.insert(0, os.path.join(HERE, "oracle"))
 
 METRIC = "Nesterov iters/s & time-to-10% overflow, 2M cells: mixed+surrogate vs plain"
 UNIT = "iters/s"
-KERNELS_PER_TRIAL = 12  # update, scatter, rho, 4x WA (degree buckets), 4x field, gather
+# per trial: update, scatter, rho, 4x WA (degree buckets), the field solve, gather
+KERNELS_BESIDE_FIELD = 8
+
+
+def field_launches(info: dict, solver: str) -> int:
+    """Launches of one field solve: four stage launches, or one for the
+    persistent tensor-core candidates (3, 4)."""
+    return 1 if solver == "bf16x3" and info.get("tc_variant", -1) in (3, 4) else 4
+
+
 STAGES = ["scatter+update", "density+overflow", "wirelength", "field", "gather+control"]
 
 
@@ -581,6 +590,7 @@ def main():
     se1 = pl.stats()
     e2e_iters = se1["iteration"] - se0["iteration"]
     n_mov = int((nl["node_fixed"] == 0).sum())
+    launches_per_trial = KERNELS_BESIDE_FIELD + field_launches(pl.solver_info(), solver)
     pl.close()
 
     t_max = ms / 1000.0
@@ -653,7 +663,7 @@ def main():
                        "step": "one trial step (one gradient evaluation); value counts accepted iterations",
                        "parallelism": "replicas" if world > 1 else "single"},
             "iterations": total_iters, "evals": evals, "evals_per_s": evals / t_max,
-            "gpu_launches": KERNELS_PER_TRIAL * args.steps,
+            "gpu_launches": launches_per_trial * args.steps,
             "e2e": {"value": e2e_iters / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 8 * n_mov,
                     "d2h_bytes_per_step": 8 * n + 160, "steps": e2e_steps},
             "roofline": roof, "clocks": clk, "time_to_10pct_overflow": ttt, "cpu_baseline": cpu,
