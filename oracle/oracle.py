@@ -18,6 +18,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "liboracle.so")
 SYNTH_PATH = os.path.join(HERE, "libsynth.so")
 REF_PATH = os.path.join(HERE, "_ref", "libref.so")
+REF_PLACER_PATH = os.path.join(HERE, "_ref", "libref_placer.so")
 # the reference checkout, where one exists: AP_REFERENCE_DIR, or the
 # `ref_dir` argument of build(); there is no default location
 REF_SRC = os.environ.get("AP_REFERENCE_DIR", "")
@@ -30,8 +31,9 @@ _u8p = np.ctypeslib.ndpointer(np.uint8, flags="C_CONTIGUOUS")
 
 
 def build(with_ref: bool | None = None, ref_dir: str | None = None) -> None:
-    """Compile liboracle.so and libsynth.so, and _ref/libref.so when a
-    reference checkout is named (ref_dir, else AP_REFERENCE_DIR) and exists."""
+    """Compile liboracle.so and libsynth.so, and _ref/libref.so and
+    _ref/libref_placer.so when a reference checkout is named (ref_dir, else
+    AP_REFERENCE_DIR) and exists."""
     global REF_SRC
     if ref_dir:
         REF_SRC = ref_dir
@@ -39,7 +41,12 @@ def build(with_ref: bool | None = None, ref_dir: str | None = None) -> None:
     if with_ref is None:
         with_ref = bool(REF_SRC) and os.path.isdir(REF_SRC)
     if with_ref:
-        subprocess.run(["make", "-s", "-C", HERE, f"REF={REF_SRC}", "ref"], check=True)
+        subprocess.run(["make", "-s", "-j8", "-C", HERE, f"REF={REF_SRC}", "ref"], check=True)
+        # the reference's Placer (test infrastructure for its CPU loop): a
+        # failure here leaves only the tests that need it skipped
+        r = subprocess.run(["make", "-s", "-j8", "-C", HERE, f"REF={REF_SRC}", "refplacer"])
+        if r.returncode != 0:
+            print("oracle: the reference placer library did not build; its tests will skip")
 
 
 class OrGrid(C.Structure):
@@ -129,6 +136,143 @@ def ref_lib():
         R.ref_replace_field.argtypes = [C.c_int, _f32p, C.c_void_p, _f32p, _f32p]
         _ref = R
     return _ref
+
+
+_refp = {}
+
+
+def ref_placer_lib(opt: str = "O2"):
+    """The reference's Placer built for the CPU (_ref/libref_placer.so at -O2,
+    _ref/libref_placer_O0.so at -O0), or None where it was not built."""
+    path = REF_PLACER_PATH if opt == "O2" else os.path.join(HERE, "_ref", f"libref_placer_{opt}.so")
+    if opt not in _refp and os.path.exists(path):
+        try:
+            R = C.CDLL(path)
+        except OSError:
+            return None
+        dp = C.POINTER(C.c_double)
+        R.ref_placer_create.restype = C.c_void_p
+        R.ref_placer_create.argtypes = [C.c_int, _f32p, _f32p, _f32p, _f32p, _u8p, C.c_int, _i32p, _i32p,
+                                        C.c_float, C.c_float, C.c_int, C.c_float, C.c_float, C.c_float,
+                                        C.c_char_p]
+        R.ref_placer_destroy.argtypes = [C.c_void_p]
+        R.ref_placer_set_positions.argtypes = [C.c_void_p, _f32p, _f32p]
+        R.ref_placer_partials.argtypes = [C.c_void_p, _f32p, _f32p, dp]
+        R.ref_placer_overlaps.argtypes = [C.c_void_p, _f32p, dp, dp]
+        R.ref_placer_fields_dct.argtypes = [C.c_void_p, _f32p, _f32p, dp]
+        R.ref_placer_nudge.argtypes = [C.c_void_p, _f32p, _f32p, _f32p, _f32p, _f32p, _f32p, dp]
+        R.ref_placer_fields_naive.argtypes = [C.c_void_p, _f32p, _f32p, dp]
+        R.ref_placer_iterate.argtypes = [C.c_void_p, C.c_int, dp]
+        R.ref_placer_get_positions.argtypes = [C.c_void_p, _f32p, _f32p]
+        R.ref_placer_hpwl.restype = C.c_double
+        R.ref_placer_hpwl.argtypes = [C.c_void_p]
+        _refp[opt] = R
+    return _refp.get(opt)
+
+
+class quiet_stdout:
+    """Send file descriptor 1 to /dev/null for the block: the reference's
+    placer prints its tables and transform traces there."""
+
+    def __enter__(self):
+        import sys
+        sys.stdout.flush()
+        self._saved = os.dup(1)
+        dn = os.open(os.devnull, os.O_WRONLY)
+        os.dup2(dn, 1)
+        os.close(dn)
+        return self
+
+    def __exit__(self, *exc):
+        import sys
+        try:
+            C.CDLL(None).fflush(None)
+        except (OSError, AttributeError):
+            pass
+        sys.stdout.flush()
+        os.dup2(self._saved, 1)
+        os.close(self._saved)
+        return False
+
+
+class RefPlacer:
+    """The reference's own Placer (vck5000/host/src/AIEplace.cpp) on a CSR
+    netlist, through ref_placer.cpp.  Every call returns the reference's
+    result and the seconds its own function took."""
+
+    def __init__(self, net_ptr, pin_node, w, h, x, y, fixed, die_w, die_h, bins,
+                 gamma=1.0, learning_rate=1e-3, global_lambda=1.0, opt="O2"):
+        import tempfile
+        R = ref_placer_lib(opt)
+        if R is None:
+            raise RuntimeError("the reference placer library was not built (make refplacer REF=<checkout>)")
+        self._R = R
+        self.n = len(x)
+        self.bins = bins
+        self._dir = tempfile.mkdtemp(prefix="ref_placer_")
+        self._h = R.ref_placer_create(self.n, _f32(w), _f32(h), _f32(x), _f32(y),
+                                      np.ascontiguousarray(fixed, dtype=np.uint8), len(net_ptr) - 1,
+                                      _i32(net_ptr), _i32(pin_node), die_w, die_h, bins, gamma,
+                                      learning_rate, global_lambda, self._dir.encode())
+        if not self._h:
+            raise RuntimeError("ref_placer_create failed")
+
+    def close(self):
+        import shutil
+        if self._h:
+            self._R.ref_placer_destroy(self._h)
+            self._h = None
+            shutil.rmtree(self._dir, ignore_errors=True)
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_positions(self, x, y):
+        self._R.ref_placer_set_positions(self._h, _f32(x), _f32(y))
+
+    def partials(self):
+        gx, gy, t = np.zeros(self.n, np.float32), np.zeros(self.n, np.float32), C.c_double()
+        self._R.ref_placer_partials(self._h, gx, gy, C.byref(t))
+        return gx, gy, t.value
+
+    def overlaps(self):
+        M = self.bins
+        rho, ovf, t = np.zeros(M * M, np.float32), C.c_double(), C.c_double()
+        self._R.ref_placer_overlaps(self._h, rho, C.byref(ovf), C.byref(t))
+        return rho.reshape(M, M), ovf.value, t.value
+
+    def fields_dct(self):
+        M = self.bins
+        ex, ey, t = np.zeros(M * M, np.float32), np.zeros(M * M, np.float32), C.c_double()
+        self._R.ref_placer_fields_dct(self._h, ex, ey, C.byref(t))
+        return ex.reshape(M, M), ey.reshape(M, M), t.value
+
+    def fields_naive(self):
+        M = self.bins
+        ex, ey, t = np.zeros(M * M, np.float32), np.zeros(M * M, np.float32), C.c_double()
+        self._R.ref_placer_fields_naive(self._h, ex, ey, C.byref(t))
+        return ex.reshape(M, M), ey.reshape(M, M), t.value
+
+    def iterate(self, iters: int) -> float:
+        t = C.c_double()
+        self._R.ref_placer_iterate(self._h, iters, C.byref(t))
+        return t.value
+
+    def positions(self):
+        x, y = np.zeros(self.n, np.float32), np.zeros(self.n, np.float32)
+        self._R.ref_placer_get_positions(self._h, x, y)
+        return x, y
+
+    def nudge(self, ex, ey, px, py):
+        mx, my, t = np.zeros(self.n, np.float32), np.zeros(self.n, np.float32), C.c_double()
+        self._R.ref_placer_nudge(self._h, _f32(ex), _f32(ey), _f32(px), _f32(py), mx, my, C.byref(t))
+        return mx, my, t.value
+
+    def hpwl(self) -> float:
+        return self._R.ref_placer_hpwl(self._h)
 
 
 def set_threads(n: int) -> int:
