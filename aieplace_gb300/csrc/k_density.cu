@@ -174,6 +174,7 @@ __device__ __forceinline__ void for_each_overlap(const Grid &g, float x, float y
 // streaming pass; block sums of |u' - u|^2 folded by the last block.  Split
 // from the bin adds, which need few threads per SM's worth of registers and
 // shared memory, so that this part runs at full occupancy.
+template <bool kPair>
 __device__ __forceinline__ void update_body(const ScatterArgs &a, VBlock vb) {
     __shared__ double red[32];  // 64 floats: two block sums
     const float alpha = a.sc->f_alpha, mom = a.sc->f_mom;
@@ -192,13 +193,10 @@ __device__ __forceinline__ void update_body(const ScatterArgs &a, VBlock vb) {
     int *__restrict__ rbin = a.rec_bin;
     int4 *__restrict__ rov = a.rec_ov;
     const int lo = a.upd_hi > 0 ? a.upd_lo : 0, hi = a.upd_hi > 0 ? a.upd_hi : a.n_mov;
-    for (int i = lo + vb.id * blockDim.x + threadIdx.x; i < hi; i += vb.n * blockDim.x) {
-        const float w = __ldg(a.w + i), h = __ldg(a.h + i);
+    auto node = [&](int i, float w, float h, float ux, float uy, float vx, float vy, float gx, float gy) {
         const float xhi = fmaxf(a.die_w - w, 0.f), yhi = fmaxf(a.die_h - h, 0.f);
-        const float ux = uxc[i], uy = uyc[i];
-        const float vx = vxc[i], vy = vyc[i];
-        const float nux = clampf(vx - alpha * gxc[i], 0.f, xhi);
-        const float nuy = clampf(vy - alpha * gyc[i], 0.f, yhi);
+        const float nux = clampf(vx - alpha * gx, 0.f, xhi);
+        const float nuy = clampf(vy - alpha * gy, 0.f, yhi);
         const float x = clampf(nux + mom * (nux - ux), 0.f, xhi);
         const float y = clampf(nuy + mom * (nuy - uy), 0.f, yhi);
         uxn[i] = nux;
@@ -216,7 +214,25 @@ __device__ __forceinline__ void update_body(const ScatterArgs &a, VBlock vb) {
         const NodeRec r = make_rec(g, x, y, w, h, c0, c1, r0, r1);
         rbin[i] = r.bin;
         rov[i] = make_int4(r.xr, r.wq, r.yr, r.hq);
+    };
+    // two nodes of the thread's grid-stride sequence per trip, every load of
+    // both issued before either is used (twice the loads in flight per warp);
+    // the nodes are taken in the same order as one per trip, so the FP32
+    // partial sums are the same
+    // (kPair; the persistent batched form keeps one node per trip, where the
+    // pair's registers would cost it a resident block per SM)
+    const int S = vb.n * blockDim.x;
+    int i = lo + vb.id * blockDim.x + threadIdx.x;
+    for (; kPair && i + S < hi; i += 2 * S) {
+        const int j = i + S;
+        const float w0 = __ldg(a.w + i), h0 = __ldg(a.h + i), w1 = __ldg(a.w + j), h1 = __ldg(a.h + j);
+        const float ux0 = uxc[i], uy0 = uyc[i], ux1 = uxc[j], uy1 = uyc[j];
+        const float vx0 = vxc[i], vy0 = vyc[i], vx1 = vxc[j], vy1 = vyc[j];
+        const float gx0 = gxc[i], gy0 = gyc[i], gx1 = gxc[j], gy1 = gyc[j];
+        node(i, w0, h0, ux0, uy0, vx0, vy0, gx0, gy0);
+        node(j, w1, h1, ux1, uy1, vx1, vy1, gx1, gy1);
     }
+    for (; i < hi; i += S) node(i, __ldg(a.w + i), __ldg(a.h + i), uxc[i], uyc[i], vxc[i], vyc[i], gxc[i], gyc[i]);
     float *pf = reinterpret_cast<float *>(a.partials);
     float bs[2] = {du, dv};
     block_sums_ff<2>(bs, reinterpret_cast<float *>(red));
@@ -240,7 +256,7 @@ __device__ __forceinline__ void update_fold(const ScatterArgs &a, int nb) {
 }
 
 __global__ void __launch_bounds__(kThreads) update_kernel(ScatterArgs a) {
-    update_body(a, grid_block());
+    update_body<true>(a, grid_block());
     if (a.no_fold) return;  // uniform: an earlier chunk of a chunked update
     // the partials of this launch and of the chunks before it (launched
     // earlier on the same stream, so complete)
@@ -1016,7 +1032,7 @@ __global__ void numerics_selftest_kernel(long long n, ull seed, int *mism) {
 
 __global__ void __launch_bounds__(kThreads) persist_update_kernel(PersistQueue q, const ScatterArgs *recs) {
     persist_loop(q, recs, [](const ScatterArgs &a, VBlock vb, int) {
-        update_body(a, vb);
+        update_body<false>(a, vb);
         if (arrive_last(a.counter, vb.n)) update_fold(a, vb.n);
     });
 }
