@@ -322,6 +322,47 @@ def test_step_host_output_only_and_in_place(ap):
         assert s["iteration"] == 6
 
 
+@pytest.mark.parametrize("preset,bins", [("c0", 32), ("c2_small", 512)])
+def test_step_host_pinned_buffers_match_eager_host_step(ap, preset, bins):
+    """Host steps on pinned buffers (asynchronous copies; 200k cells: the
+    input copied in four chunks, each with its own update launch) step
+    exactly as the same calls on pageable buffers, with two buffer sets
+    alternating, in place, and with pageable calls in between."""
+    torch = pytest.importorskip("torch")
+    nl = ap.synth.generate(preset, seed=4)
+    with ap.Placer(nl, bins=bins) as a, ap.Placer(nl, bins=bins) as b:
+        a.initialize_placement(nl["node_x"], nl["node_y"])
+        b.initialize_placement(nl["node_x"], nl["node_y"])
+        n = b.num_nodes
+
+        def pinned():
+            return torch.empty(n, dtype=torch.float32, pin_memory=True).numpy()
+
+        ax, ay = a.positions()
+        axo, ayo = np.zeros_like(ax), np.zeros_like(ay)
+        ix, iy, ox, oy = pinned(), pinned(), pinned(), pinned()  # input, output
+        ix[:], iy[:] = b.positions()
+        for k in range(10):
+            sa = a.step_host(ax, ay, axo, ayo)
+            ax, ay = axo.copy(), ayo.copy()
+            if k == 6:  # in place
+                ox, oy = ix, iy
+            elif k == 7:  # pageable input and output
+                ix, iy = ix.copy(), iy.copy()
+                ox, oy = ix, iy
+            elif k == 8:  # pinned again (new buffers), from the pageable result
+                px, py = pinned(), pinned()
+                px[:], py[:] = ix, iy
+                ix, iy, ox, oy = px, py, pinned(), pinned()
+            s = b.step_host(ix, iy, ox, oy)
+            np.testing.assert_array_equal(ax, ox)
+            np.testing.assert_array_equal(ay, oy)
+            assert s["hpwl"] == sa["hpwl"] and s["overflow"] == sa["overflow"]
+            if ox is not ix:  # the two buffer sets alternate
+                ix, iy, ox, oy = ox, oy, ix, iy
+        assert s["iteration"] == 10
+
+
 def test_errors_are_status_codes(ap):
     from aieplace_gb300 import APError
 
