@@ -229,8 +229,7 @@ int field_solver_bind_bf16(FieldSolver &f, const __nv_bfloat16 *d_hi, const __nv
 // density as bf16 hi/lo split (the bound buffers) -> ex, ey; tcgen05 BF16x3 contraction
 int field_solve_bf16x3(FieldSolver &f, const __nv_bfloat16 *d_hi, const __nv_bfloat16 *d_lo,
                        float *ex, float *ey, cudaStream_t st, const int *gate = nullptr, int gate_mask = 0);
-// nonzero once a bounded wait in a tcgen05 kernel gave up
-int field_solver_status(FieldSolver &f, unsigned int *out);
+// tc_status (nonzero once a bounded wait in a tcgen05 kernel gave up) back to zero
 int field_solver_clear_status(FieldSolver &f);
 // float -> bf16 hi/lo split (for per-stage API calls)
 void launch_split_bf16(int n, const float *src, __nv_bfloat16 *hi, __nv_bfloat16 *lo, cudaStream_t st);

@@ -80,6 +80,7 @@ struct ap_handle {
     unsigned int *d_counters = nullptr;
     double *d_out = nullptr;
     double *h_out = nullptr;  // pinned [4]
+    unsigned int *h_status = nullptr;  // pinned: the tensor-core solve's status word, read by sync()
     int bucket_lo[kWaBuckets + 1] = {};
     FieldSolver fs{};
     cudaStream_t stream = nullptr;
@@ -341,13 +342,16 @@ int enqueue_eval(ap_handle *h, int at, int rho_mode, int wa_mode, cudaStream_t s
     return run_field(h, h->p.field_solver, st);
 }
 
+// Waits for the handle's stream; a tensor-core solve that gave up reports
+// AP_ERR_TIMEOUT.  Its status word is copied behind the stream's work, so
+// one wait covers both (a separate read after the wait was a second round
+// trip per call).
 int sync(ap_handle *h) {
+    const bool tc = h->fs.tc_ready && h->fs.tc_status;
+    if (tc)
+        CK(cudaMemcpyAsync(h->h_status, h->fs.tc_status, sizeof(unsigned int), cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
-    if (h->fs.tc_ready) {
-        unsigned int st = 0;
-        if (field_solver_status(h->fs, &st) != AP_OK) return AP_ERR_CUDA;
-        if (st) return AP_ERR_TIMEOUT;
-    }
+    if (tc && *h->h_status) return AP_ERR_TIMEOUT;
     return AP_OK;
 }
 
@@ -914,6 +918,7 @@ int ap_create(const ap_netlist *nl, const ap_params *params, ap_handle **out) {
     A(dalloc(&h->d_out, 8));
     A(cudaMallocHost((void **)&h->h_sc, sizeof(DevScalars)));
     A(cudaMallocHost((void **)&h->h_out, sizeof(double) * 8));
+    A(cudaMallocHost((void **)&h->h_status, sizeof(unsigned int)));
     // the density chain (scatter -> rho -> field) is the trial's critical
     // path; the WA launches beside it yield the SMs to it
     int prio_low = 0, prio_high = 0;
@@ -1035,6 +1040,7 @@ int ap_destroy(ap_handle *h) {
         if (q) cudaFree(q);
     if (h->h_sc) cudaFreeHost(h->h_sc);
     if (h->h_out) cudaFreeHost(h->h_out);
+    if (h->h_status) cudaFreeHost(h->h_status);
     if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
     delete h;
     return AP_OK;

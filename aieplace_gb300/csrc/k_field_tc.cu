@@ -1403,13 +1403,4 @@ int field_solver_clear_status(FieldSolver &f) {
     return cudaMemset(f.tc_status, 0, sizeof(unsigned int)) == cudaSuccess ? AP_OK : AP_ERR_CUDA;
 }
 
-int field_solver_status(FieldSolver &f, unsigned int *out) {
-    if (!f.tc_status) {
-        *out = 0;
-        return AP_OK;
-    }
-    return cudaMemcpy(out, f.tc_status, sizeof(unsigned int), cudaMemcpyDeviceToHost) == cudaSuccess ? AP_OK
-                                                                                               : AP_ERR_CUDA;
-}
-
 }  // namespace ap
