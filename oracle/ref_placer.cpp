@@ -36,6 +36,8 @@
 #include <string>
 #include <vector>
 
+#include <cerrno>
+#include <sys/stat.h>
 #include <unistd.h>
 
 #include "Common.h"
@@ -177,7 +179,8 @@ void *ref_placer_create(int n, const float *w, const float *h, const float *x, c
                         int bins, float gamma, float learning_rate, float global_lambda, const char *workdir) {
     const std::string wd(workdir);
     const std::string design = wd + "/design";
-    if (system(("mkdir -p '" + wd + "/host' '" + design + "'").c_str()) != 0) return nullptr;
+    for (const std::string &d : {wd, wd + "/host", design})
+        if (mkdir(d.c_str(), 0755) != 0 && errno != EEXIST) return nullptr;
     {
         std::ofstream(design + "/cells.lef") << "";
         std::ofstream(design + "/floorplan.def") << "";
