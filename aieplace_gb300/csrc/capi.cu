@@ -1274,9 +1274,14 @@ int ap_step_host(ap_handle *h, const float *x_in, const float *y_in, float *x_ou
                 sa.in_x = h->d_ix;
                 sa.in_y = h->d_iy;
             }
+            // chunk k's update runs while chunk k + 1 is copied; only the last
+            // chunk's update runs after the whole input has landed, so the
+            // chunks shrink: 40, 30, 20, 10% of the nodes (tenths)
+            static const int kCut[5] = {0, 4, 7, 9, 10};
             int base = 0;
             for (int k = 0; k < nc; ++k) {
-                const int lo = (int)((long long)h->n_mov * k / nc), hi = (int)((long long)h->n_mov * (k + 1) / nc);
+                const int lo = nc == 4 ? (int)((long long)h->n_mov * kCut[k] / 10) : 0;
+                const int hi = nc == 4 ? (int)((long long)h->n_mov * kCut[k + 1] / 10) : h->n_mov;
                 if (in) {
                     const size_t b = sizeof(float) * (size_t)(hi - lo);
                     CK(cudaMemcpyAsync(h->d_ix + lo, x_in + lo, b, cudaMemcpyHostToDevice, h->copy_in));
