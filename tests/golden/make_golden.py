@@ -4,8 +4,8 @@ Run here (not on the GPU machine, which has no reference checkout):
 
     python tests/golden/make_golden.py <path of the reference checkout>
 
-(it builds oracle/_ref/libref.so from the reference sources first, through
-`make -C oracle ref REF=<path>`).
+(it builds oracle/_ref/libref.so and oracle/_ref/libref_placer.so from the
+reference sources first, through `make -C oracle ref refplacer REF=<path>`).
 
 Sources of each fixture:
   aie_partials.npz   vck5000/aie/golden_data/partials/*.dat (createGoldenPartials.py:28-132)
@@ -15,6 +15,11 @@ Sources of each fixture:
   replace_field.npz  replace::FFT::doFFT (fft_replace/fft.cpp:204-299) via oracle/_ref
   ref_grid.npz       Grid::computeBinOverlaps/getRho/computeTotalOverflow and
                      Net::computeWirelength_HPWL via oracle/_ref
+  ref_placer.npz     the reference's own Placer (vck5000/host/src/AIEplace.cpp)
+                     via oracle/_ref/libref_placer.so on the inputs of
+                     ref_placer_inputs.py: computeAllPartials_CPU partials,
+                     computeOverlaps / getRho, computeTotalOverflow, nudgeNode
+                     forces, computeTotalWirelength("HPWL")
 """
 from __future__ import annotations
 
@@ -149,6 +154,41 @@ def ref_grid(R):
     np.savez_compressed(os.path.join(HERE, "ref_grid.npz"), **out)
 
 
+def ref_placer(ref):
+    """Per case: the reference Placer's partials and nudge forces of every
+    SUBSAMPLE-th node, its density map and absolute overflow, its HPWL."""
+    import oracle
+    import ref_placer_inputs as I
+
+    sys.path.insert(0, REPO)
+    from aieplace_gb300.presets import PRESETS
+
+    out = {}
+    for name in I.CASES:
+        nl = I.small_nets(oracle.synth_generate(PRESETS[name], seed=I.SEED))
+        x, y = I.positions(nl)
+        die, M = nl["die"], nl["bins"]
+        with oracle.quiet_stdout():
+            rp = oracle.RefPlacer(nl["net_ptr"], nl["pin_node"], nl["node_w"], nl["node_h"], x, y,
+                                  nl["node_fixed"], float(die[2]), float(die[3]), M, gamma=I.GAMMA,
+                                  learning_rate=I.LEARNING_RATE, global_lambda=I.GLOBAL_LAMBDA)
+            gx, gy, _ = rp.partials()
+            rho, ovf, _ = rp.overlaps()
+            ex, ey = I.field(M)
+            zero = np.zeros(len(x), np.float32)
+            mx, my, _ = rp.nudge(ex, ey, zero, zero)
+            hp = rp.hpwl()
+        rp.close()
+        # nudgeNode's move is learning_rate min(W, H) global_lambda F (zero partials)
+        coeff = np.float32(I.LEARNING_RATE) * np.float32(min(float(die[2]), float(die[3]))) * np.float32(
+            I.GLOBAL_LAMBDA)
+        sub = slice(0, None, I.SUBSAMPLE)
+        out.update({f"{name}_gx": gx[sub], f"{name}_gy": gy[sub], f"{name}_fx": (mx / coeff)[sub],
+                    f"{name}_fy": (my / coeff)[sub], f"{name}_rho": rho, f"{name}_overflow": np.array(ovf),
+                    f"{name}_hpwl": np.array(hp), f"{name}_n_nets": np.array(len(nl["net_ptr"]) - 1)})
+    np.savez_compressed(os.path.join(HERE, "ref_placer.npz"), **out)
+
+
 def main():
     ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("AP_REFERENCE_DIR", "")
     if not ref or not os.path.isdir(ref):
@@ -158,12 +198,14 @@ def main():
     oracle.build(with_ref=True, ref_dir=ref)
     R = oracle.ref_lib()
     assert R is not None, "oracle/_ref/libref.so did not build"
+    assert oracle.ref_placer_lib() is not None, "oracle/_ref/libref_placer.so did not build"
     aie_partials(ref)
     aie_dct(ref)
     computeterm(ref)
     customdct(ref)
     replace_field(R)
     ref_grid(R)
+    ref_placer(ref)
     print("fixtures written to", HERE)
 
 

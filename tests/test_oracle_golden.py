@@ -167,3 +167,40 @@ def test_reference_lib_live_when_built(oracle_lib):
     mex, mey = oracle_lib.field_solve(d.astype(np.float64), 16)
     assert np.abs(mex - ex).max() <= 2e-6 * np.abs(ex).max()
     assert np.abs(mey - ey).max() <= 2e-6 * np.abs(ey).max()
+
+
+def test_oracle_matches_reference_placer_fixture(oracle_lib):
+    """The reference's own Placer (ref_placer.npz, made by make_golden.py from
+    AIEplace.cpp built for the CPU) against the oracle on the same netlists
+    and inputs (ref_placer_inputs.py): partials, density map, overflow,
+    nudgeNode force, HPWL."""
+    import ref_placer_inputs as I
+    from aieplace_gb300.presets import PRESETS
+
+    g = golden("ref_placer.npz")
+    for name in I.CASES:
+        nl = I.small_nets(oracle_lib.synth_generate(PRESETS[name], seed=I.SEED))
+        assert int(g[f"{name}_n_nets"]) == len(nl["net_ptr"]) - 1
+        x, y = I.positions(nl)
+        W, H, M = float(nl["die"][2]), float(nl["die"][3]), nl["bins"]
+        sub = slice(0, None, I.SUBSAMPLE)
+        ox, oy, _, hp = oracle_lib.wa_grad(nl["net_ptr"], nl["pin_node"], x, y, I.GAMMA)
+        tol = (I.partials_rounding(nl) + 1e-6 * max(np.abs(ox).max(), np.abs(oy).max()))[sub]
+        assert np.all(np.abs(g[f"{name}_gx"] - ox[sub]) <= tol)
+        assert np.all(np.abs(g[f"{name}_gy"] - oy[sub]) <= tol)
+        assert abs(hp - float(g[f"{name}_hpwl"])) <= 1e-6 * hp
+        grid = oracle_lib.grid(W, H, M)
+        q = oracle_lib.density_q(grid, x, y, nl["node_w"], nl["node_h"])
+        mine, ref = (q / 2.0 ** 32).reshape(M, M), g[f"{name}_rho"]
+        assert np.array_equal(mine != 0, ref != 0)
+        assert np.abs(mine - ref).max() <= 2e-5 * max(1.0, np.abs(ref).max())
+        zero = np.zeros_like(q)
+        _, ab = oracle_lib.overflow(grid, q, zero, zero, 1.0, 1.0)
+        assert abs(ab - float(g[f"{name}_overflow"])) <= 2e-5 * max(1.0, ab)
+        ex, ey = I.field(M)
+        fx, fy = oracle_lib.node_force(grid, x, y, nl["node_w"], nl["node_h"], ex.astype(np.float64),
+                                       ey.astype(np.float64))
+        mov = (nl["node_fixed"] == 0)[sub]
+        scale = max(np.abs(fx).max(), np.abs(fy).max())
+        assert np.abs(g[f"{name}_fx"][mov] - fx[sub][mov]).max() <= 1e-4 * scale
+        assert np.abs(g[f"{name}_fy"][mov] - fy[sub][mov]).max() <= 1e-4 * scale
