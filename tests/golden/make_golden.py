@@ -19,7 +19,8 @@ Sources of each fixture:
                      via oracle/_ref/libref_placer.so on the inputs of
                      ref_placer_inputs.py: computeAllPartials_CPU partials,
                      computeOverlaps / getRho, computeTotalOverflow, nudgeNode
-                     forces, computeTotalWirelength("HPWL")
+                     forces, computeTotalWirelength("HPWL"), the host DCT field
+                     path (compute_a_uv_DCT / compute_eField_DCT)
 """
 from __future__ import annotations
 
@@ -178,6 +179,9 @@ def ref_placer(ref):
             zero = np.zeros(len(x), np.float32)
             mx, my, _ = rp.nudge(ex, ey, zero, zero)
             hp = rp.hpwl()
+            if M <= 128:  # the host DCT path (naive O(M^3) transforms) at the two small sizes
+                dex, dey, _ = rp.fields_dct()
+                out.update({f"{name}_dct_ex": dex, f"{name}_dct_ey": dey})
         rp.close()
         # nudgeNode's move is learning_rate min(W, H) global_lambda F (zero partials)
         coeff = np.float32(I.LEARNING_RATE) * np.float32(min(float(die[2]), float(die[3]))) * np.float32(

@@ -12,6 +12,10 @@ cells / 128^2 bins; nets of degree 2..8):
   overflow      computeTotalOverflow: 2e-5 relative
   node force    nudgeNode's force on given fields: 1e-4 of the largest
   HPWL          computeTotalWirelength("HPWL"): 1e-6 relative
+  field         the host DCT path (compute_a_uv_DCT / compute_eField_DCT),
+                the FP32 solver at both sizes and the tensor-core BF16x3 one
+                at 128^2, on the CUDA density map: 1e-4 of the largest, after
+                the M^2 / 8 of the reference's unnormalised transforms
 """
 import numpy as np
 import pytest
@@ -46,10 +50,15 @@ def test_cuda_path_matches_reference_placer(ap, name):
     W, H, M = float(nl["die"][2]), float(nl["die"][3]), int(g[f"{name}_rho"].shape[0])
     sub = slice(0, None, I.SUBSAMPLE)
     ex, ey = I.field(M)
+    fields = {}
     with ap.Placer(nl, bins=M) as pl:
         gx, gy, _, hp = pl.compute_all_partials(x, y, I.GAMMA)
         q = pl.compute_overlaps(x, y)
         fx, fy = pl.compute_node_forces(x, y, ex, ey)
+        if f"{name}_dct_ex" in g:
+            area = (q / 2.0 ** 32).astype(np.float32)
+            for solver in ("fp32", "bf16x3") if M % 128 == 0 else ("fp32",):  # tcgen05 tiles: 128
+                fields[solver] = pl.compute_electric_fields(area, solver)
     # WA partials
     rx, ry = g[f"{name}_gx"], g[f"{name}_gy"]
     tol = I.partials_rounding(nl)[sub] + 1e-4 * max(np.abs(rx).max(), np.abs(ry).max())
@@ -71,3 +80,8 @@ def test_cuda_path_matches_reference_placer(ap, name):
     scale = max(np.abs(rfx[mov]).max(), np.abs(rfy[mov]).max())
     assert np.abs(fx[sub][mov] - rfx[mov]).max() <= 1e-4 * scale
     assert np.abs(fy[sub][mov] - rfy[mov]).max() <= 1e-4 * scale
+    # the field (reference: host DCT path, x M^2 / 8)
+    for solver, (cex, cey) in fields.items():
+        for ref_e, e in ((g[f"{name}_dct_ex"], cex), (g[f"{name}_dct_ey"], cey)):
+            k = M * M / 8.0 * e.reshape(M, M).astype(np.float64)
+            assert np.abs(ref_e - k).max() <= 1e-4 * np.abs(ref_e).max(), solver

@@ -204,3 +204,10 @@ def test_oracle_matches_reference_placer_fixture(oracle_lib):
         scale = max(np.abs(fx).max(), np.abs(fy).max())
         assert np.abs(g[f"{name}_fx"][mov] - fx[sub][mov]).max() <= 1e-4 * scale
         assert np.abs(g[f"{name}_fy"][mov] - fy[sub][mov]).max() <= 1e-4 * scale
+        if f"{name}_dct_ex" in g:
+            # the host DCT path's field is the spectral solve of the area map
+            # times M^2 / 8 (its transforms are unnormalised)
+            mex, mey = oracle_lib.field_solve((q / 2.0 ** 32).reshape(M, M), M)
+            for ref_e, e in ((g[f"{name}_dct_ex"], mex), (g[f"{name}_dct_ey"], mey)):
+                k = M * M / 8.0 * np.asarray(e).reshape(M, M)
+                assert np.abs(ref_e - k).max() <= 1e-5 * np.abs(ref_e).max()
