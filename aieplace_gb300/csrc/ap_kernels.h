@@ -102,7 +102,13 @@ struct ScatterArgs {
     // [16, 48) in two 32-bit words (set by the launcher where no word can
     // overflow); 0: one 64-bit word
     int tile32;
+    // optional: each node's fixed-point width and height (to_q(w), to_q(h);
+    // kSizeQNone where they do not fit int32), made once by launch_size_q:
+    // the position update reads them instead of converting every iteration
+    const int2 *whq;
 };
+constexpr int kSizeQNone = (int)0x80000000u;
+void launch_size_q(int n, const float *w, const float *h, int2 *out, cudaStream_t st);
 void launch_scatter(const ScatterArgs &a, cudaStream_t st);
 // the two launches of launch_scatter: the position update and records (update
 // mode only), then the bin adds

@@ -55,6 +55,7 @@ struct ap_handle {
     // device state
     int *d_net_ptr = nullptr, *d_pin_node = nullptr;
     float *d_w = nullptr, *d_h = nullptr;
+    int2 *d_whq = nullptr;  // to_q of the sizes, made once (launch_size_q)
     float *d_px[2] = {nullptr, nullptr}, *d_py[2] = {nullptr, nullptr};
     // all nodes' positions interleaved for the WA kernels: the loop's trial
     // point (movable nodes written by each position update, fixed nodes at
@@ -135,6 +136,7 @@ ScatterArgs scatter_args(ap_handle *h) {
     a.g = h->g;
     a.w = h->d_w;
     a.h = h->d_h;
+    a.whq = h->d_whq;
     a.die_w = h->die_w;
     a.die_h = h->die_h;
     a.sc = h->d_sc;
@@ -882,6 +884,7 @@ int ap_create(const ap_netlist *nl, const ap_params *params, ap_handle **out) {
     A(dalloc(&h->d_pin_node, pin_node.size()));
     A(dalloc(&h->d_w, N));
     A(dalloc(&h->d_h, N));
+    A(dalloc(&h->d_whq, N));
     for (int b = 0; b < 2; ++b) {
         A(dalloc(&h->d_px[b], N));
         A(dalloc(&h->d_py[b], N));
@@ -945,6 +948,11 @@ int ap_create(const ap_netlist *nl, const ap_params *params, ap_handle **out) {
         A(cudaMemcpy(h->d_pin_node, pin_node.data(), sizeof(int) * pin_node.size(), cudaMemcpyHostToDevice));
     A(cudaMemcpy(h->d_w, w.data(), sizeof(float) * N, cudaMemcpyHostToDevice));
     A(cudaMemcpy(h->d_h, hh.data(), sizeof(float) * N, cudaMemcpyHostToDevice));
+    if (ok) {
+        launch_size_q(N, h->d_w, h->d_h, h->d_whq, 0);
+        A(cudaGetLastError());
+        A(cudaStreamSynchronize(0));
+    }
     for (int b = 0; b < 2; ++b) {
         A(cudaMemcpy(h->d_px[b], x.data(), sizeof(float) * N, cudaMemcpyHostToDevice));
         A(cudaMemcpy(h->d_py[b], y.data(), sizeof(float) * N, cudaMemcpyHostToDevice));
@@ -1035,7 +1043,7 @@ int ap_destroy(ap_handle *h) {
                     h->d_mov_q,   h->d_fill_q,   h->d_fix_q,  h->d_fixs_q,  h->d_dens,  h->d_ex,    h->d_ey,
                     h->d_dens_hi, h->d_dens_lo,  h->d_sx,     h->d_sy,      h->d_sc,    h->d_partials,
                     h->d_partials_ll, h->d_counters, h->d_out, h->d_rec_bin, h->d_rec_ov, h->d_gq,
-                    h->d_ix,      h->d_iy,       h->d_xy_loop, h->d_xy_tmp};
+                    h->d_ix,      h->d_iy,       h->d_xy_loop, h->d_xy_tmp, h->d_whq};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     if (h->h_sc) cudaFreeHost(h->h_sc);

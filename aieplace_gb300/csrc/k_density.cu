@@ -100,14 +100,16 @@ __device__ __forceinline__ int rec_nr(int b) { return ((b >> 27) & 7) + 1; }
 __device__ __forceinline__ bool fits_i32(long long v) { return v >= -2147483647ll && v <= 2147483647ll; }
 
 __device__ __forceinline__ NodeRec make_rec(const Grid &g, float x, float y, float w, float h, int &c0, int &c1,
-                                            int &r0, int &r1) {
+                                            int &r0, int &r1, int2 whq = make_int2(kSizeQNone, kSizeQNone)) {
     NodeRec r{kRecNone, 0, 0, 0, 0};
     bool small;
     if (!bin_range(g, x, y, w, h, c0, c1, r0, r1, small)) {
         c1 = r1 = -1;
         return r;
     }
-    const long long wq = to_q(w), hq = to_q(h);
+    // the sizes' fixed point from launch_size_q where it was made (the same integers)
+    const long long wq = whq.x != kSizeQNone ? (long long)whq.x : to_q(w);
+    const long long hq = whq.y != kSizeQNone ? (long long)whq.y : to_q(h);
     if (small) {
         if (!fits_i32(wq) || !fits_i32(hq)) {
             r.bin = kRecFull;
@@ -193,7 +195,8 @@ __device__ __forceinline__ void update_body(const ScatterArgs &a, VBlock vb) {
     int *__restrict__ rbin = a.rec_bin;
     int4 *__restrict__ rov = a.rec_ov;
     const int lo = a.upd_hi > 0 ? a.upd_lo : 0, hi = a.upd_hi > 0 ? a.upd_hi : a.n_mov;
-    auto node = [&](int i, float w, float h, float ux, float uy, float vx, float vy, float gx, float gy) {
+    auto node = [&](int i, float w, float h, int2 whq, float ux, float uy, float vx, float vy, float gx,
+                    float gy) {
         const float xhi = fmaxf(a.die_w - w, 0.f), yhi = fmaxf(a.die_h - h, 0.f);
         const float nux = clampf(vx - alpha * gx, 0.f, xhi);
         const float nuy = clampf(vy - alpha * gy, 0.f, yhi);
@@ -211,10 +214,12 @@ __device__ __forceinline__ void update_body(const ScatterArgs &a, VBlock vb) {
         du += (nux - ux) * (nux - ux) + (nuy - uy) * (nuy - uy);
         dv += (x - vx) * (x - vx) + (y - vy) * (y - vy);
         int c0, c1, r0, r1;
-        const NodeRec r = make_rec(g, x, y, w, h, c0, c1, r0, r1);
+        const NodeRec r = make_rec(g, x, y, w, h, c0, c1, r0, r1, whq);
         rbin[i] = r.bin;
         rov[i] = make_int4(r.xr, r.wq, r.yr, r.hq);
     };
+    const int2 *__restrict__ whqa = a.whq;
+    auto size_q = [&](int i) { return whqa ? __ldg(whqa + i) : make_int2(kSizeQNone, kSizeQNone); };
     // two nodes of the thread's grid-stride sequence per trip, every load of
     // both issued before either is used (twice the loads in flight per warp);
     // the nodes are taken in the same order as one per trip, so the FP32
@@ -229,10 +234,12 @@ __device__ __forceinline__ void update_body(const ScatterArgs &a, VBlock vb) {
         const float ux0 = uxc[i], uy0 = uyc[i], ux1 = uxc[j], uy1 = uyc[j];
         const float vx0 = vxc[i], vy0 = vyc[i], vx1 = vxc[j], vy1 = vyc[j];
         const float gx0 = gxc[i], gy0 = gyc[i], gx1 = gxc[j], gy1 = gyc[j];
-        node(i, w0, h0, ux0, uy0, vx0, vy0, gx0, gy0);
-        node(j, w1, h1, ux1, uy1, vx1, vy1, gx1, gy1);
+        const int2 q0 = size_q(i), q1 = size_q(j);
+        node(i, w0, h0, q0, ux0, uy0, vx0, vy0, gx0, gy0);
+        node(j, w1, h1, q1, ux1, uy1, vx1, vy1, gx1, gy1);
     }
-    for (; i < hi; i += S) node(i, __ldg(a.w + i), __ldg(a.h + i), uxc[i], uyc[i], vxc[i], vyc[i], gxc[i], gyc[i]);
+    for (; i < hi; i += S)
+        node(i, __ldg(a.w + i), __ldg(a.h + i), size_q(i), uxc[i], uyc[i], vxc[i], vyc[i], gxc[i], gyc[i]);
     float *pf = reinterpret_cast<float *>(a.partials);
     float bs[2] = {du, dv};
     block_sums_ff<2>(bs, reinterpret_cast<float *>(red));
@@ -449,6 +456,18 @@ int wave_of(const void *kernel, int threads, int fallback, int dyn_smem) {
         sms * per_sm > 0)
         return sms * per_sm;
     return fallback;
+}
+
+__global__ void size_q_kernel(int n, const float *__restrict__ w, const float *__restrict__ h, int2 *out) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const long long wq = to_q(w[i]), hq = to_q(h[i]);
+        out[i] = make_int2(fits_i32(wq) ? (int)wq : kSizeQNone, fits_i32(hq) ? (int)hq : kSizeQNone);
+    }
+}
+
+void launch_size_q(int n, const float *w, const float *h, int2 *out, cudaStream_t st) {
+    if (n <= 0) return;
+    size_q_kernel<<<std::min((n + kThreads - 1) / kThreads, 4096), kThreads, 0, st>>>(n, w, h, out);
 }
 
 int update_grid(const ScatterArgs &a) {
