@@ -108,23 +108,20 @@ struct Grid {
 // Integer <-> float conversions execute on the FP64 pipe, which is narrow on
 // this part; the helpers below do them with integer and FMA-pipe arithmetic.
 
-// Round-to-nearest-even of s to an integer for |s| < 2^31, from the bit
-// fields of s (the same integer llrintf gives).
+// Round-to-nearest-even of s to an integer for |s| < 2^31 (the same integer
+// llrintf gives), in FMA-pipe and integer arithmetic without branches:
+// adding M = 1.5 2^32 (whose binade has an ulp of 512) rounds s to 512 k,
+// read off as the difference of the bit patterns; the remainder
+// l = s - 512 k (|l| <= 256) is exact, and RNE(s) = 512 k + RNE(l) because
+// 512 k is an even integer; RNE(l) by the 1.5 2^23 magic number.  The sum is
+// formed in unsigned arithmetic (512 k can be 2^31 when s rounds to 2^31 - 128).
 __device__ __forceinline__ int f2i_rn_bits(float s) {
-    const unsigned b = __float_as_uint(s);
-    const unsigned ex = (b >> 23) & 0xFFu;
-    const unsigned m = ex ? ((b & 0x7FFFFFu) | 0x800000u) : 0u;
-    const int e = (int)ex - 150;  // |s| = m * 2^e
-    unsigned r;
-    if (e >= 0) {
-        r = m << e;
-    } else if (e < -24) {
-        r = 0u;  // |s| < 0.5
-    } else {
-        const unsigned sh = (unsigned)(-e), q = m >> sh, rem = m & ((1u << sh) - 1u), half = 1u << (sh - 1u);
-        r = q + ((rem > half || (rem == half && (q & 1u))) ? 1u : 0u);
-    }
-    return (b >> 31) ? -(int)r : (int)r;
+    const float M = 6442450944.0f;  // 1.5 * 2^32
+    const float t = __fadd_rn(s, M);
+    const unsigned k = (unsigned)(__float_as_int(t) - __float_as_int(M));
+    const float l = __fsub_rn(s, __fsub_rn(t, M));
+    const unsigned r = (unsigned)(__float_as_int(__fadd_rn(l, 12582912.0f)) - 0x4B400000);
+    return (int)(k * 512u + r);
 }
 
 // Truncation toward zero of s to an integer for |s| < 2^31 (= (int)s).
