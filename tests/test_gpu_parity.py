@@ -148,6 +148,71 @@ def test_wirelength_gradient_every_degree_bucket(ap, oracle_lib):
     assert abs(wa - rwa) <= 1e-5 * rwa
 
 
+def test_nets_below_two_pins_change_nothing(ap, oracle_lib):
+    """Nets of 0 and 1 pins interleaved in the CSR.  The reference takes no
+    partials from them (computeNetPartials_CPU returns below degree 2,
+    AIEplace.cpp:655) and their HPWL is 0: the gradient, HPWL and WA equal
+    the oracle's, and the loop is bit-identical to the loop on the netlist
+    without them."""
+    base = ap.synth.generate("c0", seed=6)
+    rng = np.random.default_rng(6)
+    n = len(base["node_w"])
+    bptr, bpins = base["net_ptr"], base["pin_node"]
+    ptr, pins = [0], []
+    for e in range(len(bptr) - 1):
+        if rng.random() < 0.05:  # an empty net
+            ptr.append(len(pins))
+        if rng.random() < 0.05:  # a one-pin net
+            pins.append(int(rng.integers(n)))
+            ptr.append(len(pins))
+        pins += [int(p) for p in bpins[bptr[e]:bptr[e + 1]]]
+        ptr.append(len(pins))
+    nl = dict(base)
+    nl["net_ptr"], nl["pin_node"] = np.array(ptr, np.int32), np.array(pins, np.int32)
+    assert len(ptr) - 1 > len(bptr) - 1
+    x, y = spread_positions(nl, rng, margin=0.0)
+    with ap.Placer(nl, bins=32) as pl:
+        gx, gy, wa, hp = pl.compute_all_partials(x, y, 2.0)
+    rx, ry, rwa, rhp = oracle_lib.wa_grad(nl["net_ptr"], nl["pin_node"], x, y, 2.0)
+    scale = max(np.abs(rx).max(), np.abs(ry).max())
+    assert np.abs(gx - rx).max() <= 1e-4 * scale
+    assert np.abs(gy - ry).max() <= 1e-4 * scale
+    assert abs(hp - rhp) <= 1e-6 * rhp
+    assert abs(wa - rwa) <= 1e-5 * rwa
+    with ap.Placer(base, bins=32) as a, ap.Placer(nl, bins=32) as b:
+        a.initialize_placement(base["node_x"], base["node_y"])
+        b.initialize_placement(base["node_x"], base["node_y"])
+        a.perform_iteration(20)
+        b.perform_iteration(20)
+        (ax, ay), (bx, by) = a.positions(), b.positions()
+        np.testing.assert_array_equal(ax, bx)
+        np.testing.assert_array_equal(ay, by)
+        assert a.stats()["hpwl"] == b.stats()["hpwl"]
+
+
+def test_netlist_without_nets(ap):
+    """No nets at all: zero gradient, HPWL and WA.  ePlace's initial density
+    weight is the ratio of the wirelength and density gradient norms, 0
+    here, and the step length of a zero gradient difference is 0: the loop
+    runs without error and leaves every cell where it is."""
+    nl = dict(ap.synth.generate("c0", seed=7))
+    nl["net_ptr"] = np.zeros(1, np.int32)
+    nl["pin_node"] = np.zeros(0, np.int32)
+    x, y = nl["node_x"], nl["node_y"]
+    with ap.Placer(nl, bins=32) as pl:
+        gx, gy, wa, hp = pl.compute_all_partials(x, y, 2.0)
+        assert not gx.any() and not gy.any() and wa == 0.0 and hp == 0.0
+        pl.initialize_placement(seed=3, sigma=1.0)
+        tau0 = pl.overflow()[0]
+        x0, y0 = pl.positions()
+        pl.perform_iteration(30)
+        s = pl.stats()
+        assert s["status"] == 0 and s["hpwl"] == 0.0 and s["overflow"] == tau0
+        x1, y1 = pl.positions()
+        np.testing.assert_array_equal(x0, x1)
+        np.testing.assert_array_equal(y0, y1)
+
+
 def with_hub_nodes(ap, seed=3):
     """c0 plus 600 two-pin nets on one movable node and 700 on one fixed node:
     more pins than one packed two-axis accumulator holds (512), so those two
