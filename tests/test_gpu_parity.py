@@ -190,6 +190,43 @@ def test_nets_below_two_pins_change_nothing(ap, oracle_lib):
         assert a.stats()["hpwl"] == b.stats()["hpwl"]
 
 
+@pytest.mark.parametrize("solver", ["fp32", "bf16x3"])
+def test_rectangular_die_against_oracle(ap, oracle_lib, solver):
+    """A die 1.5 times as wide as high (bins 1.5 times as wide as tall; 20k
+    cells, 128^2 bins): the density map bit-exact, the field within 1e-4 of
+    the largest against the oracle's solve with the same bin ratio, and the
+    per-node force within 1e-5 of the force on |E|."""
+    nl = dict(ap.synth.generate("c1_small", seed=9))
+    nl["die"] = nl["die"].copy()
+    nl["die"][2] *= 1.5
+    nl["node_x"] = (nl["node_x"] * np.float32(1.5)).astype(np.float32)
+    rng = np.random.default_rng(9)
+    x, y = spread_positions(nl, rng, margin=0.0)
+    M = 128
+    W, H = float(nl["die"][2]), float(nl["die"][3])
+    g = oracle_lib.grid(W, H, M)
+    mov = nl["node_fixed"] == 0
+    area = (nl["node_w"] * nl["node_h"]) > 0
+    ref = oracle_lib.density_q(g, x, y, nl["node_w"], nl["node_h"], area.astype(np.uint8))
+    d = (ref.reshape(M, M) / float(g.bw_q * g.bh_q)).astype(np.float32)
+    ratio = float(np.float32(g.bh / g.bw))
+    rex, rey = oracle_lib.field_solve(d.astype(np.float64), M, bin_ratio=ratio)
+    with ap.Placer(nl, bins=M) as pl:
+        got = pl.compute_overlaps(x, y)
+        ex, ey = pl.compute_electric_fields(d, solver)
+        fx, fy = pl.compute_node_forces(x, y, ex, ey)
+    assert np.array_equal(got, ref)
+    scale = max(np.abs(rex).max(), np.abs(rey).max())
+    assert np.abs(ex - rex).max() <= 1e-4 * scale
+    assert np.abs(ey - rey).max() <= 1e-4 * scale
+    rfx, rfy = oracle_lib.node_force(g, x, y, nl["node_w"], nl["node_h"], ex.astype(np.float64),
+                                     ey.astype(np.float64), include=mov.astype(np.uint8))
+    afx, afy = oracle_lib.node_force(g, x, y, nl["node_w"], nl["node_h"], np.abs(ex).astype(np.float64),
+                                     np.abs(ey).astype(np.float64), include=mov.astype(np.uint8))
+    assert np.all(np.abs(fx[mov] - rfx[mov]) <= 1e-5 * np.abs(afx[mov]) + 1e-12)
+    assert np.all(np.abs(fy[mov] - rfy[mov]) <= 1e-5 * np.abs(afy[mov]) + 1e-12)
+
+
 def test_netlist_without_nets(ap):
     """No nets at all: zero gradient, HPWL and WA.  ePlace's initial density
     weight is the ratio of the wirelength and density gradient norms, 0
