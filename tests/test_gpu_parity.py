@@ -227,6 +227,29 @@ def test_rectangular_die_against_oracle(ap, oracle_lib, solver):
     assert np.all(np.abs(fy[mov] - rfy[mov]) <= 1e-5 * np.abs(afy[mov]) + 1e-12)
 
 
+def test_largest_bin_count(ap, oracle_lib):
+    """4096^2 bins, the largest grid ap_create takes (20k cells, each over
+    tens of bins: the general overlap path): the density map bit-exact, both
+    field solvers within 1e-4 of the largest against the oracle's FP64 fast
+    transforms."""
+    nl = ap.synth.generate("c1_small", seed=10)
+    rng = np.random.default_rng(10)
+    x, y = spread_positions(nl, rng, margin=0.0)
+    M = 4096
+    g = oracle_lib.grid(float(nl["die"][2]), float(nl["die"][3]), M)
+    area = (nl["node_w"] * nl["node_h"]) > 0
+    ref = oracle_lib.density_q(g, x, y, nl["node_w"], nl["node_h"], area.astype(np.uint8))
+    d = (ref.reshape(M, M) / float(g.bw_q * g.bh_q)).astype(np.float32)
+    rex, rey = oracle_lib.field_solve_fft(d.astype(np.float64), M)
+    scale = max(np.abs(rex).max(), np.abs(rey).max())
+    with ap.Placer(nl, bins=M) as pl:
+        assert np.array_equal(pl.compute_overlaps(x, y), ref)
+        for solver in ("fp32", "bf16x3"):
+            ex, ey = pl.compute_electric_fields(d, solver)
+            assert np.abs(ex - rex).max() <= 1e-4 * scale, solver
+            assert np.abs(ey - rey).max() <= 1e-4 * scale, solver
+
+
 def test_netlist_without_nets(ap):
     """No nets at all: zero gradient, HPWL and WA.  ePlace's initial density
     weight is the ratio of the wirelength and density gradient norms, 0
