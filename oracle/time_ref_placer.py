@@ -40,7 +40,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path[:] = [p for p in sys.path if os.path.abspath(p or ".") != HERE]
 sys.path.insert(0, os.path.dirname(HERE))
 
-from oracle import oracle as O  # noqa: E402
+try:
+    from oracle import oracle as O  # noqa: E402  (oracle/ as a package, from the repository root)
+except ImportError:
+    import oracle as O  # noqa: E402  (oracle/ itself on the path, as the tests have it)
 from aieplace_gb300.presets import PRESETS  # noqa: E402
 
 

@@ -170,3 +170,21 @@ def test_cpu_loop_moves_by_density_force_alone():
     # tolerance: from these positions it is larger than the density move
     wx, wy, _, _ = O.wa_grad(nl["net_ptr"], nl["pin_node"], x, y, GAMMA, min_deg=2, max_deg=8)
     assert LR * 0.8 * min(float(die[2]), float(die[3])) * np.abs(wx[comp]).max() > scale
+
+
+def test_timing_script_runs_at_c0(capsys):
+    """oracle/time_ref_placer.py (the reference's CPU functions timed) on the
+    576-cell case: one JSON object with every function's time."""
+    import json
+    import os
+    import sys
+
+    sys.path.insert(0, os.path.dirname(O.__file__))
+    import time_ref_placer
+
+    assert time_ref_placer.main(["--configs", "c0", "--reps", "1", "--loop-iters", "2"]) == 0
+    r = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
+    assert r["config"] == "c0" and r["threads"] == 1
+    for k in ("partials_s", "overlaps_s", "nudge_s", "field_naive_s", "field_dct_s", "loop_s"):
+        assert r[k] > 0.0
+    assert r["iters_per_s_as_shipped"] > 0.0
