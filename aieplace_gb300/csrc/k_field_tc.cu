@@ -191,14 +191,6 @@ __device__ __forceinline__ float ld_shared_f1(uint32_t addr) {
 
 // explicit global stores: a generic store could alias shared memory, and the
 // staging loads that follow it would wait for it
-__device__ __forceinline__ void st_global_f2(float *p, float a, float b) {
-    asm volatile("st.global.v2.f32 [%0], {%1, %2};" ::"l"(p), "f"(a), "f"(b) : "memory");
-}
-
-__device__ __forceinline__ void st_global_u32(void *p, uint32_t v) {
-    asm volatile("st.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
-
 __device__ __forceinline__ float4 ld_shared_f4(uint32_t addr) {
     float4 v;
     asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];" : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "r"(addr));
@@ -278,13 +270,6 @@ __device__ __forceinline__ void store_split_vec(const float (&v)[VEC], __nv_bflo
 }
 
 // Two adjacent FP32 outputs -> their BF16 hi and lo pairs (4-byte stores)
-__device__ __forceinline__ void st_split2(__nv_bfloat16 *hi, __nv_bfloat16 *lo, float a, float b) {
-    const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
-    const float2 hf = __bfloat1622float2(h);
-    st_global_u32(hi, *reinterpret_cast<const uint32_t *>(&h));
-    st_global_u32(lo, pack_bf16(a - hf.x, b - hf.y));
-}
-
 // Output pointers of one CTA's stage epilogue, resolved before the row loop:
 // indexing the parameter block by blockIdx.z inside the loop made the compiler
 // copy it to local memory.
