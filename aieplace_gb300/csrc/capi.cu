@@ -922,13 +922,13 @@ int ap_create(const ap_netlist *nl, const ap_params *params, ap_handle **out) {
     A(cudaMallocHost((void **)&h->h_sc, sizeof(DevScalars)));
     A(cudaMallocHost((void **)&h->h_out, sizeof(double) * 8));
     A(cudaMallocHost((void **)&h->h_status, sizeof(unsigned int)));
-    // the density chain (scatter -> rho -> field) is the trial's critical
-    // path; the WA launches beside it yield the SMs to it
-    int prio_low = 0, prio_high = 0;
-    A(cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high));
-    A(cudaStreamCreateWithPriority(&h->stream, cudaStreamNonBlocking, prio_high));
+    // the WA launches run beside the density chain (scatter -> rho -> field)
+    // at the same priority: with the chain's stream at the highest priority a
+    // 2M-cell trial took 1.5% longer (its blocks kept the WA blocks waiting
+    // where both would have shared the SMs)
+    A(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
     h->own_stream = true;
-    A(cudaStreamCreateWithPriority(&h->wa_stream, cudaStreamNonBlocking, prio_low));
+    A(cudaStreamCreateWithFlags(&h->wa_stream, cudaStreamNonBlocking));
     A(cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming));
     A(cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming));
     A(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
